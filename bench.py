@@ -1,0 +1,314 @@
+#!/usr/bin/env python
+"""Benchmark: particle-steps/s of the explicit GIMP MPM step on one GB300.
+
+Workload: the 3D Newtonian dam break (domain 4 x 2 x 2 m, cellsize 0.01 m, psep 0.005 m,
+water column 1.0 x 1.96 x 0.765 m against the x = 0 wall, 11,997,600 particles, gravity
+-9.81 in z, zero-velocity node walls two cells deep), seeded synthetic lattice input.
+A step is one full explicit step (sort, P2G, fold + nodal solve + BCs, G2P + update +
+constitutive) over all particles.  State stays resident in HBM; the particle and grid state
+(1.1 GB + 0.5 GB) is far larger than L2, so no explicit L2 flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+With N > 1 (torchrun) every rank advances an independent replica: the step has no
+partition without a halo exchange, so this is replicas only and value = all ranks'
+particle-steps / the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/sec, 1 GB300: plain MPM vs DP surrogate at <=1e-3 rel stress err"
+UNIT = "particle-steps/s"
+
+# algorithmic bytes (FP32 SoA state read once and written once per step)
+P2G_BYTES_PER_PARTICLE = 64        # key, offsets, v, sigma, m, rho, info
+P2G_BYTES_PER_NODE = 28            # m, p(3), f(3) accumulated per active node
+G2P_BYTES_PER_PARTICLE = 168       # full particle state read + written (models 1-2)
+G2P_BYTES_PER_NODE = 24            # v(3), a(3) read per active node
+SOLVE_BYTES_PER_NODE = 52          # m, p, f read; v, a written
+STEP_BYTES_PER_PARTICLE = 168
+STEP_BYTES_PER_NODE = 104
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    def __init__(self, world, local):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch
+            import torch.distributed as dist
+            self.torch, self.dist = torch, dist
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(local)
+            dist.init_process_group(backend)
+
+    def barrier(self):
+        if self.world > 1:
+            self.dist.barrier()
+
+    def max(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        t = self.torch.tensor([x], dtype=self.torch.float64,
+                              device="cuda" if self.dist.get_backend() == "nccl" else "cpu")
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.dist.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
+        os.unlink(self.path)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                smax = float(r[2])
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if r[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """Per-launch DRAM bytes of the dominant kernels from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        return json.load(open(path))
+    except Exception:
+        return {}
+
+
+def cpu_sample_scene():
+    """Bounded CPU sample of the same workload: a 0.14 m wide y-slab of the dam break at the
+    same resolution (200 x 20 x 153 = 612,000 particles, 1.2 M nodes)."""
+    from graphyt_gb300 import scenes
+    return scenes.dam_break(scale=1.0, width=0.14)
+
+
+def run_cpu(nsteps: int, warmup: int, prefer_reference: bool = True):
+    """Time the reference's CPU step (oracle/_ref when built, else the FP64 restatement) on
+    the bounded sample.  Returns (particle-steps/s, kind, threads, sample description)."""
+    from oracle import oracle as O
+    kind = "ref" if (prefer_reference and O.available("ref")) else "port"
+    if not O.available(kind):
+        O.build()
+    sc = cpu_sample_scene()
+    o = O.Oracle(sc, kind, mode=1)
+    o.run(warmup)
+    t0 = time.perf_counter()
+    o.run(nsteps)
+    dt = time.perf_counter() - t0
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    o.close()
+    sample = (f"dam break y-slab 4 x 0.14 x 2 m, cellsize 0.01, {sc.n} particles, {sc.num_nodes()} nodes, "
+              f"{nsteps} timed steps after {warmup}")
+    return sc.n * nsteps / dt, ("reference" if kind == "ref" else "port"), threads, sample
+
+
+def bench_reference(args, rank):
+    if rank != 0:
+        return
+    value, kind, threads, sample = run_cpu(args.steps, args.warmup)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "dam_break_3d_newtonian", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--sort-every", type=int, default=1)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        bench_reference(args, rank)
+        return
+
+    from graphyt_gb300 import build as gbuild
+    if not os.path.exists(gbuild.LIB):
+        gbuild.build()
+    from graphyt_gb300 import _lib as L
+    from graphyt_gb300 import graphyt, scenes
+
+    dist = Dist(world, local)
+    sc = scenes.dam_break(scale=args.scale)
+    n = sc.n
+    solver = graphyt.from_scene(sc, device=local, options=dict(sort_every=args.sort_every))
+    lib, h = solver.lib, solver.h
+    dt = solver.dt
+    for k in range(args.warmup):
+        solver.iterate_GPU(k * dt, k)
+    solver.Synchronise()
+    dist.barrier()
+
+    sampler = ClockSampler(local)
+    if rank == 0:
+        sampler.start()
+    L.check(lib.gy_set_phase_timing(h, 1), h)
+    launches0 = lib.gy_kernel_launches()
+    ms = C.c_float()
+    step0 = args.warmup
+    L.check(lib.gy_time_steps(h, step0 * dt, step0, args.steps, C.byref(ms)), h, "timed steps")
+    launches = lib.gy_kernel_launches() - launches0
+    phase = (C.c_float * 5)()
+    nph = C.c_int64()
+    L.check(lib.gy_get_phase_times(h, phase, C.byref(nph)), h)
+    L.check(lib.gy_set_phase_timing(h, 0), h)
+    clocks = sampler.stop() if rank == 0 else None
+    solver.Synchronise()
+    ms_max = dist.max(ms.value)
+    ms_per_step = ms_max / args.steps
+    value = n * args.steps * world / (ms_max / 1e3)
+
+    st = solver.stats()
+    n_active = int(st["active_nodes"])
+
+    # end to end through the public API: per step the parameter block goes host->device
+    # with the launch and the step's FP64 conservation sums come back device->host
+    prm = solver.params
+    dist.barrier()
+    t0 = time.perf_counter()
+    s0 = step0 + args.steps
+    for k in range(args.steps):
+        solver.iterate_GPU((s0 + k) * dt, s0 + k, prm)
+        solver.stats()
+    e2e_s = dist.max(time.perf_counter() - t0)
+    e2e_value = n * args.steps * world / e2e_s
+
+    # roofline of the dominant kernel
+    names = ["sort", "p2g", "grid", "g2p_update"]
+    per_step = [phase[k] / max(nph.value, 1) for k in range(4)]
+    algo = {
+        "sort": 0.0,
+        "p2g": P2G_BYTES_PER_PARTICLE * n + P2G_BYTES_PER_NODE * n_active,
+        "grid": SOLVE_BYTES_PER_NODE * n_active,
+        "g2p_update": G2P_BYTES_PER_PARTICLE * n + G2P_BYTES_PER_NODE * n_active,
+    }
+    dom = max(range(4), key=lambda k: per_step[k] if names[k] != "sort" else -1)
+    peak, peak_kind = measured_peak()
+    achieved = algo[names[dom]] / (per_step[dom] / 1e3) / 1e9
+    traffic = profiled_traffic().get(names[dom])
+    roofline = {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+                "algorithmic_bytes": algo[names[dom]]}
+    step_bytes = STEP_BYTES_PER_PARTICLE * n + STEP_BYTES_PER_NODE * n_active
+    whole = step_bytes / (ms_per_step / 1e3) / 1e9
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, kind, threads, sample = run_cpu(2, 1)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "dam_break_3d_newtonian", "particles": n, "nodes": sc.num_nodes(),
+                       "active_nodes": n_active, "cellsize": sc.cellsize, "psep": sc.psep, "model": "newtonian",
+                       "sort_every": args.sort_every, "l2": "state larger than L2 (no flush needed)",
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "phase_ms_per_step": dict(zip(names, per_step)),
+            "roofline": roofline,
+            "step_roofline": {"achieved": whole, "peak": peak, "unit": "GB/s", "frac": whole / peak,
+                              "bytes_per_step": step_bytes},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": C.sizeof(L.Params),
+                    "d2h_bytes_per_step": C.sizeof(L.Stats)},
+            "gpu_launches": int(launches),
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    solver.close()
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,1020 @@
+// gy_api.cu -- host runtime behind the C ABI (include/graphyt_gpu.h).
+//
+// Owns the device state of one simulation, converts the reference's host-side model
+// (Nodes, MaterialPoints, MaterialModels, Parameters, Solver) into the GPU layout and
+// sequences the kernels of one step on the handle's stream.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/graphyt_gpu.h"
+#include "gy_kernels.cuh"
+
+using namespace gy;
+
+struct gy_solver {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+
+    // grid (Nodes)
+    double L[3] = {0, 0, 0}, h = 0, psep = 0;
+    int nx = 0, ny = 0, nz = 0;
+    long long nn = 0;
+    GridGeom g{};
+    std::vector<int> nidx[3];
+
+    // host staging, insertion order (MaterialPoints)
+    std::vector<double> pos, vel, stress, dmg;
+    std::vector<int> mat, obj, pbc_type;
+    std::vector<double> pbc_val;
+    std::vector<unsigned char> hold;
+    std::vector<unsigned char> nbc_type;
+    std::vector<float> nbc_val;
+    bool any_node_bc = false;
+
+    // model
+    std::vector<gy_material> mats;
+    gy_params prm{};
+    double dt = 0.0;
+    bool initialized = false;
+    gy_options opt{1, 0, 256, 0, 0, 0};
+    std::vector<int> slot_obj;       // dense object slot -> objectID
+    bool multi = false, has_dp = false;
+    int nbody = 1;
+
+    // device particle state
+    long long n = 0, cap = 0;
+    float *slab[2] = {nullptr, nullptr};
+    int cur = 0;
+    int *d_keys = nullptr, *d_perm = nullptr, *d_fields = nullptr;
+    int nfields = 0;
+    SortScratch ws{};
+    void *sort_mem = nullptr;
+    float4 *d_pbc_val = nullptr;
+    int *d_refkey0 = nullptr;
+    DevMaterial *d_mats = nullptr;
+    int *d_status = nullptr;
+    double *d_stats = nullptr;
+
+    // device node state
+    NodeBufs nb{};
+    void *node_mem = nullptr;
+    int *d_cell_min = nullptr;
+    int *d_nidx[3] = {nullptr, nullptr, nullptr};
+
+    // stepping
+    double t_prev = 0.0;
+    long long steps = 0;
+    long long since_sort = 1 << 30;
+    bool tables_valid = false;
+    bool phase_timing = false;
+    cudaEvent_t ev[6] = {};
+    std::vector<cudaEvent_t> tev;   // phase-timing pool: 5 events per timed step
+    long long tev_used = 0;
+};
+
+static constexpr long long kMaxTimedSteps = 4096;
+
+namespace {
+
+gy_status fail(gy_solver *h, gy_status code, const std::string &msg)
+{
+    if (h) h->err = msg;
+    return code;
+}
+
+#define CK(h, call)                                                                        \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess)                                                             \
+            return fail(h, e_ == cudaErrorMemoryAllocation ? GY_ERR_NOMEM : GY_ERR_CUDA,   \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));               \
+    } while (0)
+
+template <class T> gy_status dalloc(gy_solver *h, T **p, size_t count)
+{
+    cudaError_t e = cudaMalloc((void **)p, count * sizeof(T) + 16);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return fail(h, GY_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    return GY_OK;
+}
+
+PView pview(gy_solver *h, int which) { return PView{h->slab[which], h->cap}; }
+
+void free_device(gy_solver *h)
+{
+    void *ptrs[] = {h->slab[0], h->slab[1], h->d_keys, h->d_perm, h->d_fields, h->sort_mem, h->d_pbc_val,
+                    h->d_refkey0, h->d_mats, h->d_status, h->d_stats, h->node_mem, h->d_cell_min,
+                    h->d_nidx[0], h->d_nidx[1], h->d_nidx[2]};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    h->slab[0] = h->slab[1] = nullptr;
+    h->d_keys = h->d_perm = h->d_fields = nullptr;
+    h->sort_mem = nullptr;
+    h->d_pbc_val = nullptr;
+    h->d_refkey0 = nullptr;
+    h->d_mats = nullptr;
+    h->d_status = nullptr;
+    h->d_stats = nullptr;
+    h->node_mem = nullptr;
+    h->d_cell_min = nullptr;
+    for (int a = 0; a < 3; a++) h->d_nidx[a] = nullptr;
+}
+
+bool valid_index(const gy_solver *h, int64_t i) { return i >= 0 && i < (int64_t)h->mat.size(); }
+
+}  // namespace
+
+extern "C" {
+
+int gy_abi_version(void) { return GY_ABI_VERSION; }
+
+const char *gy_last_error(const gy_solver *h) { return h ? h->err.c_str() : "null handle"; }
+
+gy_status gy_create(const gy_grid_desc *grid, int device, gy_solver **out)
+{
+    if (!grid || !out) return GY_ERR_ARG;
+    *out = nullptr;
+    const double h = grid->cellsize;
+    if (!(h > 0) || !(grid->psep > 0) || grid->L[0] <= 0 || grid->L[1] <= 0 || grid->L[2] < 0) return GY_ERR_ARG;
+    // Nodes.cpp:12 rounds numNodes while :71-73 truncate Nx, Ny, Nz
+    const double nn_r = std::round((1.0 + grid->L[0] / h) * (1.0 + grid->L[1] / h) * (1.0 + grid->L[2] / h));
+    const int nx = (int)(1.0 + grid->L[0] / h), ny = (int)(1.0 + grid->L[1] / h), nz = (int)(1.0 + grid->L[2] / h);
+    if ((double)nx * ny * nz != nn_r) return GY_ERR_ARG;
+    const bool is3d = nz > 1;
+    if (nx < 6 || ny < 6 || (is3d && nz < 6)) return GY_ERR_ARG;  // the periodic fold pairs 3 layers per side
+    if (grid->psep > h) return GY_ERR_UNSUPPORTED;                  // 3-node stencil needs psep/2 <= h/2
+    gy_solver *s = new gy_solver();
+    s->device = device;
+    if (device >= 0) {
+        if (cudaSetDevice(device) != cudaSuccess) {
+            delete s;
+            return GY_ERR_CUDA;
+        }
+    } else {
+        cudaGetDevice(&s->device);
+    }
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete s;
+        return GY_ERR_CUDA;
+    }
+    for (int i = 0; i < 6; i++) cudaEventCreate(&s->ev[i]);
+    for (int a = 0; a < 3; a++) s->L[a] = grid->L[a];
+    s->h = h;
+    s->psep = grid->psep;
+    s->nx = nx; s->ny = ny; s->nz = nz;
+    s->nn = (long long)nx * ny * nz;
+    GridGeom &g = s->g;
+    g.nx = nx; g.ny = ny; g.nz = nz;
+    g.ncx = nx - 1; g.ncy = ny - 1; g.ncz = is3d ? nz - 1 : 1;
+    g.nn = s->nn;
+    g.nc = (long long)g.ncx * g.ncy * g.ncz;
+    g.h = (float)h;
+    g.inv_h = (float)(1.0 / h);
+    g.lp = (float)(0.5 * grid->psep / h);
+    g.is3d = is3d ? 1 : 0;
+    for (int a = 0; a < 3; a++) {
+        const double W = grid->L[a] / h - 2.0;  // the wrap limit L - 2h in cells
+        const double shift = 1.0 - W;           // x > L-2h:  x -> h + (x - (L-2h))
+        g.wrap_hi[a] = (float)W;
+        g.wrap_shift_int[a] = (int)std::floor(shift);
+        g.wrap_shift_frac[a] = (float)(shift - std::floor(shift));
+    }
+    // node cell index as extrapToNodes derives it from the node position (Extrapolation.cpp:43-45)
+    const int dims[3] = {nx, ny, nz};
+    for (int a = 0; a < 3; a++) {
+        s->nidx[a].resize(dims[a]);
+        for (int i = 0; i < dims[a]; i++) {
+            const double p = i * h;
+            s->nidx[a][i] = (int)((p - 0.0) / h);
+        }
+    }
+    s->nbc_type.assign((size_t)s->nn, 0);
+    s->nbc_val.assign((size_t)s->nn * 4, 0.0f);
+    *out = s;
+    return GY_OK;
+}
+
+gy_status gy_destroy(gy_solver *h)
+{
+    if (!h) return GY_ERR_ARG;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    free_device(h);
+    for (int i = 0; i < 6; i++)
+        if (h->ev[i]) cudaEventDestroy(h->ev[i]);
+    for (cudaEvent_t e : h->tev) cudaEventDestroy(e);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return GY_OK;
+}
+
+gy_status gy_grid_dims(const gy_solver *h, int *nxyz, int64_t *num_nodes)
+{
+    if (!h) return GY_ERR_ARG;
+    if (nxyz) { nxyz[0] = h->nx; nxyz[1] = h->ny; nxyz[2] = h->nz; }
+    if (num_nodes) *num_nodes = h->nn;
+    return GY_OK;
+}
+
+gy_status gy_add_particles(gy_solver *h, int64_t n, const double *pos3, const int *mat, const int *obj)
+{
+    if (!h || n < 0 || (n > 0 && !pos3)) return GY_ERR_ARG;
+    if (h->initialized) return fail(h, GY_ERR_STATE, "particles must be added before gy_initialize");
+    if ((int64_t)h->mat.size() + n > (int64_t)0x7fffffff) return fail(h, GY_ERR_ARG, "too many particles");
+    for (int64_t i = 0; i < n; i++) {
+        for (int k = 0; k < 3; k++) {
+            h->pos.push_back(pos3[3 * i + k]);
+            h->vel.push_back(0.0);
+        }
+        for (int k = 0; k < 6; k++) h->stress.push_back(0.0);
+        h->dmg.push_back(0.0);
+        h->mat.push_back(mat ? mat[i] : 0);
+        h->obj.push_back(obj ? obj[i] : 0);
+        h->pbc_type.push_back(0);
+        for (int k = 0; k < 4; k++) h->pbc_val.push_back(0.0);
+        h->hold.push_back(0);
+    }
+    return GY_OK;
+}
+
+#define PRE_INIT(h)                                                                                   \
+    do {                                                                                              \
+        if (!(h)) return GY_ERR_ARG;                                                                  \
+        if ((h)->initialized) return fail(h, GY_ERR_STATE, "particle/node setters must precede gy_initialize"); \
+    } while (0)
+
+gy_status gy_set_particle_vel(gy_solver *h, int64_t count, const int64_t *idx, const double *v)
+{
+    PRE_INIT(h);
+    for (int64_t q = 0; q < count; q++) {
+        if (!valid_index(h, idx[q])) return fail(h, GY_ERR_ARG, "particle index out of range");
+        for (int k = 0; k < 3; k++) h->vel[3 * idx[q] + k] = v[3 * q + k];
+    }
+    return GY_OK;
+}
+
+gy_status gy_set_particle_stress(gy_solver *h, int64_t count, const int64_t *idx, const double *s6)
+{
+    PRE_INIT(h);
+    for (int64_t q = 0; q < count; q++) {
+        if (!valid_index(h, idx[q])) return fail(h, GY_ERR_ARG, "particle index out of range");
+        for (int k = 0; k < 6; k++) h->stress[6 * idx[q] + k] = s6[6 * q + k];
+    }
+    return GY_OK;
+}
+
+gy_status gy_set_particle_damage(gy_solver *h, int64_t count, const int64_t *idx, const double *d)
+{
+    PRE_INIT(h);
+    for (int64_t q = 0; q < count; q++) {
+        if (!valid_index(h, idx[q])) return fail(h, GY_ERR_ARG, "particle index out of range");
+        h->dmg[idx[q]] = d[q];
+    }
+    return GY_OK;
+}
+
+gy_status gy_hold_particles(gy_solver *h, int64_t count, const int64_t *idx)
+{
+    PRE_INIT(h);
+    for (int64_t q = 0; q < count; q++) {
+        if (!valid_index(h, idx[q])) return fail(h, GY_ERR_ARG, "particle index out of range");
+        h->hold[idx[q]] = 1;
+    }
+    return GY_OK;
+}
+
+gy_status gy_set_particle_bc(gy_solver *h, int64_t count, const int64_t *idx, const int *type, const double *val4)
+{
+    PRE_INIT(h);
+    for (int64_t q = 0; q < count; q++) {
+        if (!valid_index(h, idx[q])) return fail(h, GY_ERR_ARG, "particle index out of range");
+        if (type[q] < 0 || type[q] > 255) return fail(h, GY_ERR_ARG, "BC type out of range");
+        h->pbc_type[idx[q]] = type[q];
+        for (int k = 0; k < 4; k++) h->pbc_val[4 * idx[q] + k] = val4[4 * q + k];
+    }
+    return GY_OK;
+}
+
+gy_status gy_set_node_bc(gy_solver *h, int64_t count, const int64_t *nodes, const int *type, const double *val4)
+{
+    PRE_INIT(h);
+    for (int64_t q = 0; q < count; q++) {
+        const int64_t nd = nodes[q];
+        if (nd < 0 || nd >= h->nn) return fail(h, GY_ERR_ARG, "node index out of range");
+        if (type[q] < 0 || type[q] > 255) return fail(h, GY_ERR_ARG, "BC type out of range");
+        h->nbc_type[nd] = (unsigned char)type[q];
+        for (int k = 0; k < 4; k++) h->nbc_val[4 * nd + k] = (float)val4[4 * q + k];
+        if (type[q]) h->any_node_bc = true;
+    }
+    return GY_OK;
+}
+
+static DevMaterial to_dev(const gy_material &m)
+{
+    DevMaterial d{};
+    d.K = (float)m.bulkMod;
+    d.G = (float)m.shearMod;
+    d.rho0 = (float)m.density;
+    d.viscosity = (float)m.viscosity;
+    d.yield = (float)m.yieldStress;
+    d.cohesion = (float)m.cohesion;
+    d.crit_strain = (float)m.criticalStrain;
+    // Drucker-Prager cone (ConstitutiveModels.cpp:247-295, pi as 3.14159)
+    const double phi = m.phi * 3.14159 / 180.0, psi = m.psi * 3.14159 / 180.0;
+    const double eta = 6.0 * std::sin(phi) / (std::sqrt(3.0) * (3.0 - std::sin(phi)));
+    const double xi = 6.0 * std::cos(phi) / (std::sqrt(3.0) * (3.0 - std::sin(phi)));
+    const double etab = (phi == psi) ? eta : 6.0 * std::sin(psi) / (std::sqrt(3.0) * (3.0 - std::sin(psi)));
+    d.eta = (float)eta;
+    d.xi = (float)xi;
+    d.eta_bar = (float)etab;
+    // Grady-Kipp (DamageModels.cpp:96-106): alpha = 8 pi Cg^3 k / ((m+1)(m+2)(m+3)) overflows
+    // FP32, so ((m+3)/3) alpha^(1/3) is formed in FP64 here
+    const double mm = m.damageM;
+    const double alpha = (8.0 * 3.14159 * m.Cg * m.Cg * m.Cg * m.damageK) / ((mm + 1.0) * (mm + 2.0) * (mm + 3.0));
+    d.gk_m = (float)mm;
+    d.gk_rate_coef = (float)(((mm + 3.0) / 3.0) * std::pow(alpha, 1.0 / 3.0));
+    d.gk_logk = (float)std::log(m.damageK > 0 ? m.damageK : 1e-300);
+    d.turb_stress = (float)m.turbStress;
+    d.model = m.model;
+    d.rigid = m.isRigid ? 1 : 0;
+    d.damage = m.isDamage ? 1 : 0;
+    d.damage_model = m.damageModel;
+    return d;
+}
+
+static gy_status alloc_nodes(gy_solver *h)
+{
+    const long long nn = h->nn;
+    // node buffers in one allocation of float4 rows
+    int rows = 4;                    // acc0, acc1, gv, ga
+    if (h->opt.keep_node_fields) rows += 2;
+    if (h->multi) rows += 2 * 5;     // bacc0, bacc1, bnrm, bgv, bga per slot
+    if (h->multi && h->opt.track_normals) rows += 2;
+    size_t bytes = (size_t)rows * nn * sizeof(float4);
+    size_t extra = 0;
+    if (h->multi) extra = (size_t)nn * sizeof(int2) + (size_t)nn + 64;
+    if (h->any_node_bc) extra += (size_t)nn * sizeof(float4) + (size_t)nn + 64;
+    char *mem = nullptr;
+    cudaError_t e = cudaMalloc((void **)&mem, bytes + extra + 4096);
+    if (e != cudaSuccess) return fail(h, GY_ERR_NOMEM, std::string("node buffers: ") + cudaGetErrorString(e));
+    h->node_mem = mem;
+    CK(h, cudaMemsetAsync(mem, 0, bytes + extra + 4096, h->stream));
+    float4 *f4 = (float4 *)mem;
+    NodeBufs &nb = h->nb;
+    nb = NodeBufs{};
+    nb.acc0 = f4; f4 += nn;
+    nb.acc1 = f4; f4 += nn;
+    nb.gv = f4; f4 += nn;
+    nb.ga = f4; f4 += nn;
+    if (h->opt.keep_node_fields) {
+        nb.out_com = f4; f4 += nn;
+        nb.out_force = f4; f4 += nn;
+    }
+    if (h->multi) {
+        for (int b = 0; b < 2; b++) {
+            nb.bacc0[b] = f4; f4 += nn;
+            nb.bacc1[b] = f4; f4 += nn;
+            nb.bnrm[b] = f4; f4 += nn;
+            nb.bgv[b] = f4; f4 += nn;
+            nb.bga[b] = f4; f4 += nn;
+        }
+        if (h->opt.track_normals) {
+            nb.nrm_out[0] = f4; f4 += nn;
+            nb.nrm_out[1] = f4; f4 += nn;
+        }
+    }
+    char *c = (char *)f4;
+    if (h->any_node_bc) {
+        nb.bc_val = (const float4 *)c;
+        CK(h, cudaMemcpyAsync(c, h->nbc_val.data(), (size_t)nn * sizeof(float4), cudaMemcpyHostToDevice, h->stream));
+        c += (size_t)nn * sizeof(float4);
+        nb.bc_type = (const unsigned char *)c;
+        CK(h, cudaMemcpyAsync(c, h->nbc_type.data(), (size_t)nn, cudaMemcpyHostToDevice, h->stream));
+        c += (size_t)nn;
+        c = (char *)(((uintptr_t)c + 15) & ~(uintptr_t)15);
+    }
+    if (h->multi) {
+        nb.body = (int2 *)c;
+        c += (size_t)nn * sizeof(int2);
+        nb.has_rigid = (unsigned char *)c;
+        c += (size_t)nn;
+        // per-(cell, object) smallest particle id + rigid bits
+        gy_status st = dalloc(h, &h->d_cell_min, (size_t)h->g.nc * (h->nbody + 1));
+        if (st) return st;
+        for (int a = 0; a < 3; a++) {
+            st = dalloc(h, &h->d_nidx[a], h->nidx[a].size());
+            if (st) return st;
+            CK(h, cudaMemcpyAsync(h->d_nidx[a], h->nidx[a].data(), h->nidx[a].size() * sizeof(int),
+                                  cudaMemcpyHostToDevice, h->stream));
+        }
+    }
+    return GY_OK;
+}
+
+gy_status gy_initialize(gy_solver *h, const gy_material *mats, int nmat, const gy_params *prm)
+{
+    if (!h || !mats || nmat <= 0 || !prm) return GY_ERR_ARG;
+    if (h->initialized) return fail(h, GY_ERR_STATE, "already initialized");
+    if (nmat > MAX_MATERIALS) return fail(h, GY_ERR_UNSUPPORTED, "more than 32 materials");
+    if ((prm->is3D != 0) != (h->g.is3d != 0))
+        return fail(h, GY_ERR_ARG, "Parameters.is3D does not match the grid (L[2] == 0 means 2D)");
+    cudaSetDevice(h->device);
+    h->mats.assign(mats, mats + nmat);
+    h->prm = *prm;
+    const long long n = (long long)h->mat.size();
+    h->n = n;
+    // Solver::Solver dt (Solver.cpp:15-32): maxK seeded with 1, minRho with 1e15
+    double maxK = 1.0, minrho = 1e15;
+    for (int i = 0; i < nmat; i++) {
+        if (mats[i].bulkMod > maxK) maxK = mats[i].bulkMod;
+        if (mats[i].density < minrho) minrho = mats[i].density;
+    }
+    h->dt = prm->CFL * (h->h / std::sqrt(maxK / minrho));
+    // object slots, model coverage
+    std::map<int, int> slot_of;
+    bool any_rigid = false;
+    for (long long i = 0; i < n; i++) {
+        const int m = h->mat[i];
+        if (m < 0 || m >= nmat) return fail(h, GY_ERR_ARG, "particle material id out of range");
+        if (slot_of.find(h->obj[i]) == slot_of.end()) {
+            const int s = (int)slot_of.size();
+            slot_of[h->obj[i]] = s;
+        }
+        if (mats[m].isRigid) any_rigid = true;
+        if (mats[m].model == 3 || mats[m].model == 4 || mats[m].model == 5 || mats[m].isDamage) h->has_dp = true;
+    }
+    for (long long i = 0; i < n; i++)
+        if (h->dmg[i] != 0.0) h->has_dp = true;
+    if ((int)slot_of.size() > MAX_BODIES) return fail(h, GY_ERR_UNSUPPORTED, "more than 16 objects");
+    h->nbody = std::max(1, (int)slot_of.size());
+    h->slot_obj.assign(h->nbody, 0);
+    for (auto &kv : slot_of) h->slot_obj[kv.second] = kv.first;
+    h->multi = (h->nbody > 1) || any_rigid || h->opt.track_normals;
+    for (long long i = 0; i < n; i++)
+        if (h->pbc_type[i] >= 33 && h->pbc_type[i] != BC_MP_VX && h->pbc_type[i] != BC_MP_VY &&
+            h->pbc_type[i] != BC_MP_VZ && h->pbc_type[i] != BC_MP_VX_VY && h->pbc_type[i] != BC_MP_VXSIN &&
+            h->pbc_type[i] != BC_MP_VYSIN && h->pbc_type[i] != BC_MP_SYYSIN && h->pbc_type[i] != BC_MP_FX &&
+            h->pbc_type[i] != BC_MP_FY && h->pbc_type[i] != BC_MP_FZ && h->pbc_type[i] != BC_MP_FX_FY &&
+            h->pbc_type[i] != BC_MP_STRESS_XX_YY)
+            h->pbc_type[i] = 0;  // every other particle BC has no body in the reference
+
+    // ---- particle slab ----
+    h->cap = std::max<long long>(n, 1);
+    const size_t slab_floats = (size_t)PF_COUNT * h->cap;
+    for (int s = 0; s < 2; s++) {
+        gy_status st = dalloc(h, &h->slab[s], slab_floats);
+        if (st) return st;
+    }
+    std::vector<float> hs(slab_floats, 0.0f);
+    std::vector<int> refkey0(h->cap, 0);
+    std::vector<float4> pbcv(h->cap, make_float4(0.f, 0.f, 0.f, 0.f));
+    auto F = [&](int f, long long i) -> float & { return hs[(size_t)f * h->cap + i]; };
+    auto I = [&](int f, long long i) -> int & { return reinterpret_cast<int *>(hs.data())[(size_t)f * h->cap + i]; };
+    const double hh = h->h, ps2 = h->psep / 2;
+    const double init_vol = h->g.is3d ? h->psep * h->psep * h->psep : h->psep * h->psep;
+    const int dims_c[3] = {h->g.ncx, h->g.ncy, h->g.ncz};
+    for (long long i = 0; i < n; i++) {
+        int c[3] = {0, 0, 0};
+        for (int a = 0; a < 3; a++) {
+            const double x = h->pos[3 * i + a];
+            if (a == 2 && !h->g.is3d) {
+                F(PF_OZ, i) = 0.0f;
+                continue;
+            }
+            // stencil base as getGIMPNodes computes it (Extrapolation.cpp:658-660)
+            int ci = (int)((x - ps2 - 0.0) / hh);
+            double off = x / hh - ci;
+            // keep the offset in [lp, 1+lp) after rounding
+            const double lp = ps2 / hh;
+            if (off < lp) { ci -= 1; off += 1.0; }
+            if (off >= 1.0 + lp) { ci += 1; off -= 1.0; }
+            if (ci < 0 || ci > dims_c[a] - 2)
+                return fail(h, GY_ERR_RANGE, "particle " + std::to_string(i) + " lies outside the grid's stencil range");
+            c[a] = ci;
+            F(PF_OX + a, i) = (float)off;
+        }
+        I(PF_KEY, i) = c[0] + c[1] * h->g.ncx + (h->g.is3d ? c[2] * h->g.ncx * h->g.ncy : 0);
+        for (int k = 0; k < 3; k++) F(PF_VX + k, i) = (float)h->vel[3 * i + k];
+        for (int k = 0; k < 6; k++) F(PF_S0 + k, i) = (float)h->stress[6 * i + k];
+        const gy_material &M = mats[h->mat[i]];
+        // Solver::initialize (Solver.cpp:40-69)
+        const double rho = M.density;
+        double mass = rho * init_vol;
+        if (h->g.is3d && M.isRigid) mass = 1.0;
+        F(PF_RHO, i) = (float)rho;
+        F(PF_MASS, i) = (float)mass;
+        uint32_t info = (uint32_t)h->mat[i] | ((uint32_t)slot_of[h->obj[i]] << INFO_OBJ_SHIFT) |
+                        ((uint32_t)h->pbc_type[i] << INFO_BC_SHIFT) | INFO_INIT_VOL;
+        if (h->hold[i]) info |= INFO_HOLD;
+        if (M.isRigid) info |= INFO_RIGID;
+        I(PF_INFO, i) = (int)info;
+        I(PF_PID, i) = (int)i;
+        F(PF_DMG, i) = (float)h->dmg[i];
+        for (int k = 0; k < 4; k++) (&pbcv[i].x)[k] = (float)h->pbc_val[4 * i + k];
+        // the initial binning key has no quarter-cell shift (MaterialPoints.cpp:228-231)
+        const int ix = (int)((h->pos[3 * i + 0] - 0.0) / hh), iy = (int)((h->pos[3 * i + 1] - 0.0) / hh),
+                  iz = (int)((h->pos[3 * i + 2] - 0.0) / hh);
+        refkey0[i] = ix + iy * (h->nx - 1) + iz * (h->nx - 1) * (h->ny - 1);
+    }
+    CK(h, cudaMemcpyAsync(h->slab[0], hs.data(), slab_floats * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    h->cur = 0;
+    gy_status st;
+    if ((st = dalloc(h, &h->d_pbc_val, h->cap))) return st;
+    CK(h, cudaMemcpyAsync(h->d_pbc_val, pbcv.data(), h->cap * sizeof(float4), cudaMemcpyHostToDevice, h->stream));
+    if (h->multi) {
+        if ((st = dalloc(h, &h->d_refkey0, h->cap))) return st;
+        CK(h, cudaMemcpyAsync(h->d_refkey0, refkey0.data(), h->cap * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    }
+    std::vector<DevMaterial> dm(nmat);
+    for (int i = 0; i < nmat; i++) dm[i] = to_dev(mats[i]);
+    if ((st = dalloc(h, &h->d_mats, nmat))) return st;
+    CK(h, cudaMemcpyAsync(h->d_mats, dm.data(), nmat * sizeof(DevMaterial), cudaMemcpyHostToDevice, h->stream));
+    if ((st = dalloc(h, &h->d_status, 4))) return st;
+    CK(h, cudaMemsetAsync(h->d_status, 0, 4 * sizeof(int), h->stream));
+    if ((st = dalloc(h, &h->d_stats, 8))) return st;
+    // sort scratch
+    h->sort_mem = nullptr;
+    const size_t sbytes = sort_scratch_bytes(h->cap);
+    CK(h, cudaMalloc(&h->sort_mem, sbytes + 4096));
+    {
+        int *p = (int *)h->sort_mem;
+        const long long nbk = (h->cap + 2047) / 2048;
+        h->ws.keys[0] = p; p += h->cap;
+        h->ws.keys[1] = p; p += h->cap;
+        h->ws.vals[0] = p; p += h->cap;
+        h->ws.vals[1] = p; p += h->cap;
+        h->ws.hist = p; p += 2 * 256 * nbk;
+        h->ws.scan_tmp = p;
+        h->ws.cap = h->cap;
+        h->ws.nblocks_cap = (int)nbk;
+    }
+    if ((st = dalloc(h, &h->d_keys, h->cap))) return st;
+    if ((st = dalloc(h, &h->d_perm, h->cap))) return st;
+    // fields carried by the permutation
+    std::vector<int> fields;
+    for (int f = PF_OX; f <= PF_PID; f++) fields.push_back(f);
+    if (h->has_dp)
+        for (int f = PF_EQPS; f <= PF_SMAX; f++) fields.push_back(f);
+    if (h->opt.track_normals)
+        for (int f = PF_NX; f <= PF_NZ; f++) fields.push_back(f);
+    h->nfields = (int)fields.size();
+    if ((st = dalloc(h, &h->d_fields, fields.size()))) return st;
+    CK(h, cudaMemcpyAsync(h->d_fields, fields.data(), fields.size() * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    if ((st = alloc_nodes(h))) return st;
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->initialized = true;
+    h->steps = 0;
+    h->t_prev = 0.0;
+    h->since_sort = 1 << 30;
+    h->tables_valid = false;
+    return GY_OK;
+}
+
+gy_status gy_set_dt(gy_solver *h, double dt)
+{
+    if (!h || !(dt > 0)) return GY_ERR_ARG;
+    h->dt = dt;
+    return GY_OK;
+}
+
+gy_status gy_get_dt(const gy_solver *h, double *dt)
+{
+    if (!h || !dt) return GY_ERR_ARG;
+    *dt = h->dt;
+    return GY_OK;
+}
+
+gy_status gy_set_params(gy_solver *h, const gy_params *prm)
+{
+    if (!h || !prm) return GY_ERR_ARG;
+    if ((prm->is3D != 0) != (h->g.is3d != 0)) return fail(h, GY_ERR_ARG, "is3D does not match the grid");
+    h->prm = *prm;
+    return GY_OK;
+}
+
+gy_status gy_set_options(gy_solver *h, const gy_options *opt)
+{
+    if (!h || !opt) return GY_ERR_ARG;
+    if (opt->sort_every < 1) return fail(h, GY_ERR_ARG, "sort_every must be >= 1");
+    if (h->initialized && (opt->track_normals != h->opt.track_normals || opt->keep_node_fields != h->opt.keep_node_fields))
+        return fail(h, GY_ERR_STATE, "track_normals / keep_node_fields must be set before gy_initialize");
+    h->opt = *opt;
+    return GY_OK;
+}
+
+gy_status gy_get_options(const gy_solver *h, gy_options *opt)
+{
+    if (!h || !opt) return GY_ERR_ARG;
+    *opt = h->opt;
+    return GY_OK;
+}
+
+void *gy_stream(gy_solver *h) { return h ? (void *)h->stream : nullptr; }
+
+static StepArgs make_args(gy_solver *h, double t, int step)
+{
+    (void)t;
+    StepArgs a{};
+    a.g = h->g;
+    StepScalars &sc = a.sc;
+    sc.dt = (float)h->dt;
+    sc.dt_node = (float)(step == 1 ? 0.5 * h->dt : h->dt);
+    for (int k = 0; k < 3; k++) sc.gravity[k] = (float)h->prm.gravity[k];
+    sc.damping = (float)h->prm.damping;
+    sc.mu = (float)h->prm.mu;
+    sc.t_bc = (float)h->t_prev;
+    sc.fixed_grid_bcs = h->prm.fixed_grid_bcs;
+    sc.multi_body = h->multi ? 1 : 0;
+    sc.init_volume = (float)(h->g.is3d ? h->psep * h->psep * h->psep : h->psep * h->psep);
+    a.mats = h->d_mats;
+    a.pbc_val = h->d_pbc_val;
+    a.status = h->d_status;
+    return a;
+}
+
+static gy_status enqueue_step(gy_solver *h, double t, int step)
+{
+    StepArgs a = make_args(h, t, step);
+    cudaStream_t s = h->stream;
+    const bool timing = h->phase_timing && h->tev_used < kMaxTimedSteps;
+    cudaEvent_t *tev = nullptr;
+    if (timing) {
+        const size_t need = (size_t)(h->tev_used + 1) * 5;
+        while (h->tev.size() < need) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            h->tev.push_back(e);
+        }
+        tev = &h->tev[(size_t)h->tev_used * 5];
+        h->tev_used++;
+        cudaEventRecord(tev[0], s);
+    }
+    // (a) counting sort by cell + permutation of the particle state
+    if (h->since_sort >= h->opt.sort_every) {
+        int key_bits = 1;
+        while ((1LL << key_bits) < h->g.nc) key_bits++;
+        launch_extract_keys(pview(h, h->cur), h->n, h->d_keys, s);
+        sort_pairs(h->d_keys, h->d_perm, h->n, key_bits, h->ws, s);
+        launch_permute(h->slab[h->cur], h->slab[h->cur ^ 1], h->cap, h->n, h->d_perm, h->d_fields, h->nfields, s);
+        h->cur ^= 1;
+        h->since_sort = 0;
+    }
+    h->since_sort++;
+    PView P = pview(h, h->cur);
+    // body slots from the sort table of the reference's cadence (Solver.cpp:91)
+    if (h->multi && ((step % 10 == 0) || step == 1 || !h->tables_valid)) {
+        launch_body_tables(P, h->n, a, h->d_cell_min, h->nbody, h->steps == 0 ? h->d_refkey0 : nullptr, s);
+        launch_body_assign(h->nb, a, h->d_cell_min, h->nbody, h->d_nidx[0], h->d_nidx[1], h->d_nidx[2], s);
+        h->tables_valid = true;
+    }
+    if (timing) cudaEventRecord(tev[1], s);
+    // (b) P2G
+    launch_p2g(P, h->n, h->nb, a, h->opt.p2g_tile, h->opt.block_particles, s);
+    if (timing) cudaEventRecord(tev[2], s);
+    // (c) periodic fold, nodal solve, grid BCs
+    launch_fold(h->nb, a, s);
+    launch_solve(h->nb, a, h->opt.keep_node_fields != 0, s);
+    if (timing) cudaEventRecord(tev[3], s);
+    // (d) G2P + particle BCs + update + constitutive + damage
+    launch_g2p_update(P, h->n, h->nb, a, h->opt.track_normals != 0, h->opt.check_finite != 0, h->has_dp,
+                      h->opt.block_particles, s);
+    if (timing) cudaEventRecord(tev[4], s);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(h, GY_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+    h->t_prev = t;
+    h->steps++;
+    return GY_OK;
+}
+
+gy_status gy_step(gy_solver *h, double t, int step)
+{
+    if (!h) return GY_ERR_ARG;
+    if (!h->initialized) return fail(h, GY_ERR_STATE, "gy_step before gy_initialize");
+    cudaSetDevice(h->device);
+    if (h->nb.active_count == nullptr) h->nb.active_count = h->d_status + 2;
+    cudaMemsetAsync(h->nb.active_count, 0, sizeof(int), h->stream);
+    return enqueue_step(h, t, step);
+}
+
+gy_status gy_steps(gy_solver *h, double t0, int step0, int nsteps, int use_graph)
+{
+    (void)use_graph;
+    if (!h || nsteps < 0) return GY_ERR_ARG;
+    for (int k = 0; k < nsteps; k++) {
+        gy_status st = gy_step(h, t0 + k * h->dt, step0 + k);
+        if (st) return st;
+    }
+    return GY_OK;
+}
+
+gy_status gy_sync(gy_solver *h)
+{
+    if (!h) return GY_ERR_ARG;
+    cudaSetDevice(h->device);
+    CK(h, cudaStreamSynchronize(h->stream));
+    if (!h->initialized) return GY_OK;
+    int flags[4] = {0, 0, 0, 0};
+    CK(h, cudaMemcpy(flags, h->d_status, sizeof(flags), cudaMemcpyDeviceToHost));
+    if (flags[0]) {
+        CK(h, cudaMemsetAsync(h->d_status, 0, sizeof(int), h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
+        if (flags[0] & ERR_NONFINITE) return fail(h, GY_ERR_NONFINITE, "NaN or Inf in particle state");
+        return fail(h, GY_ERR_RANGE, "a particle left the grid's stencil range (clamped)");
+    }
+    return GY_OK;
+}
+
+gy_status gy_num_particles(const gy_solver *h, int64_t *n)
+{
+    if (!h || !n) return GY_ERR_ARG;
+    *n = (int64_t)h->mat.size();
+    return GY_OK;
+}
+
+static gy_status fetch_slab(gy_solver *h, std::vector<float> &hs)
+{
+    cudaSetDevice(h->device);
+    hs.resize((size_t)PF_COUNT * h->cap);
+    CK(h, cudaStreamSynchronize(h->stream));
+    CK(h, cudaMemcpy(hs.data(), h->slab[h->cur], hs.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    return GY_OK;
+}
+
+static const int kPWidth[GY_P_NFIELDS] = {3, 3, 3, 3, 6, 6, 6, 1, 1, 1, 1, 1, 1, 3};
+
+gy_status gy_get_particles(gy_solver *h, int field, double *out, int64_t count)
+{
+    if (!h || !out || field < 0 || field >= GY_P_NFIELDS) return GY_ERR_ARG;
+    const int w = kPWidth[field];
+    const long long n = (long long)h->mat.size();
+    if (count != (int64_t)n * w) return fail(h, GY_ERR_ARG, "count must be n * width");
+    if (!h->initialized) {
+        // before the solver exists the host staging is authoritative
+        for (long long i = 0; i < n; i++) {
+            for (int k = 0; k < w; k++) {
+                double v = 0.0;
+                switch (field) {
+                case GY_P_POS: case GY_P_POS0: v = h->pos[3 * i + k]; break;
+                case GY_P_VEL: v = h->vel[3 * i + k]; break;
+                case GY_P_STRESS: v = h->stress[6 * i + k]; break;
+                case GY_P_DAMAGE: v = h->dmg[i]; break;
+                default: v = 0.0;
+                }
+                out[(size_t)i * w + k] = v;
+            }
+        }
+        return GY_OK;
+    }
+    std::vector<float> hs;
+    gy_status st = fetch_slab(h, hs);
+    if (st) return st;
+    auto F = [&](int f, long long i) { return hs[(size_t)f * h->cap + i]; };
+    auto I = [&](int f, long long i) { return reinterpret_cast<const int *>(hs.data())[(size_t)f * h->cap + i]; };
+    const double hh = h->h;
+    for (long long i = 0; i < n; i++) {
+        const long long pid = I(PF_PID, i);
+        double *o = out + (size_t)pid * w;
+        const uint32_t info = (uint32_t)I(PF_INFO, i);
+        switch (field) {
+        case GY_P_POS:
+        case GY_P_DISP: {
+            int c[3];
+            const int key = I(PF_KEY, i);
+            c[2] = h->g.is3d ? key / (h->g.ncx * h->g.ncy) : 0;
+            const int r = key - c[2] * h->g.ncx * h->g.ncy;
+            c[1] = r / h->g.ncx;
+            c[0] = r - c[1] * h->g.ncx;
+            for (int k = 0; k < 3; k++) {
+                double x = (c[k] + (double)F(PF_OX + k, i)) * hh;
+                if (k == 2 && !h->g.is3d) x = h->pos[3 * pid + 2];
+                o[k] = field == GY_P_POS ? x : x - h->pos[3 * pid + k];
+            }
+            break;
+        }
+        case GY_P_POS0: for (int k = 0; k < 3; k++) o[k] = h->pos[3 * pid + k]; break;
+        case GY_P_VEL: for (int k = 0; k < 3; k++) o[k] = F(PF_VX + k, i); break;
+        case GY_P_STRESS: for (int k = 0; k < 6; k++) o[k] = F(PF_S0 + k, i); break;
+        case GY_P_STRAIN: for (int k = 0; k < 6; k++) o[k] = F(PF_E0 + k, i); break;
+        case GY_P_PSTRAIN: for (int k = 0; k < 6; k++) o[k] = h->has_dp ? F(PF_EP0 + k, i) : 0.0; break;
+        case GY_P_EQPS: o[0] = h->has_dp ? F(PF_EQPS, i) : 0.0; break;
+        case GY_P_DAMAGE: o[0] = h->has_dp ? F(PF_DMG, i) : 0.0; break;
+        case GY_P_SMAX: o[0] = h->has_dp ? F(PF_SMAX, i) : 0.0; break;
+        case GY_P_MASS: o[0] = F(PF_MASS, i); break;
+        case GY_P_DENSITY: o[0] = F(PF_RHO, i); break;
+        case GY_P_VOLUME:
+            o[0] = (info & INFO_INIT_VOL) ? (h->g.is3d ? h->psep * h->psep * h->psep : h->psep * h->psep)
+                                          : (double)F(PF_MASS, i) / (double)F(PF_RHO, i);
+            break;
+        case GY_P_NORMALS: for (int k = 0; k < 3; k++) o[k] = h->opt.track_normals ? F(PF_NX + k, i) : 0.0; break;
+        default: break;
+        }
+    }
+    return GY_OK;
+}
+
+gy_status gy_get_particles_int(gy_solver *h, int field, int *out, int64_t count)
+{
+    if (!h || !out) return GY_ERR_ARG;
+    const long long n = (long long)h->mat.size();
+    if (count != (int64_t)n) return fail(h, GY_ERR_ARG, "count must be n");
+    if (!h->initialized) {
+        for (long long i = 0; i < n; i++) {
+            if (field == GY_PI_MATERIAL) out[i] = h->mat[i];
+            else if (field == GY_PI_OBJECT) out[i] = h->obj[i];
+            else if (field == GY_PI_DEVICE_SLOT) out[i] = (int)i;
+            else if (field == GY_PI_CELLID) {
+                const int ix = (int)(h->pos[3 * i] / h->h), iy = (int)(h->pos[3 * i + 1] / h->h),
+                          iz = (int)(h->pos[3 * i + 2] / h->h);
+                out[i] = ix + iy * (h->nx - 1) + iz * (h->nx - 1) * (h->ny - 1);
+            } else return GY_ERR_ARG;
+        }
+        return GY_OK;
+    }
+    std::vector<float> hs;
+    gy_status st = fetch_slab(h, hs);
+    if (st) return st;
+    auto F = [&](int f, long long i) { return hs[(size_t)f * h->cap + i]; };
+    auto I = [&](int f, long long i) { return reinterpret_cast<const int *>(hs.data())[(size_t)f * h->cap + i]; };
+    for (long long i = 0; i < n; i++) {
+        const long long pid = I(PF_PID, i);
+        const uint32_t info = (uint32_t)I(PF_INFO, i);
+        switch (field) {
+        case GY_PI_MATERIAL: out[pid] = info_mat(info); break;
+        case GY_PI_OBJECT: out[pid] = h->slot_obj[info_obj(info)]; break;
+        case GY_PI_DEVICE_SLOT: out[pid] = (int)i; break;
+        case GY_PI_CELLID: {
+            if (info & INFO_INIT_VOL) {
+                // no update yet: the initial unshifted key (MaterialPoints.cpp:228-231)
+                const int ix = (int)(h->pos[3 * pid] / h->h), iy = (int)(h->pos[3 * pid + 1] / h->h),
+                          iz = (int)(h->pos[3 * pid + 2] / h->h);
+                out[pid] = ix + iy * (h->nx - 1) + iz * (h->nx - 1) * (h->ny - 1);
+                break;
+            }
+            const int key = I(PF_KEY, i);
+            int c[3];
+            c[2] = h->g.is3d ? key / (h->g.ncx * h->g.ncy) : 0;
+            const int r = key - c[2] * h->g.ncx * h->g.ncy;
+            c[1] = r / h->g.ncx;
+            c[0] = r - c[1] * h->g.ncx;
+            int id[3] = {0, 0, 0};
+            for (int k = 0; k < (h->g.is3d ? 3 : 2); k++) id[k] = (int)((c[k] + (double)F(PF_OX + k, i)) - 0.25);
+            out[pid] = id[0] + id[1] * (h->nx - 1) + id[2] * (h->nx - 1) * (h->ny - 1);
+            break;
+        }
+        default: return GY_ERR_ARG;
+        }
+    }
+    return GY_OK;
+}
+
+gy_status gy_get_nodes(gy_solver *h, int field, double *out, int64_t count)
+{
+    if (!h || !out || field < 0 || field >= GY_N_NFIELDS) return GY_ERR_ARG;
+    const int w = field == GY_N_MASS ? 1 : 3;
+    if (count != (int64_t)h->nn * w) return fail(h, GY_ERR_ARG, "count must be numNodes * width");
+    if (!h->initialized) {
+        std::fill(out, out + count, 0.0);
+        return GY_OK;
+    }
+    if ((field == GY_N_VEL || field == GY_N_FORCE) && !h->opt.keep_node_fields)
+        return fail(h, GY_ERR_STATE, "node velocity/force need gy_options.keep_node_fields = 1");
+    cudaSetDevice(h->device);
+    CK(h, cudaStreamSynchronize(h->stream));
+    std::vector<float4> buf((size_t)h->nn);
+    const float4 *src = field == GY_N_MASS || field == GY_N_VEL1 ? h->nb.gv
+                        : field == GY_N_ACC1                     ? h->nb.ga
+                        : field == GY_N_VEL                      ? h->nb.out_com
+                                                                 : h->nb.out_force;
+    CK(h, cudaMemcpy(buf.data(), src, (size_t)h->nn * sizeof(float4), cudaMemcpyDeviceToHost));
+    for (long long i = 0; i < h->nn; i++) {
+        const float4 v = buf[i];
+        if (field == GY_N_MASS) out[i] = v.x;
+        else if (field == GY_N_VEL1) { out[3 * i] = v.y; out[3 * i + 1] = v.z; out[3 * i + 2] = v.w; }
+        else { out[3 * i] = v.x; out[3 * i + 1] = v.y; out[3 * i + 2] = v.z; }
+    }
+    return GY_OK;
+}
+
+gy_status gy_get_stats(gy_solver *h, gy_stats *out)
+{
+    if (!h || !out) return GY_ERR_ARG;
+    std::memset(out, 0, sizeof(*out));
+    if (!h->initialized) return GY_OK;
+    cudaSetDevice(h->device);
+    StepArgs a = make_args(h, 0.0, 0);
+    launch_stats(pview(h, h->cur), h->n, a, h->d_stats, h->stream);
+    double v[8];
+    int flags[4];
+    CK(h, cudaMemcpyAsync(v, h->d_stats, sizeof(v), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaMemcpyAsync(flags, h->d_status, sizeof(flags), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    out->mass = v[0];
+    out->momentum[0] = v[1];
+    out->momentum[1] = v[2];
+    out->momentum[2] = v[3];
+    out->kinetic = v[4];
+    out->strain_energy = v[5];
+    out->active_nodes = flags[2];
+    out->steps = h->steps;
+    out->status_flags = flags[0];
+    return GY_OK;
+}
+
+gy_status gy_set_phase_timing(gy_solver *h, int on)
+{
+    if (!h) return GY_ERR_ARG;
+    h->phase_timing = on != 0;
+    h->tev_used = 0;
+    return GY_OK;
+}
+
+gy_status gy_get_phase_times(gy_solver *h, float *ms5, int64_t *steps)
+{
+    if (!h || !ms5) return GY_ERR_ARG;
+    cudaSetDevice(h->device);
+    CK(h, cudaStreamSynchronize(h->stream));
+    for (int k = 0; k < 5; k++) ms5[k] = 0.f;
+    for (long long q = 0; q < h->tev_used; q++) {
+        cudaEvent_t *e = &h->tev[(size_t)q * 5];
+        for (int k = 0; k < 4; k++) {
+            float ms = 0.f;
+            CK(h, cudaEventElapsedTime(&ms, e[k], e[k + 1]));
+            ms5[k] += ms;
+        }
+        float tot = 0.f;
+        CK(h, cudaEventElapsedTime(&tot, e[0], e[4]));
+        ms5[4] += tot;
+    }
+    if (steps) *steps = h->tev_used;
+    h->tev_used = 0;
+    return GY_OK;
+}
+
+gy_status gy_time_steps(gy_solver *h, double t0, int step0, int nsteps, float *ms)
+{
+    if (!h || !ms || nsteps < 0) return GY_ERR_ARG;
+    if (!h->initialized) return fail(h, GY_ERR_STATE, "gy_time_steps before gy_initialize");
+    cudaSetDevice(h->device);
+    CK(h, cudaEventRecord(h->ev[0], h->stream));
+    gy_status st = gy_steps(h, t0, step0, nsteps, 0);
+    if (st) return st;
+    CK(h, cudaEventRecord(h->ev[5], h->stream));
+    CK(h, cudaEventSynchronize(h->ev[5]));
+    CK(h, cudaEventElapsedTime(ms, h->ev[0], h->ev[5]));
+    return GY_OK;
+}
+
+int64_t gy_kernel_launches(void) { return (int64_t)launch_count(); }
+
+gy_status gy_sort_keys(const int *keys, int64_t n, int *perm_out, int device)
+{
+    if (n < 0 || (n > 0 && (!keys || !perm_out))) return GY_ERR_ARG;
+    if (n == 0) return GY_OK;
+    if (device >= 0 && cudaSetDevice(device) != cudaSuccess) return GY_ERR_CUDA;
+    int maxk = 0;
+    for (int64_t i = 0; i < n; i++) {
+        if (keys[i] < 0) return GY_ERR_ARG;
+        maxk = std::max(maxk, keys[i]);
+    }
+    int bits = 1;
+    while ((1LL << bits) <= maxk) bits++;
+    cudaStream_t s;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return GY_ERR_CUDA;
+    int *d_in = nullptr, *d_perm = nullptr, *mem = nullptr;
+    gy_status st = GY_OK;
+    const long long nbk = (n + 2047) / 2048;
+    if (cudaMalloc(&d_in, n * sizeof(int)) != cudaSuccess || cudaMalloc(&d_perm, n * sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&mem, sort_scratch_bytes(n) + 4096) != cudaSuccess) {
+        st = GY_ERR_NOMEM;
+    } else {
+        SortScratch ws{};
+        int *p = mem;
+        ws.keys[0] = p; p += n;
+        ws.keys[1] = p; p += n;
+        ws.vals[0] = p; p += n;
+        ws.vals[1] = p; p += n;
+        ws.hist = p; p += 2 * 256 * nbk;
+        ws.scan_tmp = p;
+        ws.cap = n;
+        ws.nblocks_cap = (int)nbk;
+        cudaMemcpyAsync(d_in, keys, n * sizeof(int), cudaMemcpyHostToDevice, s);
+        sort_pairs(d_in, d_perm, n, bits, ws, s);
+        cudaMemcpyAsync(perm_out, d_perm, n * sizeof(int), cudaMemcpyDeviceToHost, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) st = GY_ERR_CUDA;
+    }
+    if (d_in) cudaFree(d_in);
+    if (d_perm) cudaFree(d_perm);
+    if (mem) cudaFree(mem);
+    cudaStreamDestroy(s);
+    return st;
+}
+
+}  // extern "C"

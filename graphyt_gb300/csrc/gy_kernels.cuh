@@ -1,0 +1,81 @@
+// gy_kernels.cuh -- launch interface between the host runtime (gy_api.cu) and the kernels.
+#pragma once
+
+#include "gy_common.cuh"
+
+namespace gy {
+
+// Device view of one particle slab.
+struct PView {
+    float *base;
+    long long cap;
+    __device__ __forceinline__ float &f(int field, long long i) const { return base[(long long)field * cap + i]; }
+    __device__ __forceinline__ int &ii(int field, long long i) const
+    {
+        return reinterpret_cast<int *>(base)[(long long)field * cap + i];
+    }
+};
+
+// Single-body node buffers.  Accumulators (P2G target, zeroed by the solve):
+//   acc0 = (m, px, py, pz), acc1 = (fx, fy, fz, -).
+// Solved fields (read by G2P): gv = (m, v1x, v1y, v1z), ga = (a1x, a1y, a1z, -).
+// Multi-body adds per-slot accumulators and solved fields.
+struct NodeBufs {
+    float4 *acc0, *acc1;
+    float4 *gv, *ga;
+    float4 *out_com;        // optional (vcom, -) for node getters
+    float4 *out_force;      // optional COM force for node getters
+    const unsigned char *bc_type;
+    const float4 *bc_val;
+    // multi-body
+    float4 *bacc0[2], *bacc1[2];  // per body slot: (m, p), (f, -)
+    float4 *bnrm[2];              // per body slot: (n, -)
+    float4 *bgv[2], *bga[2];      // solved per slot: (m, v), (a, -)
+    float4 *nrm_out[2];           // normalised slot normals (only when normals are tracked)
+    int2 *body;                   // body slot objects (dense ids) or -1
+    unsigned char *has_rigid;     // bit0: slot 0 rigid, bit1: slot 1 rigid
+    int *active_count;            // nodes with mass (stats)
+};
+
+struct StepArgs {
+    GridGeom g;
+    StepScalars sc;
+    const DevMaterial *mats;
+    const float4 *pbc_val;   // particle BC values by pid
+    int *status;
+};
+
+// process-wide count of kernel launches (for the benchmark's launch accounting)
+void note_launch(int k);
+long long launch_count();
+
+// launchers (gy_kernels.cu)
+void launch_p2g(const PView &p, long long n, const NodeBufs &nb, const StepArgs &a, int tile, int block, cudaStream_t s);
+void launch_fold(const NodeBufs &nb, const StepArgs &a, cudaStream_t s);
+void launch_solve(const NodeBufs &nb, const StepArgs &a, bool keep_node_fields, cudaStream_t s);
+void launch_g2p_update(const PView &p, long long n, const NodeBufs &nb, const StepArgs &a, bool track_normals,
+                       bool check_finite, bool has_dp, int block, cudaStream_t s);
+void launch_body_tables(const PView &p, long long n, const StepArgs &a, int *cell_min, int nbody,
+                        const int *refkey_src_unused, cudaStream_t s);
+void launch_body_assign(const NodeBufs &nb, const StepArgs &a, const int *cell_min, int nbody,
+                        const int *nidx_x, const int *nidx_y, const int *nidx_z, cudaStream_t s);
+void launch_stats(const PView &p, long long n, const StepArgs &a, double *out8, cudaStream_t s);
+
+// sort (gy_sort.cu): stable LSD radix sort of (key, value) pairs
+struct SortScratch {
+    int *keys[2], *vals[2];
+    int *hist;          // 256 * nblocks
+    int *scan_tmp;      // scan workspace
+    long long cap;
+    int nblocks_cap;
+};
+size_t sort_scratch_bytes(long long n);
+void sort_pairs(const int *keys_in, int *perm_out, long long n, int key_bits, SortScratch &ws, cudaStream_t s);
+void launch_permute(const float *in, float *out, long long cap, long long n, const int *perm, const int *fields,
+                    int nfields, cudaStream_t s);
+void launch_iota(int *out, long long n, cudaStream_t s);
+void launch_extract_keys(const PView &p, long long n, int *keys, cudaStream_t s);
+void exclusive_scan_int(const int *in, int *out, long long n, int *tmp, cudaStream_t s);
+size_t scan_tmp_ints(long long n);
+
+}  // namespace gy

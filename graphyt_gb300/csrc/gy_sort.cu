@@ -1,0 +1,245 @@
+// gy_sort.cu -- stable counting sort of particles by cell, and the state permutation.
+//
+// The reference sorts particle indices by cellID with std::sort and permutes ~40 arrays
+// (Extrapolation.cpp:370-503).  Here the sort is a stable least-significant-digit radix
+// sort over 8-bit digits of the cell key: per pass one histogram kernel, one exclusive scan
+// over the (digit, block) counts and one stable scatter.  Stability within a pass comes
+// from a block-local rank: warps walk their elements in order, peers with the same digit
+// are found with __match_any_sync, and per-warp digit counters are prefix-summed across
+// warps.  The result is bit-identical to a CPU stable sort of the same keys.
+#include "gy_kernels.cuh"
+
+namespace gy {
+
+constexpr int SORT_THREADS = 256;
+constexpr int SORT_ITEMS = 8;                       // per thread
+constexpr int SORT_TILE = SORT_THREADS * SORT_ITEMS; // 2048 elements per block
+constexpr int SORT_WARPS = SORT_THREADS / 32;
+constexpr int RADIX = 256;
+
+__global__ void __launch_bounds__(SORT_THREADS) k_radix_hist(const int *keys, long long n, int shift, int *hist, int nblocks)
+{
+    __shared__ int cnt[RADIX];
+    for (int d = threadIdx.x; d < RADIX; d += SORT_THREADS) cnt[d] = 0;
+    __syncthreads();
+    const long long base = (long long)blockIdx.x * SORT_TILE;
+    for (int it = 0; it < SORT_ITEMS; it++) {
+        const long long e = base + (long long)it * SORT_THREADS + threadIdx.x;
+        if (e < n) atomicAdd(&cnt[(keys[e] >> shift) & 0xFF], 1);
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < RADIX; d += SORT_THREADS) hist[(long long)d * nblocks + blockIdx.x] = cnt[d];
+}
+
+__global__ void __launch_bounds__(SORT_THREADS) k_radix_scatter(const int *keys_in, const int *vals_in, int *keys_out,
+                                                                 int *vals_out, long long n, int shift,
+                                                                 const int *offsets, int nblocks)
+{
+    __shared__ int wcnt[SORT_WARPS][RADIX];   // per-warp digit counts, then per-warp bases
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int d = lane; d < RADIX; d += 32) wcnt[warp][d] = 0;
+    __syncwarp();
+    // warp w owns elements [base + w*256, base + (w+1)*256), walked in 8 rounds of 32
+    const long long wbase = (long long)blockIdx.x * SORT_TILE + (long long)warp * (32 * SORT_ITEMS);
+    int key[SORT_ITEMS], val[SORT_ITEMS], rnk[SORT_ITEMS];
+    const unsigned lt = (1u << lane) - 1u;
+    for (int r = 0; r < SORT_ITEMS; r++) {
+        const long long e = wbase + (long long)r * 32 + lane;
+        const bool ok = e < n;
+        key[r] = ok ? keys_in[e] : 0;
+        val[r] = ok ? vals_in[e] : 0;
+        const int d = ok ? ((key[r] >> shift) & 0xFF) : RADIX;  // sentinel digit for padding
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const int before = __popc(peers & lt);
+        int basecnt = 0;
+        if (ok) basecnt = wcnt[warp][d];
+        __syncwarp();
+        rnk[r] = basecnt + before;
+        if (ok && before == 0) wcnt[warp][d] = basecnt + __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    // exclusive prefix over warps for each digit; add the global (digit, block) offset
+    for (int d = threadIdx.x; d < RADIX; d += SORT_THREADS) {
+        int run = offsets[(long long)d * nblocks + blockIdx.x];
+        for (int w = 0; w < SORT_WARPS; w++) {
+            const int c = wcnt[w][d];
+            wcnt[w][d] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+    for (int r = 0; r < SORT_ITEMS; r++) {
+        const long long e = wbase + (long long)r * 32 + lane;
+        if (e < n) {
+            const int d = (key[r] >> shift) & 0xFF;
+            const int pos = wcnt[warp][d] + rnk[r];
+            keys_out[pos] = key[r];
+            vals_out[pos] = val[r];
+        }
+    }
+}
+
+// ---- exclusive scan of int arrays (three-phase, recursive over block sums) ----
+constexpr int SCAN_THREADS = 512;
+constexpr int SCAN_ITEMS = 4;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_tile(const int *in, int *out, long long n, int *block_sums)
+{
+    __shared__ int wsum[SCAN_THREADS / 32];
+    const long long base = (long long)blockIdx.x * SCAN_TILE + (long long)threadIdx.x * SCAN_ITEMS;
+    int v[SCAN_ITEMS], tsum = 0;
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        v[k] = (base + k < n) ? in[base + k] : 0;
+        tsum += v[k];
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int incl = tsum;
+    for (int off = 1; off < 32; off <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off) incl += y;
+    }
+    if (lane == 31) wsum[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        int w = (lane < SCAN_THREADS / 32) ? wsum[lane] : 0;
+        for (int off = 1; off < 32; off <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, w, off);
+            if (lane >= off) w += y;
+        }
+        if (lane < SCAN_THREADS / 32) wsum[lane] = w;
+    }
+    __syncthreads();
+    int run = incl - tsum + (warp > 0 ? wsum[warp - 1] : 0);
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        if (base + k < n) out[base + k] = run;
+        run += v[k];
+    }
+    if (threadIdx.x == SCAN_THREADS - 1 && block_sums) block_sums[blockIdx.x] = wsum[SCAN_THREADS / 32 - 1];
+}
+
+__global__ void k_scan_add(int *out, long long n, const int *block_off)
+{
+    const long long i = (long long)blockIdx.x * SCAN_TILE + threadIdx.x;
+    const int add = block_off[blockIdx.x];
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        const long long e = i + (long long)k * SCAN_THREADS;
+        if (e < n) out[e] += add;
+    }
+}
+
+size_t scan_tmp_ints(long long n)
+{
+    size_t total = 0;
+    long long m = n;
+    while (m > SCAN_TILE) {
+        m = (m + SCAN_TILE - 1) / SCAN_TILE;
+        total += (size_t)m * 2 + 32;
+    }
+    return total + 64;
+}
+
+void exclusive_scan_int(const int *in, int *out, long long n, int *tmp, cudaStream_t s)
+{
+    if (n <= 0) return;
+    const long long nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+    if (nb == 1) {
+        k_scan_tile<<<1, SCAN_THREADS, 0, s>>>(in, out, n, nullptr);
+        note_launch(1);
+        return;
+    }
+    int *sums = tmp, *sums_scan = tmp + nb + 16;
+    k_scan_tile<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, out, n, sums);
+    note_launch(1);
+    exclusive_scan_int(sums, sums_scan, nb, tmp + 2 * nb + 32, s);
+    k_scan_add<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(out, n, sums_scan);
+    note_launch(1);
+}
+
+// ---- sort driver ----
+size_t sort_scratch_bytes(long long n)
+{
+    const long long nblocks = (n + SORT_TILE - 1) / SORT_TILE;
+    return (size_t)(4 * n + 2 * RADIX * nblocks) * sizeof(int) + scan_tmp_ints(RADIX * nblocks) * sizeof(int);
+}
+
+__global__ void k_iota(int *out, long long n)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (int)i;
+}
+
+void launch_iota(int *out, long long n, cudaStream_t s)
+{
+    if (n > 0) {
+        k_iota<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(out, n);
+        note_launch(1);
+    }
+}
+
+__global__ void k_extract_keys(PView P, long long n, int *keys)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) keys[i] = P.ii(PF_KEY, i);
+}
+
+void launch_extract_keys(const PView &p, long long n, int *keys, cudaStream_t s)
+{
+    if (n > 0) {
+        k_extract_keys<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p, n, keys);
+        note_launch(1);
+    }
+}
+
+// Sorts keys_in[0..n) (non-negative, < 2^key_bits) stably; perm_out[i] is the input index
+// of the i-th element in sorted order.
+void sort_pairs(const int *keys_in, int *perm_out, long long n, int key_bits, SortScratch &ws, cudaStream_t s)
+{
+    if (n <= 0) return;
+    const int nblocks = (int)((n + SORT_TILE - 1) / SORT_TILE);
+    int passes = (key_bits + 7) / 8;
+    if (passes < 1) passes = 1;
+    launch_iota(ws.vals[0], n, s);
+    const int *kin = keys_in;
+    const int *vin = ws.vals[0];
+    int cur = 0;
+    for (int p = 0; p < passes; p++) {
+        const int shift = 8 * p;
+        int *kout = ws.keys[cur ^ 1];
+        int *vout = (p == passes - 1) ? perm_out : ws.vals[cur ^ 1];
+        k_radix_hist<<<nblocks, SORT_THREADS, 0, s>>>(kin, n, shift, ws.hist, nblocks);
+        note_launch(1);
+        exclusive_scan_int(ws.hist, ws.hist + (long long)RADIX * nblocks, (long long)RADIX * nblocks, ws.scan_tmp, s);
+        k_radix_scatter<<<nblocks, SORT_THREADS, 0, s>>>(kin, vin, kout, vout, n, shift,
+                                                         ws.hist + (long long)RADIX * nblocks, nblocks);
+        note_launch(1);
+        kin = kout;
+        vin = vout;
+        cur ^= 1;
+    }
+}
+
+// out[f][i] = in[f][perm[i]] for the listed fields
+__global__ void k_permute(const float *__restrict__ in, float *__restrict__ out, long long cap, long long n,
+                          const int *__restrict__ perm, const int *__restrict__ fields, int nfields)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const long long src = perm[i];
+    for (int k = 0; k < nfields; k++) {
+        const long long f = fields[k];
+        out[f * cap + i] = __ldg(&in[f * cap + src]);
+    }
+}
+
+void launch_permute(const float *in, float *out, long long cap, long long n, const int *perm, const int *fields,
+                    int nfields, cudaStream_t s)
+{
+    if (n > 0) {
+        k_permute<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(in, out, cap, n, perm, fields, nfields);
+        note_launch(1);
+    }
+}
+
+}  // namespace gy

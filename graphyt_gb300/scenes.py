@@ -1,0 +1,285 @@
+"""Seeded synthetic scenes for the explicit GIMP MPM step.
+
+Graphyt scripts build geometry with the external ``pyck`` packer (e.g.
+``test/test_2d_impact_elastic.py:36-54``), which is not available.  This module stands
+in for it: particles sit on a cubic lattice of spacing ``psep`` whose first point is at
+``lower + psep/2`` in every shape, with objectID / material fields per shape, the same
+fields ``MaterialPoints::addPyckIntField`` consumes (``MaterialPoints.cpp:32-54``).
+
+A :class:`Scene` is plain numpy data; both the GPU solver (through the
+``graphyt_gb300.graphyt`` surface) and the CPU oracle are built from the same scene, so
+parity runs see bit-identical inputs.  Particle order is shuffled with
+``numpy.random.default_rng(seed)`` so that the sort has real work to do.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+from typing import Dict, List, Optional
+
+import numpy as np
+
+# BCTypes::function values (BoundaryConditions.hpp:6-77)
+BC = dict(none=0, grid_vx=1, grid_vy=2, grid_vz=3, grid_vx_vy=11, grid_vx_vz=12, grid_vy_vz=13,
+          grid_vx_vy_vz=18, mp_vx=33, mp_vy=34, mp_vz=35, mp_fx=37, mp_fy=38, mp_fz=39,
+          mp_vx_vy=40, mp_fx_fy=43, mp_stress_xx_yy=63, mp_vxsin=65, mp_vysin=66, mp_syysin=67)
+
+# MaterialModels defaults (MaterialModels.cpp:4-26)
+MATERIAL_DEFAULTS = dict(bulkMod=1e7, shearMod=5000.0, density=1000.0, isRigid=0, viscosity=1.0,
+                         thermalConductivity=391.0, specificHeatCapacity=385.2, yieldStress=1e7,
+                         phi=40.0, psi=10.0, cohesion=100000.0, criticalStrain=0.01, isDamage=0,
+                         damageModel=1, Cg=586.52, damageM=9.0, damageK=5.39e36, turbStress=1e10,
+                         model=1)
+
+
+def material(**kw) -> Dict:
+    m = dict(MATERIAL_DEFAULTS)
+    for k, v in kw.items():
+        if k not in m:
+            raise KeyError(f"unknown material property {k!r}")
+        m[k] = v
+    return m
+
+
+@dataclasses.dataclass
+class Scene:
+    name: str
+    L: List[float]
+    cellsize: float
+    psep: float
+    pos: np.ndarray                    # (N, 3) float64
+    mat: np.ndarray                    # (N,) int32
+    obj: np.ndarray                    # (N,) int32
+    materials: List[Dict]
+    gravity: List[float] = dataclasses.field(default_factory=lambda: [0.0, 0.0, 0.0])
+    damping: float = 0.0
+    mu: float = 0.0
+    CFL: float = 0.1
+    tmax: float = 1.0
+    dt: Optional[float] = None         # setDt override; None keeps the Solver's CFL dt
+    fixed_grid_bcs: int = 0
+    vel: Optional[np.ndarray] = None   # (N, 3)
+    stress: Optional[np.ndarray] = None  # (N, 6)
+    pbc_type: Optional[np.ndarray] = None  # (N,)
+    pbc_val: Optional[np.ndarray] = None   # (N, 4)
+    hold: Optional[np.ndarray] = None      # (N,) bool
+    node_bc_type: Optional[np.ndarray] = None  # (Nn,)
+    node_bc_val: Optional[np.ndarray] = None   # (Nn, 4)
+
+    @property
+    def is3D(self) -> bool:
+        return self.L[2] > 0.0
+
+    @property
+    def n(self) -> int:
+        return int(self.pos.shape[0])
+
+    def dims(self):
+        nx = int(1.0 + self.L[0] / self.cellsize)
+        ny = int(1.0 + self.L[1] / self.cellsize)
+        nz = int(1.0 + self.L[2] / self.cellsize)
+        return nx, ny, nz
+
+    def num_nodes(self) -> int:
+        nx, ny, nz = self.dims()
+        return nx * ny * nz
+
+    def node_positions(self) -> np.ndarray:
+        """Node coordinates i*h, laid out i + j*Nx + k*Nx*Ny (Nodes.cpp:77-139)."""
+        nx, ny, nz = self.dims()
+        k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+        h = self.cellsize
+        return np.stack([i.ravel() * h, j.ravel() * h, k.ravel() * h], axis=1)
+
+
+def lattice_box(lower, upper, psep):
+    """Lattice points lower + psep/2 + i*psep strictly inside [lower, upper)."""
+    axes = []
+    for lo, hi in zip(lower, upper):
+        if hi <= lo:
+            axes.append(np.array([lo]))
+            continue
+        n = int(math.floor((hi - lo) / psep + 1e-9))
+        axes.append(lo + psep / 2 + psep * np.arange(n))
+    z, y, x = np.meshgrid(axes[2], axes[1], axes[0], indexing="ij")
+    return np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1)
+
+
+def lattice_cylinder_z(center, radius, z0, z1, psep):
+    """Lattice points of a cylinder whose axis is parallel to z."""
+    lo = [center[0] - radius, center[1] - radius, z0]
+    hi = [center[0] + radius, center[1] + radius, z1]
+    p = lattice_box(lo, hi, psep)
+    r2 = (p[:, 0] - center[0]) ** 2 + (p[:, 1] - center[1]) ** 2
+    return p[r2 <= radius * radius]
+
+
+def _finish(scene: Scene, seed: int) -> Scene:
+    n = scene.n
+    if scene.vel is None:
+        scene.vel = np.zeros((n, 3))
+    if scene.stress is None:
+        scene.stress = np.zeros((n, 6))
+    if scene.pbc_type is None:
+        scene.pbc_type = np.zeros(n, np.int32)
+    if scene.pbc_val is None:
+        scene.pbc_val = np.zeros((n, 4))
+    if scene.hold is None:
+        scene.hold = np.zeros(n, bool)
+    nn = scene.num_nodes()
+    if scene.node_bc_type is None:
+        scene.node_bc_type = np.zeros(nn, np.int32)
+    if scene.node_bc_val is None:
+        scene.node_bc_val = np.zeros((nn, 4))
+    if seed is not None:
+        perm = np.random.default_rng(seed).permutation(n)
+        for f in ("pos", "mat", "obj", "vel", "stress", "pbc_type", "pbc_val", "hold"):
+            setattr(scene, f, np.ascontiguousarray(getattr(scene, f)[perm]))
+    scene.pos = np.ascontiguousarray(scene.pos, np.float64)
+    scene.mat = np.ascontiguousarray(scene.mat, np.int32)
+    scene.obj = np.ascontiguousarray(scene.obj, np.int32)
+    scene.pbc_type = np.ascontiguousarray(scene.pbc_type, np.int32)
+    scene.node_bc_type = np.ascontiguousarray(scene.node_bc_type, np.int32)
+    return scene
+
+
+# ------------------------------------------------------------------------------------------
+# named workloads
+
+def elastic_cube(variant: str = "particle", scale: int = 1, seed: int = 0) -> Scene:
+    """Elastic cube compression: 1 m periodic domain, cellsize 0.05/scale, psep half of it,
+    a 0.5 m cube centred in the domain (20^3 = 8000 particles at scale 1), K 1e7, G 5e6,
+    rho 1000, no gravity, dt = 0.3*dx/sqrt((K+4G/3)/rho) through setDt.
+
+    variant "nodal":    grid_vz on the node layer touching the cube top (-0.1 m/s) and
+                         bottom (0); these bodies are empty in the reference, so the cube stays
+                         at rest (bug-compatible run).
+    variant "fixed":    the same nodal BCs with fixed_grid_bcs=1 (working z BCs).
+    variant "particle": mp_vz on the top particle layer (-0.1) and bottom layer (0).
+    """
+    h = 0.05 / scale
+    psep = h / 2
+    pos = lattice_box([0.25, 0.25, 0.25], [0.75, 0.75, 0.75], psep)
+    n = len(pos)
+    K, G, rho = 1e7, 5e6, 1000.0
+    sc = Scene("elastic_cube_" + variant, [1.0, 1.0, 1.0], h, psep, pos, np.zeros(n, np.int32),
+               np.zeros(n, np.int32), [material(bulkMod=K, shearMod=G, density=rho, model=1)])
+    sc.dt = 0.3 * h / math.sqrt((K + 4.0 * G / 3.0) / rho)
+    sc.tmax = 1000 * sc.dt
+    if variant == "particle":
+        ztop, zbot = pos[:, 2].max(), pos[:, 2].min()
+        sc.pbc_type = np.zeros(n, np.int32)
+        sc.pbc_val = np.zeros((n, 4))
+        top = np.isclose(pos[:, 2], ztop)
+        bot = np.isclose(pos[:, 2], zbot)
+        sc.pbc_type[top | bot] = BC["mp_vz"]
+        sc.pbc_val[top, 0] = -0.1
+    else:
+        nodes = sc.node_positions()
+        nn = len(nodes)
+        sc.node_bc_type = np.zeros(nn, np.int32)
+        sc.node_bc_val = np.zeros((nn, 4))
+        inside = ((nodes[:, 0] >= 0.25 - 1e-9) & (nodes[:, 0] <= 0.75 + 1e-9) &
+                  (nodes[:, 1] >= 0.25 - 1e-9) & (nodes[:, 1] <= 0.75 + 1e-9))
+        top = inside & np.isclose(nodes[:, 2], 0.75)
+        bot = inside & np.isclose(nodes[:, 2], 0.25)
+        sc.node_bc_type[top | bot] = BC["grid_vz"]
+        sc.node_bc_val[top, 0] = -0.1
+        sc.fixed_grid_bcs = 1 if variant == "fixed" else 0
+    return _finish(sc, seed)
+
+
+def dam_break(scale: float = 1.0, height: float = 0.765, seed: int = 0, walls: bool = True,
+              width: float = 2.0) -> Scene:
+    """3D Newtonian dam break: domain 4 x width x 2 m (width 2 by default), cellsize
+    0.01/scale, psep half of it.
+    Water (K 2e6, viscosity 1e-3, rho 1000) fills x in [2h, 2h+1.0], y in [2h, width-2h],
+    z in [2h, 2h+height] against the x=0 wall; gravity -9.81 in z; CFL 0.3 with the
+    Solver's own dt formula (Solver.cpp:32).  At scale 1 and the default height this is
+    200 x 392 x 153 = 11,997,600 particles.  With walls=True every node within two cells
+    of a face carries grid_vx_vy_vz = 0 with fixed_grid_bcs=1 (the reference's
+    grid_vx_vy_vz body is empty, Grid.cpp:1050-1052)."""
+    h = 0.01 / scale
+    psep = h / 2
+    L = [4.0, float(width), 2.0]
+    w = 2 * h
+    pos = lattice_box([w, w, w], [w + 1.0, L[1] - w, w + height], psep)
+    n = len(pos)
+    sc = Scene("dam_break", L, h, psep, pos, np.zeros(n, np.int32), np.zeros(n, np.int32),
+               [material(bulkMod=2e6, viscosity=1e-3, density=1000.0, shearMod=0.0, model=2)])
+    sc.gravity = [0.0, 0.0, -9.81]
+    sc.CFL = 0.3
+    sc.tmax = 1.0
+    if walls:
+        nx, ny, nz = sc.dims()
+        k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+        i, j, k = i.ravel(), j.ravel(), k.ravel()
+        near = ((i <= 2) | (i >= nx - 3) | (j <= 2) | (j >= ny - 3) | (k <= 2) | (k >= nz - 3))
+        sc.node_bc_type = np.where(near, BC["grid_vx_vy_vz"], 0).astype(np.int32)
+        sc.node_bc_val = np.zeros((nx * ny * nz, 4))
+        sc.fixed_grid_bcs = 1
+    return _finish(sc, seed)
+
+
+def brazilian_disc(scale: float = 1.0, seed: int = 0, platen_speed: float = 0.5) -> Scene:
+    """3D Brazilian disc: a Drucker-Prager + Grady-Kipp cylinder (radius 0.05 m, thickness
+    0.02 m, axis along z) squeezed along y by two rigid platens at +/-platen_speed.
+    cellsize 5e-4/scale, psep half of it.  DP: K 3e10, G 2e10, rho 2600, cohesion 1e7,
+    friction 30 deg, dilatancy 0, critical strain 0.01.  GK: m 9, k 5e32, Cg = 0.4 x the
+    P-wave speed (1867.40 m/s).  objectIDs: disc 1, top platen 2, bottom platen 3 (the
+    layout of Examples/brazillian3D.py:31-108).  At scale 1 this is about 10 M particles;
+    the reference's Grady-Kipp has no per-particle Weibull flaws (DamageModels.cpp:102-103),
+    so the flaw threshold is the deterministic e_min = (V k)^(-1/m)."""
+    h = 5e-4 / scale
+    psep = h / 2
+    R, T = 0.05, 0.02
+    margin = 8 * h
+    Lx = 2 * R + 2 * margin
+    Ly = 2 * R + 2 * margin + 4 * h + 2 * 4 * h
+    Lz = T + 2 * margin
+    L = [round(Lx / h) * h, round(Ly / h) * h, round(Lz / h) * h]
+    cx, cy = L[0] / 2, L[1] / 2
+    z0 = margin
+    disc = lattice_cylinder_z([cx, cy], R, z0, z0 + T, psep)
+    pw = 4 * h  # platen thickness
+    half = 0.25 * R
+    top = lattice_box([cx - half, cy + R + psep, z0], [cx + half, cy + R + psep + pw, z0 + T], psep)
+    bot = lattice_box([cx - half, cy - R - psep - pw, z0], [cx + half, cy - R - psep, z0 + T], psep)
+    pos = np.concatenate([disc, top, bot])
+    mat = np.concatenate([np.zeros(len(disc)), np.ones(len(top)), np.ones(len(bot))]).astype(np.int32)
+    obj = np.concatenate([np.full(len(disc), 1), np.full(len(top), 2), np.full(len(bot), 3)]).astype(np.int32)
+    K, G, rho = 3e10, 2e10, 2600.0
+    cp = math.sqrt((K + 4.0 * G / 3.0) / rho)
+    rock = material(bulkMod=K, shearMod=G, density=rho, cohesion=1e7, phi=30.0, psi=0.0,
+                    criticalStrain=0.01, isDamage=1, damageModel=1, Cg=0.4 * cp, damageM=9.0,
+                    damageK=5e32, model=4)
+    platen = material(isRigid=1)
+    sc = Scene("brazilian_disc", L, h, psep, pos, mat, obj, [rock, platen])
+    sc.CFL = 0.3
+    sc.tmax = 1.0
+    vel = np.zeros((len(pos), 3))
+    vel[obj == 2, 1] = -platen_speed
+    vel[obj == 3, 1] = platen_speed
+    sc.vel = vel
+    return _finish(sc, seed)
+
+
+def tiny_block(seed: int = 0, model: int = 1, n_side: int = 4, cellsize: float = 0.125,
+               L=(1.5, 1.5, 1.5), gravity=(0.0, 0.0, -9.81), vel=(0.3, -0.2, 0.1)) -> Scene:
+    """A small block for fast parity cases: n_side^3 particles on a 12^3-cell grid."""
+    h = cellsize
+    psep = h / 2
+    lo = np.array([0.5, 0.45, 0.4])
+    pos = lattice_box(lo, lo + n_side * psep, psep)
+    n = len(pos)
+    mats = [material(bulkMod=1e6, shearMod=4e5, density=1200.0, viscosity=0.5, yieldStress=2e3,
+                     cohesion=2e3, phi=30.0, psi=10.0, criticalStrain=0.05, model=model)]
+    sc = Scene(f"tiny_block_m{model}", list(L), h, psep, pos, np.zeros(n, np.int32),
+               np.zeros(n, np.int32), mats)
+    sc.gravity = list(gravity)
+    sc.CFL = 0.3
+    v = np.zeros((n, 3))
+    v[:] = vel
+    v += 0.05 * np.random.default_rng(seed + 1).standard_normal((n, 3))
+    sc.vel = v
+    return _finish(sc, seed)

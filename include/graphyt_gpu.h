@@ -1,0 +1,210 @@
+/*
+ * graphyt_gpu.h -- C ABI of the GB300 explicit GIMP MPM step (libgraphyt_gpu.so).
+ *
+ * One handle holds one simulation: a uniform background grid (the reference's Nodes), a
+ * particle set (MaterialPoints), a material table (std::vector<MaterialModels>), the global
+ * Parameters and the Solver's dt.  Particle and grid state live on one GPU in SoA layout
+ * from gy_initialize() on; gy_step() advances one explicit step on the handle's CUDA stream
+ * without a host sync; downloads sync.
+ *
+ * Conventions
+ *   - Plain pointers and sizes only; every host array is caller-owned and only read or
+ *     written during the call.
+ *   - Every call returns gy_status (0 = GY_OK).  On error, gy_last_error(h) describes it.
+ *   - Calls on one handle are not re-entrant; different handles are independent.
+ *   - Particle arrays are exchanged in insertion order (particle i is the i-th particle
+ *     given to gy_add_particles), whatever order the device currently keeps them in.
+ *
+ * Each entry point names the reference interface it replaces (file:line in the reference
+ * tree).  The reference has no GPU path: its Solver::iterate_GPU (Solver.cpp:293-302) is a
+ * stub, so gy_step is the first GPU implementation of iterate_CPU (Solver.cpp:86-292).
+ */
+#ifndef GRAPHYT_GPU_H
+#define GRAPHYT_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GY_ABI_VERSION 1
+
+typedef int gy_status;
+enum {
+    GY_OK = 0,
+    GY_ERR_ARG = -1,         /* invalid argument or handle */
+    GY_ERR_CUDA = -2,        /* a CUDA call failed (message in gy_last_error) */
+    GY_ERR_STATE = -3,       /* call out of order (e.g. gy_step before gy_initialize) */
+    GY_ERR_RANGE = -4,       /* a particle left the grid the reference can index */
+    GY_ERR_UNSUPPORTED = -5, /* input the GPU path does not implement */
+    GY_ERR_NONFINITE = -6,   /* a NaN or Inf appeared in particle state */
+    GY_ERR_NOMEM = -7        /* device allocation failed */
+};
+
+typedef struct gy_solver gy_solver;
+
+/* Background grid, Nodes::Nodes(std::vector<double> L, double cellsize) (Nodes.cpp:8-141),
+ * plus MaterialPoints::psep (MaterialPoints.hpp:82).  L[2] == 0 selects a 2D grid. */
+typedef struct gy_grid_desc {
+    double L[3];
+    double cellsize;
+    double psep;
+} gy_grid_desc;
+
+/* One material, MaterialModels (MaterialModels.hpp:5-48); field order is part of the ABI. */
+typedef struct gy_material {
+    double bulkMod, shearMod, density, viscosity, thermalConductivity, specificHeatCapacity;
+    double yieldStress, cohesion, criticalStrain, phi, psi, Cg, damageM, damageK, turbStress;
+    int isRigid, isDamage, damageModel, model;
+} gy_material;
+
+/* Parameters (Parameters.hpp:16-32) plus one switch: fixed_grid_bcs = 1 gives
+ * grid_vz / grid_vx_vz / grid_vy_vz / grid_vx_vy_vz a body (empty in the reference,
+ * Grid.cpp:872-873, 1032-1052); 0 keeps the reference's behaviour. */
+typedef struct gy_params {
+    double gravity[3];
+    double damping;
+    double mu;
+    double CFL;
+    double tmax;
+    int is3D;
+    int fixed_grid_bcs;
+} gy_params;
+
+/* Tuning knobs that change speed, never results beyond summation order. */
+typedef struct gy_options {
+    int sort_every;     /* reorder particle state by cell every n steps (>= 1) */
+    int p2g_tile;       /* 1: shared-memory node tiles in P2G; 0: direct global atomics */
+    int block_particles;/* particles per CTA in the particle kernels (64..1024) */
+    int track_normals;  /* 1: keep per-particle contact normals (getNormalsArr) */
+    int check_finite;   /* 1: flag NaN/Inf in particle state every step */
+    int keep_node_fields; /* 1: keep centre-of-mass node velocity/force for node getters */
+} gy_options;
+
+/* FP64 conservation sums and counters, Solver.cpp:264-289's printout made a struct. */
+typedef struct gy_stats {
+    double mass;           /* sum m_p */
+    double momentum[3];    /* sum m_p v_p */
+    double kinetic;        /* sum 0.5 m_p |v_p|^2 */
+    double strain_energy;  /* sum 0.5 V_p sigma_p : eps_p */
+    int64_t active_nodes;  /* nodes with nonzero mass after the last P2G */
+    int64_t steps;         /* steps taken by this handle */
+    int64_t status_flags;  /* device error bits (range / nonfinite) */
+} gy_stats;
+
+/* Particle fields for gy_get_particles / gy_set_particles (double, insertion order).
+ * Widths: POS 3, POS0 3, DISP 3, VEL 3, STRESS 6, STRAIN 6, PSTRAIN 6, EQPS 1, DAMAGE 1,
+ * SMAX 1, MASS 1, DENSITY 1, VOLUME 1, NORMALS 3.  Stress/strain order xx yy zz xy yz xz. */
+enum gy_pfield {
+    GY_P_POS = 0, GY_P_POS0, GY_P_DISP, GY_P_VEL, GY_P_STRESS, GY_P_STRAIN, GY_P_PSTRAIN,
+    GY_P_EQPS, GY_P_DAMAGE, GY_P_SMAX, GY_P_MASS, GY_P_DENSITY, GY_P_VOLUME, GY_P_NORMALS,
+    GY_P_NFIELDS
+};
+/* Integer particle fields: CELLID (the reference's binning key, TimeIntegration.cpp:110-115),
+ * MATERIAL, OBJECT, DEVICE_SLOT (where the device keeps the particle now). */
+enum gy_pifield { GY_PI_CELLID = 0, GY_PI_MATERIAL, GY_PI_OBJECT, GY_PI_DEVICE_SLOT };
+/* Node fields (double, node order i + j*Nx + k*Nx*Ny): MASS 1 (centre of mass), VEL 3
+ * (centre-of-mass velocity), FORCE 3, VEL1 3 / ACC1 3 (body-1 field after the solve).
+ * VEL and FORCE need gy_options.keep_node_fields = 1 during the step. */
+enum gy_nfield { GY_N_MASS = 0, GY_N_VEL, GY_N_FORCE, GY_N_VEL1, GY_N_ACC1, GY_N_NFIELDS };
+
+/* ---------------------------------------------------------------------------------------- */
+
+/* Library ABI version (GY_ABI_VERSION). */
+int gy_abi_version(void);
+
+/* Nodes::Nodes (Nodes.cpp:8-141) + MaterialPoints::MaterialPoints (MaterialPoints.cpp:10-17).
+ * device < 0 uses the current device.  Rejects grids where the reference's truncated
+ * Nx*Ny*Nz differs from its rounded numNodes (Nodes.cpp:12, 71-73). */
+gy_status gy_create(const gy_grid_desc *grid, int device, gy_solver **out);
+
+/* Releases every device and host resource of the handle. */
+gy_status gy_destroy(gy_solver *h);
+
+/* Message for the last failed call on this handle (never NULL). */
+const char *gy_last_error(const gy_solver *h);
+
+/* Grid size: nxyz[3] = Nx, Ny, Nz; numNodes = Nx*Ny*Nz (Nodes.cpp:12, 71-73). */
+gy_status gy_grid_dims(const gy_solver *h, int *nxyz, int64_t *num_nodes);
+
+/* MaterialPoints::addPyckGeom + addPyckIntField("material"/"objectID")
+ * (MaterialPoints.cpp:24-54, add() at :95-235).  mat/obj may be NULL (zeros).  Appends. */
+gy_status gy_add_particles(gy_solver *h, int64_t n, const double *pos3, const int *mat, const int *obj);
+
+/* MaterialPoints::setVel (MaterialPoints.cpp:302-306), setStress (:312-319), setDamage
+ * (:308-310), holdParticle (:336-340), setBC (:88-93), for many particles at once.
+ * idx lists insertion indices; values are per listed particle. */
+gy_status gy_set_particle_vel(gy_solver *h, int64_t count, const int64_t *idx, const double *vel3);
+gy_status gy_set_particle_stress(gy_solver *h, int64_t count, const int64_t *idx, const double *s6);
+gy_status gy_set_particle_damage(gy_solver *h, int64_t count, const int64_t *idx, const double *d);
+gy_status gy_hold_particles(gy_solver *h, int64_t count, const int64_t *idx);
+gy_status gy_set_particle_bc(gy_solver *h, int64_t count, const int64_t *idx, const int *type, const double *val4);
+
+/* Nodes::setBC (Nodes.cpp:155-163) for many nodes: node index, BCTypes value, 4 values. */
+gy_status gy_set_node_bc(gy_solver *h, int64_t count, const int64_t *nodes, const int *type, const double *val4);
+
+/* Solver::Solver (Solver.cpp:7-37): stores the materials and parameters, sets dt =
+ * CFL*h/sqrt(maxK/minRho) and runs initialize() (Solver.cpp:40-69); uploads all state. */
+gy_status gy_initialize(gy_solver *h, const gy_material *mats, int nmat, const gy_params *prm);
+
+/* Solver::setDt (Solver.cpp:70-73) and the dt attribute (Solver.i:17). */
+gy_status gy_set_dt(gy_solver *h, double dt);
+gy_status gy_get_dt(const gy_solver *h, double *dt);
+
+/* The Parameters* passed to every iterate call (gravity, damping, friction may change). */
+gy_status gy_set_params(gy_solver *h, const gy_params *prm);
+
+gy_status gy_set_options(gy_solver *h, const gy_options *opt);
+gy_status gy_get_options(const gy_solver *h, gy_options *opt);
+
+/* Solver::iterate_GPU(double t, int step, Parameters*) -- the GPU counterpart of
+ * iterate_CPU (Solver.cpp:86-292).  Enqueues one step on the handle's stream and returns
+ * without waiting.  step selects the reference's step-dependent rules (half dt at step 1,
+ * Grid.cpp:126-131); t is the time stored for the next step's sine-ramped particle BCs. */
+gy_status gy_step(gy_solver *h, double t, int step);
+
+/* Solver::iterate_CPU_steps (Solver.cpp:75-84) on the GPU: nsteps steps from step0/t0,
+ * t advancing by dt.  use_graph = 1 replays the steps as a captured CUDA graph. */
+gy_status gy_steps(gy_solver *h, double t0, int step0, int nsteps, int use_graph);
+
+/* Waits for all queued work, then reports device error flags (GY_ERR_RANGE /
+ * GY_ERR_NONFINITE) raised since the last gy_sync. */
+gy_status gy_sync(gy_solver *h);
+
+/* The handle's CUDA stream (a cudaStream_t), for callers that time or order work. */
+void *gy_stream(gy_solver *h);
+
+/* Particle getters (MaterialPoints.cpp:238-273) and setters; count must equal n*width. */
+gy_status gy_num_particles(const gy_solver *h, int64_t *n);
+gy_status gy_get_particles(gy_solver *h, int field, double *out, int64_t count);
+gy_status gy_get_particles_int(gy_solver *h, int field, int *out, int64_t count);
+/* Node getters (Nodes.cpp:147-153): getMassArr, getVelArr, getForceArr and body-1 fields. */
+gy_status gy_get_nodes(gy_solver *h, int field, double *out, int64_t count);
+
+/* Stable sort of n non-negative keys on the device, the counting sort the step uses:
+ * perm_out[i] = index of the i-th key in ascending order, ties in input order.  Host
+ * arrays; for testing the sort against a CPU stable sort. */
+gy_status gy_sort_keys(const int *keys, int64_t n, int *perm_out, int device);
+
+/* FP64 conservation sums over the particles (waits for queued work). */
+gy_status gy_get_stats(gy_solver *h, gy_stats *out);
+
+/* Phase timing with CUDA events on the handle's stream, recorded around every phase of
+ * every step while on, without host syncs.  gy_get_phase_times waits, returns the summed
+ * milliseconds per phase since timing was switched on -- [0] sort+permute, [1] P2G,
+ * [2] fold+solve, [3] G2P+update, [4] total -- with the number of timed steps, and resets. */
+gy_status gy_set_phase_timing(gy_solver *h, int on);
+gy_status gy_get_phase_times(gy_solver *h, float *ms5, int64_t *steps);
+
+/* Device time of nsteps consecutive steps (as gy_steps), from CUDA events recorded on the
+ * handle's stream before the first and after the last step. */
+gy_status gy_time_steps(gy_solver *h, double t0, int step0, int nsteps, float *ms);
+
+/* Number of kernels this library has launched in the process so far. */
+int64_t gy_kernel_launches(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GRAPHYT_GPU_H */

@@ -1,0 +1,54 @@
+"""CPU checks of the C ABI: the library loads and exports every symbol the header declares."""
+import ctypes
+import os
+import re
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "graphyt_gpu.h")
+
+
+def declared_symbols():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(gy_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    assert "gy_step" in syms and "gy_create" in syms and "gy_initialize" in syms
+    assert len(syms) >= 25
+
+
+def test_library_exports_every_declared_symbol(gpu_lib):
+    for name in declared_symbols():
+        assert hasattr(gpu_lib, name), name
+
+
+def test_python_binding_covers_header(gpu_lib):
+    from graphyt_gb300 import _lib
+    assert set(declared_symbols()) <= set(_lib.SIGNATURES)
+
+
+def test_abi_version(gpu_lib):
+    assert gpu_lib.gy_abi_version() == 1
+
+
+def test_create_rejects_inconsistent_grid(gpu_lib):
+    """Nx*Ny*Nz != numNodes (Nodes.cpp:12 vs :71-73) is refused before any CUDA work."""
+    from graphyt_gb300 import _lib
+    g = _lib.GridDesc()
+    g.L[0], g.L[1], g.L[2] = 1.2, 1.2, 1.2
+    g.cellsize = 0.1
+    g.psep = 0.05
+    h = ctypes.c_void_p()
+    assert gpu_lib.gy_create(ctypes.byref(g), -1, ctypes.byref(h)) == _lib.GY_ERR_ARG
+    g.L[0] = g.L[1] = g.L[2] = 1.0
+    g.psep = 0.2  # psep > cellsize
+    assert gpu_lib.gy_create(ctypes.byref(g), -1, ctypes.byref(h)) == _lib.GY_ERR_UNSUPPORTED
+
+
+def test_null_handles_are_errors(gpu_lib):
+    from graphyt_gb300 import _lib
+    assert gpu_lib.gy_step(None, 0.0, 0) == _lib.GY_ERR_ARG
+    assert gpu_lib.gy_destroy(None) == _lib.GY_ERR_ARG
+    assert gpu_lib.gy_last_error(None) == b"null handle"

@@ -1,0 +1,129 @@
+"""GPU parity: the CUDA step through the C ABI against the FP64 oracle and the reference's
+golden fixtures.
+
+Tolerances (FP32 GPU state against the FP64 reference): relative L2 over particles of
+velocity and stress <= 1e-5 after one step; <= 1e-3 after many steps.  Integer work (the
+sort) is bit-exact.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from graphyt_gb300 import scenes
+from tests.golden import make_golden
+from tests.helpers import rel_l2, run_gpu, run_oracle
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+ONE_STEP_TOL = 1e-5
+MANY_STEP_TOL = 1e-3
+
+
+# ---- (a) sort: bit-exact against a CPU stable sort --------------------------------------
+@pytest.mark.parametrize("n", [0, 1, 2, 31, 2047, 2048, 2049, 100_003, 1_000_000])
+def test_sort_matches_cpu_stable_sort(gpu_lib, n):
+    from graphyt_gb300 import _lib
+    rng = np.random.default_rng(n)
+    for hi in (1, 7, 4096, 16_000_000):
+        keys = rng.integers(0, hi, n).astype(np.int32)
+        perm = _lib.sort_keys(keys)
+        assert np.array_equal(perm, np.argsort(keys, kind="stable")), (n, hi)
+
+
+def test_sort_presorted_and_reversed(gpu_lib):
+    from graphyt_gb300 import _lib
+    keys = np.repeat(np.arange(50_000, dtype=np.int32), 8)
+    assert np.array_equal(_lib.sort_keys(keys), np.arange(len(keys)))
+    rev = keys[::-1].copy()
+    assert np.array_equal(_lib.sort_keys(rev), np.argsort(rev, kind="stable"))
+
+
+# ---- one step and many steps against the oracle -----------------------------------------
+ONE_STEP_CASES = {
+    "tiny_elastic": lambda: scenes.tiny_block(model=1),
+    "tiny_newtonian": lambda: scenes.tiny_block(model=2),
+    "tiny_vonmises": lambda: scenes.tiny_block(model=3),
+    "tiny_druckerprager": lambda: scenes.tiny_block(model=4),
+    "cube_particle_bc": lambda: scenes.elastic_cube("particle"),
+    "cube_nodal_fixed": lambda: scenes.elastic_cube("fixed"),
+    "dam_break_coarse": lambda: scenes.dam_break(scale=0.125),
+}
+
+
+@pytest.mark.parametrize("name", sorted(ONE_STEP_CASES))
+def test_one_step_parity(gpu_lib, oracle_built, name):
+    sc = ONE_STEP_CASES[name]()
+    nsteps = 2  # steps 0 and 1 (step 1 uses the half-dt nodal update)
+    gpu = run_gpu(sc, nsteps)
+    ref = run_oracle(sc, nsteps)
+    for f in ("vel", "stress", "pos", "density"):
+        a = gpu._get_particles(f)
+        b = ref.pfield(f)
+        err = rel_l2(a, b)
+        if np.linalg.norm(b) == 0:
+            assert np.max(np.abs(a)) < 1e-9, (name, f)
+        else:
+            assert err <= ONE_STEP_TOL, (name, f, err)
+
+
+@pytest.mark.parametrize("name", ["tiny_elastic", "tiny_newtonian", "tiny_vonmises", "tiny_druckerprager",
+                                  "cube_particle_bc", "cube_nodal_fixed", "dam_break_coarse"])
+def test_golden_parity(gpu_lib, name):
+    """The GPU path reproduces the reference's own output (golden fixture) over many steps."""
+    gold = np.load(os.path.join(GOLDEN, name + ".npz"))
+    make, steps, _ = make_golden.CASES[name]
+    gpu = run_gpu(make(), int(gold["steps"]))
+    ids = gold["ids"]
+    for f in ("vel", "stress", "density"):
+        a = gpu._get_particles(f)[ids]
+        b = gold[f]
+        if np.linalg.norm(b) == 0:
+            assert np.max(np.abs(a)) < 1e-9
+        else:
+            assert rel_l2(a, b) <= MANY_STEP_TOL, (name, f, rel_l2(a, b))
+
+
+def test_cube_1000_steps(gpu_lib, oracle_built):
+    """Elastic cube compression, 8000 particles, 1000 steps: relative L2 <= 1e-3."""
+    sc = scenes.elastic_cube("particle")
+    gpu = run_gpu(sc, 1000)
+    ref = run_oracle(sc, 1000)
+    for f in ("vel", "stress"):
+        err = rel_l2(gpu._get_particles(f), ref.pfield(f))
+        assert err <= MANY_STEP_TOL, (f, err)
+
+
+def test_literal_nodal_bcs_stay_at_rest(gpu_lib):
+    """grid_vz has an empty body in the reference (Grid.cpp:872-873): the cube does not move."""
+    gpu = run_gpu(scenes.elastic_cube("nodal"), 30)
+    assert np.all(gpu._get_particles("vel") == 0.0)
+    assert np.all(gpu._get_particles("stress") == 0.0)
+
+
+def test_do_nothing_invariant(gpu_lib):
+    sc = scenes.tiny_block(model=1, n_side=6, gravity=(0, 0, 0), vel=(0, 0, 0))
+    sc.vel[:] = 0.0
+    gpu = run_gpu(sc, 50)
+    assert np.all(gpu._get_particles("disp") == 0.0)
+    assert np.all(gpu._get_particles("stress") == 0.0)
+
+
+def test_mass_conservation_and_stats(gpu_lib):
+    sc = scenes.dam_break(scale=0.125)
+    gpu = run_gpu(sc, 5)
+    st = gpu.stats()
+    m = gpu._get_particles("mass").sum()
+    assert abs(st["mass"] - m) <= 1e-9 * m
+    assert st["active_nodes"] > 0
+    assert st["steps"] == 5
+
+
+def test_sort_every_does_not_change_results(gpu_lib):
+    """Reordering is a performance knob: with and without per-step sorting the state agrees
+    to FP32 summation order."""
+    sc = scenes.dam_break(scale=0.125)
+    a = run_gpu(sc, 12, options=dict(sort_every=1))
+    b = run_gpu(sc, 12, options=dict(sort_every=7))
+    assert rel_l2(a._get_particles("vel"), b._get_particles("vel")) < 1e-5

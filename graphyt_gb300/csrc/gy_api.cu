@@ -33,6 +33,8 @@ struct gy_solver {
     std::vector<int> mat, obj, pbc_type;
     std::vector<double> pbc_val;
     std::vector<unsigned char> hold;
+    std::vector<int> key0;           // uploaded cell key by particle id
+    std::vector<float> off0;         // uploaded FP32 offsets by particle id (3 per particle)
     std::vector<unsigned char> nbc_type;
     std::vector<float> nbc_val;
     bool any_node_bc = false;
@@ -51,8 +53,10 @@ struct gy_solver {
     long long n = 0, cap = 0;
     float *slab[2] = {nullptr, nullptr};
     int cur = 0;
-    int *d_keys = nullptr, *d_perm = nullptr, *d_fields = nullptr;
-    int nfields = 0;
+    int *d_perm = nullptr;
+    int *d_seg = nullptr, *d_nseg = nullptr;   // non-empty cell-block segments
+    int persist_grid = 1;
+    bool acc_ready = false;                    // accumulators already hold this step's P2G
     SortScratch ws{};
     void *sort_mem = nullptr;
     float4 *d_pbc_val = nullptr;
@@ -110,13 +114,13 @@ PView pview(gy_solver *h, int which) { return PView{h->slab[which], h->cap}; }
 
 void free_device(gy_solver *h)
 {
-    void *ptrs[] = {h->slab[0], h->slab[1], h->d_keys, h->d_perm, h->d_fields, h->sort_mem, h->d_pbc_val,
+    void *ptrs[] = {h->slab[0], h->slab[1], h->d_perm, h->d_seg, h->d_nseg, h->sort_mem, h->d_pbc_val,
                     h->d_refkey0, h->d_mats, h->d_status, h->d_stats, h->node_mem, h->d_cell_min,
                     h->d_nidx[0], h->d_nidx[1], h->d_nidx[2]};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     h->slab[0] = h->slab[1] = nullptr;
-    h->d_keys = h->d_perm = h->d_fields = nullptr;
+    h->d_perm = h->d_seg = h->d_nseg = nullptr;
     h->sort_mem = nullptr;
     h->d_pbc_val = nullptr;
     h->d_refkey0 = nullptr;
@@ -176,6 +180,18 @@ gy_status gy_create(const gy_grid_desc *grid, int device, gy_solver **out)
     g.ncx = nx - 1; g.ncy = ny - 1; g.ncz = is3d ? nz - 1 : 1;
     g.nn = s->nn;
     g.nc = (long long)g.ncx * g.ncy * g.ncz;
+    g.nbx = (g.ncx + CB - 1) / CB;
+    g.nby = (g.ncy + CB - 1) / CB;
+    g.nbz = (g.ncz + CB - 1) / CB;
+    g.nnbx = (nx + 3) / 4;
+    g.nnby = (ny + 3) / 4;
+    g.nnbz = (nz + 3) / 4;
+    g.nnb = (long long)g.nnbx * g.nnby * g.nnbz;
+    if ((long long)g.nbx * g.nby * g.nbz * 64 >= (1LL << 31)) {
+        cudaStreamDestroy(s->stream);
+        delete s;
+        return GY_ERR_UNSUPPORTED;  // cell keys must fit in 31 bits
+    }
     g.h = (float)h;
     g.inv_h = (float)(1.0 / h);
     g.lp = (float)(0.5 * grid->psep / h);
@@ -361,6 +377,7 @@ static gy_status alloc_nodes(gy_solver *h)
     size_t bytes = (size_t)rows * nn * sizeof(float4);
     size_t extra = 0;
     if (h->multi) extra = (size_t)nn * sizeof(int2) + (size_t)nn + 64;
+    extra += (size_t)h->g.nnb + 64;
     if (h->any_node_bc) extra += (size_t)nn * sizeof(float4) + (size_t)nn + 64;
     char *mem = nullptr;
     cudaError_t e = cudaMalloc((void **)&mem, bytes + extra + 4096);
@@ -392,6 +409,9 @@ static gy_status alloc_nodes(gy_solver *h)
         }
     }
     char *c = (char *)f4;
+    nb.flags = (unsigned char *)c;
+    c += (size_t)h->g.nnb;
+    c = (char *)(((uintptr_t)c + 15) & ~(uintptr_t)15);
     if (h->any_node_bc) {
         nb.bc_val = (const float4 *)c;
         CK(h, cudaMemcpyAsync(c, h->nbc_val.data(), (size_t)nn * sizeof(float4), cudaMemcpyHostToDevice, h->stream));
@@ -475,6 +495,8 @@ gy_status gy_initialize(gy_solver *h, const gy_material *mats, int nmat, const g
     }
     std::vector<float> hs(slab_floats, 0.0f);
     std::vector<int> refkey0(h->cap, 0);
+    h->key0.assign((size_t)n, 0);
+    h->off0.assign((size_t)n * 3, 0.0f);
     std::vector<float4> pbcv(h->cap, make_float4(0.f, 0.f, 0.f, 0.f));
     auto F = [&](int f, long long i) -> float & { return hs[(size_t)f * h->cap + i]; };
     auto I = [&](int f, long long i) -> int & { return reinterpret_cast<int *>(hs.data())[(size_t)f * h->cap + i]; };
@@ -501,7 +523,9 @@ gy_status gy_initialize(gy_solver *h, const gy_material *mats, int nmat, const g
             c[a] = ci;
             F(PF_OX + a, i) = (float)off;
         }
-        I(PF_KEY, i) = c[0] + c[1] * h->g.ncx + (h->g.is3d ? c[2] * h->g.ncx * h->g.ncy : 0);
+        I(PF_KEY, i) = encode_key(c[0], c[1], h->g.is3d ? c[2] : 0, h->g);
+        h->key0[i] = I(PF_KEY, i);
+        for (int a = 0; a < 3; a++) h->off0[3 * i + a] = F(PF_OX + a, i);
         for (int k = 0; k < 3; k++) F(PF_VX + k, i) = (float)h->vel[3 * i + k];
         for (int k = 0; k < 6; k++) F(PF_S0 + k, i) = (float)h->stress[6 * i + k];
         const gy_material &M = mats[h->mat[i]];
@@ -556,18 +580,15 @@ gy_status gy_initialize(gy_solver *h, const gy_material *mats, int nmat, const g
         h->ws.cap = h->cap;
         h->ws.nblocks_cap = (int)nbk;
     }
-    if ((st = dalloc(h, &h->d_keys, h->cap))) return st;
     if ((st = dalloc(h, &h->d_perm, h->cap))) return st;
-    // fields carried by the permutation
-    std::vector<int> fields;
-    for (int f = PF_OX; f <= PF_PID; f++) fields.push_back(f);
-    if (h->has_dp)
-        for (int f = PF_EQPS; f <= PF_SMAX; f++) fields.push_back(f);
-    if (h->opt.track_normals)
-        for (int f = PF_NX; f <= PF_NZ; f++) fields.push_back(f);
-    h->nfields = (int)fields.size();
-    if ((st = dalloc(h, &h->d_fields, fields.size()))) return st;
-    CK(h, cudaMemcpyAsync(h->d_fields, fields.data(), fields.size() * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    if ((st = dalloc(h, &h->d_seg, h->cap))) return st;
+    if ((st = dalloc(h, &h->d_nseg, 4))) return st;
+    {
+        int dev = 0, sms = 1;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        h->persist_grid = sms * g2p2g_blocks_per_sm(h->has_dp);
+    }
     if ((st = alloc_nodes(h))) return st;
     CK(h, cudaStreamSynchronize(h->stream));
     h->initialized = true;
@@ -575,6 +596,7 @@ gy_status gy_initialize(gy_solver *h, const gy_material *mats, int nmat, const g
     h->t_prev = 0.0;
     h->since_sort = 1 << 30;
     h->tables_valid = false;
+    h->acc_ready = false;
     return GY_OK;
 }
 
@@ -657,35 +679,46 @@ static gy_status enqueue_step(gy_solver *h, double t, int step)
         h->tev_used++;
         cudaEventRecord(tev[0], s);
     }
-    // (a) counting sort by cell + permutation of the particle state
+    // (a) stable counting sort of the cell keys; the particle kernels read through perm
+    const int *perm = nullptr;
+    const int *skey = reinterpret_cast<const int *>(h->slab[h->cur]) + (size_t)PF_KEY * h->cap;
     if (h->since_sort >= h->opt.sort_every) {
         int key_bits = 1;
-        while ((1LL << key_bits) < h->g.nc) key_bits++;
-        launch_extract_keys(pview(h, h->cur), h->n, h->d_keys, s);
-        sort_pairs(h->d_keys, h->d_perm, h->n, key_bits, h->ws, s);
-        launch_permute(h->slab[h->cur], h->slab[h->cur ^ 1], h->cap, h->n, h->d_perm, h->d_fields, h->nfields, s);
-        h->cur ^= 1;
+        const long long maxkey = (long long)h->g.nbx * h->g.nby * h->g.nbz * 64;
+        while ((1LL << key_bits) < maxkey) key_bits++;
+        skey = sort_pairs(skey, h->d_perm, h->n, key_bits, h->ws, s);
+        perm = h->d_perm;
         h->since_sort = 0;
     }
     h->since_sort++;
-    PView P = pview(h, h->cur);
+    launch_block_heads(skey, h->n, h->d_seg, h->d_nseg, s);
+    PView src = pview(h, h->cur), dst = pview(h, h->cur ^ 1);
     // body slots from the sort table of the reference's cadence (Solver.cpp:91)
     if (h->multi && ((step % 10 == 0) || step == 1 || !h->tables_valid)) {
-        launch_body_tables(P, h->n, a, h->d_cell_min, h->nbody, h->steps == 0 ? h->d_refkey0 : nullptr, s);
+        launch_body_tables(src, h->n, a, h->d_cell_min, h->nbody, h->steps == 0 ? h->d_refkey0 : nullptr, s);
         launch_body_assign(h->nb, a, h->d_cell_min, h->nbody, h->d_nidx[0], h->d_nidx[1], h->d_nidx[2], s);
         h->tables_valid = true;
     }
     if (timing) cudaEventRecord(tev[1], s);
-    // (b) P2G
-    launch_p2g(P, h->n, h->nb, a, h->opt.p2g_tile, h->opt.block_particles, s);
+    // (b) P2G, unless the previous step's fused pass already accumulated it
+    if (h->multi || !h->acc_ready)
+        launch_p2g(src, perm, skey, h->n, h->d_seg, h->d_nseg, h->persist_grid, h->nb, a, s);
     if (timing) cudaEventRecord(tev[2], s);
     // (c) periodic fold, nodal solve, grid BCs
     launch_fold(h->nb, a, s);
     launch_solve(h->nb, a, h->opt.keep_node_fields != 0, s);
     if (timing) cudaEventRecord(tev[3], s);
-    // (d) G2P + particle BCs + update + constitutive + damage
-    launch_g2p_update(P, h->n, h->nb, a, h->opt.track_normals != 0, h->opt.check_finite != 0, h->has_dp,
-                      h->opt.block_particles, s);
+    // (d) G2P + particle BCs + update + constitutive + damage (+ next step's P2G)
+    if (h->multi) {
+        launch_g2p_update(src, dst, perm, h->n, h->nb, a, h->opt.track_normals != 0, h->opt.check_finite != 0,
+                          h->has_dp, s);
+        h->acc_ready = false;
+    } else {
+        launch_g2p2g(src, dst, perm, skey, h->n, h->d_seg, h->d_nseg, h->persist_grid, h->nb, a,
+                     h->opt.check_finite != 0, h->has_dp, s);
+        h->acc_ready = true;
+    }
+    h->cur ^= 1;
     if (timing) cudaEventRecord(tev[4], s);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(h, GY_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
@@ -786,16 +819,17 @@ gy_status gy_get_particles(gy_solver *h, int field, double *out, int64_t count)
         switch (field) {
         case GY_P_POS:
         case GY_P_DISP: {
-            int c[3];
-            const int key = I(PF_KEY, i);
-            c[2] = h->g.is3d ? key / (h->g.ncx * h->g.ncy) : 0;
-            const int r = key - c[2] * h->g.ncx * h->g.ncy;
-            c[1] = r / h->g.ncx;
-            c[0] = r - c[1] * h->g.ncx;
+            // displacement from the change of (cell, FP32 offset) since upload, so that a
+            // particle that has not moved reports exactly zero; position = pos0 + disp
+            int c[3], c0[3];
+            auto split = [&](int key, int *cc) { decode_key(key, h->g, cc[0], cc[1], cc[2]); };
+            split(I(PF_KEY, i), c);
+            split(h->key0[pid], c0);
             for (int k = 0; k < 3; k++) {
-                double x = (c[k] + (double)F(PF_OX + k, i)) * hh;
-                if (k == 2 && !h->g.is3d) x = h->pos[3 * pid + 2];
-                o[k] = field == GY_P_POS ? x : x - h->pos[3 * pid + k];
+                double d = 0.0;
+                if (k < 2 || h->g.is3d)
+                    d = ((double)(c[k] - c0[k]) + ((double)F(PF_OX + k, i) - (double)h->off0[3 * pid + k])) * hh;
+                o[k] = field == GY_P_POS ? h->pos[3 * pid + k] + d : d;
             }
             break;
         }
@@ -858,12 +892,8 @@ gy_status gy_get_particles_int(gy_solver *h, int field, int *out, int64_t count)
                 out[pid] = ix + iy * (h->nx - 1) + iz * (h->nx - 1) * (h->ny - 1);
                 break;
             }
-            const int key = I(PF_KEY, i);
             int c[3];
-            c[2] = h->g.is3d ? key / (h->g.ncx * h->g.ncy) : 0;
-            const int r = key - c[2] * h->g.ncx * h->g.ncy;
-            c[1] = r / h->g.ncx;
-            c[0] = r - c[1] * h->g.ncx;
+            decode_key(I(PF_KEY, i), h->g, c[0], c[1], c[2]);
             int id[3] = {0, 0, 0};
             for (int k = 0; k < (h->g.is3d ? 3 : 2); k++) id[k] = (int)((c[k] + (double)F(PF_OX + k, i)) - 0.25);
             out[pid] = id[0] + id[1] * (h->nx - 1) + id[2] * (h->nx - 1) * (h->ny - 1);
@@ -909,8 +939,7 @@ gy_status gy_get_stats(gy_solver *h, gy_stats *out)
     std::memset(out, 0, sizeof(*out));
     if (!h->initialized) return GY_OK;
     cudaSetDevice(h->device);
-    StepArgs a = make_args(h, 0.0, 0);
-    launch_stats(pview(h, h->cur), h->n, a, h->d_stats, h->stream);
+    launch_stats(pview(h, h->cur), h->n, h->d_stats, h->stream);
     double v[8];
     int flags[4];
     CK(h, cudaMemcpyAsync(v, h->d_stats, sizeof(v), cudaMemcpyDeviceToHost, h->stream));
@@ -1006,7 +1035,7 @@ gy_status gy_sort_keys(const int *keys, int64_t n, int *perm_out, int device)
         ws.cap = n;
         ws.nblocks_cap = (int)nbk;
         cudaMemcpyAsync(d_in, keys, n * sizeof(int), cudaMemcpyHostToDevice, s);
-        sort_pairs(d_in, d_perm, n, bits, ws, s);
+        (void)sort_pairs(d_in, d_perm, n, bits, ws, s);
         cudaMemcpyAsync(perm_out, d_perm, n * sizeof(int), cudaMemcpyDeviceToHost, s);
         if (cudaStreamSynchronize(s) != cudaSuccess) st = GY_ERR_CUDA;
     }

@@ -67,6 +67,9 @@ constexpr int MAX_BODIES = 16;
 struct GridGeom {
     int nx, ny, nz;           // nodes per axis
     int ncx, ncy, ncz;        // cells per axis (ncz = 1 in 2D)
+    int nbx, nby, nbz;        // 4x4x4 cell blocks per axis (nbz = 1 in 2D)
+    int nnbx, nnby, nnbz;     // 4x4x4 node blocks per axis
+    long long nnb;            // node blocks
     long long nn;             // nodes
     long long nc;             // cells
     float h, inv_h;           // cell size
@@ -120,12 +123,38 @@ __device__ __forceinline__ void gimp_axis(float u, float l, float S[3], float G[
     }
 }
 
-__device__ __forceinline__ void decode_key(int key, const GridGeom &g, int &ci, int &cj, int &ck)
+// Cell keys are block-major: 4x4x4 cell blocks in x-fastest order, cells x-fastest inside
+// a block, key = block * 64 + (lz*4 + ly)*4 + lx.  Sorting by key groups each block's
+// particles contiguously, which the tiled P2G needs.
+constexpr int CB = 4;           // cells per block edge
+constexpr int CB_SHIFT = 6;     // log2(CB^3)
+
+__host__ __device__ __forceinline__ int encode_key(int ci, int cj, int ck, const GridGeom &g)
 {
-    ck = key / (g.ncx * g.ncy);
-    int r = key - ck * g.ncx * g.ncy;
-    cj = r / g.ncx;
-    ci = r - cj * g.ncx;
+    const int blk = ((ck >> 2) * g.nby + (cj >> 2)) * g.nbx + (ci >> 2);
+    return (blk << CB_SHIFT) | ((ck & 3) << 4) | ((cj & 3) << 2) | (ci & 3);
+}
+
+__host__ __device__ __forceinline__ void decode_block(int blk, const GridGeom &g, int &bx, int &by, int &bz)
+{
+    bx = blk % g.nbx;
+    const int t = blk / g.nbx;
+    by = t % g.nby;
+    bz = t / g.nby;
+}
+
+__host__ __device__ __forceinline__ void decode_key(int key, const GridGeom &g, int &ci, int &cj, int &ck)
+{
+    int bx, by, bz;
+    decode_block(key >> CB_SHIFT, g, bx, by, bz);
+    ci = (bx << 2) | (key & 3);
+    cj = (by << 2) | ((key >> 2) & 3);
+    ck = (bz << 2) | ((key >> 4) & 3);
+}
+
+__host__ __device__ __forceinline__ long long node_block(int i, int j, int k, const GridGeom &g)
+{
+    return ((long long)(k >> 2) * g.nnby + (j >> 2)) * g.nnbx + (i >> 2);
 }
 
 __device__ __forceinline__ long long node_index(int i, int j, int k, const GridGeom &g)

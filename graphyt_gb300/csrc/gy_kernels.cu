@@ -1,16 +1,23 @@
 // gy_kernels.cu -- the GB300 kernels of one explicit GIMP MPM step.
 //
-//   P2G        particle-centric scatter of mass, momentum, internal+external force (and,
-//              with several bodies, per-body fields and normals) into the node grid.  The
-//              reference gathers per node over a 4x4x4 cell window (Extrapolation.cpp:31-125,
-//              166-286); a particle contributes to exactly the nodes of its GIMP support,
-//              so scattering over the 3x3x3 stencil sums the same terms.
-//   fold       periodic node-layer fold (Grid.cpp:310-795), one launch per axis.
-//   solve      nodal momentum update, contact and grid BCs (Grid.cpp:9-245, 862-1094).
-//   G2P+update gather of grid velocity/acceleration/strain rate (Extrapolation.cpp:127-163,
-//              288-367), particle BCs (TimeIntegration.cpp:177-296), particle update,
-//              constitutive + damage, periodic wrap and the new cell key
-//              (TimeIntegration.cpp:11-117), fused in one pass over the particles.
+// Data flow of a step (single body, the fast path):
+//   sort      stable counting sort of the particle cell keys (gy_sort.cu) -> perm, plus the
+//             list of non-empty 4x4x4 cell blocks ("segments");
+//   fold      periodic node-layer fold of the accumulated P2G fields (Grid.cpp:310-795);
+//   solve     nodal momentum update + grid BCs over the active 4x4x4 node blocks only
+//             (Grid.cpp:9-245, 862-1094); it also clears the accumulators it read;
+//   G2P2G     one pass over the particles in sorted order: G2P (Extrapolation.cpp:127-163,
+//             288-367), particle BCs (TimeIntegration.cpp:177-296), update + constitutive +
+//             damage + wrap (TimeIntegration.cpp:11-117), the state written back in sorted
+//             order, and the *next* step's P2G (Extrapolation.cpp:166-286) scattered from
+//             the updated state into a shared-memory node tile, flushed with vector
+//             reductions.  Each particle's state is read once and written once per step.
+// The first step (and every step of multi-body problems, whose body slots depend on the
+// whole particle set) runs a standalone P2G before the fold.
+//
+// P2G is a particle-centric scatter: the reference gathers per node over a 4x4x4 cell
+// window (Extrapolation.cpp:31-125), but a particle contributes exactly to the nodes of its
+// GIMP support, so scattering over its 3x3x3 stencil sums the same terms.
 #include <atomic>
 #include <cstdio>
 
@@ -24,137 +31,343 @@ void note_launch(int k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
 long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 // ---------------------------------------------------------------------------------------
-// P2G
-
-__device__ __forceinline__ void red_add(float *a, float v)
-{
-    if (v != 0.0f) atomicAdd(a, v);
-}
+// helpers
 
 __device__ __forceinline__ void red_add4(float4 *a, float x, float y, float z, float w)
 {
-    // vector reduction into global memory (sm_90+): one request for four floats
+    // one vector reduction request for four floats into global memory (sm_90+)
     asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(a), "f"(x), "f"(y), "f"(z), "f"(w)
                  : "memory");
 }
 
-template <bool MULTI>
-__global__ void __launch_bounds__(256) k_p2g_global(PView P, long long n, NodeBufs nb, StepArgs a)
+__device__ __forceinline__ void mark_node(unsigned char *flags, int i, int j, int k, const GridGeom &g)
+{
+    flags[node_block(i, j, k, g)] = 1;
+}
+
+struct PState {
+    int key, pid;
+    uint32_t info;
+    float o[3], v[3], s[6], e[6], rho, mass;
+    float eqps, ep[6], dmg, smax;
+};
+
+template <bool HAS_DP>
+__device__ __forceinline__ void load_state(const PView &P, long long j, PState &st)
+{
+    st.key = P.ii(PF_KEY, j);
+    st.info = (uint32_t)P.ii(PF_INFO, j);
+    st.pid = P.ii(PF_PID, j);
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        st.o[k] = P.f(PF_OX + k, j);
+        st.v[k] = P.f(PF_VX + k, j);
+    }
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        st.s[k] = P.f(PF_S0 + k, j);
+        st.e[k] = P.f(PF_E0 + k, j);
+    }
+    st.rho = P.f(PF_RHO, j);
+    st.mass = P.f(PF_MASS, j);
+    if (HAS_DP) {
+        st.eqps = P.f(PF_EQPS, j);
+#pragma unroll
+        for (int k = 0; k < 6; k++) st.ep[k] = P.f(PF_EP0 + k, j);
+        st.dmg = P.f(PF_DMG, j);
+        st.smax = P.f(PF_SMAX, j);
+    } else {
+        st.eqps = 0.f;
+#pragma unroll
+        for (int k = 0; k < 6; k++) st.ep[k] = 0.f;
+        st.dmg = 0.f;
+        st.smax = 0.f;
+    }
+}
+
+template <bool HAS_DP>
+__device__ __forceinline__ void store_state(const PView &P, long long i, const PState &st)
+{
+    P.ii(PF_KEY, i) = st.key;
+    P.ii(PF_INFO, i) = (int)st.info;
+    P.ii(PF_PID, i) = st.pid;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        P.f(PF_OX + k, i) = st.o[k];
+        P.f(PF_VX + k, i) = st.v[k];
+    }
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        P.f(PF_S0 + k, i) = st.s[k];
+        P.f(PF_E0 + k, i) = st.e[k];
+    }
+    P.f(PF_RHO, i) = st.rho;
+    P.f(PF_MASS, i) = st.mass;
+    if (HAS_DP) {
+        P.f(PF_EQPS, i) = st.eqps;
+#pragma unroll
+        for (int k = 0; k < 6; k++) P.f(PF_EP0 + k, i) = st.ep[k];
+        P.f(PF_DMG, i) = st.dmg;
+        P.f(PF_SMAX, i) = st.smax;
+    }
+}
+
+// register-array element with a run-time index, without spilling the array to local memory
+__device__ __forceinline__ float sel3(const float a[3], int i) { return i == 0 ? a[0] : (i == 1 ? a[1] : a[2]); }
+
+// GIMP weights of a particle: S/G per axis and how many stencil nodes carry weight
+struct Stencil {
+    int c[3];
+    float S[3][3], G[3][3];
+    int cnt[3];
+};
+
+__device__ __forceinline__ void make_stencil(const PState &st, const GridGeom &g, Stencil &w)
+{
+    decode_key(st.key, g, w.c[0], w.c[1], w.c[2]);
+    gimp_axis(st.o[0], g.lp, w.S[0], w.G[0]);
+    gimp_axis(st.o[1], g.lp, w.S[1], w.G[1]);
+    w.cnt[0] = (st.o[0] < 1.0f - g.lp) ? 2 : 3;
+    w.cnt[1] = (st.o[1] < 1.0f - g.lp) ? 2 : 3;
+    if (g.is3d) {
+        gimp_axis(st.o[2], g.lp, w.S[2], w.G[2]);
+        w.cnt[2] = (st.o[2] < 1.0f - g.lp) ? 2 : 3;
+    } else {
+        w.c[2] = 0;
+        w.S[2][0] = 1.f; w.S[2][1] = 0.f; w.S[2][2] = 0.f;
+        w.G[2][0] = 0.f; w.G[2][1] = 0.f; w.G[2][2] = 0.f;
+        w.cnt[2] = 1;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// P2G of one particle, single-body: mass, momentum and internal force.  Gravity is added
+// per node in the solve as m_node * g, which equals sum_p w m_p g (Extrapolation.cpp:226-278).
+
+constexpr int TILE = 8;                 // node tile edge: a cell block's stencil nodes +- 1
+constexpr int TILE_NODES = TILE * TILE * TILE;
+constexpr int TILE_FIELDS = 7;          // m, px, py, pz, fx, fy, fz
+
+__device__ __forceinline__ void p2g_single(const PState &st, const GridGeom &g, float *tile, int tox, int toy, int toz,
+                                           const NodeBufs &nb, int rot)
+{
+    Stencil w;
+    make_stencil(st, g, w);
+    const float m = st.mass;
+    const float sc = (m / st.rho) * g.inv_h;  // V sigma with the gradient's 1/h
+    const float s0 = st.s[0] * sc, s1 = st.s[1] * sc, s2 = st.s[2] * sc;
+    const float s3 = st.s[3] * sc, s4 = st.s[4] * sc, s5 = st.s[5] * sc;
+    const float mvx = m * st.v[0], mvy = m * st.v[1], mvz = m * st.v[2];
+    const int ti = w.c[0] - tox, tj = w.c[1] - toy, tk = w.c[2] - toz;
+    const bool in_tile = tile && ti >= 0 && tj >= 0 && tk >= 0 && ti + w.cnt[0] <= TILE && tj + w.cnt[1] <= TILE &&
+                         tk + w.cnt[2] <= TILE;
+    const int nxy = w.cnt[0] * w.cnt[1];
+    const int total = nxy * w.cnt[2];
+    for (int q0 = 0; q0 < total; q0++) {
+        // rotate the visiting order per lane so that particles of one cell hit different nodes
+        int q = q0 + rot;
+        while (q >= total) q -= total;
+        const int kk = q / nxy;
+        const int r = q - kk * nxy;
+        const int jj = r / w.cnt[0];
+        const int ii = r - jj * w.cnt[0];
+        const float sx = sel3(w.S[0], ii), sy = sel3(w.S[1], jj), sz = sel3(w.S[2], kk);
+        const float syz = sy * sz;
+        const float wgt = sx * syz;
+        const float gx = sel3(w.G[0], ii) * syz;
+        const float gy = sx * sel3(w.G[1], jj) * sz;
+        const float gz = sx * sy * sel3(w.G[2], kk);
+        const float fx = -(gx * s0 + gy * s3 + gz * s5);
+        const float fy = -(gx * s3 + gy * s1 + gz * s4);
+        const float fz = -(gx * s5 + gy * s4 + gz * s2);
+        if (in_tile) {
+            const int t = ((tk + kk) * TILE + (tj + jj)) * TILE + (ti + ii);
+            atomicAdd(&tile[0 * TILE_NODES + t], wgt * m);
+            atomicAdd(&tile[1 * TILE_NODES + t], wgt * mvx);
+            atomicAdd(&tile[2 * TILE_NODES + t], wgt * mvy);
+            atomicAdd(&tile[3 * TILE_NODES + t], wgt * mvz);
+            atomicAdd(&tile[4 * TILE_NODES + t], fx);
+            atomicAdd(&tile[5 * TILE_NODES + t], fy);
+            atomicAdd(&tile[6 * TILE_NODES + t], fz);
+        } else {
+            const int ni = w.c[0] + ii, nj = w.c[1] + jj, nk = w.c[2] + kk;
+            const long long nd = node_index(ni, nj, nk, g);
+            red_add4(&nb.acc0[nd], wgt * m, wgt * mvx, wgt * mvy, wgt * mvz);
+            red_add4(&nb.acc1[nd], fx, fy, fz, 0.f);
+            mark_node(nb.flags, ni, nj, nk, g);
+        }
+    }
+}
+
+__device__ __forceinline__ void tile_zero(float *tile)
+{
+    for (int t = threadIdx.x; t < TILE_FIELDS * TILE_NODES; t += blockDim.x) tile[t] = 0.f;
+}
+
+__device__ __forceinline__ void tile_flush(const float *tile, int tox, int toy, int toz, const GridGeom &g,
+                                           const NodeBufs &nb)
+{
+    for (int t = threadIdx.x; t < TILE_NODES; t += blockDim.x) {
+        const float m = tile[t], px = tile[TILE_NODES + t], py = tile[2 * TILE_NODES + t],
+                    pz = tile[3 * TILE_NODES + t];
+        const float fx = tile[4 * TILE_NODES + t], fy = tile[5 * TILE_NODES + t], fz = tile[6 * TILE_NODES + t];
+        if (m == 0.f && px == 0.f && py == 0.f && pz == 0.f && fx == 0.f && fy == 0.f && fz == 0.f) continue;
+        const int ni = tox + (t % TILE), nj = toy + ((t / TILE) % TILE), nk = toz + t / (TILE * TILE);
+        if (ni < 0 || nj < 0 || nk < 0 || ni >= g.nx || nj >= g.ny || nk >= g.nz) continue;
+        const long long nd = node_index(ni, nj, nk, g);
+        red_add4(&nb.acc0[nd], m, px, py, pz);
+        red_add4(&nb.acc1[nd], fx, fy, fz, 0.f);
+        mark_node(nb.flags, ni, nj, nk, g);
+    }
+}
+
+// Segment bounds: segments start where the cell block of the sorted key changes.
+__device__ __forceinline__ int seg_block(const int *skey, int start) { return skey[start] >> CB_SHIFT; }
+
+__device__ __forceinline__ void tile_origin(int blk, const GridGeom &g, int &tox, int &toy, int &toz)
+{
+    int bx, by, bz;
+    decode_block(blk, g, bx, by, bz);
+    tox = bx * CB - 1;
+    toy = by * CB - 1;
+    toz = g.is3d ? bz * CB - 1 : 0;
+}
+
+// Standalone tiled P2G over the segments (single body).
+__global__ void __launch_bounds__(256) k_p2g_tiled(PView P, const int *perm, const int *skey, long long n,
+                                                    const int *seg_start, const int *nseg_ptr, NodeBufs nb, GridGeom g)
+{
+    __shared__ float tile[TILE_FIELDS * TILE_NODES];
+    const int nseg = *nseg_ptr;
+    for (int sgi = blockIdx.x; sgi < nseg; sgi += gridDim.x) {
+        const int start = seg_start[sgi];
+        const int blk = seg_block(skey, start);
+        int tox, toy, toz;
+        tile_origin(blk, g, tox, toy, toz);
+        tile_zero(tile);
+        __syncthreads();
+        for (long long base = start;; base += blockDim.x) {
+            const long long i = base + threadIdx.x;
+            const bool valid = i < n && (skey[i] >> CB_SHIFT) == blk;
+            if (!__syncthreads_or(valid)) break;
+            if (valid) {
+                PState st;
+                load_state<false>(P, perm ? perm[i] : i, st);
+                p2g_single(st, g, tile, tox, toy, toz, nb, threadIdx.x & 31);
+            }
+        }
+        __syncthreads();
+        tile_flush(tile, tox, toy, toz, g, nb);
+        __syncthreads();
+    }
+}
+
+// Multi-body P2G: centre-of-mass fields plus the particle's body slot (Extrapolation.cpp:
+// 191-256): per-body gravity skips rigid particles, normals use the stored volume.
+__global__ void __launch_bounds__(256) k_p2g_multi(PView P, const int *perm, long long n, NodeBufs nb, StepArgs a)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const GridGeom &g = a.g;
-    const uint32_t info = (uint32_t)P.ii(PF_INFO, i);
-    const int key = P.ii(PF_KEY, i);
-    int ci, cj, ck;
-    decode_key(key, g, ci, cj, ck);
-    float Sx[3], Gx[3], Sy[3], Gy[3], Sz[3] = {1.f, 0.f, 0.f}, Gz[3] = {0.f, 0.f, 0.f};
-    const float ox = P.f(PF_OX, i), oy = P.f(PF_OY, i);
-    gimp_axis(ox, g.lp, Sx, Gx);
-    gimp_axis(oy, g.lp, Sy, Gy);
-    int nkz = 1;
-    if (g.is3d) {
-        const float oz = P.f(PF_OZ, i);
-        gimp_axis(oz, g.lp, Sz, Gz);
-        nkz = (oz < 1.0f - g.lp) ? 2 : 3;
-    } else {
-        ck = 0;
-    }
-    const int nix = (ox < 1.0f - g.lp) ? 2 : 3;
-    const int njy = (oy < 1.0f - g.lp) ? 2 : 3;
-    const float m = P.f(PF_MASS, i);
-    const float rho = P.f(PF_RHO, i);
-    const float vx = P.f(PF_VX, i), vy = P.f(PF_VY, i), vz = P.f(PF_VZ, i);
-    const float Vf = m / rho;  // force volume m/rho (Extrapolation.cpp:221)
-    // V * sigma, with the 1/h of the gradient folded in
+    PState st;
+    load_state<false>(P, perm ? perm[i] : i, st);
+    Stencil w;
+    make_stencil(st, g, w);
+    const float m = st.mass;
+    const float Vf = m / st.rho;
     const float sc = Vf * g.inv_h;
-    const float s0 = P.f(PF_S0, i) * sc, s1 = P.f(PF_S1, i) * sc, s2 = P.f(PF_S2, i) * sc;
-    const float s3 = P.f(PF_S3, i) * sc, s4 = P.f(PF_S4, i) * sc, s5 = P.f(PF_S5, i) * sc;
+    const float s0 = st.s[0] * sc, s1 = st.s[1] * sc, s2 = st.s[2] * sc;
+    const float s3 = st.s[3] * sc, s4 = st.s[4] * sc, s5 = st.s[5] * sc;
     const float mgx = m * a.sc.gravity[0], mgy = m * a.sc.gravity[1], mgz = m * a.sc.gravity[2];
-    const bool rigid = (info & INFO_RIGID) != 0;
-    const int obj = info_obj(info);
-    const float vol_n = ((info & INFO_INIT_VOL) ? a.sc.init_volume : Vf) * g.inv_h;  // normals use the stored volume
-    for (int kk = 0; kk < nkz; kk++)
-        for (int jj = 0; jj < njy; jj++) {
-            const float syz = Sy[jj] * Sz[kk], gyz = Gy[jj] * Sz[kk], syg = Sy[jj] * Gz[kk];
-            for (int ii = 0; ii < nix; ii++) {
-                const float w = Sx[ii] * syz;
-                const float gx = Gx[ii] * syz, gy = Sx[ii] * gyz, gz = Sx[ii] * syg;
-                const long long nd = node_index(ci + ii, cj + jj, ck + kk, g);
-                const float wm = w * m;
+    const bool rigid = (st.info & INFO_RIGID) != 0;
+    const int obj = info_obj(st.info);
+    const float vol_n = ((st.info & INFO_INIT_VOL) ? a.sc.init_volume : Vf) * g.inv_h;
+#pragma unroll
+    for (int kk = 0; kk < 3; kk++)
+#pragma unroll
+        for (int jj = 0; jj < 3; jj++)
+#pragma unroll
+            for (int ii = 0; ii < 3; ii++) {
+                if (kk >= w.cnt[2] || jj >= w.cnt[1] || ii >= w.cnt[0]) continue;
+                const float syz = w.S[1][jj] * w.S[2][kk];
+                const float wgt = w.S[0][ii] * syz;
+                const float gx = w.G[0][ii] * syz;
+                const float gy = w.S[0][ii] * w.G[1][jj] * w.S[2][kk];
+                const float gz = w.S[0][ii] * w.S[1][jj] * w.G[2][kk];
+                const int ni = w.c[0] + ii, nj = w.c[1] + jj, nk = w.c[2] + kk;
+                const long long nd = node_index(ni, nj, nk, g);
+                const float wm = wgt * m;
                 const float fx = -(gx * s0 + gy * s3 + gz * s5);
                 const float fy = -(gx * s3 + gy * s1 + gz * s4);
                 const float fz = -(gx * s5 + gy * s4 + gz * s2);
-                red_add4(&nb.acc0[nd], wm, wm * vx, wm * vy, wm * vz);
-                red_add4(&nb.acc1[nd], fx + w * mgx, fy + w * mgy, fz + w * mgz, 0.0f);
-                if (MULTI) {
-                    const int2 b = nb.body[nd];
-                    const int slot = (b.x == obj) ? 0 : ((b.y == obj) ? 1 : -1);
-                    if (slot >= 0) {
-                        red_add4(&nb.bacc0[slot][nd], wm, wm * vx, wm * vy, wm * vz);
-                        if (rigid) red_add4(&nb.bacc1[slot][nd], fx, fy, fz, 0.0f);
-                        else red_add4(&nb.bacc1[slot][nd], fx + w * mgx, fy + w * mgy, fz + w * mgz, 0.0f);
-                        red_add4(&nb.bnrm[slot][nd], gx * vol_n, gy * vol_n, gz * vol_n, 0.0f);
-                    }
+                red_add4(&nb.acc0[nd], wm, wm * st.v[0], wm * st.v[1], wm * st.v[2]);
+                red_add4(&nb.acc1[nd], fx + wgt * mgx, fy + wgt * mgy, fz + wgt * mgz, 0.0f);
+                const int2 b = nb.body[nd];
+                const int slot = (b.x == obj) ? 0 : ((b.y == obj) ? 1 : -1);
+                if (slot >= 0) {
+                    red_add4(&nb.bacc0[slot][nd], wm, wm * st.v[0], wm * st.v[1], wm * st.v[2]);
+                    if (rigid) red_add4(&nb.bacc1[slot][nd], fx, fy, fz, 0.0f);
+                    else red_add4(&nb.bacc1[slot][nd], fx + wgt * mgx, fy + wgt * mgy, fz + wgt * mgz, 0.0f);
+                    red_add4(&nb.bnrm[slot][nd], gx * vol_n, gy * vol_n, gz * vol_n, 0.0f);
                 }
+                mark_node(nb.flags, ni, nj, nk, g);
             }
-        }
 }
 
-void launch_p2g(const PView &p, long long n, const NodeBufs &nb, const StepArgs &a, int tile, int block, cudaStream_t s)
+void launch_p2g(const PView &p, const int *perm, const int *skey, long long n, const int *seg_start,
+                const int *nseg, int persist_grid, const NodeBufs &nb, const StepArgs &a, cudaStream_t s)
 {
-    (void)tile;
-    (void)block;
     if (n == 0) return;
-    const int B = 256;
-    const unsigned grid = (unsigned)((n + B - 1) / B);
     if (a.sc.multi_body) {
-        k_p2g_global<true><<<grid, B, 0, s>>>(p, n, nb, a);
-        note_launch(1);
+        k_p2g_multi<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p, perm, n, nb, a);
+    } else {
+        k_p2g_tiled<<<persist_grid, 256, 0, s>>>(p, perm, skey, n, seg_start, nseg, nb, a.g);
     }
-    else {
-        k_p2g_global<false><<<grid, B, 0, s>>>(p, n, nb, a);
-        note_launch(1);
-    }
+    note_launch(1);
 }
 
 // ---------------------------------------------------------------------------------------
 // periodic fold, Grid.cpp:310-795: node i and node N-3+i (i < 3) both take their sum, for
 // mass, momentum and force of the centre-of-mass field and both body fields.
 
-__device__ __forceinline__ void fold4(float4 *arr, long long p, long long q)
+__device__ __forceinline__ bool fold4(float4 *arr, long long p, long long q)
 {
-    float4 x = arr[p], y = arr[q];
-    float4 s = make_float4(x.x + y.x, x.y + y.y, x.z + y.z, x.w + y.w);
+    const float4 x = arr[p], y = arr[q];
+    const float4 s = make_float4(x.x + y.x, x.y + y.y, x.z + y.z, x.w + y.w);
     arr[p] = s;
     arr[q] = s;
+    return s.x != 0.f || s.y != 0.f || s.z != 0.f || s.w != 0.f;
 }
 
 template <bool MULTI>
 __global__ void k_fold(NodeBufs nb, GridGeom g, int axis)
 {
-    // pairs: 3 layers x the plane orthogonal to `axis`
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    int d0, d1, l;  // plane extents
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int d0, d1;
     if (axis == 0) { d0 = g.ny; d1 = g.nz; }
     else if (axis == 1) { d0 = g.nx; d1 = g.nz; }
     else { d0 = g.nx; d1 = g.ny; }
     const long long plane = (long long)d0 * d1;
     if (t >= 3 * plane) return;
-    l = (int)(t / plane);
+    const int l = (int)(t / plane);
     const long long r = t - (long long)l * plane;
     const int a0 = (int)(r % d0), a1 = (int)(r / d0);
-    long long p, q;
-    if (axis == 0) { p = node_index(l, a0, a1, g); q = node_index(g.nx - 3 + l, a0, a1, g); }
-    else if (axis == 1) { p = node_index(a0, l, a1, g); q = node_index(a0, g.ny - 3 + l, a1, g); }
-    else { p = node_index(a0, a1, l, g); q = node_index(a0, a1, g.nz - 3 + l, g); }
-    fold4(nb.acc0, p, q);
-    fold4(nb.acc1, p, q);
+    int pi, pj, pk, qi, qj, qk;
+    if (axis == 0) { pi = l; pj = a0; pk = a1; qi = g.nx - 3 + l; qj = a0; qk = a1; }
+    else if (axis == 1) { pi = a0; pj = l; pk = a1; qi = a0; qj = g.ny - 3 + l; qk = a1; }
+    else { pi = a0; pj = a1; pk = l; qi = a0; qj = a1; qk = g.nz - 3 + l; }
+    const long long p = node_index(pi, pj, pk, g), q = node_index(qi, qj, qk, g);
+    bool any = fold4(nb.acc0, p, q);
+    any |= fold4(nb.acc1, p, q);
     if (MULTI) {
         for (int b = 0; b < 2; b++) {
-            fold4(nb.bacc0[b], p, q);
-            fold4(nb.bacc1[b], p, q);
+            any |= fold4(nb.bacc0[b], p, q);
+            any |= fold4(nb.bacc1[b], p, q);
         }
+    }
+    if (any) {
+        mark_node(nb.flags, pi, pj, pk, g);
+        mark_node(nb.flags, qi, qj, qk, g);
     }
 }
 
@@ -163,28 +376,21 @@ void launch_fold(const NodeBufs &nb, const StepArgs &a, cudaStream_t s)
     const GridGeom &g = a.g;
     const int naxes = g.is3d ? 3 : 2;
     for (int ax = 0; ax < naxes; ax++) {
-        long long plane = ax == 0 ? (long long)g.ny * g.nz : ax == 1 ? (long long)g.nx * g.nz : (long long)g.nx * g.ny;
-        long long total = 3 * plane;
-        unsigned grid = (unsigned)((total + 255) / 256);
-        if (a.sc.multi_body) {
-            k_fold<true><<<grid, 256, 0, s>>>(nb, g, ax);
-            note_launch(1);
-        }
-        else {
-            k_fold<false><<<grid, 256, 0, s>>>(nb, g, ax);
-            note_launch(1);
-        }
+        const long long plane = ax == 0 ? (long long)g.ny * g.nz : ax == 1 ? (long long)g.nx * g.nz : (long long)g.nx * g.ny;
+        const unsigned grid = (unsigned)((3 * plane + 255) / 256);
+        if (a.sc.multi_body) k_fold<true><<<grid, 256, 0, s>>>(nb, g, ax);
+        else k_fold<false><<<grid, 256, 0, s>>>(nb, g, ax);
+        note_launch(1);
     }
 }
 
 // ---------------------------------------------------------------------------------------
-// nodal solve (Grid.cpp:9-245) + grid BC phase 2 (Grid.cpp:862-1094)
+// nodal solve (Grid.cpp:9-245) + grid BC phase 2 (Grid.cpp:862-1094), active node blocks
 
 struct BCApply {
     int type;
     float4 val;
     int fixed;
-    // which components are set and to which value
     __device__ __forceinline__ void comps(bool set[3], float v[3]) const
     {
         set[0] = set[1] = set[2] = false;
@@ -230,161 +436,178 @@ __device__ __forceinline__ void contact_normal(const float rv[3], const float n[
 }
 
 template <bool MULTI>
-__global__ void __launch_bounds__(256) k_solve(NodeBufs nb, StepArgs a, int keep)
+__global__ void __launch_bounds__(256) k_solve_blocks(NodeBufs nb, StepArgs a, int keep)
 {
-    const long long nd = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (nd >= a.g.nn) return;
-    const float4 A0 = nb.acc0[nd], A1 = nb.acc1[nd];
-    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-    nb.acc0[nd] = z4;
-    nb.acc1[nd] = z4;
-    const float m = A0.x;
-    const float dtn = a.sc.dt_node, dt = a.sc.dt;
-    float vc[3] = {0.f, 0.f, 0.f};
-    float v1[3] = {0.f, 0.f, 0.f}, a1[3] = {0.f, 0.f, 0.f};
-    float v2[3] = {0.f, 0.f, 0.f}, a2[3] = {0.f, 0.f, 0.f};
-    float n1[3] = {0.f, 0.f, 0.f};
-    const bool active = (m != 0.0f);
-    if (!MULTI) {
-        if (active) {
-            vc[0] = A0.y / m; vc[1] = A0.z / m; vc[2] = A0.w / m;
-            body_update(m, A0, A1, dtn, v1, a1);
-        }
-    } else {
-        float4 B0[2], B1[2], BN[2];
-        for (int b = 0; b < 2; b++) {
-            B0[b] = nb.bacc0[b][nd];
-            B1[b] = nb.bacc1[b][nd];
-            BN[b] = nb.bnrm[b][nd];
-            nb.bacc0[b][nd] = z4;
-            nb.bacc1[b][nd] = z4;
-            nb.bnrm[b][nd] = z4;
-        }
-        if (active) {
-            vc[0] = A0.y / m; vc[1] = A0.z / m; vc[2] = A0.w / m;
-            const float mag1 = sqrtf(BN[0].x * BN[0].x + BN[0].y * BN[0].y + BN[0].z * BN[0].z);
-            if (mag1 > 1e-8f) { n1[0] = BN[0].x / mag1; n1[1] = BN[0].y / mag1; n1[2] = BN[0].z / mag1; }
-            const float n2[3] = {-n1[0], -n1[1], -n1[2]};  // Grid.cpp:45-47
-            const float m1 = B0[0].x, m2 = B0[1].x;
-            const int2 body = nb.body[nd];
-            const unsigned char hr = nb.has_rigid[nd];
-            if (body.y != -1) {
-                float ap1 = 0.f, ap2 = 0.f, rv1[3] = {0.f, 0.f, 0.f}, rv2[3] = {0.f, 0.f, 0.f};
-                if (m1 != 0.0f) {
-                    rv1[0] = B0[0].y / m1 - vc[0]; rv1[1] = B0[0].z / m1 - vc[1]; rv1[2] = B0[0].w / m1 - vc[2];
-                    ap1 = rv1[0] * n1[0] + rv1[1] * n1[1] + rv1[2] * n1[2];
-                }
-                if (m2 != 0.0f) {
-                    rv2[0] = B0[1].y / m2 - vc[0]; rv2[1] = B0[1].z / m2 - vc[1]; rv2[2] = B0[1].w / m2 - vc[2];
-                    ap2 = rv2[0] * n2[0] + rv2[1] * n2[1] + rv2[2] * n2[2];
-                }
-                if (ap1 > 0.01f || ap2 > 0.01f) {
-                    if (hr & 1) {
-                        // body 1 rigid: body 2 takes body 1's velocity (Grid.cpp:78-91)
-                        if (m1 != 0.0f) {
-                            v1[0] = B0[0].y / m1; v1[1] = B0[0].z / m1; v1[2] = B0[0].w / m1;
-                            if (m2 != 0.0f) {
-                                v2[0] = B0[1].y / m2 - (B0[1].y - m2 * v1[0]) / m2;
-                                v2[1] = B0[1].z / m2 - (B0[1].z - m2 * v1[1]) / m2;
-                                v2[2] = B0[1].w / m2 - (B0[1].w - m2 * v1[2]) / m2;
-                            }
-                        }
-                    } else if (hr & 2) {
-                        if (m2 != 0.0f) {
-                            v2[0] = B0[1].y / m2; v2[1] = B0[1].z / m2; v2[2] = B0[1].w / m2;
-                            if (m1 != 0.0f) {
-                                v1[0] = B0[0].y / m1 - (B0[0].y - m1 * v2[0]) / m1;
-                                v1[1] = B0[0].z / m1 - (B0[0].z - m1 * v2[1]) / m1;
-                                v1[2] = B0[0].w / m1 - (B0[0].w - m1 * v2[2]) / m1;
-                            }
-                        }
-                    } else {
-                        if (m1 != 0.0f) {
-                            float cn[3];
-                            contact_normal(rv1, n1, a.sc.mu, cn);
-                            v1[0] = B0[0].y / m1 - ap1 * cn[0];
-                            v1[1] = B0[0].z / m1 - ap1 * cn[1];
-                            v1[2] = B0[0].w / m1 - ap1 * cn[2];
-                            a1[0] = B1[0].x / m1 - (ap1 * cn[0]) / dt;
-                            a1[1] = B1[0].y / m1 - (ap1 * cn[1]) / dt;
-                            a1[2] = B1[0].z / m1 - (ap1 * cn[2]) / dt;
-                            for (int k = 0; k < 3; k++) v1[k] += a1[k] * dtn;
-                        }
-                        if (m2 != 0.0f) {
-                            float cn[3];
-                            contact_normal(rv2, n2, a.sc.mu, cn);
-                            v2[0] = B0[1].y / m2 - ap2 * cn[0];
-                            v2[1] = B0[1].z / m2 - ap2 * cn[1];
-                            v2[2] = B0[1].w / m2 - ap2 * cn[2];
-                            a2[0] = B1[1].x / m2 - (ap2 * cn[0]) / dt;
-                            a2[1] = B1[1].y / m2 - (ap2 * cn[1]) / dt;
-                            a2[2] = B1[1].z / m2 - (ap2 * cn[2]) / dt;
-                            for (int k = 0; k < 3; k++) v2[k] += a2[k] * dtn;
-                        }
-                    }
-                } else {
-                    if (m1 != 0.0f) body_update(m1, B0[0], B1[0], dtn, v1, a1);
-                    if (m2 != 0.0f) body_update(m2, B0[1], B1[1], dtn, v2, a2);
+    const GridGeom &g = a.g;
+    const long long blk = (long long)blockIdx.x * 4 + (threadIdx.x >> 6);
+    const bool blk_ok = blk < g.nnb;
+    const bool active_blk = blk_ok && nb.flags[blk] != 0;
+    const int warp_any = __syncthreads_or(active_blk);
+    if (!warp_any) return;
+    bool active = false;
+    if (active_blk) {
+        const int lx = threadIdx.x & 3, ly = (threadIdx.x >> 2) & 3, lz = (threadIdx.x >> 4) & 3;
+        const int bx = (int)(blk % g.nnbx);
+        const long long tb = blk / g.nnbx;
+        const int by = (int)(tb % g.nnby), bz = (int)(tb / g.nnby);
+        const int i = bx * 4 + lx, j = by * 4 + ly, k = bz * 4 + lz;
+        if (i < g.nx && j < g.ny && k < g.nz) {
+            const long long nd = node_index(i, j, k, g);
+            const float4 A0 = nb.acc0[nd];
+            float4 A1 = nb.acc1[nd];
+            const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+            nb.acc0[nd] = z4;
+            nb.acc1[nd] = z4;
+            const float m = A0.x;
+            if (!MULTI) {
+                // single body: gravity enters here as m_node * g (Extrapolation.cpp:226-228)
+                A1.x += m * a.sc.gravity[0];
+                A1.y += m * a.sc.gravity[1];
+                A1.z += m * a.sc.gravity[2];
+            }
+            const float dtn = a.sc.dt_node, dt = a.sc.dt;
+            float vc[3] = {0.f, 0.f, 0.f};
+            float v1[3] = {0.f, 0.f, 0.f}, a1[3] = {0.f, 0.f, 0.f};
+            float v2[3] = {0.f, 0.f, 0.f}, a2[3] = {0.f, 0.f, 0.f};
+            float n1[3] = {0.f, 0.f, 0.f};
+            active = (m != 0.0f);
+            if (!MULTI) {
+                if (active) {
+                    vc[0] = A0.y / m; vc[1] = A0.z / m; vc[2] = A0.w / m;
+                    body_update(m, A0, A1, dtn, v1, a1);
                 }
             } else {
-                if (m1 != 0.0f) body_update(m1, B0[0], B1[0], dtn, v1, a1);
+                float4 B0[2], B1[2], BN[2];
+                for (int b = 0; b < 2; b++) {
+                    B0[b] = nb.bacc0[b][nd];
+                    B1[b] = nb.bacc1[b][nd];
+                    BN[b] = nb.bnrm[b][nd];
+                    nb.bacc0[b][nd] = z4;
+                    nb.bacc1[b][nd] = z4;
+                    nb.bnrm[b][nd] = z4;
+                }
+                if (active) {
+                    vc[0] = A0.y / m; vc[1] = A0.z / m; vc[2] = A0.w / m;
+                    const float mag1 = sqrtf(BN[0].x * BN[0].x + BN[0].y * BN[0].y + BN[0].z * BN[0].z);
+                    if (mag1 > 1e-8f) { n1[0] = BN[0].x / mag1; n1[1] = BN[0].y / mag1; n1[2] = BN[0].z / mag1; }
+                    const float n2[3] = {-n1[0], -n1[1], -n1[2]};  // Grid.cpp:45-47
+                    const float m1 = B0[0].x, m2 = B0[1].x;
+                    const int2 body = nb.body[nd];
+                    const unsigned char hr = nb.has_rigid[nd];
+                    if (body.y != -1) {
+                        float ap1 = 0.f, ap2 = 0.f, rv1[3] = {0.f, 0.f, 0.f}, rv2[3] = {0.f, 0.f, 0.f};
+                        if (m1 != 0.0f) {
+                            rv1[0] = B0[0].y / m1 - vc[0]; rv1[1] = B0[0].z / m1 - vc[1]; rv1[2] = B0[0].w / m1 - vc[2];
+                            ap1 = rv1[0] * n1[0] + rv1[1] * n1[1] + rv1[2] * n1[2];
+                        }
+                        if (m2 != 0.0f) {
+                            rv2[0] = B0[1].y / m2 - vc[0]; rv2[1] = B0[1].z / m2 - vc[1]; rv2[2] = B0[1].w / m2 - vc[2];
+                            ap2 = rv2[0] * n2[0] + rv2[1] * n2[1] + rv2[2] * n2[2];
+                        }
+                        if (ap1 > 0.01f || ap2 > 0.01f) {
+                            if (hr & 1) {
+                                // body 1 rigid: body 2 takes body 1's velocity (Grid.cpp:78-91)
+                                if (m1 != 0.0f) {
+                                    v1[0] = B0[0].y / m1; v1[1] = B0[0].z / m1; v1[2] = B0[0].w / m1;
+                                    if (m2 != 0.0f) {
+                                        v2[0] = B0[1].y / m2 - (B0[1].y - m2 * v1[0]) / m2;
+                                        v2[1] = B0[1].z / m2 - (B0[1].z - m2 * v1[1]) / m2;
+                                        v2[2] = B0[1].w / m2 - (B0[1].w - m2 * v1[2]) / m2;
+                                    }
+                                }
+                            } else if (hr & 2) {
+                                if (m2 != 0.0f) {
+                                    v2[0] = B0[1].y / m2; v2[1] = B0[1].z / m2; v2[2] = B0[1].w / m2;
+                                    if (m1 != 0.0f) {
+                                        v1[0] = B0[0].y / m1 - (B0[0].y - m1 * v2[0]) / m1;
+                                        v1[1] = B0[0].z / m1 - (B0[0].z - m1 * v2[1]) / m1;
+                                        v1[2] = B0[0].w / m1 - (B0[0].w - m1 * v2[2]) / m1;
+                                    }
+                                }
+                            } else {
+                                if (m1 != 0.0f) {
+                                    float cn[3];
+                                    contact_normal(rv1, n1, a.sc.mu, cn);
+                                    v1[0] = B0[0].y / m1 - ap1 * cn[0];
+                                    v1[1] = B0[0].z / m1 - ap1 * cn[1];
+                                    v1[2] = B0[0].w / m1 - ap1 * cn[2];
+                                    a1[0] = B1[0].x / m1 - (ap1 * cn[0]) / dt;
+                                    a1[1] = B1[0].y / m1 - (ap1 * cn[1]) / dt;
+                                    a1[2] = B1[0].z / m1 - (ap1 * cn[2]) / dt;
+                                    for (int c = 0; c < 3; c++) v1[c] += a1[c] * dtn;
+                                }
+                                if (m2 != 0.0f) {
+                                    float cn[3];
+                                    contact_normal(rv2, n2, a.sc.mu, cn);
+                                    v2[0] = B0[1].y / m2 - ap2 * cn[0];
+                                    v2[1] = B0[1].z / m2 - ap2 * cn[1];
+                                    v2[2] = B0[1].w / m2 - ap2 * cn[2];
+                                    a2[0] = B1[1].x / m2 - (ap2 * cn[0]) / dt;
+                                    a2[1] = B1[1].y / m2 - (ap2 * cn[1]) / dt;
+                                    a2[2] = B1[1].z / m2 - (ap2 * cn[2]) / dt;
+                                    for (int c = 0; c < 3; c++) v2[c] += a2[c] * dtn;
+                                }
+                            }
+                        } else {
+                            if (m1 != 0.0f) body_update(m1, B0[0], B1[0], dtn, v1, a1);
+                            if (m2 != 0.0f) body_update(m2, B0[1], B1[1], dtn, v2, a2);
+                        }
+                    } else {
+                        if (m1 != 0.0f) body_update(m1, B0[0], B1[0], dtn, v1, a1);
+                    }
+                }
+            }
+            // grid BC, phase 2 (phase 1 is overwritten by the solve for every node the
+            // particles read; phase 3 repeats phase 2)
+            const int bt = nb.bc_type ? nb.bc_type[nd] : 0;
+            if (bt) {
+                BCApply bc{bt, nb.bc_val[nd], a.sc.fixed_grid_bcs};
+                bool set[3];
+                float val[3];
+                bc.comps(set, val);
+                for (int c = 0; c < 3; c++)
+                    if (set[c]) {
+                        v1[c] = val[c]; a1[c] = 0.f;
+                        v2[c] = val[c]; a2[c] = 0.f;
+                        vc[c] = val[c];
+                    }
+            }
+            nb.gv[nd] = make_float4(m, v1[0], v1[1], v1[2]);
+            nb.ga[nd] = make_float4(a1[0], a1[1], a1[2], 0.f);
+            if (MULTI) {
+                nb.bgv[0][nd] = make_float4(m, v1[0], v1[1], v1[2]);
+                nb.bga[0][nd] = make_float4(a1[0], a1[1], a1[2], 0.f);
+                nb.bgv[1][nd] = make_float4(m, v2[0], v2[1], v2[2]);
+                nb.bga[1][nd] = make_float4(a2[0], a2[1], a2[2], 0.f);
+                if (nb.nrm_out[0]) {
+                    nb.nrm_out[0][nd] = make_float4(n1[0], n1[1], n1[2], 0.f);
+                    nb.nrm_out[1][nd] = make_float4(-n1[0], -n1[1], -n1[2], 0.f);
+                }
+            }
+            if (keep) {
+                nb.out_com[nd] = make_float4(vc[0], vc[1], vc[2], 0.f);
+                nb.out_force[nd] = make_float4(A1.x, A1.y, A1.z, 0.f);
             }
         }
-    }
-    // grid BC, phase 2 (phase 1 values are overwritten by the solve for every node the
-    // particles read; phase 3 repeats phase 2)
-    const int bt = nb.bc_type ? nb.bc_type[nd] : 0;
-    if (bt) {
-        BCApply bc{bt, nb.bc_val[nd], a.sc.fixed_grid_bcs};
-        bool set[3];
-        float val[3];
-        bc.comps(set, val);
-        for (int k = 0; k < 3; k++)
-            if (set[k]) {
-                v1[k] = val[k]; a1[k] = 0.f;
-                v2[k] = val[k]; a2[k] = 0.f;
-                vc[k] = val[k];
-            }
-    }
-    nb.gv[nd] = make_float4(m, v1[0], v1[1], v1[2]);
-    nb.ga[nd] = make_float4(a1[0], a1[1], a1[2], 0.f);
-    if (MULTI) {
-        nb.bgv[0][nd] = make_float4(m, v1[0], v1[1], v1[2]);
-        nb.bga[0][nd] = make_float4(a1[0], a1[1], a1[2], 0.f);
-        nb.bgv[1][nd] = make_float4(m, v2[0], v2[1], v2[2]);
-        nb.bga[1][nd] = make_float4(a2[0], a2[1], a2[2], 0.f);
-        if (nb.nrm_out[0]) {
-            nb.nrm_out[0][nd] = make_float4(n1[0], n1[1], n1[2], 0.f);
-            nb.nrm_out[1][nd] = make_float4(-n1[0], -n1[1], -n1[2], 0.f);
-        }
-    }
-    if (keep) {
-        nb.out_com[nd] = make_float4(vc[0], vc[1], vc[2], 0.f);
-        nb.out_force[nd] = make_float4(A1.x, A1.y, A1.z, 0.f);
     }
     if (nb.active_count) {
-        const unsigned mask = __ballot_sync(__activemask(), active);
-        if ((threadIdx.x & 31) == __ffs(__activemask()) - 1 && mask) atomicAdd(nb.active_count, __popc(mask));
+        const unsigned mask = __ballot_sync(0xffffffffu, active);
+        if ((threadIdx.x & 31) == 0 && mask) atomicAdd(nb.active_count, __popc(mask));
     }
+    __syncthreads();
+    if (active_blk && (threadIdx.x & 63) == 0) nb.flags[blk] = 0;
 }
 
 void launch_solve(const NodeBufs &nb, const StepArgs &a, bool keep_node_fields, cudaStream_t s)
 {
-    const unsigned grid = (unsigned)((a.g.nn + 255) / 256);
-    if (a.sc.multi_body) {
-        k_solve<true><<<grid, 256, 0, s>>>(nb, a, keep_node_fields ? 1 : 0);
-        note_launch(1);
-    }
-    else {
-        k_solve<false><<<grid, 256, 0, s>>>(nb, a, keep_node_fields ? 1 : 0);
-        note_launch(1);
-    }
+    const unsigned grid = (unsigned)((a.g.nnb + 3) / 4);
+    if (a.sc.multi_body) k_solve_blocks<true><<<grid, 256, 0, s>>>(nb, a, keep_node_fields ? 1 : 0);
+    else k_solve_blocks<false><<<grid, 256, 0, s>>>(nb, a, keep_node_fields ? 1 : 0);
+    note_launch(1);
 }
 
 // ---------------------------------------------------------------------------------------
-// G2P + particle BCs + update + constitutive + damage + wrap + key
-
-__device__ __forceinline__ float sinf_ref(float x) { return sinf(x); }
+// G2P + particle BCs + update + constitutive + damage + wrap + key, one particle
 
 // particle BCs, TimeIntegration.cpp:177-296
 __device__ __forceinline__ void particle_bc(int type, const float4 &val, float t, float mass, float v[3], float acc[3],
@@ -396,10 +619,10 @@ __device__ __forceinline__ void particle_bc(int type, const float4 &val, float t
     case BC_MP_VY: v[0] = 0.f; v[1] = val.x; v[2] = 0.f; break;
     case BC_MP_VZ: v[0] = 0.f; v[1] = 0.f; v[2] = val.x; break;
     case BC_MP_VX_VY: v[0] = val.x; v[1] = val.y; v[2] = 0.f; break;
-    case BC_MP_VXSIN: v[0] = val.x * sinf_ref(w * val.y * t); break;
-    case BC_MP_VYSIN: v[1] = val.x * sinf_ref(w * val.y * t); vg[1] = 0.f; acc[1] = 0.f; break;
+    case BC_MP_VXSIN: v[0] = val.x * sinf(w * val.y * t); break;
+    case BC_MP_VYSIN: v[1] = val.x * sinf(w * val.y * t); vg[1] = 0.f; acc[1] = 0.f; break;
     case BC_MP_SYYSIN:
-        s[1] = val.x * sinf_ref(w * val.y * t);
+        s[1] = val.x * sinf(w * val.y * t);
         v[0] = v[1] = v[2] = 0.f;
         vg[0] = vg[1] = vg[2] = 0.f;
         break;
@@ -412,7 +635,7 @@ __device__ __forceinline__ void particle_bc(int type, const float4 &val, float t
     }
 }
 
-// move an (offset, cell) pair by delta cells and renormalise the offset into [lp, 1+lp)
+// move the offset into [lp, 1+lp) and carry whole cells into c
 __device__ __forceinline__ void renorm(float &o, int &c, float lp)
 {
     const float k = floorf(o - lp);
@@ -422,64 +645,55 @@ __device__ __forceinline__ void renorm(float &o, int &c, float lp)
     }
 }
 
-template <bool MULTI>
-__global__ void __launch_bounds__(256) k_g2p_update(PView P, long long n, NodeBufs nb, StepArgs a, int track_normals,
-                                                    int check_finite, int has_dp)
+template <bool MULTI, bool HAS_DP>
+__device__ __forceinline__ void g2p_update_one(PState &st, const NodeBufs &nb, const StepArgs &a, bool track_normals,
+                                               bool check_finite, float nrm[3])
 {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
     const GridGeom &g = a.g;
     const StepScalars &sc = a.sc;
-    const uint32_t info = (uint32_t)P.ii(PF_INFO, i);
-    int ci, cj, ck;
-    decode_key(P.ii(PF_KEY, i), g, ci, cj, ck);
-    float o[3] = {P.f(PF_OX, i), P.f(PF_OY, i), P.f(PF_OZ, i)};
-    float Sx[3], Gx[3], Sy[3], Gy[3], Sz[3] = {1.f, 0.f, 0.f}, Gz[3] = {0.f, 0.f, 0.f};
-    gimp_axis(o[0], g.lp, Sx, Gx);
-    gimp_axis(o[1], g.lp, Sy, Gy);
-    int nkz = 1;
-    if (g.is3d) {
-        gimp_axis(o[2], g.lp, Sz, Gz);
-        nkz = (o[2] < 1.0f - g.lp) ? 2 : 3;
-    } else {
-        ck = 0;
-    }
-    const int nix = (o[0] < 1.0f - g.lp) ? 2 : 3;
-    const int njy = (o[1] < 1.0f - g.lp) ? 2 : 3;
-    const int obj = info_obj(info);
+    Stencil w;
+    make_stencil(st, g, w);
+    const int obj = info_obj(st.info);
 
     // ---- G2P (Extrapolation.cpp:288-367) ----
-    float acc[3] = {0.f, 0.f, 0.f}, vg[3] = {0.f, 0.f, 0.f}, nrm[3] = {0.f, 0.f, 0.f};
+    float acc[3] = {0.f, 0.f, 0.f}, vg[3] = {0.f, 0.f, 0.f};
     float L[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};  // L[a][b] = sum v_a dW/dx_b
-    for (int kk = 0; kk < nkz; kk++)
-        for (int jj = 0; jj < njy; jj++) {
-            const float syz = Sy[jj] * Sz[kk], gyz = Gy[jj] * Sz[kk], syg = Sy[jj] * Gz[kk];
-            for (int ii = 0; ii < nix; ii++) {
-                const long long nd = node_index(ci + ii, cj + jj, ck + kk, g);
+    nrm[0] = nrm[1] = nrm[2] = 0.f;
+#pragma unroll
+    for (int kk = 0; kk < 3; kk++)
+#pragma unroll
+        for (int jj = 0; jj < 3; jj++) {
+            if (kk >= w.cnt[2] || jj >= w.cnt[1]) continue;
+            const float syz = w.S[1][jj] * w.S[2][kk];
+            const float gyz = w.G[1][jj] * w.S[2][kk] * g.inv_h, syg = w.S[1][jj] * w.G[2][kk] * g.inv_h;
+#pragma unroll
+            for (int ii = 0; ii < 3; ii++) {
+                if (ii >= w.cnt[0]) continue;
+                const long long nd = node_index(w.c[0] + ii, w.c[1] + jj, w.c[2] + kk, g);
                 const float4 V = __ldg(&nb.gv[nd]);
                 if (V.x == 0.0f) continue;  // nodes without mass are skipped
                 float4 Vb, Ab;
+                int slot = 0;
                 if (!MULTI) {
                     Vb = V;
                     Ab = __ldg(&nb.ga[nd]);
                 } else {
                     const int2 b = __ldg(&nb.body[nd]);
-                    const int slot = (b.x == obj) ? 0 : ((b.y == obj) ? 1 : -1);
+                    slot = (b.x == obj) ? 0 : ((b.y == obj) ? 1 : -1);
                     if (slot < 0) continue;  // a third body sees nothing from this node
                     Vb = __ldg(&nb.bgv[slot][nd]);
                     Ab = __ldg(&nb.bga[slot][nd]);
                 }
-                const float w = Sx[ii] * syz;
-                const float gx = Gx[ii] * syz * g.inv_h, gy = Sx[ii] * gyz * g.inv_h, gz = Sx[ii] * syg * g.inv_h;
-                acc[0] += w * Ab.x; acc[1] += w * Ab.y; acc[2] += w * Ab.z;
-                vg[0] += w * Vb.y; vg[1] += w * Vb.z; vg[2] += w * Vb.w;
+                const float wgt = w.S[0][ii] * syz;
+                const float gx = w.G[0][ii] * syz * g.inv_h, gy = w.S[0][ii] * gyz, gz = w.S[0][ii] * syg;
+                acc[0] += wgt * Ab.x; acc[1] += wgt * Ab.y; acc[2] += wgt * Ab.z;
+                vg[0] += wgt * Vb.y; vg[1] += wgt * Vb.z; vg[2] += wgt * Vb.w;
                 L[0][0] += Vb.y * gx; L[0][1] += Vb.y * gy; L[0][2] += Vb.y * gz;
                 L[1][0] += Vb.z * gx; L[1][1] += Vb.z * gy; L[1][2] += Vb.z * gz;
                 L[2][0] += Vb.w * gx; L[2][1] += Vb.w * gy; L[2][2] += Vb.w * gz;
                 if (MULTI && track_normals) {
-                    const int2 b = __ldg(&nb.body[nd]);
-                    const float4 N = __ldg(&nb.nrm_out[(b.x == obj) ? 0 : 1][nd]);
-                    nrm[0] += w * N.x; nrm[1] += w * N.y; nrm[2] += w * N.z;
+                    const float4 N = __ldg(&nb.nrm_out[slot][nd]);
+                    nrm[0] += wgt * N.x; nrm[1] += wgt * N.y; nrm[2] += wgt * N.z;
                 }
             }
         }
@@ -491,130 +705,186 @@ __global__ void __launch_bounds__(256) k_g2p_update(PView P, long long n, NodeBu
     c.r[3] = 0.5f * (L[1][0] + L[0][1]);
     c.r[4] = 0.5f * (L[2][1] + L[1][2]);
     c.r[5] = 0.5f * (L[2][0] + L[0][2]);
-    float rho = P.f(PF_RHO, i);
-    const float rho_rate = -rho * (L[0][0] + L[1][1] + L[2][2]);
-    float v[3] = {P.f(PF_VX, i), P.f(PF_VY, i), P.f(PF_VZ, i)};
+    const float rho_rate = -st.rho * (L[0][0] + L[1][1] + L[2][2]);
 #pragma unroll
     for (int k = 0; k < 6; k++) {
-        c.s[k] = P.f(PF_S0 + k, i);
-        c.e[k] = P.f(PF_E0 + k, i);
+        c.s[k] = st.s[k];
+        c.e[k] = st.e[k];
+        c.ep[k] = st.ep[k];
     }
-    const float mass = P.f(PF_MASS, i);
-    const int bct = info_bc(info);
+    c.eqps = st.eqps;
+    c.dmg = st.dmg;
+    c.smax = st.smax;
+    const int bct = info_bc(st.info);
     float4 bcv = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (bct) bcv = __ldg(&a.pbc_val[P.ii(PF_PID, i)]);
+    if (bct) bcv = __ldg(&a.pbc_val[st.pid]);
 
     // ---- particle BC, phase 4 ----
-    if (bct) particle_bc(bct, bcv, sc.t_bc, mass, v, acc, vg, c.s);
+    if (bct) particle_bc(bct, bcv, sc.t_bc, st.mass, st.v, acc, vg, c.s);
 
     // ---- update (TimeIntegration.cpp:11-117) ----
     const float dt = sc.dt;
-    rho += rho_rate * dt;
-    if (!(info & INFO_HOLD)) {
-        v[0] = v[0] + (acc[0] - sc.damping * v[0]) * dt;
-        v[1] = v[1] + (acc[1] - sc.damping * v[1]) * dt;
-        if (g.is3d) v[2] = v[2] + (acc[2] - sc.damping * v[2]) * dt;
-        o[0] += vg[0] * dt * g.inv_h;
-        o[1] += vg[1] * dt * g.inv_h;
-        if (g.is3d) o[2] += vg[2] * dt * g.inv_h;
+    st.rho += rho_rate * dt;
+    if (!(st.info & INFO_HOLD)) {
+        st.v[0] = st.v[0] + (acc[0] - sc.damping * st.v[0]) * dt;
+        st.v[1] = st.v[1] + (acc[1] - sc.damping * st.v[1]) * dt;
+        if (g.is3d) st.v[2] = st.v[2] + (acc[2] - sc.damping * st.v[2]) * dt;
+        st.o[0] += vg[0] * dt * g.inv_h;
+        st.o[1] += vg[1] * dt * g.inv_h;
+        if (g.is3d) st.o[2] += vg[2] * dt * g.inv_h;
     }
 #pragma unroll
     for (int k = 0; k < 6; k++) c.e[k] += c.r[k] * dt;
-    const DevMaterial &M = a.mats[info_mat(info)];
-    if (has_dp) {
-        c.eqps = P.f(PF_EQPS, i);
-#pragma unroll
-        for (int k = 0; k < 6; k++) c.ep[k] = P.f(PF_EP0 + k, i);
-        c.dmg = P.f(PF_DMG, i);
-        c.smax = P.f(PF_SMAX, i);
-    } else {
-        c.eqps = 0.f;
-        c.dmg = 0.f;
-        c.smax = 0.f;
-#pragma unroll
-        for (int k = 0; k < 6; k++) c.ep[k] = 0.f;
+    c.mass = st.mass;
+    c.rho = st.rho;
+    c.v[0] = st.v[0]; c.v[1] = st.v[1]; c.v[2] = st.v[2];
+    if (!(st.info & INFO_RIGID)) {
+        const DevMaterial &M = a.mats[info_mat(st.info)];
+        if (HAS_DP) {
+            constitutive_update(c, M, dt, g.is3d);
+        } else {
+            if (M.model == 1) cm_elastic(c, M, dt);
+            else if (M.model == 2) cm_newtonian(c, M.K, M.viscosity, dt, g.is3d, false);
+        }
     }
-    c.mass = mass;
-    c.rho = rho;
-    c.v[0] = v[0]; c.v[1] = v[1]; c.v[2] = v[2];
-    if (!(info & INFO_RIGID)) constitutive_update(c, M, dt, g.is3d);
 
-    // ---- periodic wrap (TimeIntegration.cpp:80-108) and new cell ----
-    int cc[3] = {ci, cj, ck};
+    // ---- periodic wrap (TimeIntegration.cpp:80-108) and the new cell ----
+    int cc[3] = {w.c[0], w.c[1], w.c[2]};
     const int naxes = g.is3d ? 3 : 2;
-    for (int ax = 0; ax < naxes; ax++) {
-        renorm(o[ax], cc[ax], g.lp);
-        const float X = (float)cc[ax] + o[ax];
+#pragma unroll
+    for (int ax = 0; ax < 3; ax++) {
+        if (ax >= naxes) break;
+        renorm(st.o[ax], cc[ax], g.lp);
+        const float X = (float)cc[ax] + st.o[ax];
         int sh = 0;
         float sf = 0.f;
         if (X > g.wrap_hi[ax]) { sh = g.wrap_shift_int[ax]; sf = g.wrap_shift_frac[ax]; }
         if (X + (float)sh + sf < 1.0f) { sh -= g.wrap_shift_int[ax]; sf -= g.wrap_shift_frac[ax]; }
         if (sh != 0 || sf != 0.f) {
             cc[ax] += sh;
-            o[ax] += sf;
-            renorm(o[ax], cc[ax], g.lp);
+            st.o[ax] += sf;
+            renorm(st.o[ax], cc[ax], g.lp);
         }
     }
     const int lim[3] = {g.ncx - 2, g.ncy - 2, g.ncz - 2};
     bool bad = false;
-    for (int ax = 0; ax < naxes; ax++) {
+#pragma unroll
+    for (int ax = 0; ax < 3; ax++) {
+        if (ax >= naxes) break;
         if (cc[ax] < 0) { cc[ax] = 0; bad = true; }
         if (cc[ax] > lim[ax]) { cc[ax] = lim[ax]; bad = true; }
     }
     if (bad) atomicOr(a.status, ERR_RANGE);
-    const int nkey = cc[0] + cc[1] * g.ncx + (g.is3d ? cc[2] * g.ncx * g.ncy : 0);
+    st.key = encode_key(cc[0], cc[1], g.is3d ? cc[2] : 0, g);
 
     // ---- particle BC, phase 5 ----
-    if (bct) particle_bc(bct, bcv, sc.t_bc, mass, v, acc, vg, c.s);
+    if (bct) particle_bc(bct, bcv, sc.t_bc, st.mass, st.v, acc, vg, c.s);
 
     if (check_finite) {
-        bool fin = isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]) && isfinite(rho);
+        bool fin = isfinite(st.v[0]) && isfinite(st.v[1]) && isfinite(st.v[2]) && isfinite(st.rho);
 #pragma unroll
         for (int k = 0; k < 6; k++) fin = fin && isfinite(c.s[k]);
         if (!fin) atomicOr(a.status, ERR_NONFINITE);
     }
-
-    // ---- write back ----
-    P.f(PF_OX, i) = o[0];
-    P.f(PF_OY, i) = o[1];
-    if (g.is3d) P.f(PF_OZ, i) = o[2];
-    P.ii(PF_KEY, i) = nkey;
-    P.f(PF_VX, i) = v[0];
-    P.f(PF_VY, i) = v[1];
-    P.f(PF_VZ, i) = v[2];
 #pragma unroll
     for (int k = 0; k < 6; k++) {
-        P.f(PF_S0 + k, i) = c.s[k];
-        P.f(PF_E0 + k, i) = c.e[k];
+        st.s[k] = c.s[k];
+        st.e[k] = c.e[k];
+        st.ep[k] = c.ep[k];
     }
-    P.f(PF_RHO, i) = rho;
-    if (info & INFO_INIT_VOL) P.ii(PF_INFO, i) = (int)(info & ~INFO_INIT_VOL);
-    if (has_dp) {
-        P.f(PF_EQPS, i) = c.eqps;
-#pragma unroll
-        for (int k = 0; k < 6; k++) P.f(PF_EP0 + k, i) = c.ep[k];
-        P.f(PF_DMG, i) = c.dmg;
-        P.f(PF_SMAX, i) = c.smax;
-    }
+    st.eqps = c.eqps;
+    st.dmg = c.dmg;
+    st.smax = c.smax;
+    st.info &= ~INFO_INIT_VOL;
+}
+
+// Unfused G2P + update: one thread per particle in sorted order, state read through perm
+// and written to the other slab.
+template <bool MULTI, bool HAS_DP>
+__global__ void __launch_bounds__(256) k_g2p_update(PView src, PView dst, const int *perm, long long n, NodeBufs nb,
+                                                    StepArgs a, int track_normals, int check_finite)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    PState st;
+    load_state<HAS_DP>(src, perm ? perm[i] : i, st);
+    float nrm[3];
+    g2p_update_one<MULTI, HAS_DP>(st, nb, a, track_normals != 0, check_finite != 0, nrm);
+    store_state<HAS_DP>(dst, i, st);
     if (track_normals) {
-        P.f(PF_NX, i) = nrm[0];
-        P.f(PF_NY, i) = nrm[1];
-        P.f(PF_NZ, i) = nrm[2];
+        dst.f(PF_NX, i) = nrm[0];
+        dst.f(PF_NY, i) = nrm[1];
+        dst.f(PF_NZ, i) = nrm[2];
     }
 }
 
-void launch_g2p_update(const PView &p, long long n, const NodeBufs &nb, const StepArgs &a, bool track_normals,
-                       bool check_finite, bool has_dp, int block, cudaStream_t s)
+// Fused G2P + update + next step's P2G (single body), persistent over the segments.
+template <bool HAS_DP>
+__global__ void __launch_bounds__(256) k_g2p2g(PView src, PView dst, const int *perm, const int *skey, long long n,
+                                               const int *seg_start, const int *nseg_ptr, NodeBufs nb, StepArgs a,
+                                               int check_finite)
 {
-    (void)block;
+    __shared__ float tile[TILE_FIELDS * TILE_NODES];
+    const int nseg = *nseg_ptr;
+    for (int sgi = blockIdx.x; sgi < nseg; sgi += gridDim.x) {
+        const int start = seg_start[sgi];
+        const int blk = seg_block(skey, start);
+        int tox, toy, toz;
+        tile_origin(blk, a.g, tox, toy, toz);
+        tile_zero(tile);
+        __syncthreads();
+        for (long long base = start;; base += blockDim.x) {
+            const long long i = base + threadIdx.x;
+            const bool valid = i < n && (skey[i] >> CB_SHIFT) == blk;
+            if (!__syncthreads_or(valid)) break;
+            if (valid) {
+                PState st;
+                load_state<HAS_DP>(src, perm ? perm[i] : i, st);
+                float nrm[3];
+                g2p_update_one<false, HAS_DP>(st, nb, a, false, check_finite != 0, nrm);
+                store_state<HAS_DP>(dst, i, st);
+                p2g_single(st, a.g, tile, tox, toy, toz, nb, threadIdx.x & 31);
+            }
+        }
+        __syncthreads();
+        tile_flush(tile, tox, toy, toz, a.g, nb);
+        __syncthreads();
+    }
+}
+
+void launch_g2p_update(const PView &src, const PView &dst, const int *perm, long long n, const NodeBufs &nb,
+                       const StepArgs &a, bool track_normals, bool check_finite, bool has_dp, cudaStream_t s)
+{
     if (n == 0) return;
-    const int B = 256;
-    const unsigned grid = (unsigned)((n + B - 1) / B);
-    if (a.sc.multi_body)
-        k_g2p_update<true><<<grid, B, 0, s>>>(p, n, nb, a, track_normals ? 1 : 0, check_finite ? 1 : 0, has_dp ? 1 : 0);
-    else
-        k_g2p_update<false><<<grid, B, 0, s>>>(p, n, nb, a, 0, check_finite ? 1 : 0, has_dp ? 1 : 0);
+    const unsigned grid = (unsigned)((n + 255) / 256);
+    const int tn = track_normals ? 1 : 0, cf = check_finite ? 1 : 0;
+    if (a.sc.multi_body) {
+        if (has_dp) k_g2p_update<true, true><<<grid, 256, 0, s>>>(src, dst, perm, n, nb, a, tn, cf);
+        else k_g2p_update<true, false><<<grid, 256, 0, s>>>(src, dst, perm, n, nb, a, tn, cf);
+    } else {
+        if (has_dp) k_g2p_update<false, true><<<grid, 256, 0, s>>>(src, dst, perm, n, nb, a, 0, cf);
+        else k_g2p_update<false, false><<<grid, 256, 0, s>>>(src, dst, perm, n, nb, a, 0, cf);
+    }
     note_launch(1);
+}
+
+void launch_g2p2g(const PView &src, const PView &dst, const int *perm, const int *skey, long long n,
+                  const int *seg_start, const int *nseg, int persist_grid, const NodeBufs &nb, const StepArgs &a,
+                  bool check_finite, bool has_dp, cudaStream_t s)
+{
+    if (n == 0) return;
+    const int cf = check_finite ? 1 : 0;
+    if (has_dp) k_g2p2g<true><<<persist_grid, 256, 0, s>>>(src, dst, perm, skey, n, seg_start, nseg, nb, a, cf);
+    else k_g2p2g<false><<<persist_grid, 256, 0, s>>>(src, dst, perm, skey, n, seg_start, nseg, nb, a, cf);
+    note_launch(1);
+}
+
+int g2p2g_blocks_per_sm(bool has_dp)
+{
+    int b = 0;
+    if (has_dp) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_g2p2g<true>, 256, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_g2p2g<false>, 256, 0);
+    return b > 0 ? b : 1;
 }
 
 // ---------------------------------------------------------------------------------------
@@ -633,9 +903,10 @@ __global__ void k_body_tables(PView P, long long n, StepArgs a, int *cell_min, i
     if (i >= n) return;
     const uint32_t info = (uint32_t)P.ii(PF_INFO, i);
     const int obj = info_obj(info);
+    const int pid = P.ii(PF_PID, i);
     int rk;
     if (refkeys) {
-        rk = refkeys[P.ii(PF_PID, i)];
+        rk = refkeys[pid];
     } else {
         // the reference's binning key from the current position (TimeIntegration.cpp:110-115)
         int ci, cj, ck;
@@ -646,7 +917,7 @@ __global__ void k_body_tables(PView P, long long n, StepArgs a, int *cell_min, i
         rk = ix + iy * a.g.ncx + iz * a.g.ncx * a.g.ncy;
     }
     if (rk < 0 || rk >= a.g.nc) return;
-    atomicMin(&cell_min[(long long)rk * (nbody + 1) + obj], P.ii(PF_PID, i));
+    atomicMin(&cell_min[(long long)rk * (nbody + 1) + obj], pid);
     if (info & INFO_RIGID) atomicOr(&cell_min[(long long)rk * (nbody + 1) + nbody], 1 << obj);
 }
 
@@ -723,7 +994,7 @@ void launch_body_assign(const NodeBufs &nb, const StepArgs &a, const int *cell_m
 // ---------------------------------------------------------------------------------------
 // FP64 conservation sums: mass, momentum, kinetic energy, strain energy
 
-__global__ void k_stats(PView P, long long n, StepArgs a, double *out)
+__global__ void k_stats(PView P, long long n, double *out)
 {
     __shared__ double sh[8][8];
     double acc[6] = {0, 0, 0, 0, 0, 0};
@@ -754,13 +1025,13 @@ __global__ void k_stats(PView P, long long n, StepArgs a, double *out)
     }
 }
 
-void launch_stats(const PView &p, long long n, const StepArgs &a, double *out8, cudaStream_t s)
+void launch_stats(const PView &p, long long n, double *out8, cudaStream_t s)
 {
     cudaMemsetAsync(out8, 0, 8 * sizeof(double), s);
     if (n == 0) return;
     long long blocks = (n + 255) / 256;
     if (blocks > 4096) blocks = 4096;
-    k_stats<<<(unsigned)blocks, 256, 0, s>>>(p, n, a, out8);
+    k_stats<<<(unsigned)blocks, 256, 0, s>>>(p, n, out8);
     note_launch(1);
 }
 

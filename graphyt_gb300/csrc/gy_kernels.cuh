@@ -33,6 +33,7 @@ struct NodeBufs {
     float4 *bgv[2], *bga[2];      // solved per slot: (m, v), (a, -)
     float4 *nrm_out[2];           // normalised slot normals (only when normals are tracked)
     int2 *body;                   // body slot objects (dense ids) or -1
+    unsigned char *flags;         // active 4x4x4 node blocks (set by P2G / fold, cleared by the solve)
     unsigned char *has_rigid;     // bit0: slot 0 rigid, bit1: slot 1 rigid
     int *active_count;            // nodes with mass (stats)
 };
@@ -50,31 +51,33 @@ void note_launch(int k);
 long long launch_count();
 
 // launchers (gy_kernels.cu)
-void launch_p2g(const PView &p, long long n, const NodeBufs &nb, const StepArgs &a, int tile, int block, cudaStream_t s);
+void launch_p2g(const PView &p, const int *perm, const int *skey, long long n, const int *seg_start,
+                const int *nseg, int persist_grid, const NodeBufs &nb, const StepArgs &a, cudaStream_t s);
 void launch_fold(const NodeBufs &nb, const StepArgs &a, cudaStream_t s);
 void launch_solve(const NodeBufs &nb, const StepArgs &a, bool keep_node_fields, cudaStream_t s);
-void launch_g2p_update(const PView &p, long long n, const NodeBufs &nb, const StepArgs &a, bool track_normals,
-                       bool check_finite, bool has_dp, int block, cudaStream_t s);
+void launch_g2p_update(const PView &src, const PView &dst, const int *perm, long long n, const NodeBufs &nb,
+                       const StepArgs &a, bool track_normals, bool check_finite, bool has_dp, cudaStream_t s);
+void launch_g2p2g(const PView &src, const PView &dst, const int *perm, const int *skey, long long n,
+                  const int *seg_start, const int *nseg, int persist_grid, const NodeBufs &nb, const StepArgs &a,
+                  bool check_finite, bool has_dp, cudaStream_t s);
+int g2p2g_blocks_per_sm(bool has_dp);
 void launch_body_tables(const PView &p, long long n, const StepArgs &a, int *cell_min, int nbody,
-                        const int *refkey_src_unused, cudaStream_t s);
+                        const int *refkeys, cudaStream_t s);
 void launch_body_assign(const NodeBufs &nb, const StepArgs &a, const int *cell_min, int nbody,
                         const int *nidx_x, const int *nidx_y, const int *nidx_z, cudaStream_t s);
-void launch_stats(const PView &p, long long n, const StepArgs &a, double *out8, cudaStream_t s);
+void launch_stats(const PView &p, long long n, double *out8, cudaStream_t s);
 
-// sort (gy_sort.cu): stable LSD radix sort of (key, value) pairs
+// sort (gy_sort.cu): stable LSD radix sort of (key, index) pairs
 struct SortScratch {
     int *keys[2], *vals[2];
-    int *hist;          // 256 * nblocks
+    int *hist;          // 2 * 256 * nblocks
     int *scan_tmp;      // scan workspace
     long long cap;
     int nblocks_cap;
 };
 size_t sort_scratch_bytes(long long n);
-void sort_pairs(const int *keys_in, int *perm_out, long long n, int key_bits, SortScratch &ws, cudaStream_t s);
-void launch_permute(const float *in, float *out, long long cap, long long n, const int *perm, const int *fields,
-                    int nfields, cudaStream_t s);
-void launch_iota(int *out, long long n, cudaStream_t s);
-void launch_extract_keys(const PView &p, long long n, int *keys, cudaStream_t s);
+const int *sort_pairs(const int *keys_in, int *perm_out, long long n, int key_bits, SortScratch &ws, cudaStream_t s);
+void launch_block_heads(const int *skey, long long n, int *seg_start, int *nseg, cudaStream_t s);
 void exclusive_scan_int(const int *in, int *out, long long n, int *tmp, cudaStream_t s);
 size_t scan_tmp_ints(long long n);
 

@@ -1,7 +1,9 @@
-// gy_sort.cu -- stable counting sort of particles by cell, and the state permutation.
+// gy_sort.cu -- stable counting sort of particles by cell.
 //
 // The reference sorts particle indices by cellID with std::sort and permutes ~40 arrays
-// (Extrapolation.cpp:370-503).  Here the sort is a stable least-significant-digit radix
+// (Extrapolation.cpp:370-503).  Here only the keys are sorted -- the permutation is applied
+// by the particle kernels, which read their input through it -- with a stable
+// least-significant-digit radix
 // sort over 8-bit digits of the cell key: per pass one histogram kernel, one exclusive scan
 // over the (digit, block) counts and one stable scatter.  Stability within a pass comes
 // from a block-local rank: warps walk their elements in order, peers with the same digit
@@ -47,7 +49,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_scatter(const int *keys_
         const long long e = wbase + (long long)r * 32 + lane;
         const bool ok = e < n;
         key[r] = ok ? keys_in[e] : 0;
-        val[r] = ok ? vals_in[e] : 0;
+        val[r] = ok ? (vals_in ? vals_in[e] : (int)e) : 0;  // first pass: values are the indices
         const int d = ok ? ((key[r] >> shift) & 0xFF) : RADIX;  // sentinel digit for padding
         const unsigned peers = __match_any_sync(0xffffffffu, d);
         const int before = __popc(peers & lt);
@@ -164,50 +166,21 @@ size_t sort_scratch_bytes(long long n)
     return (size_t)(4 * n + 2 * RADIX * nblocks) * sizeof(int) + scan_tmp_ints(RADIX * nblocks) * sizeof(int);
 }
 
-__global__ void k_iota(int *out, long long n)
-{
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = (int)i;
-}
-
-void launch_iota(int *out, long long n, cudaStream_t s)
-{
-    if (n > 0) {
-        k_iota<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(out, n);
-        note_launch(1);
-    }
-}
-
-__global__ void k_extract_keys(PView P, long long n, int *keys)
-{
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) keys[i] = P.ii(PF_KEY, i);
-}
-
-void launch_extract_keys(const PView &p, long long n, int *keys, cudaStream_t s)
-{
-    if (n > 0) {
-        k_extract_keys<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p, n, keys);
-        note_launch(1);
-    }
-}
-
 // Sorts keys_in[0..n) (non-negative, < 2^key_bits) stably; perm_out[i] is the input index
-// of the i-th element in sorted order.
-void sort_pairs(const int *keys_in, int *perm_out, long long n, int key_bits, SortScratch &ws, cudaStream_t s)
+// of the i-th element in sorted order.  Returns the device array holding the sorted keys.
+const int *sort_pairs(const int *keys_in, int *perm_out, long long n, int key_bits, SortScratch &ws, cudaStream_t s)
 {
-    if (n <= 0) return;
+    if (n <= 0) return keys_in;
     const int nblocks = (int)((n + SORT_TILE - 1) / SORT_TILE);
     int passes = (key_bits + 7) / 8;
     if (passes < 1) passes = 1;
-    launch_iota(ws.vals[0], n, s);
     const int *kin = keys_in;
-    const int *vin = ws.vals[0];
+    const int *vin = nullptr;
     int cur = 0;
     for (int p = 0; p < passes; p++) {
         const int shift = 8 * p;
-        int *kout = ws.keys[cur ^ 1];
-        int *vout = (p == passes - 1) ? perm_out : ws.vals[cur ^ 1];
+        int *kout = ws.keys[cur];
+        int *vout = (p == passes - 1) ? perm_out : ws.vals[cur];
         k_radix_hist<<<nblocks, SORT_THREADS, 0, s>>>(kin, n, shift, ws.hist, nblocks);
         note_launch(1);
         exclusive_scan_int(ws.hist, ws.hist + (long long)RADIX * nblocks, (long long)RADIX * nblocks, ws.scan_tmp, s);
@@ -218,26 +191,30 @@ void sort_pairs(const int *keys_in, int *perm_out, long long n, int key_bits, So
         vin = vout;
         cur ^= 1;
     }
+    return kin;
 }
 
-// out[f][i] = in[f][perm[i]] for the listed fields
-__global__ void k_permute(const float *__restrict__ in, float *__restrict__ out, long long cap, long long n,
-                          const int *__restrict__ perm, const int *__restrict__ fields, int nfields)
+// Segments: starts of the runs of equal cell block in key order (the list is unordered).
+__global__ void k_block_heads(const int *skey, long long n, int *seg_start, int *nseg)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const long long src = perm[i];
-    for (int k = 0; k < nfields; k++) {
-        const long long f = fields[k];
-        out[f * cap + i] = __ldg(&in[f * cap + src]);
-    }
+    const bool head = (i == 0) || ((skey[i] >> CB_SHIFT) != (skey[i - 1] >> CB_SHIFT));
+    const unsigned mask = __ballot_sync(__activemask(), head);
+    if (!mask) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(nseg, __popc(mask));
+    base = __shfl_sync(__activemask(), base, leader);
+    if (head) seg_start[base + __popc(mask & ((1u << lane) - 1u))] = (int)i;
 }
 
-void launch_permute(const float *in, float *out, long long cap, long long n, const int *perm, const int *fields,
-                    int nfields, cudaStream_t s)
+void launch_block_heads(const int *skey, long long n, int *seg_start, int *nseg, cudaStream_t s)
 {
+    cudaMemsetAsync(nseg, 0, sizeof(int), s);
     if (n > 0) {
-        k_permute<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(in, out, cap, n, perm, fields, nfields);
+        k_block_heads<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(skey, n, seg_start, nseg);
         note_launch(1);
     }
 }

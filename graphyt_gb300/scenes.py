@@ -146,7 +146,7 @@ def _finish(scene: Scene, seed: int) -> Scene:
 # ------------------------------------------------------------------------------------------
 # named workloads
 
-def elastic_cube(variant: str = "particle", scale: int = 1, seed: int = 0) -> Scene:
+def elastic_cube(variant: str = "particle", scale: int = 1, seed: int = 0, offset=None) -> Scene:
     """Elastic cube compression: 1 m periodic domain, cellsize 0.05/scale, psep half of it,
     a 0.5 m cube centred in the domain (20^3 = 8000 particles at scale 1), K 1e7, G 5e6,
     rho 1000, no gravity, dt = 0.3*dx/sqrt((K+4G/3)/rho) through setDt.
@@ -156,10 +156,18 @@ def elastic_cube(variant: str = "particle", scale: int = 1, seed: int = 0) -> Sc
                          at rest (bug-compatible run).
     variant "fixed":    the same nodal BCs with fixed_grid_bcs=1 (working z BCs).
     variant "particle": mp_vz on the top particle layer (-0.1) and bottom layer (0).
+
+    offset shifts the whole lattice.  The centred lattice puts the cube's outer particles
+    exactly on the edge of the GIMP support of the next node layer; there the reference's
+    own result is discontinuous in the particle position (a node reached with a vanishing
+    weight contributes a finite strain rate through f/m), so long runs are ill-conditioned
+    in FP64 as well.  A shift of a few millimetres removes that degeneracy.
     """
     h = 0.05 / scale
     psep = h / 2
     pos = lattice_box([0.25, 0.25, 0.25], [0.75, 0.75, 0.75], psep)
+    if offset is not None:
+        pos = pos + np.asarray(offset, np.float64)
     n = len(pos)
     K, G, rho = 1e7, 5e6, 1000.0
     sc = Scene("elastic_cube_" + variant, [1.0, 1.0, 1.0], h, psep, pos, np.zeros(n, np.int32),
@@ -281,5 +289,53 @@ def tiny_block(seed: int = 0, model: int = 1, n_side: int = 4, cellsize: float =
     v = np.zeros((n, 3))
     v[:] = vel
     v += 0.05 * np.random.default_rng(seed + 1).standard_normal((n, 3))
+    sc.vel = v
+    return _finish(sc, seed)
+
+
+def damage_block(seed: int = 0, n_side: int = 8) -> Scene:
+    """A Drucker-Prager + Grady-Kipp block on a 12^3-cell grid, stretched along x and
+    squeezed along z by its initial velocity field so that both the damage growth (tension)
+    and the plastic return (compression) act within a few tens of steps."""
+    h = 0.125
+    psep = h / 2
+    lo = np.array([0.45, 0.45, 0.45])
+    pos = lattice_box(lo, lo + n_side * psep, psep)
+    n = len(pos)
+    c = pos.mean(axis=0)
+    rock = material(bulkMod=1e6, shearMod=6e5, density=1500.0, cohesion=3e3, phi=30.0, psi=5.0,
+                    criticalStrain=0.02, isDamage=1, damageModel=1, Cg=0.05, damageM=9.0,
+                    damageK=1e28, model=4)
+    sc = Scene("damage_block", [1.5, 1.5, 1.5], h, psep, pos, np.zeros(n, np.int32), np.zeros(n, np.int32),
+               [rock])
+    sc.CFL = 0.3
+    v = np.zeros((n, 3))
+    v[:, 0] = 3.0 * (pos[:, 0] - c[0])
+    v[:, 2] = -2.0 * (pos[:, 2] - c[2])
+    v += 0.02 * np.random.default_rng(seed + 5).standard_normal((n, 3))
+    sc.vel = v
+    return _finish(sc, seed)
+
+
+def two_blocks(seed: int = 0, speed: float = 1.5, rigid_second: bool = False) -> Scene:
+    """Two elastic blocks (objectIDs 1 and 2) approaching along x at +/-speed: the two-body
+    contact branch of the nodal solve (Grid.cpp:50-219).  With rigid_second the second block
+    is a rigid platen (Grid.cpp:78-105)."""
+    h = 0.0625
+    psep = h / 2
+    a = lattice_box([0.35, 0.40, 0.40], [0.60, 0.65, 0.65], psep)
+    b = lattice_box([0.66, 0.40, 0.40], [0.91, 0.65, 0.65], psep)
+    pos = np.concatenate([a, b])
+    obj = np.concatenate([np.full(len(a), 1), np.full(len(b), 2)]).astype(np.int32)
+    mat = np.concatenate([np.zeros(len(a)), np.full(len(b), 1 if rigid_second else 0)]).astype(np.int32)
+    mats = [material(bulkMod=2e6, shearMod=1e6, density=1000.0, model=1)]
+    if rigid_second:
+        mats.append(material(isRigid=1))
+    sc = Scene("two_blocks_rigid" if rigid_second else "two_blocks", [1.25, 1.0, 1.0], h, psep, pos, mat, obj, mats)
+    sc.CFL = 0.3
+    sc.mu = 0.2
+    v = np.zeros((len(pos), 3))
+    v[obj == 1, 0] = speed
+    v[obj == 2, 0] = -speed
     sc.vel = v
     return _finish(sc, seed)

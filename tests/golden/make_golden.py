@@ -32,6 +32,9 @@ CASES = {
     "cube_nodal_fixed": (lambda: scenes.elastic_cube("fixed"), 30, 2000),
     "dam_break_coarse": (lambda: scenes.dam_break(scale=0.125), 30, 2000),
     "brazilian_coarse": (lambda: scenes.brazilian_disc(scale=0.1), 20, 3000),
+    "damage_block": (lambda: scenes.damage_block(), 40, None),
+    "two_blocks": (lambda: scenes.two_blocks(), 40, None),
+    "two_blocks_rigid": (lambda: scenes.two_blocks(rigid_second=True), 40, None),
 }
 
 

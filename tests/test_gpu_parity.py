@@ -49,6 +49,10 @@ ONE_STEP_CASES = {
     "cube_particle_bc": lambda: scenes.elastic_cube("particle"),
     "cube_nodal_fixed": lambda: scenes.elastic_cube("fixed"),
     "dam_break_coarse": lambda: scenes.dam_break(scale=0.125),
+    "damage_block": lambda: scenes.damage_block(),
+    "two_blocks": lambda: scenes.two_blocks(),
+    "two_blocks_rigid": lambda: scenes.two_blocks(rigid_second=True),
+    "brazilian_coarse": lambda: scenes.brazilian_disc(scale=0.1),
 }
 
 
@@ -69,14 +73,15 @@ def test_one_step_parity(gpu_lib, oracle_built, name):
 
 
 @pytest.mark.parametrize("name", ["tiny_elastic", "tiny_newtonian", "tiny_vonmises", "tiny_druckerprager",
-                                  "cube_particle_bc", "cube_nodal_fixed", "dam_break_coarse"])
+                                  "cube_particle_bc", "cube_nodal_fixed", "dam_break_coarse", "damage_block",
+                                  "two_blocks", "two_blocks_rigid", "brazilian_coarse"])
 def test_golden_parity(gpu_lib, name):
     """The GPU path reproduces the reference's own output (golden fixture) over many steps."""
     gold = np.load(os.path.join(GOLDEN, name + ".npz"))
     make, steps, _ = make_golden.CASES[name]
     gpu = run_gpu(make(), int(gold["steps"]))
     ids = gold["ids"]
-    for f in ("vel", "stress", "density"):
+    for f in ("vel", "stress", "density", "damage", "eqps"):
         a = gpu._get_particles(f)[ids]
         b = gold[f]
         if np.linalg.norm(b) == 0:
@@ -85,9 +90,14 @@ def test_golden_parity(gpu_lib, name):
             assert rel_l2(a, b) <= MANY_STEP_TOL, (name, f, rel_l2(a, b))
 
 
+CUBE_SHIFT = (0.0031, 0.0017, 0.0023)
+
+
 def test_cube_1000_steps(gpu_lib, oracle_built):
-    """Elastic cube compression, 8000 particles, 1000 steps: relative L2 <= 1e-3."""
-    sc = scenes.elastic_cube("particle")
+    """Elastic cube compression, 8000 particles, 1000 steps: relative L2 <= 1e-3.  The
+    lattice is shifted by a few millimetres: on the centred lattice the reference itself
+    moves by 6e-2 in stress after 1000 steps under a 1e-9 m position perturbation."""
+    sc = scenes.elastic_cube("particle", offset=CUBE_SHIFT)
     gpu = run_gpu(sc, 1000)
     ref = run_oracle(sc, 1000)
     for f in ("vel", "stress"):
@@ -118,6 +128,17 @@ def test_mass_conservation_and_stats(gpu_lib):
     assert abs(st["mass"] - m) <= 1e-9 * m
     assert st["active_nodes"] > 0
     assert st["steps"] == 5
+
+
+def test_multibody_node_slots_match_reference_rule(gpu_lib, oracle_built):
+    """Two-body contact: the GPU's body-slot rule reproduces the reference's first-come
+    assignment, so contact nodes see the same bodies (compared through the particle state
+    after steps that cross the 10-step sort cadence)."""
+    sc = scenes.two_blocks()
+    gpu = run_gpu(sc, 25)
+    ref = run_oracle(sc, 25)
+    for f in ("vel", "stress"):
+        assert rel_l2(gpu._get_particles(f), ref.pfield(f)) <= MANY_STEP_TOL
 
 
 def test_sort_every_does_not_change_results(gpu_lib):

@@ -56,7 +56,6 @@ struct gy_solver {
     int *d_perm = nullptr;
     int *d_seg = nullptr, *d_nseg = nullptr;   // non-empty cell-block segments
     int persist_grid = 1;
-    bool acc_ready = false;                    // accumulators already hold this step's P2G
     SortScratch ws{};
     void *sort_mem = nullptr;
     float4 *d_pbc_val = nullptr;
@@ -587,7 +586,7 @@ gy_status gy_initialize(gy_solver *h, const gy_material *mats, int nmat, const g
         int dev = 0, sms = 1;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        h->persist_grid = sms * g2p2g_blocks_per_sm(h->has_dp);
+        h->persist_grid = sms * p2g_blocks_per_sm();
     }
     if ((st = alloc_nodes(h))) return st;
     CK(h, cudaStreamSynchronize(h->stream));
@@ -596,7 +595,6 @@ gy_status gy_initialize(gy_solver *h, const gy_material *mats, int nmat, const g
     h->t_prev = 0.0;
     h->since_sort = 1 << 30;
     h->tables_valid = false;
-    h->acc_ready = false;
     return GY_OK;
 }
 
@@ -700,24 +698,16 @@ static gy_status enqueue_step(gy_solver *h, double t, int step)
         h->tables_valid = true;
     }
     if (timing) cudaEventRecord(tev[1], s);
-    // (b) P2G, unless the previous step's fused pass already accumulated it
-    if (h->multi || !h->acc_ready)
-        launch_p2g(src, perm, skey, h->n, h->d_seg, h->d_nseg, h->persist_grid, h->nb, a, s);
+    // (b) P2G
+    launch_p2g(src, perm, skey, h->n, h->d_seg, h->d_nseg, h->persist_grid, h->nb, a, s);
     if (timing) cudaEventRecord(tev[2], s);
     // (c) periodic fold, nodal solve, grid BCs
     launch_fold(h->nb, a, s);
     launch_solve(h->nb, a, h->opt.keep_node_fields != 0, s);
     if (timing) cudaEventRecord(tev[3], s);
-    // (d) G2P + particle BCs + update + constitutive + damage (+ next step's P2G)
-    if (h->multi) {
-        launch_g2p_update(src, dst, perm, h->n, h->nb, a, h->opt.track_normals != 0, h->opt.check_finite != 0,
-                          h->has_dp, s);
-        h->acc_ready = false;
-    } else {
-        launch_g2p2g(src, dst, perm, skey, h->n, h->d_seg, h->d_nseg, h->persist_grid, h->nb, a,
-                     h->opt.check_finite != 0, h->has_dp, s);
-        h->acc_ready = true;
-    }
+    // (d) G2P + particle BCs + update + constitutive + damage, written in sorted order
+    launch_g2p_update(src, dst, perm, h->n, h->nb, a, h->opt.track_normals != 0, h->opt.check_finite != 0,
+                      h->has_dp, s);
     h->cur ^= 1;
     if (timing) cudaEventRecord(tev[4], s);
     cudaError_t e = cudaGetLastError();

@@ -18,6 +18,7 @@
 // P2G is a particle-centric scatter: the reference gathers per node over a 4x4x4 cell
 // window (Extrapolation.cpp:31-125), but a particle contributes exactly to the nodes of its
 // GIMP support, so scattering over its 3x3x3 stencil sums the same terms.
+#include <algorithm>
 #include <atomic>
 #include <cstdio>
 
@@ -141,123 +142,155 @@ __device__ __forceinline__ void make_stencil(const PState &st, const GridGeom &g
 }
 
 // ---------------------------------------------------------------------------------------
-// P2G of one particle, single-body: mass, momentum and internal force.  Gravity is added
-// per node in the solve as m_node * g, which equals sum_p w m_p g (Extrapolation.cpp:226-278).
+// Single-body P2G through a shared-memory node tile.  Gravity is added per node in the
+// solve as m_node * g, which equals sum_p w m_p g (Extrapolation.cpp:226-278).
+//
+// A CTA owns one segment (the particles of one 4x4x4 cell block, freshly sorted), whose
+// stencils lie in the 6x6x6 node tile [4b, 4b+6).  Each chunk of 256 particles is first
+// loaded in natural (coalesced) order and its P2G payload staged in shared memory; the
+// scatter then reads the payload transposed, lane l of warp w taking particle 8l + w, so
+// the 32 lanes of a warp belong to ~32 different cells (8 particles per cell) and, for a
+// given stencil offset, add into 32 different tile nodes: the shared-memory atomics of one
+// instruction do not collide.
 
-constexpr int TILE = 8;                 // node tile edge: a cell block's stencil nodes +- 1
-constexpr int TILE_NODES = TILE * TILE * TILE;
-constexpr int TILE_FIELDS = 7;          // m, px, py, pz, fx, fy, fz
+constexpr int PT = 6;                  // tile edge in nodes
+constexpr int PT_NODES = PT * PT * PT; // 216
+constexpr int P2G_FIELDS = 7;          // m, px, py, pz, fx, fy, fz
+constexpr int PAY = 14;                // staged payload per particle
 
-__device__ __forceinline__ void p2g_single(const PState &st, const GridGeom &g, float *tile, int tox, int toy, int toz,
-                                           const NodeBufs &nb, int rot)
+// end of the segment starting at `start` in block `blk`: binary search on sorted keys
+__device__ __forceinline__ long long sorted_segment_end(const int *skey, long long n, long long start, int blk)
 {
-    Stencil w;
-    make_stencil(st, g, w);
-    const float m = st.mass;
-    const float sc = (m / st.rho) * g.inv_h;  // V sigma with the gradient's 1/h
-    const float s0 = st.s[0] * sc, s1 = st.s[1] * sc, s2 = st.s[2] * sc;
-    const float s3 = st.s[3] * sc, s4 = st.s[4] * sc, s5 = st.s[5] * sc;
-    const float mvx = m * st.v[0], mvy = m * st.v[1], mvz = m * st.v[2];
-    const int ti = w.c[0] - tox, tj = w.c[1] - toy, tk = w.c[2] - toz;
-    const bool in_tile = tile && ti >= 0 && tj >= 0 && tk >= 0 && ti + w.cnt[0] <= TILE && tj + w.cnt[1] <= TILE &&
-                         tk + w.cnt[2] <= TILE;
-    const int nxy = w.cnt[0] * w.cnt[1];
-    const int total = nxy * w.cnt[2];
-    for (int q0 = 0; q0 < total; q0++) {
-        // rotate the visiting order per lane so that particles of one cell hit different nodes
-        int q = q0 + rot;
-        while (q >= total) q -= total;
-        const int kk = q / nxy;
-        const int r = q - kk * nxy;
-        const int jj = r / w.cnt[0];
-        const int ii = r - jj * w.cnt[0];
-        const float sx = sel3(w.S[0], ii), sy = sel3(w.S[1], jj), sz = sel3(w.S[2], kk);
-        const float syz = sy * sz;
-        const float wgt = sx * syz;
-        const float gx = sel3(w.G[0], ii) * syz;
-        const float gy = sx * sel3(w.G[1], jj) * sz;
-        const float gz = sx * sy * sel3(w.G[2], kk);
-        const float fx = -(gx * s0 + gy * s3 + gz * s5);
-        const float fy = -(gx * s3 + gy * s1 + gz * s4);
-        const float fz = -(gx * s5 + gy * s4 + gz * s2);
-        if (in_tile) {
-            const int t = ((tk + kk) * TILE + (tj + jj)) * TILE + (ti + ii);
-            atomicAdd(&tile[0 * TILE_NODES + t], wgt * m);
-            atomicAdd(&tile[1 * TILE_NODES + t], wgt * mvx);
-            atomicAdd(&tile[2 * TILE_NODES + t], wgt * mvy);
-            atomicAdd(&tile[3 * TILE_NODES + t], wgt * mvz);
-            atomicAdd(&tile[4 * TILE_NODES + t], fx);
-            atomicAdd(&tile[5 * TILE_NODES + t], fy);
-            atomicAdd(&tile[6 * TILE_NODES + t], fz);
-        } else {
-            const int ni = w.c[0] + ii, nj = w.c[1] + jj, nk = w.c[2] + kk;
+    long long lo = start, hi = n;  // first index with block > blk
+    while (lo < hi) {
+        const long long mid = (lo + hi) >> 1;
+        if ((skey[mid] >> CB_SHIFT) <= blk) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Segment bounds when the keys are not freshly sorted: runs of one block can repeat, so
+// the run ends at the first index after `base` whose block differs (per chunk).
+__device__ __forceinline__ long long segment_chunk_end(const int *skey, long long n, int blk, long long base,
+                                                       long long *s_end)
+{
+    if (threadIdx.x == 0) *s_end = base + blockDim.x;
+    __syncthreads();
+    const long long i = base + threadIdx.x;
+    const bool inb = i < n && (skey[i] >> CB_SHIFT) == blk;
+    if (!inb) atomicMin((unsigned long long *)s_end, (unsigned long long)i);
+    __syncthreads();
+    const long long e = *s_end;
+    __syncthreads();  // every thread has read s_end before thread 0 resets it
+    return e;
+}
+
+__device__ __forceinline__ int seg_block(const int *skey, long long start) { return skey[start] >> CB_SHIFT; }
+
+__global__ void __launch_bounds__(256) k_p2g_tiled(PView P, const int *perm, const int *skey, long long n,
+                                                    const int *seg_start, const int *nseg_ptr, int sorted,
+                                                    NodeBufs nb, GridGeom g)
+{
+    __shared__ float tile[P2G_FIELDS * PT_NODES];
+    __shared__ float pay[PAY * 256];
+    __shared__ long long s_end;
+    const int nseg = *nseg_ptr;
+    const int tid = threadIdx.x;
+    const int jt = (tid & 31) * 8 + (tid >> 5);  // transposed slot (blockDim.x == 256)
+    for (int sgi = blockIdx.x; sgi < nseg; sgi += gridDim.x) {
+        const long long start = seg_start[sgi];
+        const int blk = seg_block(skey, start);
+        int bx, by, bz;
+        decode_block(blk, g, bx, by, bz);
+        const int tox = bx * CB, toy = by * CB, toz = g.is3d ? bz * CB : 0;
+        for (int t = tid; t < P2G_FIELDS * PT_NODES; t += 256) tile[t] = 0.f;
+        const long long send = sorted ? sorted_segment_end(skey, n, start, blk) : -1;
+        for (long long base = start;; base += 256) {
+            long long end = send;
+            if (!sorted) end = segment_chunk_end(skey, n, blk, base, &s_end);
+            const int cnt = (int)min((long long)256, end - base);
+            if (cnt <= 0) break;
+            // ---- stage the payload in natural order ----
+            __syncthreads();
+            if (tid < cnt) {
+                const long long i = base + tid;
+                const long long j = perm ? perm[i] : i;
+                int ci, cj, ck;
+                decode_key(P.ii(PF_KEY, j), g, ci, cj, ck);
+                const float m = P.f(PF_MASS, j);
+                const float sc = (m / P.f(PF_RHO, j)) * g.inv_h;  // V sigma with the gradient's 1/h
+                pay[0 * 256 + tid] = __int_as_float((ci - tox) | ((cj - toy) << 8) | ((g.is3d ? ck - toz : 0) << 16));
+                pay[1 * 256 + tid] = P.f(PF_OX, j);
+                pay[2 * 256 + tid] = P.f(PF_OY, j);
+                pay[3 * 256 + tid] = P.f(PF_OZ, j);
+                pay[4 * 256 + tid] = m;
+                pay[5 * 256 + tid] = m * P.f(PF_VX, j);
+                pay[6 * 256 + tid] = m * P.f(PF_VY, j);
+                pay[7 * 256 + tid] = m * P.f(PF_VZ, j);
+#pragma unroll
+                for (int k = 0; k < 6; k++) pay[(8 + k) * 256 + tid] = P.f(PF_S0 + k, j) * sc;
+            }
+            __syncthreads();
+            // ---- transposed scatter ----
+            if (jt < cnt) {
+                const int lc = __float_as_int(pay[jt]);
+                const int li = lc & 0xff, lj = (lc >> 8) & 0xff, lk = (lc >> 16) & 0xff;
+                float Sx[3], Gx[3], Sy[3], Gy[3], Sz[3] = {1.f, 0.f, 0.f}, Gz[3] = {0.f, 0.f, 0.f};
+                const float ox = pay[256 + jt], oy = pay[2 * 256 + jt];
+                gimp_axis(ox, g.lp, Sx, Gx);
+                gimp_axis(oy, g.lp, Sy, Gy);
+                int nkz = 1;
+                if (g.is3d) {
+                    const float oz = pay[3 * 256 + jt];
+                    gimp_axis(oz, g.lp, Sz, Gz);
+                    nkz = (oz < 1.0f - g.lp) ? 2 : 3;
+                }
+                const int nix = (ox < 1.0f - g.lp) ? 2 : 3, njy = (oy < 1.0f - g.lp) ? 2 : 3;
+                const float m = pay[4 * 256 + jt];
+                const float mvx = pay[5 * 256 + jt], mvy = pay[6 * 256 + jt], mvz = pay[7 * 256 + jt];
+                const float s0 = pay[8 * 256 + jt], s1 = pay[9 * 256 + jt], s2 = pay[10 * 256 + jt];
+                const float s3 = pay[11 * 256 + jt], s4 = pay[12 * 256 + jt], s5 = pay[13 * 256 + jt];
+                const int t0 = (lk * PT + lj) * PT + li;
+#pragma unroll
+                for (int kk = 0; kk < 3; kk++) {
+                    if (kk >= nkz) break;
+#pragma unroll
+                    for (int jj = 0; jj < 3; jj++) {
+                        if (jj >= njy) break;
+                        const float syz = Sy[jj] * Sz[kk], gyz = Gy[jj] * Sz[kk], syg = Sy[jj] * Gz[kk];
+#pragma unroll
+                        for (int ii = 0; ii < 3; ii++) {
+                            if (ii >= nix) break;
+                            const float w = Sx[ii] * syz;
+                            const float gx = Gx[ii] * syz, gy = Sx[ii] * gyz, gz = Sx[ii] * syg;
+                            const int t = t0 + (kk * PT + jj) * PT + ii;
+                            atomicAdd(&tile[0 * PT_NODES + t], w * m);
+                            atomicAdd(&tile[1 * PT_NODES + t], w * mvx);
+                            atomicAdd(&tile[2 * PT_NODES + t], w * mvy);
+                            atomicAdd(&tile[3 * PT_NODES + t], w * mvz);
+                            atomicAdd(&tile[4 * PT_NODES + t], -(gx * s0 + gy * s3 + gz * s5));
+                            atomicAdd(&tile[5 * PT_NODES + t], -(gx * s3 + gy * s1 + gz * s4));
+                            atomicAdd(&tile[6 * PT_NODES + t], -(gx * s5 + gy * s4 + gz * s2));
+                        }
+                    }
+                }
+            }
+            if (cnt < 256) break;
+        }
+        __syncthreads();
+        // ---- flush the tile: two vector reductions per touched node ----
+        for (int t = tid; t < PT_NODES; t += 256) {
+            const float m = tile[t], px = tile[PT_NODES + t], py = tile[2 * PT_NODES + t], pz = tile[3 * PT_NODES + t];
+            const float fx = tile[4 * PT_NODES + t], fy = tile[5 * PT_NODES + t], fz = tile[6 * PT_NODES + t];
+            if (m == 0.f && px == 0.f && py == 0.f && pz == 0.f && fx == 0.f && fy == 0.f && fz == 0.f) continue;
+            const int ni = tox + t % PT, nj = toy + (t / PT) % PT, nk = toz + t / (PT * PT);
+            if (ni >= g.nx || nj >= g.ny || nk >= g.nz) continue;
             const long long nd = node_index(ni, nj, nk, g);
-            red_add4(&nb.acc0[nd], wgt * m, wgt * mvx, wgt * mvy, wgt * mvz);
+            red_add4(&nb.acc0[nd], m, px, py, pz);
             red_add4(&nb.acc1[nd], fx, fy, fz, 0.f);
             mark_node(nb.flags, ni, nj, nk, g);
         }
-    }
-}
-
-__device__ __forceinline__ void tile_zero(float *tile)
-{
-    for (int t = threadIdx.x; t < TILE_FIELDS * TILE_NODES; t += blockDim.x) tile[t] = 0.f;
-}
-
-__device__ __forceinline__ void tile_flush(const float *tile, int tox, int toy, int toz, const GridGeom &g,
-                                           const NodeBufs &nb)
-{
-    for (int t = threadIdx.x; t < TILE_NODES; t += blockDim.x) {
-        const float m = tile[t], px = tile[TILE_NODES + t], py = tile[2 * TILE_NODES + t],
-                    pz = tile[3 * TILE_NODES + t];
-        const float fx = tile[4 * TILE_NODES + t], fy = tile[5 * TILE_NODES + t], fz = tile[6 * TILE_NODES + t];
-        if (m == 0.f && px == 0.f && py == 0.f && pz == 0.f && fx == 0.f && fy == 0.f && fz == 0.f) continue;
-        const int ni = tox + (t % TILE), nj = toy + ((t / TILE) % TILE), nk = toz + t / (TILE * TILE);
-        if (ni < 0 || nj < 0 || nk < 0 || ni >= g.nx || nj >= g.ny || nk >= g.nz) continue;
-        const long long nd = node_index(ni, nj, nk, g);
-        red_add4(&nb.acc0[nd], m, px, py, pz);
-        red_add4(&nb.acc1[nd], fx, fy, fz, 0.f);
-        mark_node(nb.flags, ni, nj, nk, g);
-    }
-}
-
-// Segment bounds: segments start where the cell block of the sorted key changes.
-__device__ __forceinline__ int seg_block(const int *skey, int start) { return skey[start] >> CB_SHIFT; }
-
-__device__ __forceinline__ void tile_origin(int blk, const GridGeom &g, int &tox, int &toy, int &toz)
-{
-    int bx, by, bz;
-    decode_block(blk, g, bx, by, bz);
-    tox = bx * CB - 1;
-    toy = by * CB - 1;
-    toz = g.is3d ? bz * CB - 1 : 0;
-}
-
-// Standalone tiled P2G over the segments (single body).
-__global__ void __launch_bounds__(256) k_p2g_tiled(PView P, const int *perm, const int *skey, long long n,
-                                                    const int *seg_start, const int *nseg_ptr, NodeBufs nb, GridGeom g)
-{
-    __shared__ float tile[TILE_FIELDS * TILE_NODES];
-    const int nseg = *nseg_ptr;
-    for (int sgi = blockIdx.x; sgi < nseg; sgi += gridDim.x) {
-        const int start = seg_start[sgi];
-        const int blk = seg_block(skey, start);
-        int tox, toy, toz;
-        tile_origin(blk, g, tox, toy, toz);
-        tile_zero(tile);
-        __syncthreads();
-        for (long long base = start;; base += blockDim.x) {
-            const long long i = base + threadIdx.x;
-            const bool valid = i < n && (skey[i] >> CB_SHIFT) == blk;
-            if (!__syncthreads_or(valid)) break;
-            if (valid) {
-                PState st;
-                load_state<false>(P, perm ? perm[i] : i, st);
-                p2g_single(st, g, tile, tox, toy, toz, nb, threadIdx.x & 31);
-            }
-        }
-        __syncthreads();
-        tile_flush(tile, tox, toy, toz, g, nb);
         __syncthreads();
     }
 }
@@ -321,9 +354,16 @@ void launch_p2g(const PView &p, const int *perm, const int *skey, long long n, c
     if (a.sc.multi_body) {
         k_p2g_multi<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p, perm, n, nb, a);
     } else {
-        k_p2g_tiled<<<persist_grid, 256, 0, s>>>(p, perm, skey, n, seg_start, nseg, nb, a.g);
+        k_p2g_tiled<<<persist_grid, 256, 0, s>>>(p, perm, skey, n, seg_start, nseg, perm ? 1 : 0, nb, a.g);
     }
     note_launch(1);
+}
+
+int p2g_blocks_per_sm()
+{
+    int b = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_p2g_tiled, 256, 0);
+    return b > 0 ? b : 1;
 }
 
 // ---------------------------------------------------------------------------------------
@@ -435,18 +475,14 @@ __device__ __forceinline__ void contact_normal(const float rv[3], const float n[
     cn[2] = n[2] + on2 * mu;
 }
 
+// One node of an active node block; returns whether the node carries mass.
 template <bool MULTI>
-__global__ void __launch_bounds__(256) k_solve_blocks(NodeBufs nb, StepArgs a, int keep)
+__device__ __forceinline__ bool solve_node(const NodeBufs &nb, const StepArgs &a, int keep, long long blk, int lnode)
 {
     const GridGeom &g = a.g;
-    const long long blk = (long long)blockIdx.x * 4 + (threadIdx.x >> 6);
-    const bool blk_ok = blk < g.nnb;
-    const bool active_blk = blk_ok && nb.flags[blk] != 0;
-    const int warp_any = __syncthreads_or(active_blk);
-    if (!warp_any) return;
     bool active = false;
-    if (active_blk) {
-        const int lx = threadIdx.x & 3, ly = (threadIdx.x >> 2) & 3, lz = (threadIdx.x >> 4) & 3;
+    {
+        const int lx = lnode & 3, ly = (lnode >> 2) & 3, lz = (lnode >> 4) & 3;
         const int bx = (int)(blk % g.nnbx);
         const long long tb = blk / g.nnbx;
         const int by = (int)(tb % g.nnby), bz = (int)(tb / g.nnby);
@@ -590,19 +626,49 @@ __global__ void __launch_bounds__(256) k_solve_blocks(NodeBufs nb, StepArgs a, i
             }
         }
     }
-    if (nb.active_count) {
-        const unsigned mask = __ballot_sync(0xffffffffu, active);
-        if ((threadIdx.x & 31) == 0 && mask) atomicAdd(nb.active_count, __popc(mask));
+    return active;
+}
+
+// Persistent: each warp walks node blocks with a grid stride; an active block's 64 nodes
+// take two passes of the warp.  The flag is cleared once the block's accumulators are read.
+template <bool MULTI>
+__global__ void __launch_bounds__(256) k_solve_blocks(NodeBufs nb, StepArgs a, int keep)
+{
+    const int lane = threadIdx.x & 31;
+    const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    int count = 0;
+    for (long long base = warp * 32; base < a.g.nnb; base += nwarps * 32) {
+        // 32 flags at a time, then the active blocks one by one
+        const long long fb = base + lane;
+        const bool on = fb < a.g.nnb && nb.flags[fb] != 0;
+        unsigned mask = __ballot_sync(0xffffffffu, on);
+        while (mask) {
+            const int b = __ffs(mask) - 1;
+            mask &= mask - 1;
+            const long long blk = base + b;
+            count += solve_node<MULTI>(nb, a, keep, blk, lane) ? 1 : 0;
+            count += solve_node<MULTI>(nb, a, keep, blk, lane + 32) ? 1 : 0;
+            __syncwarp();
+            if (lane == 0) nb.flags[blk] = 0;
+        }
     }
-    __syncthreads();
-    if (active_blk && (threadIdx.x & 63) == 0) nb.flags[blk] = 0;
+    if (nb.active_count) {
+        for (int off = 16; off > 0; off >>= 1) count += __shfl_down_sync(0xffffffffu, count, off);
+        if (lane == 0 && count) atomicAdd(nb.active_count, count);
+    }
 }
 
 void launch_solve(const NodeBufs &nb, const StepArgs &a, bool keep_node_fields, cudaStream_t s)
 {
-    const unsigned grid = (unsigned)((a.g.nnb + 3) / 4);
-    if (a.sc.multi_body) k_solve_blocks<true><<<grid, 256, 0, s>>>(nb, a, keep_node_fields ? 1 : 0);
-    else k_solve_blocks<false><<<grid, 256, 0, s>>>(nb, a, keep_node_fields ? 1 : 0);
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    long long want = (a.g.nnb + 255) / 256;  // one warp per 32 node blocks
+    long long grid = std::min<long long>(want, (long long)sms * 8);
+    if (grid < 1) grid = 1;
+    if (a.sc.multi_body) k_solve_blocks<true><<<(unsigned)grid, 256, 0, s>>>(nb, a, keep_node_fields ? 1 : 0);
+    else k_solve_blocks<false><<<(unsigned)grid, 256, 0, s>>>(nb, a, keep_node_fields ? 1 : 0);
     note_launch(1);
 }
 
@@ -818,40 +884,6 @@ __global__ void __launch_bounds__(256) k_g2p_update(PView src, PView dst, const 
     }
 }
 
-// Fused G2P + update + next step's P2G (single body), persistent over the segments.
-template <bool HAS_DP>
-__global__ void __launch_bounds__(256) k_g2p2g(PView src, PView dst, const int *perm, const int *skey, long long n,
-                                               const int *seg_start, const int *nseg_ptr, NodeBufs nb, StepArgs a,
-                                               int check_finite)
-{
-    __shared__ float tile[TILE_FIELDS * TILE_NODES];
-    const int nseg = *nseg_ptr;
-    for (int sgi = blockIdx.x; sgi < nseg; sgi += gridDim.x) {
-        const int start = seg_start[sgi];
-        const int blk = seg_block(skey, start);
-        int tox, toy, toz;
-        tile_origin(blk, a.g, tox, toy, toz);
-        tile_zero(tile);
-        __syncthreads();
-        for (long long base = start;; base += blockDim.x) {
-            const long long i = base + threadIdx.x;
-            const bool valid = i < n && (skey[i] >> CB_SHIFT) == blk;
-            if (!__syncthreads_or(valid)) break;
-            if (valid) {
-                PState st;
-                load_state<HAS_DP>(src, perm ? perm[i] : i, st);
-                float nrm[3];
-                g2p_update_one<false, HAS_DP>(st, nb, a, false, check_finite != 0, nrm);
-                store_state<HAS_DP>(dst, i, st);
-                p2g_single(st, a.g, tile, tox, toy, toz, nb, threadIdx.x & 31);
-            }
-        }
-        __syncthreads();
-        tile_flush(tile, tox, toy, toz, a.g, nb);
-        __syncthreads();
-    }
-}
-
 void launch_g2p_update(const PView &src, const PView &dst, const int *perm, long long n, const NodeBufs &nb,
                        const StepArgs &a, bool track_normals, bool check_finite, bool has_dp, cudaStream_t s)
 {
@@ -866,25 +898,6 @@ void launch_g2p_update(const PView &src, const PView &dst, const int *perm, long
         else k_g2p_update<false, false><<<grid, 256, 0, s>>>(src, dst, perm, n, nb, a, 0, cf);
     }
     note_launch(1);
-}
-
-void launch_g2p2g(const PView &src, const PView &dst, const int *perm, const int *skey, long long n,
-                  const int *seg_start, const int *nseg, int persist_grid, const NodeBufs &nb, const StepArgs &a,
-                  bool check_finite, bool has_dp, cudaStream_t s)
-{
-    if (n == 0) return;
-    const int cf = check_finite ? 1 : 0;
-    if (has_dp) k_g2p2g<true><<<persist_grid, 256, 0, s>>>(src, dst, perm, skey, n, seg_start, nseg, nb, a, cf);
-    else k_g2p2g<false><<<persist_grid, 256, 0, s>>>(src, dst, perm, skey, n, seg_start, nseg, nb, a, cf);
-    note_launch(1);
-}
-
-int g2p2g_blocks_per_sm(bool has_dp)
-{
-    int b = 0;
-    if (has_dp) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_g2p2g<true>, 256, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_g2p2g<false>, 256, 0);
-    return b > 0 ? b : 1;
 }
 
 // ---------------------------------------------------------------------------------------

@@ -229,7 +229,7 @@ def dam_break(scale: float = 1.0, height: float = 0.765, seed: int = 0, walls: b
     return _finish(sc, seed)
 
 
-def brazilian_disc(scale: float = 1.0, seed: int = 0, platen_speed: float = 0.5) -> Scene:
+def brazilian_disc(scale: float = 1.0, seed: int = 0, platen_speed: float = 0.5, shift: bool = True) -> Scene:
     """3D Brazilian disc: a Drucker-Prager + Grady-Kipp cylinder (radius 0.05 m, thickness
     0.02 m, axis along z) squeezed along y by two rigid platens at +/-platen_speed.
     cellsize 5e-4/scale, psep half of it.  DP: K 3e10, G 2e10, rho 2600, cohesion 1e7,
@@ -237,7 +237,12 @@ def brazilian_disc(scale: float = 1.0, seed: int = 0, platen_speed: float = 0.5)
     P-wave speed (1867.40 m/s).  objectIDs: disc 1, top platen 2, bottom platen 3 (the
     layout of Examples/brazillian3D.py:31-108).  At scale 1 this is about 10 M particles;
     the reference's Grady-Kipp has no per-particle Weibull flaws (DamageModels.cpp:102-103),
-    so the flaw threshold is the deterministic e_min = (V k)^(-1/m)."""
+    so the flaw threshold is the deterministic e_min = (V k)^(-1/m).
+
+    shift moves the whole lattice by (0.0931, 0.0517, 0.0713) psep.  Unshifted, particles sit
+    exactly on the reference's quarter-cell binning boundaries (TimeIntegration.cpp:111-113),
+    where its own FP64 rounding decides which cell -- and so which body slot of a contact
+    node (Extrapolation.cpp:191-198) -- a particle lands in."""
     h = 5e-4 / scale
     psep = h / 2
     R, T = 0.05, 0.02
@@ -254,6 +259,8 @@ def brazilian_disc(scale: float = 1.0, seed: int = 0, platen_speed: float = 0.5)
     top = lattice_box([cx - half, cy + R + psep, z0], [cx + half, cy + R + psep + pw, z0 + T], psep)
     bot = lattice_box([cx - half, cy - R - psep - pw, z0], [cx + half, cy - R - psep, z0 + T], psep)
     pos = np.concatenate([disc, top, bot])
+    if shift:
+        pos = pos + np.array([0.0931, 0.0517, 0.0713]) * psep
     mat = np.concatenate([np.zeros(len(disc)), np.ones(len(top)), np.ones(len(bot))]).astype(np.int32)
     obj = np.concatenate([np.full(len(disc), 1), np.full(len(top), 2), np.full(len(bot), 3)]).astype(np.int32)
     K, G, rho = 3e10, 2e10, 2600.0
@@ -337,5 +344,35 @@ def two_blocks(seed: int = 0, speed: float = 1.5, rigid_second: bool = False) ->
     v = np.zeros((len(pos), 3))
     v[obj == 1, 0] = speed
     v[obj == 2, 0] = -speed
+    sc.vel = v
+    return _finish(sc, seed)
+
+
+def block_2d(seed: int = 0, model: int = 1, platen: bool = True) -> Scene:
+    """2D plane-strain block (L[2] = 0) in the layout of the reference's 2D tests
+    (test/test_2d_elastic_uniaxial_compression.py): a rock block, optionally under a rigid
+    platen moving down at 0.2 m/s, gravity off."""
+    h = 0.01
+    psep = h / 2
+    blk = lattice_box([0.05, 0.03, 0.0], [0.15, 0.23, 0.0], psep)
+    parts = [blk]
+    mat = [np.zeros(len(blk))]
+    obj = [np.full(len(blk), 1)]
+    if platen:
+        pl = lattice_box([0.04, 0.23 + psep, 0.0], [0.16, 0.23 + psep + 3 * psep, 0.0], psep)
+        parts.append(pl)
+        mat.append(np.ones(len(pl)))
+        obj.append(np.full(len(pl), 2))
+    pos = np.concatenate(parts)
+    mats = [material(bulkMod=3.31e9, shearMod=2.48e9, density=1540.0, yieldStress=2e5, cohesion=1e5, phi=30.0,
+                     psi=5.0, model=model)]
+    if platen:
+        mats.append(material(isRigid=1))
+    sc = Scene(f"block_2d_m{model}", [0.3, 0.3, 0.0], h, psep, pos, np.concatenate(mat).astype(np.int32),
+               np.concatenate(obj).astype(np.int32), mats)
+    sc.CFL = 0.3
+    v = np.zeros((len(pos), 3))
+    if platen:
+        v[sc.obj == 2, 1] = -0.2
     sc.vel = v
     return _finish(sc, seed)

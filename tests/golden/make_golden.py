@@ -35,6 +35,8 @@ CASES = {
     "damage_block": (lambda: scenes.damage_block(), 40, None),
     "two_blocks": (lambda: scenes.two_blocks(), 40, None),
     "two_blocks_rigid": (lambda: scenes.two_blocks(rigid_second=True), 40, None),
+    "block_2d_elastic": (lambda: scenes.block_2d(model=1), 200, None),
+    "block_2d_dp": (lambda: scenes.block_2d(model=4), 200, None),
 }
 
 

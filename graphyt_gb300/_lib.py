@@ -13,6 +13,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libgraphyt_gpu.so")
 
+GY_SORT_STATIC_MAX = 262144
+
 GY_OK, GY_ERR_ARG, GY_ERR_CUDA, GY_ERR_STATE, GY_ERR_RANGE, GY_ERR_UNSUPPORTED, GY_ERR_NONFINITE, GY_ERR_NOMEM = (
     0, -1, -2, -3, -4, -5, -6, -7)
 STATUS_NAMES = {0: "GY_OK", -1: "GY_ERR_ARG", -2: "GY_ERR_CUDA", -3: "GY_ERR_STATE", -4: "GY_ERR_RANGE",
@@ -87,6 +89,7 @@ SIGNATURES = {
     "gy_get_particles_int": (C.c_int, [_vp, C.c_int, _ip, C.c_int64]),
     "gy_get_nodes": (C.c_int, [_vp, C.c_int, _dp, C.c_int64]),
     "gy_sort_keys": (C.c_int, [_ip, C.c_int64, _ip, C.c_int]),
+    "gy_sort_keys_static": (C.c_int, [C.c_void_p, C.c_int64, C.c_int, C.c_void_p, C.c_void_p]),
     "gy_get_stats": (C.c_int, [_vp, C.POINTER(Stats)]),
     "gy_set_phase_timing": (C.c_int, [_vp, C.c_int]),
     "gy_get_phase_times": (C.c_int, [_vp, C.POINTER(C.c_float), _i64p]),

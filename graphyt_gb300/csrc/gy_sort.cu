@@ -9,6 +9,9 @@
 // from a block-local rank: warps walk their elements in order, peers with the same digit
 // are found with __match_any_sync, and per-warp digit counters are prefix-summed across
 // warps.  The result is bit-identical to a CPU stable sort of the same keys.
+#include <mutex>
+
+#include "../../include/graphyt_gpu.h"
 #include "gy_kernels.cuh"
 
 namespace gy {
@@ -219,4 +222,61 @@ void launch_block_heads(const int *skey, long long n, int *seg_start, int *nseg,
     }
 }
 
+// ---- allocation-free sort (gy_sort_keys_static) ----
+// The scratch of the radix sort -- two key and two index ping-pong buffers, the per-pass
+// (digit, block) histograms and the scan workspace -- for up to GY_SORT_STATIC_MAX keys, in
+// one file-scope device array.  Every GPU that loads this library holds it (about 4.3 MB)
+// until the process exits.
+constexpr long long kStaticMax = GY_SORT_STATIC_MAX;
+constexpr long long kStaticBlocks = (kStaticMax + SORT_TILE - 1) / SORT_TILE;
+constexpr long long kStaticScanInts = 4096;
+constexpr long long kStaticInts = 4 * kStaticMax + 2 * RADIX * kStaticBlocks + kStaticScanInts;
+static __device__ __align__(256) int g_sort_static[kStaticInts];
+
+// Device address of g_sort_static per device ordinal, looked up once with that device current.
+static std::mutex g_static_mu;
+static int *g_static_addr[256] = {};
+
+static gy_status static_scratch(int **out)
+{
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) return GY_ERR_CUDA;
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (!g_static_addr[dev]) {
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_sort_static) != cudaSuccess || !p) return GY_ERR_CUDA;
+        g_static_addr[dev] = static_cast<int *>(p);
+    }
+    *out = g_static_addr[dev];
+    return GY_OK;
+}
+
 }  // namespace gy
+
+extern "C" gy_status gy_sort_keys_static(const int *d_keys, int64_t n, int key_bits, int *d_perm_out, void *stream)
+{
+    using namespace gy;
+    if (n < 0 || n > kStaticMax) return GY_ERR_ARG;  // the fixed scratch holds GY_SORT_STATIC_MAX keys
+    if (key_bits < 1 || key_bits > 31) return GY_ERR_ARG;
+    if (n == 0) return GY_OK;
+    if (!d_keys || !d_perm_out) return GY_ERR_ARG;
+    if (scan_tmp_ints(RADIX * kStaticBlocks) > (size_t)kStaticScanInts) return GY_ERR_UNSUPPORTED;
+    int *base = nullptr;
+    gy_status st = static_scratch(&base);
+    if (st != GY_OK) return st;
+    // carve the static array exactly as the allocating sort carves its buffer; every
+    // region is fully rewritten by each pass, so nothing needs clearing between calls
+    SortScratch ws{};
+    int *p = base;
+    ws.keys[0] = p; p += kStaticMax;
+    ws.keys[1] = p; p += kStaticMax;
+    ws.vals[0] = p; p += kStaticMax;
+    ws.vals[1] = p; p += kStaticMax;
+    ws.hist = p; p += 2 * RADIX * kStaticBlocks;
+    ws.scan_tmp = p;
+    ws.cap = kStaticMax;
+    ws.nblocks_cap = (int)kStaticBlocks;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    (void)sort_pairs(d_keys, d_perm_out, n, key_bits, ws, s);
+    return cudaGetLastError() == cudaSuccess ? GY_OK : GY_ERR_CUDA;
+}

@@ -187,6 +187,24 @@ gy_status gy_get_nodes(gy_solver *h, int field, double *out, int64_t count);
  * arrays; for testing the sort against a CPU stable sort. */
 gy_status gy_sort_keys(const int *keys, int64_t n, int *perm_out, int device);
 
+/* Allocation-free form of gy_sort_keys.  It has no counterpart in the reference.  Some
+ * callers cannot call cudaMalloc or cudaFree at the point where they sort: a host framework
+ * that owns all device memory through its own pool and forbids other allocations, or a
+ * step loop that cannot absorb the device-wide synchronisation cudaFree implies.  This
+ * entry point sorts device-resident keys with the same stable radix sort, taking its
+ * scratch from a fixed array compiled into the library instead of allocating it.
+ *   d_keys      n device ints, non-negative and below 2^key_bits (1 <= key_bits <= 31)
+ *   d_perm_out  n device ints: index of the i-th key in ascending order, ties in input order
+ *   stream      a cudaStream_t (NULL = legacy default stream); the call only enqueues work
+ * Limit: n <= GY_SORT_STATIC_MAX; larger n returns GY_ERR_ARG before any GPU work.  The
+ * scratch (about 4.3 MB) is held on every GPU that loads the library until the process
+ * exits.  The first call on a device looks the scratch's device address up once, on the
+ * calling thread's current device; make that first call before any stream capture.  All
+ * calls share the one scratch array: calls whose work overlaps on the GPU (two streams, or
+ * two host threads) race and corrupt each other's results; order them on one stream. */
+#define GY_SORT_STATIC_MAX 262144
+gy_status gy_sort_keys_static(const int *d_keys, int64_t n, int key_bits, int *d_perm_out, void *stream);
+
 /* FP64 conservation sums over the particles (waits for queued work). */
 gy_status gy_get_stats(gy_solver *h, gy_stats *out);
 

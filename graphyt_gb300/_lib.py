@@ -89,6 +89,9 @@ SIGNATURES = {
     "gy_get_particles_int": (C.c_int, [_vp, C.c_int, _ip, C.c_int64]),
     "gy_get_nodes": (C.c_int, [_vp, C.c_int, _dp, C.c_int64]),
     "gy_sort_keys": (C.c_int, [_ip, C.c_int64, _ip, C.c_int]),
+    "gy_state_size": (C.c_int, [_vp, _i64p]),
+    "gy_state_save": (C.c_int, [_vp, C.c_void_p, C.c_int64]),
+    "gy_state_load": (C.c_int, [_vp, C.c_void_p, C.c_int64]),
     "gy_sort_keys_static": (C.c_int, [C.c_void_p, C.c_int64, C.c_int, C.c_void_p, C.c_void_p]),
     "gy_get_stats": (C.c_int, [_vp, C.POINTER(Stats)]),
     "gy_set_phase_timing": (C.c_int, [_vp, C.c_int]),

@@ -151,6 +151,7 @@ gy_status gy_create(const gy_grid_desc *grid, int device, gy_solver **out)
     const double nn_r = std::round((1.0 + grid->L[0] / h) * (1.0 + grid->L[1] / h) * (1.0 + grid->L[2] / h));
     const int nx = (int)(1.0 + grid->L[0] / h), ny = (int)(1.0 + grid->L[1] / h), nz = (int)(1.0 + grid->L[2] / h);
     if ((double)nx * ny * nz != nn_r) return GY_ERR_ARG;
+    if ((double)nx * ny * nz >= 2147483647.0) return GY_ERR_UNSUPPORTED;  // 32-bit node indices
     const bool is3d = nz > 1;
     if (nx < 6 || ny < 6 || (is3d && nz < 6)) return GY_ERR_ARG;  // the periodic fold pairs 3 layers per side
     if (grid->psep > h) return GY_ERR_UNSUPPORTED;                  // 3-node stencil needs psep/2 <= h/2
@@ -186,7 +187,9 @@ gy_status gy_create(const gy_grid_desc *grid, int device, gy_solver **out)
     g.nnby = (ny + 3) / 4;
     g.nnbz = (nz + 3) / 4;
     g.nnb = (long long)g.nnbx * g.nnby * g.nnbz;
-    if ((long long)g.nbx * g.nby * g.nbz * 64 >= (1LL << 31)) {
+    g.div_nbx = ((1ULL << 39) + g.nbx - 1) / g.nbx;
+    g.div_nby = ((1ULL << 39) + g.nby - 1) / g.nby;
+    if ((long long)g.nbx * g.nby * g.nbz >= (1LL << 25) || g.nbx >= (1 << 14) || g.nby >= (1 << 14)) {
         cudaStreamDestroy(s->stream);
         delete s;
         return GY_ERR_UNSUPPORTED;  // cell keys must fit in 31 bits
@@ -376,7 +379,7 @@ static gy_status alloc_nodes(gy_solver *h)
     size_t bytes = (size_t)rows * nn * sizeof(float4);
     size_t extra = 0;
     if (h->multi) extra = (size_t)nn * sizeof(int2) + (size_t)nn + 64;
-    extra += (size_t)h->g.nnb + 64;
+    extra += (size_t)(2 * h->g.nnb + 16) * sizeof(int) + 64;
     if (h->any_node_bc) extra += (size_t)nn * sizeof(float4) + (size_t)nn + 64;
     char *mem = nullptr;
     cudaError_t e = cudaMalloc((void **)&mem, bytes + extra + 4096);
@@ -408,8 +411,12 @@ static gy_status alloc_nodes(gy_solver *h)
         }
     }
     char *c = (char *)f4;
-    nb.flags = (unsigned char *)c;
-    c += (size_t)h->g.nnb;
+    nb.flags = (int *)c;
+    c += (size_t)h->g.nnb * sizeof(int);
+    nb.active_list = (int *)c;
+    c += (size_t)h->g.nnb * sizeof(int);
+    nb.active_n = (int *)c;
+    c += 16 * sizeof(int);
     c = (char *)(((uintptr_t)c + 15) & ~(uintptr_t)15);
     if (h->any_node_bc) {
         nb.bc_val = (const float4 *)c;
@@ -698,6 +705,7 @@ static gy_status enqueue_step(gy_solver *h, double t, int step)
         h->tables_valid = true;
     }
     if (timing) cudaEventRecord(tev[1], s);
+    cudaMemsetAsync(h->nb.active_n, 0, sizeof(int), s);
     // (b) P2G
     launch_p2g(src, perm, skey, h->n, h->d_seg, h->d_nseg, h->persist_grid, h->nb, a, s);
     if (timing) cudaEventRecord(tev[2], s);
@@ -992,6 +1000,96 @@ gy_status gy_time_steps(gy_solver *h, double t0, int step0, int nsteps, float *m
 }
 
 int64_t gy_kernel_launches(void) { return (int64_t)launch_count(); }
+
+// ---- checkpoint / resume ----
+namespace {
+struct StateHeader {
+    char magic[8];            // "GYSTATE1"
+    int64_t n, cap, nn, nc;
+    int32_t nbody, multi, has_dp, track_normals;
+    int64_t steps;
+    double t_prev, dt;
+    int32_t tables_valid, pad;
+};
+
+size_t state_table_ints(const gy_solver *h) { return h->multi ? (size_t)h->g.nc * (h->nbody + 1) : 0; }
+size_t state_bytes(const gy_solver *h)
+{
+    return sizeof(StateHeader) + (size_t)PF_COUNT * h->n * sizeof(float) + state_table_ints(h) * sizeof(int) +
+           (h->multi ? (size_t)h->nn * (sizeof(int2) + 1) : 0);
+}
+}  // namespace
+
+gy_status gy_state_size(const gy_solver *h, int64_t *bytes)
+{
+    if (!h || !bytes) return GY_ERR_ARG;
+    if (!h->initialized) return GY_ERR_STATE;
+    *bytes = (int64_t)state_bytes(h);
+    return GY_OK;
+}
+
+gy_status gy_state_save(gy_solver *h, void *buf, int64_t bytes)
+{
+    if (!h || !buf) return GY_ERR_ARG;
+    if (!h->initialized) return fail(h, GY_ERR_STATE, "nothing to save before gy_initialize");
+    if (bytes < (int64_t)state_bytes(h)) return fail(h, GY_ERR_ARG, "buffer smaller than gy_state_size");
+    cudaSetDevice(h->device);
+    CK(h, cudaStreamSynchronize(h->stream));
+    StateHeader hd{};
+    std::memcpy(hd.magic, "GYSTATE1", 8);
+    hd.n = h->n; hd.cap = h->cap; hd.nn = h->nn; hd.nc = h->g.nc;
+    hd.nbody = h->nbody; hd.multi = h->multi; hd.has_dp = h->has_dp; hd.track_normals = h->opt.track_normals;
+    hd.steps = h->steps; hd.t_prev = h->t_prev; hd.dt = h->dt; hd.tables_valid = h->tables_valid;
+    char *p = static_cast<char *>(buf);
+    std::memcpy(p, &hd, sizeof(hd));
+    p += sizeof(hd);
+    for (int f = 0; f < PF_COUNT; f++) {
+        CK(h, cudaMemcpy(p, h->slab[h->cur] + (size_t)f * h->cap, (size_t)h->n * sizeof(float), cudaMemcpyDeviceToHost));
+        p += (size_t)h->n * sizeof(float);
+    }
+    if (h->multi) {
+        CK(h, cudaMemcpy(p, h->d_cell_min, state_table_ints(h) * sizeof(int), cudaMemcpyDeviceToHost));
+        p += state_table_ints(h) * sizeof(int);
+        CK(h, cudaMemcpy(p, h->nb.body, (size_t)h->nn * sizeof(int2), cudaMemcpyDeviceToHost));
+        p += (size_t)h->nn * sizeof(int2);
+        CK(h, cudaMemcpy(p, h->nb.has_rigid, (size_t)h->nn, cudaMemcpyDeviceToHost));
+    }
+    return GY_OK;
+}
+
+gy_status gy_state_load(gy_solver *h, const void *buf, int64_t bytes)
+{
+    if (!h || !buf) return GY_ERR_ARG;
+    if (!h->initialized) return fail(h, GY_ERR_STATE, "gy_state_load needs a handle built with gy_initialize");
+    if (bytes < (int64_t)sizeof(StateHeader)) return fail(h, GY_ERR_ARG, "buffer too small");
+    StateHeader hd;
+    std::memcpy(&hd, buf, sizeof(hd));
+    if (std::memcmp(hd.magic, "GYSTATE1", 8) != 0) return fail(h, GY_ERR_ARG, "not a graphyt GPU state");
+    if (hd.n != h->n || hd.nn != h->nn || hd.nc != h->g.nc || hd.nbody != h->nbody || hd.multi != (int)h->multi ||
+        hd.has_dp != (int)h->has_dp || hd.track_normals != h->opt.track_normals)
+        return fail(h, GY_ERR_ARG, "state belongs to a different model (grid, particles, bodies or options differ)");
+    if (bytes < (int64_t)state_bytes(h)) return fail(h, GY_ERR_ARG, "buffer shorter than the state");
+    cudaSetDevice(h->device);
+    CK(h, cudaStreamSynchronize(h->stream));
+    const char *p = static_cast<const char *>(buf) + sizeof(hd);
+    for (int f = 0; f < PF_COUNT; f++) {
+        CK(h, cudaMemcpy(h->slab[h->cur] + (size_t)f * h->cap, p, (size_t)h->n * sizeof(float), cudaMemcpyHostToDevice));
+        p += (size_t)h->n * sizeof(float);
+    }
+    if (h->multi) {
+        CK(h, cudaMemcpy(h->d_cell_min, p, state_table_ints(h) * sizeof(int), cudaMemcpyHostToDevice));
+        p += state_table_ints(h) * sizeof(int);
+        CK(h, cudaMemcpy(h->nb.body, p, (size_t)h->nn * sizeof(int2), cudaMemcpyHostToDevice));
+        p += (size_t)h->nn * sizeof(int2);
+        CK(h, cudaMemcpy(h->nb.has_rigid, p, (size_t)h->nn, cudaMemcpyHostToDevice));
+    }
+    h->steps = hd.steps;
+    h->t_prev = hd.t_prev;
+    h->dt = hd.dt;
+    h->tables_valid = hd.tables_valid != 0;
+    h->since_sort = 1 << 30;
+    return GY_OK;
+}
 
 gy_status gy_sort_keys(const int *keys, int64_t n, int *perm_out, int device)
 {

@@ -18,7 +18,7 @@ enum PField : int {
     PF_E0, PF_E1, PF_E2, PF_E3, PF_E4, PF_E5,  // strain
     PF_RHO,                           // density
     PF_MASS,                          // mass (1 for rigid particles, Solver.cpp:51-54)
-    PF_KEY,                           // int: linear base cell ci + cj*Ncx + ck*Ncx*Ncy
+    PF_KEY,                           // int: block-major cell key (encode_key)
     PF_INFO,                          // int: packed material / object slot / BC / flags
     PF_PID,                           // int: insertion index
     PF_EQPS,                          // accumulated plastic strain
@@ -50,8 +50,8 @@ enum BCType : int {
     BC_MP_VYSIN = 66, BC_MP_SYYSIN = 67
 };
 
-// Material table in constant memory (MaterialModels.hpp:29-47, FP32 where the step
-// computes in FP32; Grady-Kipp factors precomputed in FP64 on the host).
+// Material table (MaterialModels.hpp:29-47), FP32 where the step computes in FP32;
+// Grady-Kipp factors precomputed in FP64 on the host.
 struct DevMaterial {
     float K, G, rho0, viscosity, yield, cohesion, crit_strain;
     float eta, xi, eta_bar;     // Drucker-Prager cone constants from phi, psi
@@ -70,6 +70,7 @@ struct GridGeom {
     int nbx, nby, nbz;        // 4x4x4 cell blocks per axis (nbz = 1 in 2D)
     int nnbx, nnby, nnbz;     // 4x4x4 node blocks per axis
     long long nnb;            // node blocks
+    unsigned long long div_nbx, div_nby;  // ceil(2^39 / nbx), ceil(2^39 / nby): exact n / d for n < 2^25
     long long nn;             // nodes
     long long nc;             // cells
     float h, inv_h;           // cell size
@@ -135,12 +136,20 @@ __host__ __device__ __forceinline__ int encode_key(int ci, int cj, int ck, const
     return (blk << CB_SHIFT) | ((ck & 3) << 4) | ((cj & 3) << 2) | (ci & 3);
 }
 
+// n / d by multiply-shift with M = ceil(2^39 / d): the error n (M - 2^39/d) / 2^39 stays
+// below 2^-14 for n < 2^25, smaller than the 1/d gap to the next integer for d < 2^14, and
+// n * M < 2^64.
+__host__ __device__ __forceinline__ int fast_div(int n, unsigned long long M)
+{
+    return (int)(((unsigned long long)(unsigned)n * M) >> 39);
+}
+
 __host__ __device__ __forceinline__ void decode_block(int blk, const GridGeom &g, int &bx, int &by, int &bz)
 {
-    bx = blk % g.nbx;
-    const int t = blk / g.nbx;
-    by = t % g.nby;
-    bz = t / g.nby;
+    const int t = fast_div(blk, g.div_nbx);
+    bx = blk - t * g.nbx;
+    bz = fast_div(t, g.div_nby);
+    by = t - bz * g.nby;
 }
 
 __host__ __device__ __forceinline__ void decode_key(int key, const GridGeom &g, int &ci, int &cj, int &ck)
@@ -157,9 +166,10 @@ __host__ __device__ __forceinline__ long long node_block(int i, int j, int k, co
     return ((long long)(k >> 2) * g.nnby + (j >> 2)) * g.nnbx + (i >> 2);
 }
 
-__device__ __forceinline__ long long node_index(int i, int j, int k, const GridGeom &g)
+// grids hold fewer than 2^31 nodes (checked at creation), so 32-bit index math suffices
+__device__ __forceinline__ int node_index(int i, int j, int k, const GridGeom &g)
 {
-    return (long long)i + (long long)j * g.nx + (long long)k * g.nx * g.ny;
+    return i + (j + k * g.ny) * g.nx;
 }
 
 // device error bits

@@ -41,9 +41,11 @@ __device__ __forceinline__ void red_add4(float4 *a, float x, float y, float z, f
                  : "memory");
 }
 
-__device__ __forceinline__ void mark_node(unsigned char *flags, int i, int j, int k, const GridGeom &g)
+// Mark the node's 4x4x4 block active; the first marker appends it to the solve's list.
+__device__ __forceinline__ void mark_node(const NodeBufs &nb, int i, int j, int k, const GridGeom &g)
 {
-    flags[node_block(i, j, k, g)] = 1;
+    const long long b = node_block(i, j, k, g);
+    if (nb.flags[b] == 0 && atomicCAS(&nb.flags[b], 0, 1) == 0) nb.active_list[atomicAdd(nb.active_n, 1)] = (int)b;
 }
 
 struct PState {
@@ -146,12 +148,12 @@ __device__ __forceinline__ void make_stencil(const PState &st, const GridGeom &g
 // solve as m_node * g, which equals sum_p w m_p g (Extrapolation.cpp:226-278).
 //
 // A CTA owns one segment (the particles of one 4x4x4 cell block, freshly sorted), whose
-// stencils lie in the 6x6x6 node tile [4b, 4b+6).  Each chunk of 256 particles is first
-// loaded in natural (coalesced) order and its P2G payload staged in shared memory; the
-// scatter then reads the payload transposed, lane l of warp w taking particle 8l + w, so
-// the 32 lanes of a warp belong to ~32 different cells (8 particles per cell) and, for a
-// given stencil offset, add into 32 different tile nodes: the shared-memory atomics of one
-// instruction do not collide.
+// stencils lie in the 6x6x6 node tile [4b, 4b+6).  Each chunk of 256 particles is loaded in
+// natural (coalesced) order and its GIMP weights and payload staged in shared memory.  The
+// particles of one cell share their 27 stencil nodes, so a warp takes one run of equal cell
+// at a time with lane k owning stencil node k: each lane sums the run's contributions to its
+// node in registers and adds the sum into the tile once -- seven shared atomics per node per
+// cell instead of per particle, and the 27 lanes of one instruction hit 27 different nodes.
 
 constexpr int PT = 6;                  // tile edge in nodes
 constexpr int PT_NODES = PT * PT * PT; // 216
@@ -192,12 +194,21 @@ __global__ void __launch_bounds__(256) k_p2g_tiled(PView P, const int *perm, con
                                                     const int *seg_start, const int *nseg_ptr, int sorted,
                                                     NodeBufs nb, GridGeom g)
 {
+    // staged per particle: weights S/G (3 nodes x 3 axes x 2) and the payload
+    // m, m v (3), V sigma / h (6); plus the cell inside the block
     __shared__ float tile[P2G_FIELDS * PT_NODES];
-    __shared__ float pay[PAY * 256];
+    __shared__ float2 wts[9 * 256];       // (S, G) per axis and stencil node: [axis*3 + i][particle]
+    __shared__ float4 pay0[256];          // m, m vx, m vy, m vz
+    __shared__ float4 pay1[256];          // V sigma_xx, yy, zz, xy (with 1/h)
+    __shared__ float2 pay2[256];          // V sigma_yz, xz (with 1/h)
+    __shared__ int cellof[256];
+    __shared__ int run_start[257];
+    __shared__ int nruns;
     __shared__ long long s_end;
     const int nseg = *nseg_ptr;
-    const int tid = threadIdx.x;
-    const int jt = (tid & 31) * 8 + (tid >> 5);  // transposed slot (blockDim.x == 256)
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // lane -> stencil node (ii, jj, kk); lanes 27..31 idle in the scatter
+    const int ii = lane % 3, jj = (lane / 3) % 3, kk = lane / 9;
     for (int sgi = blockIdx.x; sgi < nseg; sgi += gridDim.x) {
         const long long start = seg_start[sgi];
         const int blk = seg_block(skey, start);
@@ -211,70 +222,81 @@ __global__ void __launch_bounds__(256) k_p2g_tiled(PView P, const int *perm, con
             if (!sorted) end = segment_chunk_end(skey, n, blk, base, &s_end);
             const int cnt = (int)min((long long)256, end - base);
             if (cnt <= 0) break;
-            // ---- stage the payload in natural order ----
             __syncthreads();
+            // ---- stage weights and payload, natural (coalesced) order ----
+            int mycell = -1;
             if (tid < cnt) {
                 const long long i = base + tid;
                 const long long j = perm ? perm[i] : i;
-                int ci, cj, ck;
-                decode_key(P.ii(PF_KEY, j), g, ci, cj, ck);
+                const int key = P.ii(PF_KEY, j);
+                mycell = key & 63;  // cell inside the block: (lz*4 + ly)*4 + lx
+                float S[3], G[3];
+                gimp_axis(P.f(PF_OX, j), g.lp, S, G);
+#pragma unroll
+                for (int k = 0; k < 3; k++) wts[(0 + k) * 256 + tid] = make_float2(S[k], G[k]);
+                gimp_axis(P.f(PF_OY, j), g.lp, S, G);
+#pragma unroll
+                for (int k = 0; k < 3; k++) wts[(3 + k) * 256 + tid] = make_float2(S[k], G[k]);
+                if (g.is3d) {
+                    gimp_axis(P.f(PF_OZ, j), g.lp, S, G);
+                } else {
+                    S[0] = 1.f; S[1] = 0.f; S[2] = 0.f; G[0] = 0.f; G[1] = 0.f; G[2] = 0.f;
+                }
+#pragma unroll
+                for (int k = 0; k < 3; k++) wts[(6 + k) * 256 + tid] = make_float2(S[k], G[k]);
                 const float m = P.f(PF_MASS, j);
                 const float sc = (m / P.f(PF_RHO, j)) * g.inv_h;  // V sigma with the gradient's 1/h
-                pay[0 * 256 + tid] = __int_as_float((ci - tox) | ((cj - toy) << 8) | ((g.is3d ? ck - toz : 0) << 16));
-                pay[1 * 256 + tid] = P.f(PF_OX, j);
-                pay[2 * 256 + tid] = P.f(PF_OY, j);
-                pay[3 * 256 + tid] = P.f(PF_OZ, j);
-                pay[4 * 256 + tid] = m;
-                pay[5 * 256 + tid] = m * P.f(PF_VX, j);
-                pay[6 * 256 + tid] = m * P.f(PF_VY, j);
-                pay[7 * 256 + tid] = m * P.f(PF_VZ, j);
-#pragma unroll
-                for (int k = 0; k < 6; k++) pay[(8 + k) * 256 + tid] = P.f(PF_S0 + k, j) * sc;
+                pay0[tid] = make_float4(m, m * P.f(PF_VX, j), m * P.f(PF_VY, j), m * P.f(PF_VZ, j));
+                pay1[tid] = make_float4(P.f(PF_S0, j) * sc, P.f(PF_S1, j) * sc, P.f(PF_S2, j) * sc, P.f(PF_S3, j) * sc);
+                pay2[tid] = make_float2(P.f(PF_S4, j) * sc, P.f(PF_S5, j) * sc);
             }
+            cellof[tid] = mycell;
+            if (tid == 0) nruns = 0;
             __syncthreads();
-            // ---- transposed scatter ----
-            if (jt < cnt) {
-                const int lc = __float_as_int(pay[jt]);
-                const int li = lc & 0xff, lj = (lc >> 8) & 0xff, lk = (lc >> 16) & 0xff;
-                float Sx[3], Gx[3], Sy[3], Gy[3], Sz[3] = {1.f, 0.f, 0.f}, Gz[3] = {0.f, 0.f, 0.f};
-                const float ox = pay[256 + jt], oy = pay[2 * 256 + jt];
-                gimp_axis(ox, g.lp, Sx, Gx);
-                gimp_axis(oy, g.lp, Sy, Gy);
-                int nkz = 1;
-                if (g.is3d) {
-                    const float oz = pay[3 * 256 + jt];
-                    gimp_axis(oz, g.lp, Sz, Gz);
-                    nkz = (oz < 1.0f - g.lp) ? 2 : 3;
+            // ---- runs of equal cell inside the chunk (particles are sorted by cell) ----
+            const bool head = tid < cnt && (tid == 0 || cellof[tid - 1] != mycell);
+            const unsigned hm = __ballot_sync(0xffffffffu, head);
+            int wbase = 0;
+            if (lane == 0 && hm) wbase = atomicAdd(&nruns, __popc(hm));
+            wbase = __shfl_sync(0xffffffffu, wbase, 0);
+            if (head) run_start[wbase + __popc(hm & ((1u << lane) - 1u))] = tid;
+            __syncthreads();
+            const int R = nruns;
+            // ---- warp per run: lane = stencil node; sums in registers, one atomic per field ----
+            for (int r = warp; r < R; r += 8) {
+                const int p0 = run_start[r];
+                const int cell = cellof[p0];
+                int p1 = p0 + 1;
+                while (p1 < cnt && cellof[p1] == cell) p1++;
+                if (lane >= 27) continue;
+                float am = 0.f, apx = 0.f, apy = 0.f, apz = 0.f, afx = 0.f, afy = 0.f, afz = 0.f;
+#pragma unroll 2
+                for (int p = p0; p < p1; p++) {
+                    const float2 wx = wts[(0 + ii) * 256 + p], wy = wts[(3 + jj) * 256 + p], wz = wts[(6 + kk) * 256 + p];
+                    const float4 q0 = pay0[p], q1 = pay1[p];
+                    const float2 q2 = pay2[p];
+                    const float syz = wy.x * wz.x;
+                    const float w = wx.x * syz;
+                    const float gx = wx.y * syz, gy = wx.x * wy.y * wz.x, gz = wx.x * wy.x * wz.y;
+                    am += w * q0.x;
+                    apx += w * q0.y;
+                    apy += w * q0.z;
+                    apz += w * q0.w;
+                    afx -= gx * q1.x + gy * q1.w + gz * q2.y;
+                    afy -= gx * q1.w + gy * q1.y + gz * q2.x;
+                    afz -= gx * q2.y + gy * q2.x + gz * q1.z;
                 }
-                const int nix = (ox < 1.0f - g.lp) ? 2 : 3, njy = (oy < 1.0f - g.lp) ? 2 : 3;
-                const float m = pay[4 * 256 + jt];
-                const float mvx = pay[5 * 256 + jt], mvy = pay[6 * 256 + jt], mvz = pay[7 * 256 + jt];
-                const float s0 = pay[8 * 256 + jt], s1 = pay[9 * 256 + jt], s2 = pay[10 * 256 + jt];
-                const float s3 = pay[11 * 256 + jt], s4 = pay[12 * 256 + jt], s5 = pay[13 * 256 + jt];
-                const int t0 = (lk * PT + lj) * PT + li;
-#pragma unroll
-                for (int kk = 0; kk < 3; kk++) {
-                    if (kk >= nkz) break;
-#pragma unroll
-                    for (int jj = 0; jj < 3; jj++) {
-                        if (jj >= njy) break;
-                        const float syz = Sy[jj] * Sz[kk], gyz = Gy[jj] * Sz[kk], syg = Sy[jj] * Gz[kk];
-#pragma unroll
-                        for (int ii = 0; ii < 3; ii++) {
-                            if (ii >= nix) break;
-                            const float w = Sx[ii] * syz;
-                            const float gx = Gx[ii] * syz, gy = Sx[ii] * gyz, gz = Sx[ii] * syg;
-                            const int t = t0 + (kk * PT + jj) * PT + ii;
-                            atomicAdd(&tile[0 * PT_NODES + t], w * m);
-                            atomicAdd(&tile[1 * PT_NODES + t], w * mvx);
-                            atomicAdd(&tile[2 * PT_NODES + t], w * mvy);
-                            atomicAdd(&tile[3 * PT_NODES + t], w * mvz);
-                            atomicAdd(&tile[4 * PT_NODES + t], -(gx * s0 + gy * s3 + gz * s5));
-                            atomicAdd(&tile[5 * PT_NODES + t], -(gx * s3 + gy * s1 + gz * s4));
-                            atomicAdd(&tile[6 * PT_NODES + t], -(gx * s5 + gy * s4 + gz * s2));
-                        }
-                    }
-                }
+                if (am == 0.f && afx == 0.f && afy == 0.f && afz == 0.f && apx == 0.f && apy == 0.f && apz == 0.f)
+                    continue;
+                const int li = cell & 3, lj = (cell >> 2) & 3, lk = cell >> 4;
+                const int t = ((lk + kk) * PT + (lj + jj)) * PT + (li + ii);
+                atomicAdd(&tile[0 * PT_NODES + t], am);
+                atomicAdd(&tile[1 * PT_NODES + t], apx);
+                atomicAdd(&tile[2 * PT_NODES + t], apy);
+                atomicAdd(&tile[3 * PT_NODES + t], apz);
+                atomicAdd(&tile[4 * PT_NODES + t], afx);
+                atomicAdd(&tile[5 * PT_NODES + t], afy);
+                atomicAdd(&tile[6 * PT_NODES + t], afz);
             }
             if (cnt < 256) break;
         }
@@ -286,10 +308,10 @@ __global__ void __launch_bounds__(256) k_p2g_tiled(PView P, const int *perm, con
             if (m == 0.f && px == 0.f && py == 0.f && pz == 0.f && fx == 0.f && fy == 0.f && fz == 0.f) continue;
             const int ni = tox + t % PT, nj = toy + (t / PT) % PT, nk = toz + t / (PT * PT);
             if (ni >= g.nx || nj >= g.ny || nk >= g.nz) continue;
-            const long long nd = node_index(ni, nj, nk, g);
+            const int nd = node_index(ni, nj, nk, g);
             red_add4(&nb.acc0[nd], m, px, py, pz);
             red_add4(&nb.acc1[nd], fx, fy, fz, 0.f);
-            mark_node(nb.flags, ni, nj, nk, g);
+            mark_node(nb, ni, nj, nk, g);
         }
         __syncthreads();
     }
@@ -306,15 +328,17 @@ __global__ void __launch_bounds__(256) k_p2g_multi(PView P, const int *perm, lon
     load_state<false>(P, perm ? perm[i] : i, st);
     Stencil w;
     make_stencil(st, g, w);
-    const float m = st.mass;
+    const bool rigid = (st.info & INFO_RIGID) != 0;
+    // P2G takes a rigid particle's mass as 1 in 2D and 3D (Extrapolation.cpp:183); in 2D the
+    // stored mass stays rho psep^2 (Solver.cpp:58-66) and still sets the stored volume
+    const float m = rigid ? 1.0f : st.mass;
     const float Vf = m / st.rho;
     const float sc = Vf * g.inv_h;
     const float s0 = st.s[0] * sc, s1 = st.s[1] * sc, s2 = st.s[2] * sc;
     const float s3 = st.s[3] * sc, s4 = st.s[4] * sc, s5 = st.s[5] * sc;
     const float mgx = m * a.sc.gravity[0], mgy = m * a.sc.gravity[1], mgz = m * a.sc.gravity[2];
-    const bool rigid = (st.info & INFO_RIGID) != 0;
     const int obj = info_obj(st.info);
-    const float vol_n = ((st.info & INFO_INIT_VOL) ? a.sc.init_volume : Vf) * g.inv_h;
+    const float vol_n = ((st.info & INFO_INIT_VOL) ? a.sc.init_volume : st.mass / st.rho) * g.inv_h;
 #pragma unroll
     for (int kk = 0; kk < 3; kk++)
 #pragma unroll
@@ -328,7 +352,7 @@ __global__ void __launch_bounds__(256) k_p2g_multi(PView P, const int *perm, lon
                 const float gy = w.S[0][ii] * w.G[1][jj] * w.S[2][kk];
                 const float gz = w.S[0][ii] * w.S[1][jj] * w.G[2][kk];
                 const int ni = w.c[0] + ii, nj = w.c[1] + jj, nk = w.c[2] + kk;
-                const long long nd = node_index(ni, nj, nk, g);
+                const int nd = node_index(ni, nj, nk, g);
                 const float wm = wgt * m;
                 const float fx = -(gx * s0 + gy * s3 + gz * s5);
                 const float fy = -(gx * s3 + gy * s1 + gz * s4);
@@ -343,7 +367,7 @@ __global__ void __launch_bounds__(256) k_p2g_multi(PView P, const int *perm, lon
                     else red_add4(&nb.bacc1[slot][nd], fx + wgt * mgx, fy + wgt * mgy, fz + wgt * mgz, 0.0f);
                     red_add4(&nb.bnrm[slot][nd], gx * vol_n, gy * vol_n, gz * vol_n, 0.0f);
                 }
-                mark_node(nb.flags, ni, nj, nk, g);
+                mark_node(nb, ni, nj, nk, g);
             }
 }
 
@@ -406,8 +430,8 @@ __global__ void k_fold(NodeBufs nb, GridGeom g, int axis)
         }
     }
     if (any) {
-        mark_node(nb.flags, pi, pj, pk, g);
-        mark_node(nb.flags, qi, qj, qk, g);
+        mark_node(nb, pi, pj, pk, g);
+        mark_node(nb, qi, qj, qk, g);
     }
 }
 
@@ -488,7 +512,7 @@ __device__ __forceinline__ bool solve_node(const NodeBufs &nb, const StepArgs &a
         const int by = (int)(tb % g.nnby), bz = (int)(tb / g.nnby);
         const int i = bx * 4 + lx, j = by * 4 + ly, k = bz * 4 + lz;
         if (i < g.nx && j < g.ny && k < g.nz) {
-            const long long nd = node_index(i, j, k, g);
+            const int nd = node_index(i, j, k, g);
             const float4 A0 = nb.acc0[nd];
             float4 A1 = nb.acc1[nd];
             const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -629,29 +653,22 @@ __device__ __forceinline__ bool solve_node(const NodeBufs &nb, const StepArgs &a
     return active;
 }
 
-// Persistent: each warp walks node blocks with a grid stride; an active block's 64 nodes
-// take two passes of the warp.  The flag is cleared once the block's accumulators are read.
+// One warp per active node block from the list P2G and the fold built; the block's 64
+// nodes take two passes of the warp, then its flag is cleared for the next step.
 template <bool MULTI>
-__global__ void __launch_bounds__(256) k_solve_blocks(NodeBufs nb, StepArgs a, int keep)
+__global__ void __launch_bounds__(256) k_solve_list(NodeBufs nb, StepArgs a, int keep)
 {
     const int lane = threadIdx.x & 31;
-    const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int nw = (int)((gridDim.x * blockDim.x) >> 5);
+    const int nact = *nb.active_n;
     int count = 0;
-    for (long long base = warp * 32; base < a.g.nnb; base += nwarps * 32) {
-        // 32 flags at a time, then the active blocks one by one
-        const long long fb = base + lane;
-        const bool on = fb < a.g.nnb && nb.flags[fb] != 0;
-        unsigned mask = __ballot_sync(0xffffffffu, on);
-        while (mask) {
-            const int b = __ffs(mask) - 1;
-            mask &= mask - 1;
-            const long long blk = base + b;
-            count += solve_node<MULTI>(nb, a, keep, blk, lane) ? 1 : 0;
-            count += solve_node<MULTI>(nb, a, keep, blk, lane + 32) ? 1 : 0;
-            __syncwarp();
-            if (lane == 0) nb.flags[blk] = 0;
-        }
+    for (int w = gw; w < nact; w += nw) {
+        const long long blk = nb.active_list[w];
+        count += solve_node<MULTI>(nb, a, keep, blk, lane) ? 1 : 0;
+        count += solve_node<MULTI>(nb, a, keep, blk, lane + 32) ? 1 : 0;
+        __syncwarp();
+        if (lane == 0) nb.flags[blk] = 0;
     }
     if (nb.active_count) {
         for (int off = 16; off > 0; off >>= 1) count += __shfl_down_sync(0xffffffffu, count, off);
@@ -664,11 +681,10 @@ void launch_solve(const NodeBufs &nb, const StepArgs &a, bool keep_node_fields, 
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    long long want = (a.g.nnb + 255) / 256;  // one warp per 32 node blocks
-    long long grid = std::min<long long>(want, (long long)sms * 8);
+    long long grid = std::min<long long>((a.g.nnb + 7) / 8, (long long)sms * 16);  // 8 warps per CTA
     if (grid < 1) grid = 1;
-    if (a.sc.multi_body) k_solve_blocks<true><<<(unsigned)grid, 256, 0, s>>>(nb, a, keep_node_fields ? 1 : 0);
-    else k_solve_blocks<false><<<(unsigned)grid, 256, 0, s>>>(nb, a, keep_node_fields ? 1 : 0);
+    if (a.sc.multi_body) k_solve_list<true><<<(unsigned)grid, 256, 0, s>>>(nb, a, keep_node_fields ? 1 : 0);
+    else k_solve_list<false><<<(unsigned)grid, 256, 0, s>>>(nb, a, keep_node_fields ? 1 : 0);
     note_launch(1);
 }
 
@@ -735,7 +751,7 @@ __device__ __forceinline__ void g2p_update_one(PState &st, const NodeBufs &nb, c
 #pragma unroll
             for (int ii = 0; ii < 3; ii++) {
                 if (ii >= w.cnt[0]) continue;
-                const long long nd = node_index(w.c[0] + ii, w.c[1] + jj, w.c[2] + kk, g);
+                const int nd = node_index(w.c[0] + ii, w.c[1] + jj, w.c[2] + kk, g);
                 const float4 V = __ldg(&nb.gv[nd]);
                 if (V.x == 0.0f) continue;  // nodes without mass are skipped
                 float4 Vb, Ab;
@@ -867,7 +883,7 @@ __device__ __forceinline__ void g2p_update_one(PState &st, const NodeBufs &nb, c
 // Unfused G2P + update: one thread per particle in sorted order, state read through perm
 // and written to the other slab.
 template <bool MULTI, bool HAS_DP>
-__global__ void __launch_bounds__(256) k_g2p_update(PView src, PView dst, const int *perm, long long n, NodeBufs nb,
+__global__ void __launch_bounds__(256, 3) k_g2p_update(PView src, PView dst, const int *perm, long long n, NodeBufs nb,
                                                     StepArgs a, int track_normals, int check_finite)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;

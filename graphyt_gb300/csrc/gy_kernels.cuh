@@ -33,7 +33,9 @@ struct NodeBufs {
     float4 *bgv[2], *bga[2];      // solved per slot: (m, v), (a, -)
     float4 *nrm_out[2];           // normalised slot normals (only when normals are tracked)
     int2 *body;                   // body slot objects (dense ids) or -1
-    unsigned char *flags;         // active 4x4x4 node blocks (set by P2G / fold, cleared by the solve)
+    int *flags;                   // active 4x4x4 node blocks (set by P2G / fold, cleared by the solve)
+    int *active_list;             // node blocks marked this step, in marking order
+    int *active_n;                // length of active_list
     unsigned char *has_rigid;     // bit0: slot 0 rigid, bit1: slot 1 rigid
     int *active_count;            // nodes with mass (stats)
 };

@@ -555,6 +555,20 @@ class Solver:
             setattr(o, k, int(v))
         L.check(self.lib.gy_set_options(self.h, C.byref(o)), self.h, "options")
 
+    def save(self, path: str):
+        """Write a binary snapshot of the device state (checkpoint); resume with load()."""
+        nbytes = C.c_int64()
+        L.check(self.lib.gy_state_size(self.h, C.byref(nbytes)), self.h, "state size")
+        buf = np.empty(nbytes.value, np.uint8)
+        L.check(self.lib.gy_state_save(self.h, buf.ctypes.data_as(C.c_void_p), buf.size), self.h, "save")
+        with open(path, "wb") as f:
+            f.write(buf.tobytes())
+
+    def load(self, path: str):
+        """Restore a snapshot written by save() into a Solver built from the same model."""
+        buf = np.fromfile(path, np.uint8)
+        L.check(self.lib.gy_state_load(self.h, buf.ctypes.data_as(C.c_void_p), buf.size), self.h, "load")
+
     def stats(self) -> dict:
         s = L.Stats()
         L.check(self.lib.gy_get_stats(self.h, C.byref(s)), self.h, "stats")

@@ -187,6 +187,17 @@ gy_status gy_get_nodes(gy_solver *h, int field, double *out, int64_t count);
  * arrays; for testing the sort against a CPU stable sort. */
 gy_status gy_sort_keys(const int *keys, int64_t n, int *perm_out, int device);
 
+/* Checkpoint / resume of the device state.  The reference has no checkpoint: its only
+ * output, Serialise (MaterialPoints.cpp:341-364), writes lossy %f CSV with no reader.
+ * gy_state_size gives the byte size of a snapshot; gy_state_save copies the particle state
+ * (and the body-slot table of multi-body problems) into a caller buffer after the queued
+ * work finishes; gy_state_load restores it into a handle built from the same model (same
+ * grid, particle count, materials and options).  The step index is the caller's, so a
+ * resumed run keeps the reference's step-dependent rules (sort cadence, half dt at step 1). */
+gy_status gy_state_size(const gy_solver *h, int64_t *bytes);
+gy_status gy_state_save(gy_solver *h, void *buf, int64_t bytes);
+gy_status gy_state_load(gy_solver *h, const void *buf, int64_t bytes);
+
 /* Allocation-free form of gy_sort_keys.  It has no counterpart in the reference.  Some
  * callers cannot call cudaMalloc or cudaFree at the point where they sort: a host framework
  * that owns all device memory through its own pool and forbids other allocations, or a

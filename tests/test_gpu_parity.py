@@ -149,3 +149,40 @@ def test_sort_every_does_not_change_results(gpu_lib):
     a = run_gpu(sc, 12, options=dict(sort_every=1))
     b = run_gpu(sc, 12, options=dict(sort_every=7))
     assert rel_l2(a._get_particles("vel"), b._get_particles("vel")) < 1e-5
+
+
+@pytest.mark.parametrize("make", [lambda: scenes.dam_break(scale=0.125), lambda: scenes.two_blocks()])
+def test_checkpoint_resume(gpu_lib, tmp_path, make):
+    """A snapshot taken mid-run and loaded into a fresh solver continues the same trajectory
+    (to FP32 summation order); the step index stays the caller's, so the sort cadence and
+    the half dt at step 1 survive the resume."""
+    from graphyt_gb300 import graphyt
+    sc = make()
+    a = graphyt.from_scene(sc)
+    dt = a.dt
+    for k in range(12):
+        a.iterate_GPU(k * dt, k)
+    path = str(tmp_path / "state.bin")
+    a.save(path)
+    for k in range(12, 24):
+        a.iterate_GPU(k * dt, k)
+    a.Synchronise()
+    b = graphyt.from_scene(sc)
+    b.load(path)
+    for k in range(12, 24):
+        b.iterate_GPU(k * dt, k)
+    b.Synchronise()
+    for f in ("vel", "stress", "pos"):
+        assert rel_l2(b._get_particles(f), a._get_particles(f)) < 1e-5, f
+    assert b.stats()["steps"] == a.stats()["steps"]
+
+
+def test_checkpoint_rejects_other_model(gpu_lib, tmp_path):
+    from graphyt_gb300 import _lib, graphyt
+    a = graphyt.from_scene(scenes.tiny_block(model=1))
+    a.iterate_GPU(0.0, 0)
+    path = str(tmp_path / "s.bin")
+    a.save(path)
+    b = graphyt.from_scene(scenes.tiny_block(model=1, n_side=5))
+    with pytest.raises(_lib.GraphytGPUError):
+        b.load(path)

@@ -4,16 +4,16 @@
 //   sort      stable counting sort of the particle cell keys (gy_sort.cu) -> perm, plus the
 //             list of non-empty 4x4x4 cell blocks ("segments");
 //   fold      periodic node-layer fold of the accumulated P2G fields (Grid.cpp:310-795);
+//   P2G       one CTA per segment: particles of a run of equal cell are summed in registers
+//             by one warp (lane = stencil node) into a shared-memory node tile, flushed with
+//             vector reductions (Extrapolation.cpp:166-286); multi-body problems scatter per
+//             particle into the centre-of-mass and body-slot fields;
 //   solve     nodal momentum update + grid BCs over the active 4x4x4 node blocks only
 //             (Grid.cpp:9-245, 862-1094); it also clears the accumulators it read;
-//   G2P2G     one pass over the particles in sorted order: G2P (Extrapolation.cpp:127-163,
+//   G2P       one pass over the particles in sorted order: G2P (Extrapolation.cpp:127-163,
 //             288-367), particle BCs (TimeIntegration.cpp:177-296), update + constitutive +
-//             damage + wrap (TimeIntegration.cpp:11-117), the state written back in sorted
-//             order, and the *next* step's P2G (Extrapolation.cpp:166-286) scattered from
-//             the updated state into a shared-memory node tile, flushed with vector
-//             reductions.  Each particle's state is read once and written once per step.
-// The first step (and every step of multi-body problems, whose body slots depend on the
-// whole particle set) runs a standalone P2G before the fold.
+//             damage + wrap (TimeIntegration.cpp:11-117), the state written to the other
+//             slab in sorted order.
 //
 // P2G is a particle-centric scatter: the reference gathers per node over a 4x4x4 cell
 // window (Extrapolation.cpp:31-125), but a particle contributes exactly to the nodes of its

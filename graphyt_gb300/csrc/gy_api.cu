@@ -56,6 +56,7 @@ struct gy_solver {
     int *d_perm = nullptr;
     int *d_seg = nullptr, *d_nseg = nullptr;   // non-empty cell-block segments
     int persist_grid = 1;
+    int g2p_grid = 1;
     SortScratch ws{};
     void *sort_mem = nullptr;
     float4 *d_pbc_val = nullptr;
@@ -594,6 +595,7 @@ gy_status gy_initialize(gy_solver *h, const gy_material *mats, int nmat, const g
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         h->persist_grid = sms * p2g_blocks_per_sm();
+        h->g2p_grid = sms * g2p_blocks_per_sm(h->has_dp);
     }
     if ((st = alloc_nodes(h))) return st;
     CK(h, cudaStreamSynchronize(h->stream));
@@ -714,8 +716,8 @@ static gy_status enqueue_step(gy_solver *h, double t, int step)
     launch_solve(h->nb, a, h->opt.keep_node_fields != 0, s);
     if (timing) cudaEventRecord(tev[3], s);
     // (d) G2P + particle BCs + update + constitutive + damage, written in sorted order
-    launch_g2p_update(src, dst, perm, h->n, h->nb, a, h->opt.track_normals != 0, h->opt.check_finite != 0,
-                      h->has_dp, s);
+    launch_g2p_update(src, dst, perm, skey, h->n, h->d_seg, h->d_nseg, h->g2p_grid, h->nb, a,
+                      h->opt.track_normals != 0, h->opt.check_finite != 0, h->has_dp, s);
     h->cur ^= 1;
     if (timing) cudaEventRecord(tev[4], s);
     cudaError_t e = cudaGetLastError();

@@ -41,11 +41,11 @@ __device__ __forceinline__ void red_add4(float4 *a, float x, float y, float z, f
                  : "memory");
 }
 
-// Mark the node's 4x4x4 block active; the first marker appends it to the solve's list.
+// Mark the node's 4x4x4 block active: a plain store (no round trip); k_compact_active turns
+// the flags into the solve's list.
 __device__ __forceinline__ void mark_node(const NodeBufs &nb, int i, int j, int k, const GridGeom &g)
 {
-    const long long b = node_block(i, j, k, g);
-    if (nb.flags[b] == 0 && atomicCAS(&nb.flags[b], 0, 1) == 0) nb.active_list[atomicAdd(nb.active_n, 1)] = (int)b;
+    nb.flags[node_block(i, j, k, g)] = 1;
 }
 
 struct PState {
@@ -147,30 +147,21 @@ __device__ __forceinline__ void make_stencil(const PState &st, const GridGeom &g
 // Single-body P2G through a shared-memory node tile.  Gravity is added per node in the
 // solve as m_node * g, which equals sum_p w m_p g (Extrapolation.cpp:226-278).
 //
-// A CTA owns one segment (the particles of one 4x4x4 cell block, freshly sorted), whose
-// stencils lie in the 6x6x6 node tile [4b, 4b+6).  Each chunk of 256 particles is loaded in
-// natural (coalesced) order and its GIMP weights and payload staged in shared memory.  The
-// particles of one cell share their 27 stencil nodes, so a warp takes one run of equal cell
-// at a time with lane k owning stencil node k: each lane sums the run's contributions to its
-// node in registers and adds the sum into the tile once -- seven shared atomics per node per
-// cell instead of per particle, and the 27 lanes of one instruction hit 27 different nodes.
+// A CTA owns one segment (the particles of one 4x4x4 cell block), whose stencils lie in the
+// 6x6x6 node tile [4b, 4b+6).  Each chunk of P2G_CH particles is loaded in natural
+// (coalesced) order and its GIMP weights and payload are staged in shared memory as pairs of
+// neighbouring particles.  The particles of one cell share their 27 stencil nodes, so a warp
+// takes one run of equal cell at a time with lane k owning stencil node k: each lane sums the
+// run's contributions to its node in registers, two particles per packed FP32x2 instruction,
+// and adds the sum into the tile once -- seven shared atomics per node per cell instead of
+// per particle, and the 27 lanes of one instruction hit 27 different nodes.
 
-constexpr int PT = 6;                  // tile edge in nodes
-constexpr int PT_NODES = PT * PT * PT; // 216
-constexpr int P2G_FIELDS = 7;          // m, px, py, pz, fx, fy, fz
-constexpr int PAY = 14;                // staged payload per particle
-
-// end of the segment starting at `start` in block `blk`: binary search on sorted keys
-__device__ __forceinline__ long long sorted_segment_end(const int *skey, long long n, long long start, int blk)
-{
-    long long lo = start, hi = n;  // first index with block > blk
-    while (lo < hi) {
-        const long long mid = (lo + hi) >> 1;
-        if ((skey[mid] >> CB_SHIFT) <= blk) lo = mid + 1;
-        else hi = mid;
-    }
-    return lo;
-}
+constexpr int PT = 6;                   // tile edge in nodes
+constexpr int PT_NODES = PT * PT * PT;  // 216
+constexpr int P2G_FIELDS = 7;           // m, px, py, pz, fx, fy, fz
+constexpr int P2G_CH = 256;             // particles per chunk = threads per CTA
+constexpr int P2G_NP = P2G_CH / 2 + 1;  // pairs per staged row; the odd row length (in float4)
+                                        // puts the three rows one load reads in different banks
 
 // Segment bounds when the keys are not freshly sorted: runs of one block can repeat, so
 // the run ends at the first index after `base` whose block differs (per chunk).
@@ -190,102 +181,174 @@ __device__ __forceinline__ long long segment_chunk_end(const int *skey, long lon
 
 __device__ __forceinline__ int seg_block(const int *skey, long long start) { return skey[start] >> CB_SHIFT; }
 
-__global__ void __launch_bounds__(256) k_p2g_tiled(PView P, const int *perm, const int *skey, long long n,
-                                                    const int *seg_start, const int *nseg_ptr, int sorted,
-                                                    NodeBufs nb, GridGeom g)
+// packed FP32x2 arithmetic (sm_100 and later): one instruction for two particles
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 lo2(float4 v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); }
+
+// per-lane sums of one run: m, m v, and sum V sigma . grad N (the force with its sign flipped)
+struct P2GAcc {
+    float2 m, px, py, pz, fx, fy, fz;
+};
+
+// Staged pair m: W[a][m] = (S, S', G, G') for axis/node a = 3*axis + node of particles 2m and
+// 2m+1; Q[0..4][m] = (m, m'), (m vx, ..'), then (m vy), (m vz), (s_xx), (s_yy), (s_zz),
+// (s_xy), (s_yz), (s_xz) of V sigma / h, two per float4 in that order.
+__device__ __forceinline__ void p2g_pair(P2GAcc &A, const float4 (*W)[P2G_NP], const float4 (*Q)[P2G_NP], int m,
+                                         int ii, int jj, int kk)
 {
-    // staged per particle: weights S/G (3 nodes x 3 axes x 2) and the payload
-    // m, m v (3), V sigma / h (6); plus the cell inside the block
+    const float4 X = W[ii][m], Y = W[3 + jj][m], Z = W[6 + kk][m];
+    const float4 q0 = Q[0][m], q1 = Q[1][m], q2 = Q[2][m], q3 = Q[3][m], q4 = Q[4][m];
+    const float2 Sx = lo2(X), Gx = hi2(X), Sy = lo2(Y), Gy = hi2(Y), Sz = lo2(Z), Gz = hi2(Z);
+    const float2 syz = mul2(Sy, Sz);
+    const float2 w = mul2(Sx, syz);
+    const float2 gx = mul2(Gx, syz);
+    const float2 gy = mul2(mul2(Sx, Sz), Gy);
+    const float2 gz = mul2(mul2(Sx, Sy), Gz);
+    A.m = fma2(w, lo2(q0), A.m);
+    A.px = fma2(w, hi2(q0), A.px);
+    A.py = fma2(w, lo2(q1), A.py);
+    A.pz = fma2(w, hi2(q1), A.pz);
+    const float2 s0 = lo2(q2), s1 = hi2(q2), s2 = lo2(q3), s3 = hi2(q3), s4 = lo2(q4), s5 = hi2(q4);
+    A.fx = fma2(gx, s0, fma2(gy, s3, fma2(gz, s5, A.fx)));
+    A.fy = fma2(gx, s3, fma2(gy, s1, fma2(gz, s4, A.fy)));
+    A.fz = fma2(gx, s5, fma2(gy, s4, fma2(gz, s2, A.fz)));
+}
+
+// one particle: half H (0: particle 2m, 1: particle 2m+1) of staged pair m
+template <int H>
+__device__ __forceinline__ void p2g_single(P2GAcc &A, const float4 (*W)[P2G_NP], const float4 (*Q)[P2G_NP], int m,
+                                           int ii, int jj, int kk)
+{
+    const float4 X = W[ii][m], Y = W[3 + jj][m], Z = W[6 + kk][m];
+    const float4 q0 = Q[0][m], q1 = Q[1][m], q2 = Q[2][m], q3 = Q[3][m], q4 = Q[4][m];
+    const float Sx = H ? X.y : X.x, Gx = H ? X.w : X.z, Sy = H ? Y.y : Y.x, Gy = H ? Y.w : Y.z;
+    const float Sz = H ? Z.y : Z.x, Gz = H ? Z.w : Z.z;
+    const float syz = Sy * Sz;
+    const float w = Sx * syz, gx = Gx * syz, gy = Sx * Sz * Gy, gz = Sx * Sy * Gz;
+    A.m.x = fmaf(w, H ? q0.y : q0.x, A.m.x);
+    A.px.x = fmaf(w, H ? q0.w : q0.z, A.px.x);
+    A.py.x = fmaf(w, H ? q1.y : q1.x, A.py.x);
+    A.pz.x = fmaf(w, H ? q1.w : q1.z, A.pz.x);
+    const float s0 = H ? q2.y : q2.x, s1 = H ? q2.w : q2.z, s2 = H ? q3.y : q3.x;
+    const float s3 = H ? q3.w : q3.z, s4 = H ? q4.y : q4.x, s5 = H ? q4.w : q4.z;
+    A.fx.x = fmaf(gx, s0, fmaf(gy, s3, fmaf(gz, s5, A.fx.x)));
+    A.fy.x = fmaf(gx, s3, fmaf(gy, s1, fmaf(gz, s4, A.fy.x)));
+    A.fz.x = fmaf(gx, s5, fmaf(gy, s4, fmaf(gz, s2, A.fz.x)));
+}
+
+__global__ void __launch_bounds__(P2G_CH) k_p2g_tiled(PView P, const int *perm, const int *skey, long long n,
+                                                       const int *seg_start, const int *nseg_ptr, int sorted,
+                                                       NodeBufs nb, GridGeom g)
+{
     __shared__ float tile[P2G_FIELDS * PT_NODES];
-    __shared__ float2 wts[9 * 256];       // (S, G) per axis and stencil node: [axis*3 + i][particle]
-    __shared__ float4 pay0[256];          // m, m vx, m vy, m vz
-    __shared__ float4 pay1[256];          // V sigma_xx, yy, zz, xy (with 1/h)
-    __shared__ float2 pay2[256];          // V sigma_yz, xz (with 1/h)
-    __shared__ int cellof[256];
-    __shared__ int run_start[257];
-    __shared__ int nruns;
+    __shared__ float4 W[9][P2G_NP];
+    __shared__ float4 Q[5][P2G_NP];
+    __shared__ int cellof[P2G_CH];
+    __shared__ int run_start[P2G_CH + 1];
+    __shared__ int wcount[P2G_CH / 32];
     __shared__ long long s_end;
     const int nseg = *nseg_ptr;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     // lane -> stencil node (ii, jj, kk); lanes 27..31 idle in the scatter
     const int ii = lane % 3, jj = (lane / 3) % 3, kk = lane / 9;
+    float *Wf = reinterpret_cast<float *>(&W[0][0]);
+    float *Qf = reinterpret_cast<float *>(&Q[0][0]);
     for (int sgi = blockIdx.x; sgi < nseg; sgi += gridDim.x) {
         const long long start = seg_start[sgi];
         const int blk = seg_block(skey, start);
         int bx, by, bz;
         decode_block(blk, g, bx, by, bz);
         const int tox = bx * CB, toy = by * CB, toz = g.is3d ? bz * CB : 0;
-        for (int t = tid; t < P2G_FIELDS * PT_NODES; t += 256) tile[t] = 0.f;
-        const long long send = sorted ? sorted_segment_end(skey, n, start, blk) : -1;
-        for (long long base = start;; base += 256) {
-            long long end = send;
-            if (!sorted) end = segment_chunk_end(skey, n, blk, base, &s_end);
-            const int cnt = (int)min((long long)256, end - base);
+        for (int t = tid; t < P2G_FIELDS * PT_NODES; t += P2G_CH) tile[t] = 0.f;
+        for (long long base = start;; base += P2G_CH) {
+            int cnt;
+            if (sorted) {
+                // sorted keys: the segment's particles in this chunk are a prefix of it; the
+                // barrier also ends the previous chunk's use of the staging arrays
+                const long long i = base + tid;
+                cnt = __syncthreads_count(i < n && (skey[i] >> CB_SHIFT) == blk);
+            } else {
+                cnt = (int)min((long long)P2G_CH, segment_chunk_end(skey, n, blk, base, &s_end) - base);
+            }
             if (cnt <= 0) break;
-            __syncthreads();
             // ---- stage weights and payload, natural (coalesced) order ----
-            int mycell = -1;
+            bool head = false;
             if (tid < cnt) {
                 const long long i = base + tid;
+                const int cell = skey[i] & 63;  // cell inside the block: (lz*4 + ly)*4 + lx
+                head = tid == 0 || (skey[i - 1] & 63) != cell;
+                cellof[tid] = cell;
                 const long long j = perm ? perm[i] : i;
-                const int key = P.ii(PF_KEY, j);
-                mycell = key & 63;  // cell inside the block: (lz*4 + ly)*4 + lx
+                const int m = tid >> 1, hf = tid & 1;
                 float S[3], G[3];
                 gimp_axis(P.f(PF_OX, j), g.lp, S, G);
 #pragma unroll
-                for (int k = 0; k < 3; k++) wts[(0 + k) * 256 + tid] = make_float2(S[k], G[k]);
+                for (int k = 0; k < 3; k++) {
+                    Wf[((0 + k) * P2G_NP + m) * 4 + hf] = S[k];
+                    Wf[((0 + k) * P2G_NP + m) * 4 + 2 + hf] = G[k];
+                }
                 gimp_axis(P.f(PF_OY, j), g.lp, S, G);
 #pragma unroll
-                for (int k = 0; k < 3; k++) wts[(3 + k) * 256 + tid] = make_float2(S[k], G[k]);
+                for (int k = 0; k < 3; k++) {
+                    Wf[((3 + k) * P2G_NP + m) * 4 + hf] = S[k];
+                    Wf[((3 + k) * P2G_NP + m) * 4 + 2 + hf] = G[k];
+                }
                 if (g.is3d) {
                     gimp_axis(P.f(PF_OZ, j), g.lp, S, G);
                 } else {
                     S[0] = 1.f; S[1] = 0.f; S[2] = 0.f; G[0] = 0.f; G[1] = 0.f; G[2] = 0.f;
                 }
 #pragma unroll
-                for (int k = 0; k < 3; k++) wts[(6 + k) * 256 + tid] = make_float2(S[k], G[k]);
-                const float m = P.f(PF_MASS, j);
-                const float sc = (m / P.f(PF_RHO, j)) * g.inv_h;  // V sigma with the gradient's 1/h
-                pay0[tid] = make_float4(m, m * P.f(PF_VX, j), m * P.f(PF_VY, j), m * P.f(PF_VZ, j));
-                pay1[tid] = make_float4(P.f(PF_S0, j) * sc, P.f(PF_S1, j) * sc, P.f(PF_S2, j) * sc, P.f(PF_S3, j) * sc);
-                pay2[tid] = make_float2(P.f(PF_S4, j) * sc, P.f(PF_S5, j) * sc);
-            }
-            cellof[tid] = mycell;
-            if (tid == 0) nruns = 0;
-            __syncthreads();
-            // ---- runs of equal cell inside the chunk (particles are sorted by cell) ----
-            const bool head = tid < cnt && (tid == 0 || cellof[tid - 1] != mycell);
-            const unsigned hm = __ballot_sync(0xffffffffu, head);
-            int wbase = 0;
-            if (lane == 0 && hm) wbase = atomicAdd(&nruns, __popc(hm));
-            wbase = __shfl_sync(0xffffffffu, wbase, 0);
-            if (head) run_start[wbase + __popc(hm & ((1u << lane) - 1u))] = tid;
-            __syncthreads();
-            const int R = nruns;
-            // ---- warp per run: lane = stencil node; sums in registers, one atomic per field ----
-            for (int r = warp; r < R; r += 8) {
-                const int p0 = run_start[r];
-                const int cell = cellof[p0];
-                int p1 = p0 + 1;
-                while (p1 < cnt && cellof[p1] == cell) p1++;
-                if (lane >= 27) continue;
-                float am = 0.f, apx = 0.f, apy = 0.f, apz = 0.f, afx = 0.f, afy = 0.f, afz = 0.f;
-#pragma unroll 2
-                for (int p = p0; p < p1; p++) {
-                    const float2 wx = wts[(0 + ii) * 256 + p], wy = wts[(3 + jj) * 256 + p], wz = wts[(6 + kk) * 256 + p];
-                    const float4 q0 = pay0[p], q1 = pay1[p];
-                    const float2 q2 = pay2[p];
-                    const float syz = wy.x * wz.x;
-                    const float w = wx.x * syz;
-                    const float gx = wx.y * syz, gy = wx.x * wy.y * wz.x, gz = wx.x * wy.x * wz.y;
-                    am += w * q0.x;
-                    apx += w * q0.y;
-                    apy += w * q0.z;
-                    apz += w * q0.w;
-                    afx -= gx * q1.x + gy * q1.w + gz * q2.y;
-                    afy -= gx * q1.w + gy * q1.y + gz * q2.x;
-                    afz -= gx * q2.y + gy * q2.x + gz * q1.z;
+                for (int k = 0; k < 3; k++) {
+                    Wf[((6 + k) * P2G_NP + m) * 4 + hf] = S[k];
+                    Wf[((6 + k) * P2G_NP + m) * 4 + 2 + hf] = G[k];
                 }
+                const float mass = P.f(PF_MASS, j);
+                const float sc = (mass / P.f(PF_RHO, j)) * g.inv_h;  // V sigma with the gradient's 1/h
+                Qf[(0 * P2G_NP + m) * 4 + hf] = mass;
+                Qf[(0 * P2G_NP + m) * 4 + 2 + hf] = mass * P.f(PF_VX, j);
+                Qf[(1 * P2G_NP + m) * 4 + hf] = mass * P.f(PF_VY, j);
+                Qf[(1 * P2G_NP + m) * 4 + 2 + hf] = mass * P.f(PF_VZ, j);
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    Qf[((2 + k) * P2G_NP + m) * 4 + hf] = P.f(PF_S0 + 2 * k, j) * sc;
+                    Qf[((2 + k) * P2G_NP + m) * 4 + 2 + hf] = P.f(PF_S0 + 2 * k + 1, j) * sc;
+                }
+            }
+            // ---- runs of equal cell, in order: run r is [run_start[r], run_start[r+1]) ----
+            const unsigned hm = __ballot_sync(0xffffffffu, head);
+            if (lane == 0) wcount[warp] = __popc(hm);
+            __syncthreads();
+            int wbase = 0, R = 0;
+#pragma unroll
+            for (int w2 = 0; w2 < P2G_CH / 32; w2++) {
+                const int c = wcount[w2];
+                wbase += (w2 < warp) ? c : 0;
+                R += c;
+            }
+            if (head) run_start[wbase + __popc(hm & ((1u << lane) - 1u))] = tid;
+            if (tid == 0) run_start[R] = cnt;
+            __syncthreads();
+            // ---- warp per run: lane = stencil node; sums in registers, one atomic per field ----
+            for (int r = warp; r < R; r += P2G_CH / 32) {
+                const int p0 = run_start[r], p1 = run_start[r + 1];
+                const int cell = cellof[p0];
+                if (lane >= 27) continue;
+                P2GAcc A;
+                A.m = A.px = A.py = A.pz = A.fx = A.fy = A.fz = make_float2(0.f, 0.f);
+                int p = p0;
+                if (p & 1) {  // an odd start: the second particle of its pair alone
+                    p2g_single<1>(A, W, Q, p >> 1, ii, jj, kk);
+                    p++;
+                }
+#pragma unroll 2
+                for (; p + 1 < p1; p += 2) p2g_pair(A, W, Q, p >> 1, ii, jj, kk);
+                if (p < p1) p2g_single<0>(A, W, Q, p >> 1, ii, jj, kk);
+                const float am = A.m.x + A.m.y, apx = A.px.x + A.px.y, apy = A.py.x + A.py.y;
+                const float apz = A.pz.x + A.pz.y;
+                const float afx = -(A.fx.x + A.fx.y), afy = -(A.fy.x + A.fy.y), afz = -(A.fz.x + A.fz.y);
                 if (am == 0.f && afx == 0.f && afy == 0.f && afz == 0.f && apx == 0.f && apy == 0.f && apz == 0.f)
                     continue;
                 const int li = cell & 3, lj = (cell >> 2) & 3, lk = cell >> 4;
@@ -298,11 +361,11 @@ __global__ void __launch_bounds__(256) k_p2g_tiled(PView P, const int *perm, con
                 atomicAdd(&tile[5 * PT_NODES + t], afy);
                 atomicAdd(&tile[6 * PT_NODES + t], afz);
             }
-            if (cnt < 256) break;
+            if (cnt < P2G_CH) break;
         }
         __syncthreads();
         // ---- flush the tile: two vector reductions per touched node ----
-        for (int t = tid; t < PT_NODES; t += 256) {
+        for (int t = tid; t < PT_NODES; t += P2G_CH) {
             const float m = tile[t], px = tile[PT_NODES + t], py = tile[2 * PT_NODES + t], pz = tile[3 * PT_NODES + t];
             const float fx = tile[4 * PT_NODES + t], fy = tile[5 * PT_NODES + t], fz = tile[6 * PT_NODES + t];
             if (m == 0.f && px == 0.f && py == 0.f && pz == 0.f && fx == 0.f && fy == 0.f && fz == 0.f) continue;
@@ -378,7 +441,7 @@ void launch_p2g(const PView &p, const int *perm, const int *skey, long long n, c
     if (a.sc.multi_body) {
         k_p2g_multi<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p, perm, n, nb, a);
     } else {
-        k_p2g_tiled<<<persist_grid, 256, 0, s>>>(p, perm, skey, n, seg_start, nseg, perm ? 1 : 0, nb, a.g);
+        k_p2g_tiled<<<persist_grid, P2G_CH, 0, s>>>(p, perm, skey, n, seg_start, nseg, perm ? 1 : 0, nb, a.g);
     }
     note_launch(1);
 }
@@ -386,7 +449,7 @@ void launch_p2g(const PView &p, const int *perm, const int *skey, long long n, c
 int p2g_blocks_per_sm()
 {
     int b = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_p2g_tiled, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_p2g_tiled, P2G_CH, 0);
     return b > 0 ? b : 1;
 }
 
@@ -653,6 +716,99 @@ __device__ __forceinline__ bool solve_node(const NodeBufs &nb, const StepArgs &a
     return active;
 }
 
+// Single-body nodal solve (Grid.cpp:9-245 without contact, then the grid BCs): one warp per
+// listed block, each lane owns nodes lane and lane + 32, and all loads of both nodes are
+// issued before the first result is needed.
+__global__ void __launch_bounds__(256) k_solve_single(NodeBufs nb, StepArgs a, int keep)
+{
+    const GridGeom &g = a.g;
+    const int lane = threadIdx.x & 31;
+    const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int nw = (int)((gridDim.x * blockDim.x) >> 5);
+    const int nact = *nb.active_n;
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float dtn = a.sc.dt_node;
+    int count = 0;
+    for (int w = gw; w < nact; w += nw) {
+        const int blk = nb.active_list[w];
+        const int bx = blk % g.nnbx, tb = blk / g.nnbx;
+        const int by = tb % g.nnby, bz = tb / g.nnby;
+        int nd[2];
+        bool in[2];
+        float4 A0[2], A1[2];
+        int bt[2];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int ln = lane + 32 * h;
+            const int i = bx * 4 + (ln & 3), j = by * 4 + ((ln >> 2) & 3), k = bz * 4 + (ln >> 4);
+            in[h] = i < g.nx && j < g.ny && k < g.nz;
+            nd[h] = in[h] ? node_index(i, j, k, g) : 0;
+            A0[h] = in[h] ? nb.acc0[nd[h]] : z4;
+            A1[h] = in[h] ? nb.acc1[nd[h]] : z4;
+            bt[h] = (in[h] && nb.bc_type) ? (int)nb.bc_type[nd[h]] : 0;
+        }
+        if (lane == 0) nb.flags[blk] = 0;
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            if (!in[h]) continue;
+            nb.acc0[nd[h]] = z4;
+            nb.acc1[nd[h]] = z4;
+            const float m = A0[h].x;
+            float4 F = A1[h];
+            // gravity enters here as m_node * g (Extrapolation.cpp:226-228)
+            F.x += m * a.sc.gravity[0];
+            F.y += m * a.sc.gravity[1];
+            F.z += m * a.sc.gravity[2];
+            float vc[3] = {0.f, 0.f, 0.f}, v1[3] = {0.f, 0.f, 0.f}, a1[3] = {0.f, 0.f, 0.f};
+            if (m != 0.0f) {
+                count++;
+                vc[0] = A0[h].y / m; vc[1] = A0[h].z / m; vc[2] = A0[h].w / m;
+                body_update(m, A0[h], F, dtn, v1, a1);
+            }
+            // grid BC, phase 2 (phase 1 is overwritten by the solve for every node the
+            // particles read; phase 3 repeats phase 2)
+            if (bt[h]) {
+                BCApply bc{bt[h], nb.bc_val[nd[h]], a.sc.fixed_grid_bcs};
+                bool set[3];
+                float val[3];
+                bc.comps(set, val);
+#pragma unroll
+                for (int c = 0; c < 3; c++)
+                    if (set[c]) {
+                        v1[c] = val[c]; a1[c] = 0.f;
+                        vc[c] = val[c];
+                    }
+            }
+            nb.gv[nd[h]] = make_float4(m, v1[0], v1[1], v1[2]);
+            nb.ga[nd[h]] = make_float4(a1[0], a1[1], a1[2], 0.f);
+            if (keep) {
+                nb.out_com[nd[h]] = make_float4(vc[0], vc[1], vc[2], 0.f);
+                nb.out_force[nd[h]] = make_float4(F.x, F.y, F.z, 0.f);
+            }
+        }
+    }
+    if (nb.active_count) {
+        for (int off = 16; off > 0; off >>= 1) count += __shfl_down_sync(0xffffffffu, count, off);
+        if (lane == 0 && count) atomicAdd(nb.active_count, count);
+    }
+}
+
+// The flagged node blocks, appended to the solve's list: one ballot and one atomic per warp.
+__global__ void k_compact_active(NodeBufs nb, int nnb)
+{
+    const int lane = threadIdx.x & 31;
+    for (int b0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; b0 < nnb; b0 += gridDim.x * blockDim.x) {
+        const int b = b0 + lane;
+        const bool f = b < nnb && nb.flags[b] != 0;
+        const unsigned m = __ballot_sync(0xffffffffu, f);
+        if (!m) continue;
+        int base = 0;
+        if (lane == 0) base = atomicAdd(nb.active_n, __popc(m));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (f) nb.active_list[base + __popc(m & ((1u << lane) - 1u))] = b;
+    }
+}
+
 // One warp per active node block from the list P2G and the fold built; the block's 64
 // nodes take two passes of the warp, then its flag is cleared for the next step.
 template <bool MULTI>
@@ -681,10 +837,13 @@ void launch_solve(const NodeBufs &nb, const StepArgs &a, bool keep_node_fields, 
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long cgrid = std::min<long long>((a.g.nnb + 255) / 256, (long long)sms * 8);
+    k_compact_active<<<(unsigned)std::max<long long>(cgrid, 1), 256, 0, s>>>(nb, (int)a.g.nnb);
+    note_launch(1);
     long long grid = std::min<long long>((a.g.nnb + 7) / 8, (long long)sms * 16);  // 8 warps per CTA
     if (grid < 1) grid = 1;
     if (a.sc.multi_body) k_solve_list<true><<<(unsigned)grid, 256, 0, s>>>(nb, a, keep_node_fields ? 1 : 0);
-    else k_solve_list<false><<<(unsigned)grid, 256, 0, s>>>(nb, a, keep_node_fields ? 1 : 0);
+    else k_solve_single<<<(unsigned)grid, 256, 0, s>>>(nb, a, keep_node_fields ? 1 : 0);
     note_launch(1);
 }
 
@@ -727,59 +886,15 @@ __device__ __forceinline__ void renorm(float &o, int &c, float lp)
     }
 }
 
-template <bool MULTI, bool HAS_DP>
-__device__ __forceinline__ void g2p_update_one(PState &st, const NodeBufs &nb, const StepArgs &a, bool track_normals,
-                                               bool check_finite, float nrm[3])
+// Everything after the G2P sums, for one particle: particle BCs, update, constitutive model,
+// damage, periodic wrap and the new cell key (TimeIntegration.cpp:11-296).  c0 is the cell of
+// the particle's first stencil node before the update.
+template <bool HAS_DP>
+__device__ __forceinline__ void update_after_g2p(PState &st, const int c0[3], float acc[3], float vg[3],
+                                                 const float L[3][3], const StepArgs &a, bool check_finite)
 {
     const GridGeom &g = a.g;
     const StepScalars &sc = a.sc;
-    Stencil w;
-    make_stencil(st, g, w);
-    const int obj = info_obj(st.info);
-
-    // ---- G2P (Extrapolation.cpp:288-367) ----
-    float acc[3] = {0.f, 0.f, 0.f}, vg[3] = {0.f, 0.f, 0.f};
-    float L[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};  // L[a][b] = sum v_a dW/dx_b
-    nrm[0] = nrm[1] = nrm[2] = 0.f;
-#pragma unroll
-    for (int kk = 0; kk < 3; kk++)
-#pragma unroll
-        for (int jj = 0; jj < 3; jj++) {
-            if (kk >= w.cnt[2] || jj >= w.cnt[1]) continue;
-            const float syz = w.S[1][jj] * w.S[2][kk];
-            const float gyz = w.G[1][jj] * w.S[2][kk] * g.inv_h, syg = w.S[1][jj] * w.G[2][kk] * g.inv_h;
-#pragma unroll
-            for (int ii = 0; ii < 3; ii++) {
-                if (ii >= w.cnt[0]) continue;
-                const int nd = node_index(w.c[0] + ii, w.c[1] + jj, w.c[2] + kk, g);
-                const float4 V = __ldg(&nb.gv[nd]);
-                if (V.x == 0.0f) continue;  // nodes without mass are skipped
-                float4 Vb, Ab;
-                int slot = 0;
-                if (!MULTI) {
-                    Vb = V;
-                    Ab = __ldg(&nb.ga[nd]);
-                } else {
-                    const int2 b = __ldg(&nb.body[nd]);
-                    slot = (b.x == obj) ? 0 : ((b.y == obj) ? 1 : -1);
-                    if (slot < 0) continue;  // a third body sees nothing from this node
-                    Vb = __ldg(&nb.bgv[slot][nd]);
-                    Ab = __ldg(&nb.bga[slot][nd]);
-                }
-                const float wgt = w.S[0][ii] * syz;
-                const float gx = w.G[0][ii] * syz * g.inv_h, gy = w.S[0][ii] * gyz, gz = w.S[0][ii] * syg;
-                acc[0] += wgt * Ab.x; acc[1] += wgt * Ab.y; acc[2] += wgt * Ab.z;
-                vg[0] += wgt * Vb.y; vg[1] += wgt * Vb.z; vg[2] += wgt * Vb.w;
-                L[0][0] += Vb.y * gx; L[0][1] += Vb.y * gy; L[0][2] += Vb.y * gz;
-                L[1][0] += Vb.z * gx; L[1][1] += Vb.z * gy; L[1][2] += Vb.z * gz;
-                L[2][0] += Vb.w * gx; L[2][1] += Vb.w * gy; L[2][2] += Vb.w * gz;
-                if (MULTI && track_normals) {
-                    const float4 N = __ldg(&nb.nrm_out[slot][nd]);
-                    nrm[0] += wgt * N.x; nrm[1] += wgt * N.y; nrm[2] += wgt * N.z;
-                }
-            }
-        }
-
     Constit c;
     c.r[0] = L[0][0];
     c.r[1] = L[1][1];
@@ -831,7 +946,7 @@ __device__ __forceinline__ void g2p_update_one(PState &st, const NodeBufs &nb, c
     }
 
     // ---- periodic wrap (TimeIntegration.cpp:80-108) and the new cell ----
-    int cc[3] = {w.c[0], w.c[1], w.c[2]};
+    int cc[3] = {c0[0], c0[1], c0[2]};
     const int naxes = g.is3d ? 3 : 2;
 #pragma unroll
     for (int ax = 0; ax < 3; ax++) {
@@ -880,6 +995,61 @@ __device__ __forceinline__ void g2p_update_one(PState &st, const NodeBufs &nb, c
     st.info &= ~INFO_INIT_VOL;
 }
 
+template <bool MULTI, bool HAS_DP>
+__device__ __forceinline__ void g2p_update_one(PState &st, const NodeBufs &nb, const StepArgs &a, bool track_normals,
+                                               bool check_finite, float nrm[3])
+{
+    const GridGeom &g = a.g;
+    Stencil w;
+    make_stencil(st, g, w);
+    const int obj = info_obj(st.info);
+
+    // ---- G2P (Extrapolation.cpp:288-367) ----
+    float acc[3] = {0.f, 0.f, 0.f}, vg[3] = {0.f, 0.f, 0.f};
+    float L[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};  // L[a][b] = sum v_a dW/dx_b
+    nrm[0] = nrm[1] = nrm[2] = 0.f;
+#pragma unroll
+    for (int kk = 0; kk < 3; kk++)
+#pragma unroll
+        for (int jj = 0; jj < 3; jj++) {
+            if (kk >= w.cnt[2] || jj >= w.cnt[1]) continue;
+            const float syz = w.S[1][jj] * w.S[2][kk];
+            const float gyz = w.G[1][jj] * w.S[2][kk] * g.inv_h, syg = w.S[1][jj] * w.G[2][kk] * g.inv_h;
+#pragma unroll
+            for (int ii = 0; ii < 3; ii++) {
+                if (ii >= w.cnt[0]) continue;
+                const int nd = node_index(w.c[0] + ii, w.c[1] + jj, w.c[2] + kk, g);
+                const float4 V = __ldg(&nb.gv[nd]);
+                if (V.x == 0.0f) continue;  // nodes without mass are skipped
+                float4 Vb, Ab;
+                int slot = 0;
+                if (!MULTI) {
+                    Vb = V;
+                    Ab = __ldg(&nb.ga[nd]);
+                } else {
+                    const int2 b = __ldg(&nb.body[nd]);
+                    slot = (b.x == obj) ? 0 : ((b.y == obj) ? 1 : -1);
+                    if (slot < 0) continue;  // a third body sees nothing from this node
+                    Vb = __ldg(&nb.bgv[slot][nd]);
+                    Ab = __ldg(&nb.bga[slot][nd]);
+                }
+                const float wgt = w.S[0][ii] * syz;
+                const float gx = w.G[0][ii] * syz * g.inv_h, gy = w.S[0][ii] * gyz, gz = w.S[0][ii] * syg;
+                acc[0] += wgt * Ab.x; acc[1] += wgt * Ab.y; acc[2] += wgt * Ab.z;
+                vg[0] += wgt * Vb.y; vg[1] += wgt * Vb.z; vg[2] += wgt * Vb.w;
+                L[0][0] += Vb.y * gx; L[0][1] += Vb.y * gy; L[0][2] += Vb.y * gz;
+                L[1][0] += Vb.z * gx; L[1][1] += Vb.z * gy; L[1][2] += Vb.z * gz;
+                L[2][0] += Vb.w * gx; L[2][1] += Vb.w * gy; L[2][2] += Vb.w * gz;
+                if (MULTI && track_normals) {
+                    const float4 N = __ldg(&nb.nrm_out[slot][nd]);
+                    nrm[0] += wgt * N.x; nrm[1] += wgt * N.y; nrm[2] += wgt * N.z;
+                }
+            }
+        }
+
+    update_after_g2p<HAS_DP>(st, w.c, acc, vg, L, a, check_finite);
+}
+
 // Unfused G2P + update: one thread per particle in sorted order, state read through perm
 // and written to the other slab.
 template <bool MULTI, bool HAS_DP>
@@ -900,8 +1070,180 @@ __global__ void __launch_bounds__(256, 3) k_g2p_update(PView src, PView dst, con
     }
 }
 
-void launch_g2p_update(const PView &src, const PView &dst, const int *perm, long long n, const NodeBufs &nb,
-                       const StepArgs &a, bool track_normals, bool check_finite, bool has_dp, cudaStream_t s)
+// resident CTAs per SM the G2P kernel is register-limited to (64 registers at 4)
+#ifndef GY_G2P_MINB
+#define GY_G2P_MINB 4
+#endif
+
+// 4-byte asynchronous global -> shared copy (no register holds the value in flight)
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// particle fields G2P does not need, staged in shared memory while the G2P sums run:
+// velocity, stress, strain, density, mass, info, pid, then (DP / damage) eqps, plastic
+// strain, damage, smax
+__device__ __forceinline__ constexpr int g2p_stage_field(int f)
+{
+    return f < 3 ? PF_VX + f : f < 9 ? PF_S0 + (f - 3) : f < 15 ? PF_E0 + (f - 9) : f == 15 ? PF_RHO
+         : f == 16 ? PF_MASS : f == 17 ? PF_INFO : f == 18 ? PF_PID : f == 19 ? PF_EQPS
+         : f < 26 ? PF_EP0 + (f - 20) : f == 26 ? PF_DMG : PF_SMAX;
+}
+constexpr int G2P_NBASE = 19, G2P_NDP = 9;
+
+// Single-body G2P + update through a shared-memory node tile.  A CTA owns one segment (the
+// particles of one 4x4x4 cell block): it loads the block's 6x6x6 solved node tile once, with
+// massless nodes zeroed (they are skipped, Extrapolation.cpp:301-303), then runs one thread
+// per particle in sorted order.  The G2P sums are separable per axis: for every (j, k) node
+// row the three x nodes are contracted first, then weighted by the y/z factors.
+template <bool HAS_DP>
+__global__ void __launch_bounds__(256, GY_G2P_MINB) k_g2p_tiled(PView src, PView dst, const int *perm, const int *skey,
+                                                      long long n, const int *seg_start, const int *nseg_ptr,
+                                                      int sorted, NodeBufs nb, StepArgs a, int check_finite)
+{
+    constexpr int NST = G2P_NBASE + (HAS_DP ? G2P_NDP : 0);
+    __shared__ float4 TV[PT_NODES], TA[PT_NODES];
+    __shared__ float stage[NST][256];
+    __shared__ long long s_end;
+    const GridGeom &g = a.g;
+    const int nseg = *nseg_ptr;
+    const int tid = threadIdx.x;
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int sgi = blockIdx.x; sgi < nseg; sgi += gridDim.x) {
+        const long long start = seg_start[sgi];
+        const int blk = seg_block(skey, start);
+        int bx, by, bz;
+        decode_block(blk, g, bx, by, bz);
+        const int tox = bx * CB, toy = by * CB, toz = g.is3d ? bz * CB : 0;
+        __syncthreads();  // the previous segment's particles are done with the tile
+        for (int t = tid; t < PT_NODES; t += blockDim.x) {
+            const int ni = tox + t % PT, nj = toy + (t / PT) % PT, nk = toz + t / (PT * PT);
+            float4 V = z4, A = z4;
+            if (ni < g.nx && nj < g.ny && nk < g.nz) {
+                const int nd = node_index(ni, nj, nk, g);
+                V = nb.gv[nd];
+                A = nb.ga[nd];
+                if (V.x == 0.0f) { V = z4; A = z4; }
+            }
+            TV[t] = V;
+            TA[t] = A;
+        }
+        for (long long base = start;; base += blockDim.x) {
+            int cnt;
+            if (sorted) {
+                // the barrier also publishes the tile
+                const long long i = base + tid;
+                cnt = __syncthreads_count(i < n && (skey[i] >> CB_SHIFT) == blk);
+            } else {
+                cnt = (int)min((long long)blockDim.x, segment_chunk_end(skey, n, blk, base, &s_end) - base);
+            }
+            if (cnt <= 0) break;
+            if (tid < cnt) {
+                const long long i = base + tid;
+                const long long j = perm ? perm[i] : i;
+                PState st;
+                st.key = src.ii(PF_KEY, j);
+#pragma unroll
+                for (int k = 0; k < 3; k++) st.o[k] = src.f(PF_OX + k, j);
+                // the rest of the state travels to shared memory during the G2P sums
+#pragma unroll
+                for (int f = 0; f < NST; f++) cp_async4(&stage[f][tid], &src.f(g2p_stage_field(f), j));
+                cp_async_commit();
+                float Sx[3], Gx[3], Sy[3], Gy[3], Sz[3], Gz[3];
+                gimp_axis(st.o[0], g.lp, Sx, Gx);
+                gimp_axis(st.o[1], g.lp, Sy, Gy);
+                if (g.is3d) {
+                    gimp_axis(st.o[2], g.lp, Sz, Gz);
+                } else {
+                    Sz[0] = 1.f; Sz[1] = 0.f; Sz[2] = 0.f; Gz[0] = 0.f; Gz[1] = 0.f; Gz[2] = 0.f;
+                }
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    Gx[k] *= g.inv_h;
+                    Gy[k] *= g.inv_h;
+                    Gz[k] *= g.inv_h;
+                }
+                const int lc = st.key & 63;
+                const int t0 = ((lc >> 4) * PT + ((lc >> 2) & 3)) * PT + (lc & 3);
+                float acc[3] = {0.f, 0.f, 0.f}, vg[3] = {0.f, 0.f, 0.f};
+                float L[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};  // L[a][b] = sum v_a dW/dx_b
+#pragma unroll
+                for (int kk = 0; kk < 3; kk++) {
+                    if (kk > 0 && !g.is3d) break;
+#pragma unroll
+                    for (int jj = 0; jj < 3; jj++) {
+                        const float4 *tv = TV + t0 + (kk * PT + jj) * PT;
+                        const float4 *ta = TA + t0 + (kk * PT + jj) * PT;
+                        float xv[3] = {0.f, 0.f, 0.f}, yv[3] = {0.f, 0.f, 0.f}, xa[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+                        for (int ii = 0; ii < 3; ii++) {
+                            const float4 V = tv[ii], A = ta[ii];
+                            xv[0] += Sx[ii] * V.y; xv[1] += Sx[ii] * V.z; xv[2] += Sx[ii] * V.w;
+                            yv[0] += Gx[ii] * V.y; yv[1] += Gx[ii] * V.z; yv[2] += Gx[ii] * V.w;
+                            xa[0] += Sx[ii] * A.x; xa[1] += Sx[ii] * A.y; xa[2] += Sx[ii] * A.z;
+                        }
+                        const float syz = Sy[jj] * Sz[kk], gyz = Gy[jj] * Sz[kk], syg = Sy[jj] * Gz[kk];
+#pragma unroll
+                        for (int c = 0; c < 3; c++) {
+                            vg[c] += syz * xv[c];
+                            acc[c] += syz * xa[c];
+                            L[c][0] += syz * yv[c];
+                            L[c][1] += gyz * xv[c];
+                            L[c][2] += syg * xv[c];
+                        }
+                    }
+                }
+                cp_async_wait_all();
+#pragma unroll
+                for (int k = 0; k < 3; k++) st.v[k] = stage[k][tid];
+#pragma unroll
+                for (int k = 0; k < 6; k++) {
+                    st.s[k] = stage[3 + k][tid];
+                    st.e[k] = stage[9 + k][tid];
+                }
+                st.rho = stage[15][tid];
+                st.mass = stage[16][tid];
+                st.info = __float_as_uint(stage[17][tid]);
+                st.pid = __float_as_int(stage[18][tid]);
+                if (HAS_DP) {
+                    st.eqps = stage[G2P_NBASE + (HAS_DP ? 0 : 0)][tid];
+#pragma unroll
+                    for (int k = 0; k < 6; k++) st.ep[k] = stage[G2P_NBASE + (HAS_DP ? 1 + k : 0)][tid];
+                    st.dmg = stage[G2P_NBASE + (HAS_DP ? 7 : 0)][tid];
+                    st.smax = stage[G2P_NBASE + (HAS_DP ? 8 : 0)][tid];
+                } else {
+                    st.eqps = 0.f;
+#pragma unroll
+                    for (int k = 0; k < 6; k++) st.ep[k] = 0.f;
+                    st.dmg = 0.f;
+                    st.smax = 0.f;
+                }
+                int c0[3];
+                decode_key(st.key, g, c0[0], c0[1], c0[2]);
+                if (!g.is3d) c0[2] = 0;
+                update_after_g2p<HAS_DP>(st, c0, acc, vg, L, a, check_finite != 0);
+                store_state<HAS_DP>(dst, i, st);
+            }
+            if (cnt < (int)blockDim.x) break;
+        }
+    }
+}
+
+int g2p_blocks_per_sm(bool has_dp)
+{
+    int b = 0;
+    if (has_dp) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_g2p_tiled<true>, 256, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_g2p_tiled<false>, 256, 0);
+    return b > 0 ? b : 1;
+}
+
+void launch_g2p_update(const PView &src, const PView &dst, const int *perm, const int *skey, long long n,
+                       const int *seg_start, const int *nseg, int g2p_grid, const NodeBufs &nb, const StepArgs &a,
+                       bool track_normals, bool check_finite, bool has_dp, cudaStream_t s)
 {
     if (n == 0) return;
     const unsigned grid = (unsigned)((n + 255) / 256);
@@ -910,8 +1252,9 @@ void launch_g2p_update(const PView &src, const PView &dst, const int *perm, long
         if (has_dp) k_g2p_update<true, true><<<grid, 256, 0, s>>>(src, dst, perm, n, nb, a, tn, cf);
         else k_g2p_update<true, false><<<grid, 256, 0, s>>>(src, dst, perm, n, nb, a, tn, cf);
     } else {
-        if (has_dp) k_g2p_update<false, true><<<grid, 256, 0, s>>>(src, dst, perm, n, nb, a, 0, cf);
-        else k_g2p_update<false, false><<<grid, 256, 0, s>>>(src, dst, perm, n, nb, a, 0, cf);
+        const int srt = perm ? 1 : 0;
+        if (has_dp) k_g2p_tiled<true><<<g2p_grid, 256, 0, s>>>(src, dst, perm, skey, n, seg_start, nseg, srt, nb, a, cf);
+        else k_g2p_tiled<false><<<g2p_grid, 256, 0, s>>>(src, dst, perm, skey, n, seg_start, nseg, srt, nb, a, cf);
     }
     note_launch(1);
 }
@@ -1021,28 +1364,34 @@ void launch_body_assign(const NodeBufs &nb, const StepArgs &a, const int *cell_m
 }
 
 // ---------------------------------------------------------------------------------------
-// FP64 conservation sums: mass, momentum, kinetic energy, strain energy
+// Conservation sums: mass, momentum, kinetic energy, strain energy.  Each thread sums its
+// few particles in FP32 (the state's own precision), the mass in FP64 so that its total is
+// exact to FP64 rounding; warps, CTAs and the grid add in FP64.
 
 __global__ void k_stats(PView P, long long n, double *out)
 {
     __shared__ double sh[8][8];
-    double acc[6] = {0, 0, 0, 0, 0, 0};
+    float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    double msum = 0.0;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const double m = P.f(PF_MASS, i);
-        const double vx = P.f(PF_VX, i), vy = P.f(PF_VY, i), vz = P.f(PF_VZ, i);
-        acc[0] += m;
+        const float m = P.f(PF_MASS, i);
+        const float vx = P.f(PF_VX, i), vy = P.f(PF_VY, i), vz = P.f(PF_VZ, i);
+        msum += (double)m;
         acc[1] += m * vx;
         acc[2] += m * vy;
         acc[3] += m * vz;
-        acc[4] += 0.5 * m * (vx * vx + vy * vy + vz * vz);
-        const double V = m / (double)P.f(PF_RHO, i);
-        double se = 0.0;
-        for (int k = 0; k < 3; k++) se += (double)P.f(PF_S0 + k, i) * P.f(PF_E0 + k, i);
-        for (int k = 3; k < 6; k++) se += 2.0 * (double)P.f(PF_S0 + k, i) * P.f(PF_E0 + k, i);
-        acc[5] += 0.5 * V * se;
+        acc[4] += 0.5f * m * (vx * vx + vy * vy + vz * vz);
+        const float V = m / P.f(PF_RHO, i);
+        float se = 0.f;
+#pragma unroll
+        for (int k = 0; k < 3; k++) se += P.f(PF_S0 + k, i) * P.f(PF_E0 + k, i);
+#pragma unroll
+        for (int k = 3; k < 6; k++) se += 2.f * P.f(PF_S0 + k, i) * P.f(PF_E0 + k, i);
+        acc[5] += 0.5f * V * se;
     }
+#pragma unroll
     for (int k = 0; k < 6; k++) {
-        double v = acc[k];
+        double v = k == 0 ? msum : (double)acc[k];
         for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffff, v, off);
         if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5][k] = v;
     }
@@ -1059,7 +1408,7 @@ void launch_stats(const PView &p, long long n, double *out8, cudaStream_t s)
     cudaMemsetAsync(out8, 0, 8 * sizeof(double), s);
     if (n == 0) return;
     long long blocks = (n + 255) / 256;
-    if (blocks > 4096) blocks = 4096;
+    if (blocks > 2048) blocks = 2048;
     k_stats<<<(unsigned)blocks, 256, 0, s>>>(p, n, out8);
     note_launch(1);
 }

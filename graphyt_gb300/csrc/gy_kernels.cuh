@@ -57,8 +57,10 @@ void launch_p2g(const PView &p, const int *perm, const int *skey, long long n, c
                 const int *nseg, int persist_grid, const NodeBufs &nb, const StepArgs &a, cudaStream_t s);
 void launch_fold(const NodeBufs &nb, const StepArgs &a, cudaStream_t s);
 void launch_solve(const NodeBufs &nb, const StepArgs &a, bool keep_node_fields, cudaStream_t s);
-void launch_g2p_update(const PView &src, const PView &dst, const int *perm, long long n, const NodeBufs &nb,
-                       const StepArgs &a, bool track_normals, bool check_finite, bool has_dp, cudaStream_t s);
+void launch_g2p_update(const PView &src, const PView &dst, const int *perm, const int *skey, long long n,
+                       const int *seg_start, const int *nseg, int g2p_grid, const NodeBufs &nb, const StepArgs &a,
+                       bool track_normals, bool check_finite, bool has_dp, cudaStream_t s);
+int g2p_blocks_per_sm(bool has_dp);
 int p2g_blocks_per_sm();
 void launch_body_tables(const PView &p, long long n, const StepArgs &a, int *cell_min, int nbody,
                         const int *refkeys, cudaStream_t s);

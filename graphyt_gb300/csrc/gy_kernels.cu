@@ -166,12 +166,12 @@ constexpr int P2G_NP = P2G_CH / 2 + 1;  // pairs per staged row; the odd row len
 // Segment bounds when the keys are not freshly sorted: runs of one block can repeat, so
 // the run ends at the first index after `base` whose block differs (per chunk).
 __device__ __forceinline__ long long segment_chunk_end(const int *skey, long long n, int blk, long long base,
-                                                       long long *s_end)
+                                                       int chunk, long long *s_end)
 {
-    if (threadIdx.x == 0) *s_end = base + blockDim.x;
+    if (threadIdx.x == 0) *s_end = base + chunk;
     __syncthreads();
     const long long i = base + threadIdx.x;
-    const bool inb = i < n && (skey[i] >> CB_SHIFT) == blk;
+    const bool inb = (int)threadIdx.x >= chunk || (i < n && (skey[i] >> CB_SHIFT) == blk);
     if (!inb) atomicMin((unsigned long long *)s_end, (unsigned long long)i);
     __syncthreads();
     const long long e = *s_end;
@@ -270,7 +270,7 @@ __global__ void __launch_bounds__(P2G_CH) k_p2g_tiled(PView P, const int *perm, 
                 const long long i = base + tid;
                 cnt = __syncthreads_count(i < n && (skey[i] >> CB_SHIFT) == blk);
             } else {
-                cnt = (int)min((long long)P2G_CH, segment_chunk_end(skey, n, blk, base, &s_end) - base);
+                cnt = (int)min((long long)P2G_CH, segment_chunk_end(skey, n, blk, base, P2G_CH, &s_end) - base);
             }
             if (cnt <= 0) break;
             // ---- stage weights and payload, natural (coalesced) order ----
@@ -1106,7 +1106,8 @@ __global__ void __launch_bounds__(256, GY_G2P_MINB) k_g2p_tiled(PView src, PView
                                                       int sorted, NodeBufs nb, StepArgs a, int check_finite)
 {
     constexpr int NST = G2P_NBASE + (HAS_DP ? G2P_NDP : 0);
-    __shared__ float4 TV[PT_NODES], TA[PT_NODES];
+    __shared__ float4 TV[PT_NODES];  // (v1x, v1y, v1z, a1z), zero for massless nodes
+    __shared__ float2 TA[PT_NODES];  // (a1x, a1y)
     __shared__ float stage[NST][256];
     __shared__ long long s_end;
     const GridGeom &g = a.g;
@@ -1129,8 +1130,8 @@ __global__ void __launch_bounds__(256, GY_G2P_MINB) k_g2p_tiled(PView src, PView
                 A = nb.ga[nd];
                 if (V.x == 0.0f) { V = z4; A = z4; }
             }
-            TV[t] = V;
-            TA[t] = A;
+            TV[t] = make_float4(V.y, V.z, V.w, A.z);
+            TA[t] = make_float2(A.x, A.y);
         }
         for (long long base = start;; base += blockDim.x) {
             int cnt;
@@ -1139,7 +1140,7 @@ __global__ void __launch_bounds__(256, GY_G2P_MINB) k_g2p_tiled(PView src, PView
                 const long long i = base + tid;
                 cnt = __syncthreads_count(i < n && (skey[i] >> CB_SHIFT) == blk);
             } else {
-                cnt = (int)min((long long)blockDim.x, segment_chunk_end(skey, n, blk, base, &s_end) - base);
+                cnt = (int)min((long long)blockDim.x, segment_chunk_end(skey, n, blk, base, blockDim.x, &s_end) - base);
             }
             if (cnt <= 0) break;
             if (tid < cnt) {
@@ -1169,34 +1170,52 @@ __global__ void __launch_bounds__(256, GY_G2P_MINB) k_g2p_tiled(PView src, PView
                 }
                 const int lc = st.key & 63;
                 const int t0 = ((lc >> 4) * PT + ((lc >> 2) & 3)) * PT + (lc & 3);
-                float acc[3] = {0.f, 0.f, 0.f}, vg[3] = {0.f, 0.f, 0.f};
-                float L[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};  // L[a][b] = sum v_a dW/dx_b
+                // FP32x2 sums: x/y components in pairs, the z velocity with the z acceleration
+                const float2 z2 = make_float2(0.f, 0.f);
+                float2 vg01 = z2, acc01 = z2, vz_az = z2;       // (vg_x, vg_y), (a_x, a_y), (vg_z, a_z)
+                float2 Lc0 = z2, Lc1 = z2, Lc2 = z2;            // (L[0][b], L[1][b]) for b = x, y, z
+                float L20 = 0.f, L21 = 0.f, L22 = 0.f;           // L[2][b]
+                float2 Sx2[3], Gx2[3];
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    Sx2[k] = make_float2(Sx[k], Sx[k]);
+                    Gx2[k] = make_float2(Gx[k], Gx[k]);
+                }
 #pragma unroll
                 for (int kk = 0; kk < 3; kk++) {
                     if (kk > 0 && !g.is3d) break;
 #pragma unroll
                     for (int jj = 0; jj < 3; jj++) {
                         const float4 *tv = TV + t0 + (kk * PT + jj) * PT;
-                        const float4 *ta = TA + t0 + (kk * PT + jj) * PT;
-                        float xv[3] = {0.f, 0.f, 0.f}, yv[3] = {0.f, 0.f, 0.f}, xa[3] = {0.f, 0.f, 0.f};
+                        const float2 *ta = TA + t0 + (kk * PT + jj) * PT;
+                        float2 xv01 = z2, xv2a2 = z2, yv01 = z2, xa01 = z2;
+                        float yv2 = 0.f;
 #pragma unroll
                         for (int ii = 0; ii < 3; ii++) {
-                            const float4 V = tv[ii], A = ta[ii];
-                            xv[0] += Sx[ii] * V.y; xv[1] += Sx[ii] * V.z; xv[2] += Sx[ii] * V.w;
-                            yv[0] += Gx[ii] * V.y; yv[1] += Gx[ii] * V.z; yv[2] += Gx[ii] * V.w;
-                            xa[0] += Sx[ii] * A.x; xa[1] += Sx[ii] * A.y; xa[2] += Sx[ii] * A.z;
+                            const float4 V = tv[ii];
+                            const float2 A = ta[ii];
+                            xv01 = fma2(Sx2[ii], lo2(V), xv01);
+                            xv2a2 = fma2(Sx2[ii], hi2(V), xv2a2);
+                            yv01 = fma2(Gx2[ii], lo2(V), yv01);
+                            yv2 = fmaf(Gx[ii], V.z, yv2);
+                            xa01 = fma2(Sx2[ii], A, xa01);
                         }
                         const float syz = Sy[jj] * Sz[kk], gyz = Gy[jj] * Sz[kk], syg = Sy[jj] * Gz[kk];
-#pragma unroll
-                        for (int c = 0; c < 3; c++) {
-                            vg[c] += syz * xv[c];
-                            acc[c] += syz * xa[c];
-                            L[c][0] += syz * yv[c];
-                            L[c][1] += gyz * xv[c];
-                            L[c][2] += syg * xv[c];
-                        }
+                        const float2 syz2 = make_float2(syz, syz), gyz2 = make_float2(gyz, gyz);
+                        const float2 syg2 = make_float2(syg, syg);
+                        vg01 = fma2(syz2, xv01, vg01);
+                        vz_az = fma2(syz2, xv2a2, vz_az);
+                        acc01 = fma2(syz2, xa01, acc01);
+                        Lc0 = fma2(syz2, yv01, Lc0);
+                        L20 = fmaf(syz, yv2, L20);
+                        Lc1 = fma2(gyz2, xv01, Lc1);
+                        L21 = fmaf(gyz, xv2a2.x, L21);
+                        Lc2 = fma2(syg2, xv01, Lc2);
+                        L22 = fmaf(syg, xv2a2.x, L22);
                     }
                 }
+                float acc[3] = {acc01.x, acc01.y, vz_az.y}, vg[3] = {vg01.x, vg01.y, vz_az.x};
+                const float L[3][3] = {{Lc0.x, Lc1.x, Lc2.x}, {Lc0.y, Lc1.y, Lc2.y}, {L20, L21, L22}};
                 cp_async_wait_all();
 #pragma unroll
                 for (int k = 0; k < 3; k++) st.v[k] = stage[k][tid];

@@ -198,6 +198,9 @@ gy_status gy_create(const gy_grid_desc *grid, int device, gy_solver **out)
     g.h = (float)h;
     g.inv_h = (float)(1.0 / h);
     g.lp = (float)(0.5 * grid->psep / h);
+    g.inv_l = (float)(1.0 / (double)g.lp);
+    g.inv_2l = (float)(0.5 / (double)g.lp);
+    g.inv_4l = (float)(0.25 / (double)g.lp);
     g.is3d = is3d ? 1 : 0;
     for (int a = 0; a < 3; a++) {
         const double W = grid->L[a] / h - 2.0;  // the wrap limit L - 2h in cells

@@ -75,6 +75,7 @@ struct GridGeom {
     long long nc;             // cells
     float h, inv_h;           // cell size
     float lp;                 // GIMP half-width psep/2 in cell units
+    float inv_l, inv_2l, inv_4l;  // 1/lp, 1/(2 lp), 1/(4 lp)
     int is3d;
     // periodic particle wrap (TimeIntegration.cpp:80-108) in cell units:
     // X > wrap_hi[a] -> X += shift; X < 1 -> X -= shift, shift = 1 - (L/h - 2)
@@ -105,22 +106,22 @@ struct StepScalars {
 //   u <  1-l: node 0 and 1 on the linear pieces, node 2 outside the support;
 //   u >= 1-l: q = u-(1-l) in [0, 2l): node 0 and 2 on the quadratic end pieces, node 1
 //             on the central parabola.
-__device__ __forceinline__ void gimp_axis(float u, float l, float S[3], float G[3])
+__device__ __forceinline__ void gimp_axis(float u, const GridGeom &g, float S[3], float G[3])
 {
+    const float l = g.lp;
     if (u < 1.0f - l) {
         S[0] = 1.0f - u; S[1] = u;    S[2] = 0.0f;
         G[0] = -1.0f;    G[1] = 1.0f; G[2] = 0.0f;
     } else {
         const float q = u - (1.0f - l);
         const float a = 2.0f * l - q;          // = 1 + l - u
-        const float inv4l = 0.25f / l, inv2l = 0.5f / l;
         const float d1 = 1.0f - u;
-        S[0] = a * a * inv4l;
-        S[1] = 1.0f - (d1 * d1 + l * l) * inv2l;
-        S[2] = q * q * inv4l;
-        G[0] = -a * inv2l;
-        G[1] = d1 / l;
-        G[2] = q * inv2l;
+        S[0] = a * a * g.inv_4l;
+        S[1] = 1.0f - (d1 * d1 + l * l) * g.inv_2l;
+        S[2] = q * q * g.inv_4l;
+        G[0] = -a * g.inv_2l;
+        G[1] = d1 * g.inv_l;
+        G[2] = q * g.inv_2l;
     }
 }
 

@@ -128,12 +128,12 @@ struct Stencil {
 __device__ __forceinline__ void make_stencil(const PState &st, const GridGeom &g, Stencil &w)
 {
     decode_key(st.key, g, w.c[0], w.c[1], w.c[2]);
-    gimp_axis(st.o[0], g.lp, w.S[0], w.G[0]);
-    gimp_axis(st.o[1], g.lp, w.S[1], w.G[1]);
+    gimp_axis(st.o[0], g, w.S[0], w.G[0]);
+    gimp_axis(st.o[1], g, w.S[1], w.G[1]);
     w.cnt[0] = (st.o[0] < 1.0f - g.lp) ? 2 : 3;
     w.cnt[1] = (st.o[1] < 1.0f - g.lp) ? 2 : 3;
     if (g.is3d) {
-        gimp_axis(st.o[2], g.lp, w.S[2], w.G[2]);
+        gimp_axis(st.o[2], g, w.S[2], w.G[2]);
         w.cnt[2] = (st.o[2] < 1.0f - g.lp) ? 2 : 3;
     } else {
         w.c[2] = 0;
@@ -251,8 +251,10 @@ __global__ void __launch_bounds__(P2G_CH) k_p2g_tiled(PView P, const int *perm, 
     __shared__ long long s_end;
     const int nseg = *nseg_ptr;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    // lane -> stencil node (ii, jj, kk); lanes 27..31 idle in the scatter
-    const int ii = lane % 3, jj = (lane / 3) % 3, kk = lane / 9;
+    // lane -> stencil node (ii, jj, kk); lanes 27..31 shadow valid nodes (kk clamped) so the
+    // scatter loop runs without divergence, and skip the atomics
+    const int ii = lane % 3, jj = (lane / 3) % 3, kk = min(lane / 9, 2);
+    const bool scatter_lane = lane < 27;
     float *Wf = reinterpret_cast<float *>(&W[0][0]);
     float *Qf = reinterpret_cast<float *>(&Q[0][0]);
     for (int sgi = blockIdx.x; sgi < nseg; sgi += gridDim.x) {
@@ -283,20 +285,20 @@ __global__ void __launch_bounds__(P2G_CH) k_p2g_tiled(PView P, const int *perm, 
                 const long long j = perm ? perm[i] : i;
                 const int m = tid >> 1, hf = tid & 1;
                 float S[3], G[3];
-                gimp_axis(P.f(PF_OX, j), g.lp, S, G);
+                gimp_axis(P.f(PF_OX, j), g, S, G);
 #pragma unroll
                 for (int k = 0; k < 3; k++) {
                     Wf[((0 + k) * P2G_NP + m) * 4 + hf] = S[k];
                     Wf[((0 + k) * P2G_NP + m) * 4 + 2 + hf] = G[k];
                 }
-                gimp_axis(P.f(PF_OY, j), g.lp, S, G);
+                gimp_axis(P.f(PF_OY, j), g, S, G);
 #pragma unroll
                 for (int k = 0; k < 3; k++) {
                     Wf[((3 + k) * P2G_NP + m) * 4 + hf] = S[k];
                     Wf[((3 + k) * P2G_NP + m) * 4 + 2 + hf] = G[k];
                 }
                 if (g.is3d) {
-                    gimp_axis(P.f(PF_OZ, j), g.lp, S, G);
+                    gimp_axis(P.f(PF_OZ, j), g, S, G);
                 } else {
                     S[0] = 1.f; S[1] = 0.f; S[2] = 0.f; G[0] = 0.f; G[1] = 0.f; G[2] = 0.f;
                 }
@@ -335,7 +337,6 @@ __global__ void __launch_bounds__(P2G_CH) k_p2g_tiled(PView P, const int *perm, 
             for (int r = warp; r < R; r += P2G_CH / 32) {
                 const int p0 = run_start[r], p1 = run_start[r + 1];
                 const int cell = cellof[p0];
-                if (lane >= 27) continue;
                 P2GAcc A;
                 A.m = A.px = A.py = A.pz = A.fx = A.fy = A.fz = make_float2(0.f, 0.f);
                 int p = p0;
@@ -349,8 +350,9 @@ __global__ void __launch_bounds__(P2G_CH) k_p2g_tiled(PView P, const int *perm, 
                 const float am = A.m.x + A.m.y, apx = A.px.x + A.px.y, apy = A.py.x + A.py.y;
                 const float apz = A.pz.x + A.pz.y;
                 const float afx = -(A.fx.x + A.fx.y), afy = -(A.fy.x + A.fy.y), afz = -(A.fz.x + A.fz.y);
-                if (am == 0.f && afx == 0.f && afy == 0.f && afz == 0.f && apx == 0.f && apy == 0.f && apz == 0.f)
-                    continue;
+                // a node outside every particle's support has am == 0 and then no weight and
+                // no gradient either (an axis with S = 0 has G = 0)
+                if (!scatter_lane || am == 0.f) continue;
                 const int li = cell & 3, lj = (cell >> 2) & 3, lk = cell >> 4;
                 const int t = ((lk + kk) * PT + (lj + jj)) * PT + (li + ii);
                 atomicAdd(&tile[0 * PT_NODES + t], am);
@@ -1155,10 +1157,10 @@ __global__ void __launch_bounds__(256, GY_G2P_MINB) k_g2p_tiled(PView src, PView
                 for (int f = 0; f < NST; f++) cp_async4(&stage[f][tid], &src.f(g2p_stage_field(f), j));
                 cp_async_commit();
                 float Sx[3], Gx[3], Sy[3], Gy[3], Sz[3], Gz[3];
-                gimp_axis(st.o[0], g.lp, Sx, Gx);
-                gimp_axis(st.o[1], g.lp, Sy, Gy);
+                gimp_axis(st.o[0], g, Sx, Gx);
+                gimp_axis(st.o[1], g, Sy, Gy);
                 if (g.is3d) {
-                    gimp_axis(st.o[2], g.lp, Sz, Gz);
+                    gimp_axis(st.o[2], g, Sz, Gz);
                 } else {
                     Sz[0] = 1.f; Sz[1] = 0.f; Sz[2] = 0.f; Gz[0] = 0.f; Gz[1] = 0.f; Gz[2] = 0.f;
                 }

@@ -49,7 +49,7 @@ class Params(C.Structure):
 
 
 class Options(C.Structure):
-    _fields_ = [("sort_every", C.c_int), ("p2g_tile", C.c_int), ("block_particles", C.c_int),
+    _fields_ = [("sort_every", C.c_int), ("full_sort", C.c_int), ("reserved", C.c_int),
                 ("track_normals", C.c_int), ("check_finite", C.c_int), ("keep_node_fields", C.c_int)]
 
 
@@ -89,6 +89,7 @@ SIGNATURES = {
     "gy_get_particles_int": (C.c_int, [_vp, C.c_int, _ip, C.c_int64]),
     "gy_get_nodes": (C.c_int, [_vp, C.c_int, _dp, C.c_int64]),
     "gy_sort_keys": (C.c_int, [_ip, C.c_int64, _ip, C.c_int]),
+    "gy_resort_keys": (C.c_int, [_ip, _ip, C.c_int64, _ip, _ip, C.c_int]),
     "gy_state_size": (C.c_int, [_vp, _i64p]),
     "gy_state_save": (C.c_int, [_vp, C.c_void_p, C.c_int64]),
     "gy_state_load": (C.c_int, [_vp, C.c_void_p, C.c_int64]),
@@ -150,3 +151,17 @@ def sort_keys(keys) -> np.ndarray:
     out = np.empty(len(k), np.int32)
     check(load().gy_sort_keys(iptr(k), len(k), iptr(out), -1), None, "gy_sort_keys")
     return out
+
+
+def resort_keys(keys, prev_sorted):
+    """Incremental device re-sort (the step's sort after its first): keys[i] is the current
+    key of the particle whose key at the last sort was prev_sorted[i] (non-decreasing).
+    Returns (perm, sorted keys), equal to the stable sort of keys."""
+    k = np.ascontiguousarray(keys, np.int32)
+    p = np.ascontiguousarray(prev_sorted, np.int32)
+    if len(k) != len(p):
+        raise ValueError("keys and prev_sorted differ in length")
+    perm = np.empty(len(k), np.int32)
+    srt = np.empty(len(k), np.int32)
+    check(load().gy_resort_keys(iptr(k), iptr(p), len(k), iptr(perm), iptr(srt), -1), None, "gy_resort_keys")
+    return perm, srt

@@ -44,7 +44,7 @@ struct gy_solver {
     gy_params prm{};
     double dt = 0.0;
     bool initialized = false;
-    gy_options opt{1, 0, 256, 0, 0, 0};
+    gy_options opt{1, 0, 0, 0, 0, 0};
     std::vector<int> slot_obj;       // dense object slot -> objectID
     bool multi = false, has_dp = false;
     int nbody = 1;
@@ -59,6 +59,11 @@ struct gy_solver {
     int g2p_grid = 1;
     SortScratch ws{};
     void *sort_mem = nullptr;
+    ResortScratch rs{};
+    void *resort_mem = nullptr;
+    int *skey_buf[2] = {nullptr, nullptr};  // sorted keys of the last sort and its successor
+    int sk = 0;
+    bool resort_valid = false;              // slab order = order of the sort in skey_buf[sk]
     float4 *d_pbc_val = nullptr;
     int *d_refkey0 = nullptr;
     DevMaterial *d_mats = nullptr;
@@ -114,7 +119,7 @@ PView pview(gy_solver *h, int which) { return PView{h->slab[which], h->cap}; }
 
 void free_device(gy_solver *h)
 {
-    void *ptrs[] = {h->slab[0], h->slab[1], h->d_perm, h->d_seg, h->d_nseg, h->sort_mem, h->d_pbc_val,
+    void *ptrs[] = {h->slab[0], h->slab[1], h->d_perm, h->d_seg, h->d_nseg, h->sort_mem, h->resort_mem, h->d_pbc_val,
                     h->d_refkey0, h->d_mats, h->d_status, h->d_stats, h->node_mem, h->d_cell_min,
                     h->d_nidx[0], h->d_nidx[1], h->d_nidx[2]};
     for (void *p : ptrs)
@@ -122,6 +127,8 @@ void free_device(gy_solver *h)
     h->slab[0] = h->slab[1] = nullptr;
     h->d_perm = h->d_seg = h->d_nseg = nullptr;
     h->sort_mem = nullptr;
+    h->resort_mem = nullptr;
+    h->skey_buf[0] = h->skey_buf[1] = nullptr;
     h->d_pbc_val = nullptr;
     h->d_refkey0 = nullptr;
     h->d_mats = nullptr;
@@ -590,6 +597,18 @@ gy_status gy_initialize(gy_solver *h, const gy_material *mats, int nmat, const g
         h->ws.cap = h->cap;
         h->ws.nblocks_cap = (int)nbk;
     }
+    // incremental re-sort scratch and the two sorted-key buffers, zeroed once
+    {
+        const size_t rints = resort_scratch_ints(h->cap) + 2 * (size_t)h->cap;
+        CK(h, cudaMalloc(&h->resort_mem, rints * sizeof(int) + 4096));
+        CK(h, cudaMemsetAsync(h->resort_mem, 0, rints * sizeof(int) + 4096, h->stream));
+        int *p = (int *)h->resort_mem;
+        h->skey_buf[0] = p; p += h->cap;
+        h->skey_buf[1] = p; p += h->cap;
+        resort_bind(h->rs, p, h->cap);
+        h->sk = 0;
+        h->resort_valid = false;
+    }
     if ((st = dalloc(h, &h->d_perm, h->cap))) return st;
     if ((st = dalloc(h, &h->d_seg, h->cap))) return st;
     if ((st = dalloc(h, &h->d_nseg, 4))) return st;
@@ -607,6 +626,7 @@ gy_status gy_initialize(gy_solver *h, const gy_material *mats, int nmat, const g
     h->t_prev = 0.0;
     h->since_sort = 1 << 30;
     h->tables_valid = false;
+    h->resort_valid = false;
     return GY_OK;
 }
 
@@ -636,6 +656,7 @@ gy_status gy_set_options(gy_solver *h, const gy_options *opt)
 {
     if (!h || !opt) return GY_ERR_ARG;
     if (opt->sort_every < 1) return fail(h, GY_ERR_ARG, "sort_every must be >= 1");
+    if (opt->reserved != 0) return fail(h, GY_ERR_ARG, "gy_options.reserved must be 0");
     if (h->initialized && (opt->track_normals != h->opt.track_normals || opt->keep_node_fields != h->opt.keep_node_fields))
         return fail(h, GY_ERR_STATE, "track_normals / keep_node_fields must be set before gy_initialize");
     h->opt = *opt;
@@ -693,12 +714,23 @@ static gy_status enqueue_step(gy_solver *h, double t, int step)
     const int *perm = nullptr;
     const int *skey = reinterpret_cast<const int *>(h->slab[h->cur]) + (size_t)PF_KEY * h->cap;
     if (h->since_sort >= h->opt.sort_every) {
+        int *out = h->skey_buf[h->sk ^ 1];
         int key_bits = 1;
         const long long maxkey = (long long)h->g.nbx * h->g.nby * h->g.nbz * 64;
         while ((1LL << key_bits) < maxkey) key_bits++;
-        skey = sort_pairs(skey, h->d_perm, h->n, key_bits, h->ws, s);
+        if (h->resort_valid && !h->opt.full_sort) {
+            // the slab is in the order of the last sort: re-sort only the particles that moved
+            resort_keys(skey, h->skey_buf[h->sk], out, h->d_perm, h->n, key_bits, h->rs, s);
+        } else {
+            const int *sorted = sort_pairs(skey, h->d_perm, h->n, key_bits, h->ws, s);
+            if (h->n > 0 && sorted != out)
+                cudaMemcpyAsync(out, sorted, (size_t)h->n * sizeof(int), cudaMemcpyDeviceToDevice, s);
+        }
+        h->sk ^= 1;
+        skey = out;
         perm = h->d_perm;
         h->since_sort = 0;
+        h->resort_valid = true;  // this step's G2P writes the slab in this order
     }
     h->since_sort++;
     launch_block_heads(skey, h->n, h->d_seg, h->d_nseg, s);
@@ -1093,6 +1125,7 @@ gy_status gy_state_load(gy_solver *h, const void *buf, int64_t bytes)
     h->dt = hd.dt;
     h->tables_valid = hd.tables_valid != 0;
     h->since_sort = 1 << 30;
+    h->resort_valid = false;
     return GY_OK;
 }
 
@@ -1134,6 +1167,46 @@ gy_status gy_sort_keys(const int *keys, int64_t n, int *perm_out, int device)
     }
     if (d_in) cudaFree(d_in);
     if (d_perm) cudaFree(d_perm);
+    if (mem) cudaFree(mem);
+    cudaStreamDestroy(s);
+    return st;
+}
+
+
+gy_status gy_resort_keys(const int *keys, const int *prev_sorted, int64_t n, int *perm_out, int *sorted_out,
+                         int device)
+{
+    if (n < 0 || (n > 0 && (!keys || !prev_sorted || !perm_out || !sorted_out))) return GY_ERR_ARG;
+    if (n == 0) return GY_OK;
+    if (n >= (1LL << 31) - 2) return GY_ERR_ARG;
+    int maxk = 0;
+    for (int64_t i = 0; i < n; i++) {
+        if (keys[i] < 0 || prev_sorted[i] < 0) return GY_ERR_ARG;
+        if (i > 0 && prev_sorted[i] < prev_sorted[i - 1]) return GY_ERR_ARG;
+        maxk = std::max(maxk, keys[i]);
+    }
+    int bits = 1;
+    while ((1LL << bits) <= maxk) bits++;
+    if (device >= 0 && cudaSetDevice(device) != cudaSuccess) return GY_ERR_CUDA;
+    cudaStream_t s;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return GY_ERR_CUDA;
+    int *mem = nullptr;
+    gy_status st = GY_OK;
+    const size_t rints = resort_scratch_ints(n) + 4 * (size_t)n;
+    if (cudaMalloc(&mem, rints * sizeof(int) + 4096) != cudaSuccess) {
+        st = GY_ERR_NOMEM;
+    } else {
+        int *d_key = mem, *d_prev = mem + n, *d_perm = mem + 2 * n, *d_sorted = mem + 3 * n;
+        ResortScratch rs{};
+        cudaMemsetAsync(mem + 4 * n, 0, (rints - 4 * (size_t)n) * sizeof(int) + 4096, s);
+        resort_bind(rs, mem + 4 * n, n);
+        cudaMemcpyAsync(d_key, keys, n * sizeof(int), cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(d_prev, prev_sorted, n * sizeof(int), cudaMemcpyHostToDevice, s);
+        resort_keys(d_key, d_prev, d_sorted, d_perm, n, bits, rs, s);
+        cudaMemcpyAsync(perm_out, d_perm, n * sizeof(int), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(sorted_out, d_sorted, n * sizeof(int), cudaMemcpyDeviceToHost, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) st = GY_ERR_CUDA;
+    }
     if (mem) cudaFree(mem);
     cudaStreamDestroy(s);
     return st;

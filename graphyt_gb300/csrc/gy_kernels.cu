@@ -159,7 +159,10 @@ __device__ __forceinline__ void make_stencil(const PState &st, const GridGeom &g
 constexpr int PT = 6;                   // tile edge in nodes
 constexpr int PT_NODES = PT * PT * PT;  // 216
 constexpr int P2G_FIELDS = 7;           // m, px, py, pz, fx, fy, fz
-constexpr int P2G_CH = 256;             // particles per chunk = threads per CTA
+#ifndef GY_P2G_CH
+#define GY_P2G_CH 128
+#endif
+constexpr int P2G_CH = GY_P2G_CH;       // particles per chunk = threads per CTA
 constexpr int P2G_NP = P2G_CH / 2 + 1;  // pairs per staged row; the odd row length (in float4)
                                         // puts the three rows one load reads in different banks
 
@@ -1072,9 +1075,12 @@ __global__ void __launch_bounds__(256, 3) k_g2p_update(PView src, PView dst, con
     }
 }
 
-// resident CTAs per SM the G2P kernel is register-limited to (64 registers at 4)
+// G2P CTA size and the resident CTAs per SM it is register-limited to (64 registers)
 #ifndef GY_G2P_MINB
-#define GY_G2P_MINB 4
+#define GY_G2P_MINB 8
+#endif
+#ifndef GY_G2P_THREADS
+#define GY_G2P_THREADS 128
 #endif
 
 // 4-byte asynchronous global -> shared copy (no register holds the value in flight)
@@ -1103,14 +1109,14 @@ constexpr int G2P_NBASE = 19, G2P_NDP = 9;
 // per particle in sorted order.  The G2P sums are separable per axis: for every (j, k) node
 // row the three x nodes are contracted first, then weighted by the y/z factors.
 template <bool HAS_DP>
-__global__ void __launch_bounds__(256, GY_G2P_MINB) k_g2p_tiled(PView src, PView dst, const int *perm, const int *skey,
+__global__ void __launch_bounds__(GY_G2P_THREADS, GY_G2P_MINB) k_g2p_tiled(PView src, PView dst, const int *perm, const int *skey,
                                                       long long n, const int *seg_start, const int *nseg_ptr,
                                                       int sorted, NodeBufs nb, StepArgs a, int check_finite)
 {
     constexpr int NST = G2P_NBASE + (HAS_DP ? G2P_NDP : 0);
     __shared__ float4 TV[PT_NODES];  // (v1x, v1y, v1z, a1z), zero for massless nodes
     __shared__ float2 TA[PT_NODES];  // (a1x, a1y)
-    __shared__ float stage[NST][256];
+    __shared__ float stage[NST][GY_G2P_THREADS];
     __shared__ long long s_end;
     const GridGeom &g = a.g;
     const int nseg = *nseg_ptr;
@@ -1257,8 +1263,8 @@ __global__ void __launch_bounds__(256, GY_G2P_MINB) k_g2p_tiled(PView src, PView
 int g2p_blocks_per_sm(bool has_dp)
 {
     int b = 0;
-    if (has_dp) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_g2p_tiled<true>, 256, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_g2p_tiled<false>, 256, 0);
+    if (has_dp) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_g2p_tiled<true>, GY_G2P_THREADS, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_g2p_tiled<false>, GY_G2P_THREADS, 0);
     return b > 0 ? b : 1;
 }
 
@@ -1274,8 +1280,10 @@ void launch_g2p_update(const PView &src, const PView &dst, const int *perm, cons
         else k_g2p_update<true, false><<<grid, 256, 0, s>>>(src, dst, perm, n, nb, a, tn, cf);
     } else {
         const int srt = perm ? 1 : 0;
-        if (has_dp) k_g2p_tiled<true><<<g2p_grid, 256, 0, s>>>(src, dst, perm, skey, n, seg_start, nseg, srt, nb, a, cf);
-        else k_g2p_tiled<false><<<g2p_grid, 256, 0, s>>>(src, dst, perm, skey, n, seg_start, nseg, srt, nb, a, cf);
+        if (has_dp)
+            k_g2p_tiled<true><<<g2p_grid, GY_G2P_THREADS, 0, s>>>(src, dst, perm, skey, n, seg_start, nseg, srt, nb, a, cf);
+        else
+            k_g2p_tiled<false><<<g2p_grid, GY_G2P_THREADS, 0, s>>>(src, dst, perm, skey, n, seg_start, nseg, srt, nb, a, cf);
     }
     note_launch(1);
 }

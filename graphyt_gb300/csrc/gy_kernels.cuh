@@ -77,6 +77,20 @@ struct SortScratch {
     int nblocks_cap;
 };
 size_t sort_scratch_bytes(long long n);
+
+// Incremental re-sort (gy_resort.cu): scratch, zeroed once at allocation.
+struct ResortScratch {
+    unsigned *wmask;
+    int *wcnt, *wpref, *wscan_tmp;
+    int *bkey, *bidx, *tkey, *tidx, *gap;
+    int *gapcnt, *gwcnt, *gwpref, *gscan_tmp;
+    int *hist, *hscan_tmp;
+    long long cap, ngw;
+};
+size_t resort_scratch_ints(long long cap);
+void resort_bind(ResortScratch &rs, int *mem, long long cap);
+void resort_keys(const int *key, const int *prev_skey, int *skey_out, int *perm_out, long long n, int key_bits,
+                 ResortScratch &rs, cudaStream_t s);
 const int *sort_pairs(const int *keys_in, int *perm_out, long long n, int key_bits, SortScratch &ws, cudaStream_t s);
 void launch_block_heads(const int *skey, long long n, int *seg_start, int *nseg, cudaStream_t s);
 void exclusive_scan_int(const int *in, int *out, long long n, int *tmp, cudaStream_t s);

@@ -1,0 +1,322 @@
+// gy_resort.cu -- incremental stable re-sort of the particle cell keys.
+//
+// After a sorted step the slab holds the particles in the order of that sort, and only the
+// particles that changed cell since ("movers") break it: the others ("stayers") still have
+// the key stored at their slot in the previous sorted key array, which is non-decreasing, so
+// they form a sorted run by (key, slot).  The stable order of the new keys is the merge of
+// the stayers with the movers sorted by (key, slot):
+//   * the movers, compacted in slot order, are sorted stably by key (a radix sort whose
+//     length lives on the device, so the host never waits for it); mover q of that order
+//     lands at q + g(q), g = the stayers below it -- one binary search on the previous keys;
+//   * stayer r (r-th stayer in slot order) lands at r + (movers with g <= r).
+// The result is the permutation the full stable radix sort produces, at a fraction of its
+// traffic when few particles move; the full sort runs whenever the previous order is not
+// known (first step, restored state).
+#include <algorithm>
+
+#include "gy_kernels.cuh"
+
+namespace gy {
+
+constexpr int RS_THREADS = 256;
+constexpr int RS_ITEMS = 8;                          // per thread in the mover sort
+constexpr int RS_TILE = RS_THREADS * RS_ITEMS;       // 2048
+constexpr int RS_WARPS = RS_THREADS / 32;
+constexpr int RS_RADIX = 256;
+constexpr int RS_MAX_CTAS = 1024;                    // mover-sort CTAs (2 per SM)
+
+__device__ __forceinline__ long long movers_before(long long P, const unsigned *wmask, const int *wpref)
+{
+    const long long w = P >> 5;
+    const int b = (int)(P & 31);
+    return (long long)wpref[w] + (b ? __popc(wmask[w] & ((1u << b) - 1u)) : 0);
+}
+
+// one warp per 32 slots: mover mask and count
+__global__ void __launch_bounds__(RS_THREADS) k_rs_mask(const int *key, const int *prev, long long n, unsigned *wmask,
+                                                          int *wcnt, long long nw)
+{
+    const int lane = threadIdx.x & 31;
+    const long long wstride = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nw; w += wstride) {
+        const long long i = w * 32 + lane;
+        const bool f = i < n && key[i] != prev[i];
+        const unsigned m = __ballot_sync(0xffffffffu, f);
+        if (lane == 0) {
+            wmask[w] = m;
+            wcnt[w] = __popc(m);
+        }
+    }
+}
+
+// movers (key, slot) in slot order
+__global__ void __launch_bounds__(RS_THREADS) k_rs_compact(const int *key, const unsigned *wmask, const int *wpref,
+                                                             long long nw, int *bkey, int *bidx)
+{
+    const int lane = threadIdx.x & 31;
+    const long long wstride = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nw; w += wstride) {
+        const unsigned m = wmask[w];
+        if (!((m >> lane) & 1u)) continue;
+        const long long i = w * 32 + lane;
+        const int pos = wpref[w] + __popc(m & ((1u << lane) - 1u));
+        bkey[pos] = key[i];
+        bidx[pos] = (int)i;
+    }
+}
+
+// ---- stable LSD radix sort of the m movers, m read on the device ----------------------
+// CTA c of the G owns the contiguous range [m c / G, m (c+1) / G) and walks it in tiles of
+// RS_TILE; ranks inside a tile follow k_radix_scatter (warps in order, peers by
+// __match_any_sync), and per-digit bases carry from tile to tile.
+
+__device__ __forceinline__ void cta_range(int m, int &c0, int &c1)
+{
+    c0 = (int)((long long)m * blockIdx.x / gridDim.x);
+    c1 = (int)((long long)m * (blockIdx.x + 1) / gridDim.x);
+}
+
+__global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const int *keys, const int *m_ptr, int shift, int *hist)
+{
+    __shared__ int cnt[RS_RADIX];
+    for (int d = threadIdx.x; d < RS_RADIX; d += RS_THREADS) cnt[d] = 0;
+    __syncthreads();
+    int c0, c1;
+    cta_range(*m_ptr, c0, c1);
+    for (int e = c0 + threadIdx.x; e < c1; e += RS_THREADS) atomicAdd(&cnt[(keys[e] >> shift) & 0xFF], 1);
+    __syncthreads();
+    for (int d = threadIdx.x; d < RS_RADIX; d += RS_THREADS) hist[d * gridDim.x + blockIdx.x] = cnt[d];
+}
+
+__global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const int *keys_in, const int *vals_in, int *keys_out,
+                                                             int *vals_out, const int *m_ptr, int shift,
+                                                             const int *offsets)
+{
+    __shared__ int wcnt[RS_WARPS][RS_RADIX];  // per-warp digit counts, then per-warp bases
+    __shared__ int base[RS_RADIX];            // running per-digit base of this CTA
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    for (int d = threadIdx.x; d < RS_RADIX; d += RS_THREADS) base[d] = offsets[d * gridDim.x + blockIdx.x];
+    int c0, c1;
+    cta_range(*m_ptr, c0, c1);
+    for (int t0 = c0; t0 < c1; t0 += RS_TILE) {
+        for (int d = lane; d < RS_RADIX; d += 32) wcnt[warp][d] = 0;
+        __syncthreads();  // the bases of the previous tile are final; the counters are clear
+        const int wb = t0 + warp * (32 * RS_ITEMS);
+        int key[RS_ITEMS], val[RS_ITEMS], rnk[RS_ITEMS];
+        for (int r = 0; r < RS_ITEMS; r++) {
+            const int e = wb + r * 32 + lane;
+            const bool ok = e < c1;
+            key[r] = ok ? keys_in[e] : 0;
+            val[r] = ok ? vals_in[e] : 0;
+            const int d = ok ? ((key[r] >> shift) & 0xFF) : RS_RADIX;
+            const unsigned peers = __match_any_sync(0xffffffffu, d);
+            const int before = __popc(peers & lt);
+            int bc = 0;
+            if (ok) bc = wcnt[warp][d];
+            __syncwarp();
+            rnk[r] = bc + before;
+            if (ok && before == 0) wcnt[warp][d] = bc + __popc(peers);
+            __syncwarp();
+        }
+        __syncthreads();
+        for (int d = threadIdx.x; d < RS_RADIX; d += RS_THREADS) {
+            int run = base[d];
+            for (int w = 0; w < RS_WARPS; w++) {
+                const int c = wcnt[w][d];
+                wcnt[w][d] = run;
+                run += c;
+            }
+            base[d] = run;
+        }
+        __syncthreads();
+        for (int r = 0; r < RS_ITEMS; r++) {
+            const int e = wb + r * 32 + lane;
+            if (e < c1) {
+                const int d = (key[r] >> shift) & 0xFF;
+                const int pos = wcnt[warp][d] + rnk[r];
+                keys_out[pos] = key[r];
+                vals_out[pos] = val[r];
+            }
+        }
+        __syncthreads();  // wcnt is reused by the next tile
+    }
+}
+
+// ---- placement ----------------------------------------------------------------------
+
+// mover q of the sorted order: stayers below it (gap g), placed at q + g; gaps counted
+__global__ void __launch_bounds__(RS_THREADS) k_rs_place_movers(const int *prev, long long n, const unsigned *wmask,
+                                                                  const int *wpref, long long nw, const int *skey,
+                                                                  const int *sidx, int *gap, int *gapcnt, int *gwcnt,
+                                                                  int *skey_out, int *perm_out)
+{
+    const int m = wpref[nw];
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < m; q += gridDim.x * blockDim.x) {
+        const int k = skey[q], i = sidx[q];
+        // first slot s with (prev[s], s) >= (k, i): a mover's new key is usually near its
+        // old one, so gallop out from its old slot i before bisecting (cache-near probes)
+        long long lo, hi;
+        if (prev[i] < k) {  // the answer lies above i
+            long long step = 1;
+            lo = i + 1;
+            hi = i + 1;
+            while (hi < n && prev[hi] <= k && (prev[hi] < k || hi < i)) {
+                lo = hi + 1;
+                hi = i + 1 + step;
+                step <<= 1;
+            }
+            if (hi > n) hi = n;
+        } else {  // prev[i] >= k: the answer is at or below i
+            long long step = 1;
+            hi = i;
+            lo = i;
+            while (lo > 0 && (prev[lo - 1] > k || (prev[lo - 1] == k && lo - 1 >= i))) {
+                hi = lo - 1;
+                lo = (i - step > 0) ? i - step : 0;
+                step <<= 1;
+            }
+        }
+        while (lo < hi) {
+            const long long mid = (lo + hi) >> 1;
+            const int pk = prev[mid];
+            if (pk > k || (pk == k && mid >= i)) hi = mid;
+            else lo = mid + 1;
+        }
+        const int g = (int)(lo - movers_before(lo, wmask, wpref));
+        gap[q] = g;
+        atomicAdd(&gapcnt[g], 1);
+        atomicAdd(&gwcnt[g >> 5], 1);
+        const long long pos = (long long)q + g;
+        skey_out[pos] = k;
+        perm_out[pos] = i;
+    }
+}
+
+// stayer r lands at r + (movers with gap <= r).  The stayer ranks of one warp's 32 slots lie
+// in at most two consecutive 32-gap words, whose counts the warp loads and prefix-sums.
+__global__ void __launch_bounds__(RS_THREADS) k_rs_place_stayers(const int *key, long long n, const unsigned *wmask,
+                                                                   const int *wpref, long long nw, const int *gapcnt,
+                                                                   const int *gwcnt, const int *gwpref, int *skey_out,
+                                                                   int *perm_out)
+{
+    const int lane = threadIdx.x & 31;
+    const long long wstride = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nw; w += wstride) {
+        const long long i = w * 32 + lane;
+        const unsigned m = wmask[w];
+        const long long rbase = w * 32 - wpref[w];  // rank of the warp's first stayer
+        const long long gw0 = rbase >> 5;
+        int c0 = 0, c1 = 0;
+        if (gwcnt[gw0] | gwcnt[gw0 + 1]) {  // movers in these gaps: per-gap counts, prefix-summed
+            c0 = gapcnt[gw0 * 32 + lane];
+            c1 = gapcnt[gw0 * 32 + 32 + lane];
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const int y0 = __shfl_up_sync(0xffffffffu, c0, off), y1 = __shfl_up_sync(0xffffffffu, c1, off);
+                if (lane >= off) {
+                    c0 += y0;
+                    c1 += y1;
+                }
+            }
+        }
+        const int tot0 = __shfl_sync(0xffffffffu, c0, 31);
+        const bool stay = i < n && !((m >> lane) & 1u);
+        const long long r = rbase + lane - __popc(m & ((1u << lane) - 1u));
+        const int rr = (int)(r - gw0 * 32);  // 0..62 for a stayer
+        const int in0 = __shfl_sync(0xffffffffu, c0, rr & 31), in1 = __shfl_sync(0xffffffffu, c1, rr & 31);
+        if (!stay) continue;
+        const long long pos = r + gwpref[gw0] + (rr < 32 ? in0 : tot0 + in1);
+        skey_out[pos] = key[i];
+        perm_out[pos] = (int)i;
+    }
+}
+
+// leave the gap counters zero for the next call
+__global__ void __launch_bounds__(RS_THREADS) k_rs_clear(const int *gap, const int *wpref, long long nw, int *gapcnt,
+                                                           int *gwcnt)
+{
+    const int m = wpref[nw];
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < m; q += gridDim.x * blockDim.x) {
+        gapcnt[gap[q]] = 0;
+        gwcnt[gap[q] >> 5] = 0;
+    }
+}
+
+// ---- scratch and driver ---------------------------------------------------------------
+
+size_t resort_scratch_ints(long long cap)
+{
+    const long long nw = (cap + 31) / 32;
+    const long long ngw = (cap + 2 + 63) / 32 + 2;  // 32-gap words, one spare word past the end
+    const long long hist = (long long)RS_RADIX * RS_MAX_CTAS;
+    return (size_t)(3 * (nw + 1) + scan_tmp_ints(nw + 1) + 5 * cap + ngw * 32 + 2 * (ngw + 1) +
+                    scan_tmp_ints(ngw + 1) + 2 * hist + scan_tmp_ints(hist) + 64);
+}
+
+void resort_bind(ResortScratch &rs, int *mem, long long cap)
+{
+    const long long nw = (cap + 31) / 32;
+    const long long ngw = (cap + 2 + 63) / 32 + 2;
+    const long long hist = (long long)RS_RADIX * RS_MAX_CTAS;
+    int *p = mem;
+    rs.wmask = reinterpret_cast<unsigned *>(p); p += nw + 1;
+    rs.wcnt = p; p += nw + 1;
+    rs.wpref = p; p += nw + 1;
+    rs.wscan_tmp = p; p += scan_tmp_ints(nw + 1);
+    rs.bkey = p; p += cap;
+    rs.bidx = p; p += cap;
+    rs.tkey = p; p += cap;
+    rs.tidx = p; p += cap;
+    rs.gap = p; p += cap;
+    rs.gapcnt = p; p += ngw * 32;
+    rs.gwcnt = p; p += ngw + 1;
+    rs.gwpref = p; p += ngw + 1;
+    rs.gscan_tmp = p; p += scan_tmp_ints(ngw + 1);
+    rs.hist = p; p += 2 * hist;
+    rs.hscan_tmp = p;
+    rs.cap = cap;
+    rs.ngw = ngw;
+}
+
+// gapcnt, gwcnt and wcnt[nw] must be zero on entry (the memory is zeroed once); they are
+// left zero on return.
+void resort_keys(const int *key, const int *prev_skey, int *skey_out, int *perm_out, long long n, int key_bits,
+                 ResortScratch &rs, cudaStream_t s)
+{
+    if (n <= 0) return;
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long nw = (n + 31) / 32;
+    const unsigned wgrid = (unsigned)std::min<long long>((nw + RS_WARPS - 1) / RS_WARPS, (long long)sms * 16);
+    const unsigned qgrid = (unsigned)std::min<long long>((n + RS_THREADS - 1) / RS_THREADS, (long long)sms * 8);
+    k_rs_mask<<<wgrid, RS_THREADS, 0, s>>>(key, prev_skey, n, rs.wmask, rs.wcnt, nw);
+    cudaMemsetAsync(rs.wcnt + nw, 0, sizeof(int), s);
+    exclusive_scan_int(rs.wcnt, rs.wpref, nw + 1, rs.wscan_tmp, s);
+    k_rs_compact<<<wgrid, RS_THREADS, 0, s>>>(key, rs.wmask, rs.wpref, nw, rs.bkey, rs.bidx);
+    note_launch(2);
+    // stable sort of the movers by key; their count is wpref[nw]
+    const int G = std::min(2 * sms, RS_MAX_CTAS);
+    const long long hist = (long long)RS_RADIX * RS_MAX_CTAS;
+    const int *m_ptr = rs.wpref + nw;
+    int *kin = rs.bkey, *vin = rs.bidx, *kout = rs.tkey, *vout = rs.tidx;
+    const int passes = std::max(1, (key_bits + 7) / 8);
+    for (int p = 0; p < passes; p++) {
+        k_rs_hist<<<G, RS_THREADS, 0, s>>>(kin, m_ptr, 8 * p, rs.hist);
+        exclusive_scan_int(rs.hist, rs.hist + hist, (long long)RS_RADIX * G, rs.hscan_tmp, s);
+        k_rs_scatter<<<G, RS_THREADS, 0, s>>>(kin, vin, kout, vout, m_ptr, 8 * p, rs.hist + hist);
+        note_launch(2);
+        std::swap(kin, kout);
+        std::swap(vin, vout);
+    }
+    k_rs_place_movers<<<qgrid, RS_THREADS, 0, s>>>(prev_skey, n, rs.wmask, rs.wpref, nw, kin, vin, rs.gap, rs.gapcnt,
+                                                   rs.gwcnt, skey_out, perm_out);
+    exclusive_scan_int(rs.gwcnt, rs.gwpref, rs.ngw + 1, rs.gscan_tmp, s);
+    k_rs_place_stayers<<<wgrid, RS_THREADS, 0, s>>>(key, n, rs.wmask, rs.wpref, nw, rs.gapcnt, rs.gwcnt, rs.gwpref,
+                                                    skey_out, perm_out);
+    k_rs_clear<<<qgrid, RS_THREADS, 0, s>>>(rs.gap, rs.wpref, nw, rs.gapcnt, rs.gwcnt);
+    note_launch(3);
+}
+
+}  // namespace gy

@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define GY_ABI_VERSION 1
+#define GY_ABI_VERSION 2
 
 typedef int gy_status;
 enum {
@@ -75,8 +75,9 @@ typedef struct gy_params {
 /* Tuning knobs that change speed, never results beyond summation order. */
 typedef struct gy_options {
     int sort_every;     /* reorder particle state by cell every n steps (>= 1) */
-    int p2g_tile;       /* 1: shared-memory node tiles in P2G; 0: direct global atomics */
-    int block_particles;/* particles per CTA in the particle kernels (64..1024) */
+    int full_sort;      /* 1: every sort is a full radix sort; 0: after the first, an incremental
+                           re-sort of the particles that changed cell (same permutation) */
+    int reserved;       /* must be 0 */
     int track_normals;  /* 1: keep per-particle contact normals (getNormalsArr) */
     int check_finite;   /* 1: flag NaN/Inf in particle state every step */
     int keep_node_fields; /* 1: keep centre-of-mass node velocity/force for node getters */
@@ -186,6 +187,14 @@ gy_status gy_get_nodes(gy_solver *h, int field, double *out, int64_t count);
  * perm_out[i] = index of the i-th key in ascending order, ties in input order.  Host
  * arrays; for testing the sort against a CPU stable sort. */
 gy_status gy_sort_keys(const int *keys, int64_t n, int *perm_out, int device);
+
+/* The incremental re-sort the step uses after its first sort (no counterpart in the
+ * reference, whose Extrapolation.cpp:370-503 sorts from scratch).  prev_sorted[i] is the key
+ * particle i had at the last sort, in that sort's order (non-decreasing); keys[i] is its key
+ * now.  Result: the stable ascending order of keys, equal to gy_sort_keys(keys).  Host arrays;
+ * GY_ERR_ARG if prev_sorted is not non-decreasing or a key is negative. */
+gy_status gy_resort_keys(const int *keys, const int *prev_sorted, int64_t n, int *perm_out, int *sorted_out,
+                         int device);
 
 /* Checkpoint / resume of the device state.  The reference has no checkpoint: its only
  * output, Serialise (MaterialPoints.cpp:341-364), writes lossy %f CSV with no reader.

@@ -40,6 +40,58 @@ def test_sort_presorted_and_reversed(gpu_lib):
     assert np.array_equal(_lib.sort_keys(rev), np.argsort(rev, kind="stable"))
 
 
+# ---- the incremental re-sort: the same permutation as the full stable sort --------------
+@pytest.mark.parametrize("n", [1, 2, 31, 32, 33, 2049, 100_003, 1_000_000])
+@pytest.mark.parametrize("frac", [0.0, 0.001, 0.1, 1.0])
+def test_resort_matches_full_stable_sort(gpu_lib, n, frac):
+    """Previous sorted keys (with long runs of equal keys, like cells), a fraction of the
+    particles moved to nearby or arbitrary keys: the re-sort returns the stable order."""
+    from graphyt_gb300 import _lib
+    rng = np.random.default_rng(n + int(frac * 1000))
+    prev = np.sort(rng.integers(0, max(2, n // 8), n)).astype(np.int32)
+    keys = prev.copy()
+    mv = rng.random(n) < frac
+    near = prev[mv] + rng.integers(-70, 71, mv.sum())
+    far = rng.integers(0, max(2, n // 8) + 100, mv.sum())
+    keys[mv] = np.where(rng.random(mv.sum()) < 0.8, np.maximum(near, 0), far).astype(np.int32)
+    perm, srt = _lib.resort_keys(keys, prev)
+    want = np.argsort(keys, kind="stable")
+    assert np.array_equal(perm, want)
+    assert np.array_equal(srt, keys[want])
+
+
+def test_resort_edge_cases(gpu_lib):
+    from graphyt_gb300 import _lib
+    # every key equal; all moved onto one key; movers tied with stayers on both sides
+    for prev, keys in [(np.zeros(100, np.int32), np.zeros(100, np.int32)),
+                       (np.arange(100, dtype=np.int32), np.full(100, 7, np.int32)),
+                       (np.repeat(np.arange(10, dtype=np.int32), 10), np.repeat(np.arange(10, dtype=np.int32), 10)[::-1].copy())]:
+        perm, srt = _lib.resort_keys(keys, prev)
+        assert np.array_equal(perm, np.argsort(keys, kind="stable"))
+    with pytest.raises(_lib.GraphytGPUError):
+        _lib.resort_keys(np.zeros(4, np.int32), np.array([0, 2, 1, 3], np.int32))
+
+
+def test_incremental_resort_gives_the_full_sort_trajectory(gpu_lib):
+    """The step's incremental re-sort produces the full sort's order: particles sit in the
+    same device slots as in a run that sorts from scratch every step, and the state agrees
+    to FP32 summation noise (the shared-memory and global reductions add in run-dependent
+    order, so two runs are not bit-identical even with the same sort)."""
+    sc = scenes.dam_break(scale=0.125)
+    rng = np.random.default_rng(5)
+    # a fast, uneven drift so that a varying share of particles changes cell every step
+    sc.vel[:, 0] = 30.0 + rng.normal(0.0, 4.0, len(sc.vel))
+    sc.vel[:, 1] = rng.normal(0.0, 4.0, len(sc.vel))
+    a = run_gpu(sc, 15, options=dict(full_sort=1))
+    b = run_gpu(sc, 15, options=dict(full_sort=0))
+    moved = run_gpu(sc, 0)._get_particles_int("cellid") != b._get_particles_int("cellid")
+    assert moved.mean() > 0.5
+    slot_a, slot_b = a._get_particles_int("device_slot"), b._get_particles_int("device_slot")
+    assert np.mean(slot_a != slot_b) < 1e-4
+    for f in ("pos", "vel", "stress"):
+        assert rel_l2(a._get_particles(f), b._get_particles(f)) < 1e-5, f
+
+
 # ---- one step and many steps against the oracle -----------------------------------------
 ONE_STEP_CASES = {
     "tiny_elastic": lambda: scenes.tiny_block(model=1),

@@ -49,7 +49,7 @@ class Params(C.Structure):
 
 
 class Options(C.Structure):
-    _fields_ = [("sort_every", C.c_int), ("full_sort", C.c_int), ("reserved", C.c_int),
+    _fields_ = [("sort_every", C.c_int), ("full_sort", C.c_int), ("use_graph", C.c_int),
                 ("track_normals", C.c_int), ("check_finite", C.c_int), ("keep_node_fields", C.c_int)]
 
 

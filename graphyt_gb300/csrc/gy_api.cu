@@ -16,6 +16,26 @@
 
 using namespace gy;
 
+// Everything a step enqueues is fixed by this variant; the per-step scalars live in device
+// memory, so one captured graph per variant replays any step of that variant.
+struct StepVariant {
+    int cur;       // slab read this step
+    int sk;        // sorted-key buffer written by this step's sort (the other one is read)
+    int sort;      // 0 none, 1 incremental, 2 full
+    int tables;    // 0 none, 1 rebuild body tables, 2 rebuild from the initial keys
+    bool operator==(const StepVariant &o) const
+    {
+        return cur == o.cur && sk == o.sk && sort == o.sort && tables == o.tables;
+    }
+};
+
+struct StepGraph {
+    StepVariant v;
+    cudaGraphExec_t exec;
+    long long launches;  // kernels in the graph
+};
+
+
 struct gy_solver {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -44,7 +64,7 @@ struct gy_solver {
     gy_params prm{};
     double dt = 0.0;
     bool initialized = false;
-    gy_options opt{1, 0, 0, 0, 0, 0};
+    gy_options opt{1, 0, 1, 0, 0, 0};
     std::vector<int> slot_obj;       // dense object slot -> objectID
     bool multi = false, has_dp = false;
     int nbody = 1;
@@ -64,6 +84,13 @@ struct gy_solver {
     int *skey_buf[2] = {nullptr, nullptr};  // sorted keys of the last sort and its successor
     int sk = 0;
     bool resort_valid = false;              // slab order = order of the sort in skey_buf[sk]
+    StepScalars *d_sc = nullptr;            // this step's scalars (device)
+    static constexpr int kRing = 32;        // pinned staging slots for the per-step scalars
+    StepScalars *h_ring = nullptr;
+    cudaEvent_t ring_ev[kRing] = {};
+    bool ring_busy[kRing] = {};
+    long long ring_pos = 0;
+    std::vector<StepGraph> graphs;          // captured steps, one per StepVariant
     float4 *d_pbc_val = nullptr;
     int *d_refkey0 = nullptr;
     DevMaterial *d_mats = nullptr;
@@ -117,13 +144,29 @@ template <class T> gy_status dalloc(gy_solver *h, T **p, size_t count)
 
 PView pview(gy_solver *h, int which) { return PView{h->slab[which], h->cap}; }
 
+void drop_graphs(gy_solver *h)
+{
+    for (auto &gr : h->graphs)
+        if (gr.exec) cudaGraphExecDestroy(gr.exec);
+    h->graphs.clear();
+}
+
 void free_device(gy_solver *h)
 {
+    drop_graphs(h);
+    if (h->h_ring) cudaFreeHost(h->h_ring);
+    h->h_ring = nullptr;
+    for (int k = 0; k < gy_solver::kRing; k++) {
+        if (h->ring_ev[k]) cudaEventDestroy(h->ring_ev[k]);
+        h->ring_ev[k] = nullptr;
+        h->ring_busy[k] = false;
+    }
     void *ptrs[] = {h->slab[0], h->slab[1], h->d_perm, h->d_seg, h->d_nseg, h->sort_mem, h->resort_mem, h->d_pbc_val,
                     h->d_refkey0, h->d_mats, h->d_status, h->d_stats, h->node_mem, h->d_cell_min,
-                    h->d_nidx[0], h->d_nidx[1], h->d_nidx[2]};
+                    h->d_nidx[0], h->d_nidx[1], h->d_nidx[2], h->d_sc};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    h->d_sc = nullptr;
     h->slab[0] = h->slab[1] = nullptr;
     h->d_perm = h->d_seg = h->d_nseg = nullptr;
     h->sort_mem = nullptr;
@@ -581,6 +624,9 @@ gy_status gy_initialize(gy_solver *h, const gy_material *mats, int nmat, const g
     if ((st = dalloc(h, &h->d_status, 4))) return st;
     CK(h, cudaMemsetAsync(h->d_status, 0, 4 * sizeof(int), h->stream));
     if ((st = dalloc(h, &h->d_stats, 8))) return st;
+    CK(h, cudaMalloc(&h->d_sc, sizeof(StepScalars)));
+    CK(h, cudaMallocHost(&h->h_ring, gy_solver::kRing * sizeof(StepScalars)));
+    for (int k = 0; k < gy_solver::kRing; k++) CK(h, cudaEventCreateWithFlags(&h->ring_ev[k], cudaEventDisableTiming));
     // sort scratch
     h->sort_mem = nullptr;
     const size_t sbytes = sort_scratch_bytes(h->cap);
@@ -656,10 +702,11 @@ gy_status gy_set_options(gy_solver *h, const gy_options *opt)
 {
     if (!h || !opt) return GY_ERR_ARG;
     if (opt->sort_every < 1) return fail(h, GY_ERR_ARG, "sort_every must be >= 1");
-    if (opt->reserved != 0) return fail(h, GY_ERR_ARG, "gy_options.reserved must be 0");
+    if (opt->use_graph != 0 && opt->use_graph != 1) return fail(h, GY_ERR_ARG, "use_graph must be 0 or 1");
     if (h->initialized && (opt->track_normals != h->opt.track_normals || opt->keep_node_fields != h->opt.keep_node_fields))
         return fail(h, GY_ERR_STATE, "track_normals / keep_node_fields must be set before gy_initialize");
     h->opt = *opt;
+    drop_graphs(h);  // captured steps bake the options in
     return GY_OK;
 }
 
@@ -672,12 +719,9 @@ gy_status gy_get_options(const gy_solver *h, gy_options *opt)
 
 void *gy_stream(gy_solver *h) { return h ? (void *)h->stream : nullptr; }
 
-static StepArgs make_args(gy_solver *h, double t, int step)
+static StepScalars make_scalars(const gy_solver *h, int step)
 {
-    (void)t;
-    StepArgs a{};
-    a.g = h->g;
-    StepScalars &sc = a.sc;
+    StepScalars sc{};
     sc.dt = (float)h->dt;
     sc.dt_node = (float)(step == 1 ? 0.5 * h->dt : h->dt);
     for (int k = 0; k < 3; k++) sc.gravity[k] = (float)h->prm.gravity[k];
@@ -687,15 +731,71 @@ static StepArgs make_args(gy_solver *h, double t, int step)
     sc.fixed_grid_bcs = h->prm.fixed_grid_bcs;
     sc.multi_body = h->multi ? 1 : 0;
     sc.init_volume = (float)(h->g.is3d ? h->psep * h->psep * h->psep : h->psep * h->psep);
+    return sc;
+}
+
+static StepArgs make_args(gy_solver *h)
+{
+    StepArgs a{};
+    a.g = h->g;
+    a.sc = h->d_sc;
+    a.multi_body = h->multi ? 1 : 0;
     a.mats = h->d_mats;
     a.pbc_val = h->d_pbc_val;
     a.status = h->d_status;
     return a;
 }
 
+// The stream work of one step (no host state changes): sort, P2G, fold + solve, G2P.
+static void issue_step(gy_solver *h, const StepVariant &v, cudaEvent_t *tev)
+{
+    const StepArgs a = make_args(h);
+    cudaStream_t s = h->stream;
+    if (tev) cudaEventRecord(tev[0], s);
+    cudaMemsetAsync(h->nb.active_count, 0, sizeof(int), s);
+    // (a) stable counting sort of the cell keys; the particle kernels read through perm
+    const int *perm = nullptr;
+    const int *skey = reinterpret_cast<const int *>(h->slab[v.cur]) + (size_t)PF_KEY * h->cap;
+    if (v.sort) {
+        int *out = h->skey_buf[v.sk];
+        int key_bits = 1;
+        const long long maxkey = (long long)h->g.nbx * h->g.nby * h->g.nbz * 64;
+        while ((1LL << key_bits) < maxkey) key_bits++;
+        if (v.sort == 1) {
+            // the slab is in the order of the last sort: re-sort only the particles that moved
+            resort_keys(skey, h->skey_buf[v.sk ^ 1], out, h->d_perm, h->n, key_bits, h->rs, s);
+        } else {
+            const int *sorted = sort_pairs(skey, h->d_perm, h->n, key_bits, h->ws, s);
+            if (h->n > 0 && sorted != out)
+                cudaMemcpyAsync(out, sorted, (size_t)h->n * sizeof(int), cudaMemcpyDeviceToDevice, s);
+        }
+        skey = out;
+        perm = h->d_perm;
+    }
+    launch_block_heads(skey, h->n, h->d_seg, h->d_nseg, s);
+    PView src = pview(h, v.cur), dst = pview(h, v.cur ^ 1);
+    // body slots from the sort table of the reference's cadence (Solver.cpp:91)
+    if (v.tables) {
+        launch_body_tables(src, h->n, a, h->d_cell_min, h->nbody, v.tables == 2 ? h->d_refkey0 : nullptr, s);
+        launch_body_assign(h->nb, a, h->d_cell_min, h->nbody, h->d_nidx[0], h->d_nidx[1], h->d_nidx[2], s);
+    }
+    if (tev) cudaEventRecord(tev[1], s);
+    cudaMemsetAsync(h->nb.active_n, 0, sizeof(int), s);
+    // (b) P2G
+    launch_p2g(src, perm, skey, h->n, h->d_seg, h->d_nseg, h->persist_grid, h->nb, a, s);
+    if (tev) cudaEventRecord(tev[2], s);
+    // (c) periodic fold, nodal solve, grid BCs
+    launch_fold(h->nb, a, s);
+    launch_solve(h->nb, a, h->opt.keep_node_fields != 0, s);
+    if (tev) cudaEventRecord(tev[3], s);
+    // (d) G2P + particle BCs + update + constitutive + damage, written in sorted order
+    launch_g2p_update(src, dst, perm, skey, h->n, h->d_seg, h->d_nseg, h->g2p_grid, h->nb, a,
+                      h->opt.track_normals != 0, h->opt.check_finite != 0, h->has_dp, s);
+    if (tev) cudaEventRecord(tev[4], s);
+}
+
 static gy_status enqueue_step(gy_solver *h, double t, int step)
 {
-    StepArgs a = make_args(h, t, step);
     cudaStream_t s = h->stream;
     const bool timing = h->phase_timing && h->tev_used < kMaxTimedSteps;
     cudaEvent_t *tev = nullptr;
@@ -708,55 +808,59 @@ static gy_status enqueue_step(gy_solver *h, double t, int step)
         }
         tev = &h->tev[(size_t)h->tev_used * 5];
         h->tev_used++;
-        cudaEventRecord(tev[0], s);
     }
-    // (a) stable counting sort of the cell keys; the particle kernels read through perm
-    const int *perm = nullptr;
-    const int *skey = reinterpret_cast<const int *>(h->slab[h->cur]) + (size_t)PF_KEY * h->cap;
+    // host decisions for this step
+    StepVariant v{h->cur, h->sk, 0, 0};
     if (h->since_sort >= h->opt.sort_every) {
-        int *out = h->skey_buf[h->sk ^ 1];
-        int key_bits = 1;
-        const long long maxkey = (long long)h->g.nbx * h->g.nby * h->g.nbz * 64;
-        while ((1LL << key_bits) < maxkey) key_bits++;
-        if (h->resort_valid && !h->opt.full_sort) {
-            // the slab is in the order of the last sort: re-sort only the particles that moved
-            resort_keys(skey, h->skey_buf[h->sk], out, h->d_perm, h->n, key_bits, h->rs, s);
-        } else {
-            const int *sorted = sort_pairs(skey, h->d_perm, h->n, key_bits, h->ws, s);
-            if (h->n > 0 && sorted != out)
-                cudaMemcpyAsync(out, sorted, (size_t)h->n * sizeof(int), cudaMemcpyDeviceToDevice, s);
+        v.sort = (h->resort_valid && !h->opt.full_sort) ? 1 : 2;
+        v.sk = h->sk ^ 1;
+    }
+    if (h->multi && ((step % 10 == 0) || step == 1 || !h->tables_valid)) v.tables = h->steps == 0 ? 2 : 1;
+    // the step's scalars through a pinned ring slot; a slot is rewritten only after the copy
+    // that last read it has run (the host waits only when 32 steps are queued)
+    const int slot = (int)(h->ring_pos++ % gy_solver::kRing);
+    if (h->ring_busy[slot]) CK(h, cudaEventSynchronize(h->ring_ev[slot]));
+    h->h_ring[slot] = make_scalars(h, step);
+    CK(h, cudaMemcpyAsync(h->d_sc, &h->h_ring[slot], sizeof(StepScalars), cudaMemcpyHostToDevice, s));
+    CK(h, cudaEventRecord(h->ring_ev[slot], s));
+    h->ring_busy[slot] = true;
+    if (h->opt.use_graph && !timing) {
+        StepGraph *gr = nullptr;
+        for (auto &c : h->graphs)
+            if (c.v == v) gr = &c;
+        if (!gr) {
+            if (h->graphs.size() >= 8) drop_graphs(h);
+            StepGraph ng{};
+            ng.v = v;
+            const long long l0 = launch_count();
+            CK(h, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            issue_step(h, v, nullptr);
+            cudaGraph_t graph = nullptr;
+            CK(h, cudaStreamEndCapture(s, &graph));
+            ng.launches = launch_count() - l0;
+            const cudaError_t ei = cudaGraphInstantiate(&ng.exec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (ei != cudaSuccess) return fail(h, GY_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ei));
+            note_launch(-(int)ng.launches);  // counted again per replay below
+            h->graphs.push_back(ng);
+            gr = &h->graphs.back();
         }
-        h->sk ^= 1;
-        skey = out;
-        perm = h->d_perm;
+        CK(h, cudaGraphLaunch(gr->exec, s));
+        note_launch((int)gr->launches);
+    } else {
+        issue_step(h, v, tev);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(h, GY_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+    // host bookkeeping
+    if (v.sort) {
+        h->sk = v.sk;
         h->since_sort = 0;
         h->resort_valid = true;  // this step's G2P writes the slab in this order
     }
     h->since_sort++;
-    launch_block_heads(skey, h->n, h->d_seg, h->d_nseg, s);
-    PView src = pview(h, h->cur), dst = pview(h, h->cur ^ 1);
-    // body slots from the sort table of the reference's cadence (Solver.cpp:91)
-    if (h->multi && ((step % 10 == 0) || step == 1 || !h->tables_valid)) {
-        launch_body_tables(src, h->n, a, h->d_cell_min, h->nbody, h->steps == 0 ? h->d_refkey0 : nullptr, s);
-        launch_body_assign(h->nb, a, h->d_cell_min, h->nbody, h->d_nidx[0], h->d_nidx[1], h->d_nidx[2], s);
-        h->tables_valid = true;
-    }
-    if (timing) cudaEventRecord(tev[1], s);
-    cudaMemsetAsync(h->nb.active_n, 0, sizeof(int), s);
-    // (b) P2G
-    launch_p2g(src, perm, skey, h->n, h->d_seg, h->d_nseg, h->persist_grid, h->nb, a, s);
-    if (timing) cudaEventRecord(tev[2], s);
-    // (c) periodic fold, nodal solve, grid BCs
-    launch_fold(h->nb, a, s);
-    launch_solve(h->nb, a, h->opt.keep_node_fields != 0, s);
-    if (timing) cudaEventRecord(tev[3], s);
-    // (d) G2P + particle BCs + update + constitutive + damage, written in sorted order
-    launch_g2p_update(src, dst, perm, skey, h->n, h->d_seg, h->d_nseg, h->g2p_grid, h->nb, a,
-                      h->opt.track_normals != 0, h->opt.check_finite != 0, h->has_dp, s);
+    if (v.tables) h->tables_valid = true;
     h->cur ^= 1;
-    if (timing) cudaEventRecord(tev[4], s);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return fail(h, GY_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
     h->t_prev = t;
     h->steps++;
     return GY_OK;
@@ -768,19 +872,18 @@ gy_status gy_step(gy_solver *h, double t, int step)
     if (!h->initialized) return fail(h, GY_ERR_STATE, "gy_step before gy_initialize");
     cudaSetDevice(h->device);
     if (h->nb.active_count == nullptr) h->nb.active_count = h->d_status + 2;
-    cudaMemsetAsync(h->nb.active_count, 0, sizeof(int), h->stream);
     return enqueue_step(h, t, step);
 }
 
 gy_status gy_steps(gy_solver *h, double t0, int step0, int nsteps, int use_graph)
 {
-    (void)use_graph;
-    if (!h || nsteps < 0) return GY_ERR_ARG;
-    for (int k = 0; k < nsteps; k++) {
-        gy_status st = gy_step(h, t0 + k * h->dt, step0 + k);
-        if (st) return st;
-    }
-    return GY_OK;
+    if (!h || nsteps < 0 || use_graph < 0 || use_graph > 1) return GY_ERR_ARG;
+    const int keep = h->opt.use_graph;
+    h->opt.use_graph = use_graph;
+    gy_status st = GY_OK;
+    for (int k = 0; k < nsteps && st == GY_OK; k++) st = gy_step(h, t0 + k * h->dt, step0 + k);
+    h->opt.use_graph = keep;
+    return st;
 }
 
 gy_status gy_sync(gy_solver *h)

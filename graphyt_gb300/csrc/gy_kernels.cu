@@ -404,9 +404,9 @@ __global__ void __launch_bounds__(256) k_p2g_multi(PView P, const int *perm, lon
     const float sc = Vf * g.inv_h;
     const float s0 = st.s[0] * sc, s1 = st.s[1] * sc, s2 = st.s[2] * sc;
     const float s3 = st.s[3] * sc, s4 = st.s[4] * sc, s5 = st.s[5] * sc;
-    const float mgx = m * a.sc.gravity[0], mgy = m * a.sc.gravity[1], mgz = m * a.sc.gravity[2];
+    const float mgx = m * a.sc->gravity[0], mgy = m * a.sc->gravity[1], mgz = m * a.sc->gravity[2];
     const int obj = info_obj(st.info);
-    const float vol_n = ((st.info & INFO_INIT_VOL) ? a.sc.init_volume : st.mass / st.rho) * g.inv_h;
+    const float vol_n = ((st.info & INFO_INIT_VOL) ? a.sc->init_volume : st.mass / st.rho) * g.inv_h;
 #pragma unroll
     for (int kk = 0; kk < 3; kk++)
 #pragma unroll
@@ -443,7 +443,7 @@ void launch_p2g(const PView &p, const int *perm, const int *skey, long long n, c
                 const int *nseg, int persist_grid, const NodeBufs &nb, const StepArgs &a, cudaStream_t s)
 {
     if (n == 0) return;
-    if (a.sc.multi_body) {
+    if (a.multi_body) {
         k_p2g_multi<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p, perm, n, nb, a);
     } else {
         k_p2g_tiled<<<persist_grid, P2G_CH, 0, s>>>(p, perm, skey, n, seg_start, nseg, perm ? 1 : 0, nb, a.g);
@@ -510,7 +510,7 @@ void launch_fold(const NodeBufs &nb, const StepArgs &a, cudaStream_t s)
     for (int ax = 0; ax < naxes; ax++) {
         const long long plane = ax == 0 ? (long long)g.ny * g.nz : ax == 1 ? (long long)g.nx * g.nz : (long long)g.nx * g.ny;
         const unsigned grid = (unsigned)((3 * plane + 255) / 256);
-        if (a.sc.multi_body) k_fold<true><<<grid, 256, 0, s>>>(nb, g, ax);
+        if (a.multi_body) k_fold<true><<<grid, 256, 0, s>>>(nb, g, ax);
         else k_fold<false><<<grid, 256, 0, s>>>(nb, g, ax);
         note_launch(1);
     }
@@ -589,11 +589,11 @@ __device__ __forceinline__ bool solve_node(const NodeBufs &nb, const StepArgs &a
             const float m = A0.x;
             if (!MULTI) {
                 // single body: gravity enters here as m_node * g (Extrapolation.cpp:226-228)
-                A1.x += m * a.sc.gravity[0];
-                A1.y += m * a.sc.gravity[1];
-                A1.z += m * a.sc.gravity[2];
+                A1.x += m * a.sc->gravity[0];
+                A1.y += m * a.sc->gravity[1];
+                A1.z += m * a.sc->gravity[2];
             }
-            const float dtn = a.sc.dt_node, dt = a.sc.dt;
+            const float dtn = a.sc->dt_node, dt = a.sc->dt;
             float vc[3] = {0.f, 0.f, 0.f};
             float v1[3] = {0.f, 0.f, 0.f}, a1[3] = {0.f, 0.f, 0.f};
             float v2[3] = {0.f, 0.f, 0.f}, a2[3] = {0.f, 0.f, 0.f};
@@ -655,7 +655,7 @@ __device__ __forceinline__ bool solve_node(const NodeBufs &nb, const StepArgs &a
                             } else {
                                 if (m1 != 0.0f) {
                                     float cn[3];
-                                    contact_normal(rv1, n1, a.sc.mu, cn);
+                                    contact_normal(rv1, n1, a.sc->mu, cn);
                                     v1[0] = B0[0].y / m1 - ap1 * cn[0];
                                     v1[1] = B0[0].z / m1 - ap1 * cn[1];
                                     v1[2] = B0[0].w / m1 - ap1 * cn[2];
@@ -666,7 +666,7 @@ __device__ __forceinline__ bool solve_node(const NodeBufs &nb, const StepArgs &a
                                 }
                                 if (m2 != 0.0f) {
                                     float cn[3];
-                                    contact_normal(rv2, n2, a.sc.mu, cn);
+                                    contact_normal(rv2, n2, a.sc->mu, cn);
                                     v2[0] = B0[1].y / m2 - ap2 * cn[0];
                                     v2[1] = B0[1].z / m2 - ap2 * cn[1];
                                     v2[2] = B0[1].w / m2 - ap2 * cn[2];
@@ -689,7 +689,7 @@ __device__ __forceinline__ bool solve_node(const NodeBufs &nb, const StepArgs &a
             // particles read; phase 3 repeats phase 2)
             const int bt = nb.bc_type ? nb.bc_type[nd] : 0;
             if (bt) {
-                BCApply bc{bt, nb.bc_val[nd], a.sc.fixed_grid_bcs};
+                BCApply bc{bt, nb.bc_val[nd], a.sc->fixed_grid_bcs};
                 bool set[3];
                 float val[3];
                 bc.comps(set, val);
@@ -732,7 +732,9 @@ __global__ void __launch_bounds__(256) k_solve_single(NodeBufs nb, StepArgs a, i
     const int nw = (int)((gridDim.x * blockDim.x) >> 5);
     const int nact = *nb.active_n;
     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-    const float dtn = a.sc.dt_node;
+    const float dtn = a.sc->dt_node;
+    const float grx = a.sc->gravity[0], gry = a.sc->gravity[1], grz = a.sc->gravity[2];
+    const int fixed_bcs = a.sc->fixed_grid_bcs;
     int count = 0;
     for (int w = gw; w < nact; w += nw) {
         const int blk = nb.active_list[w];
@@ -761,9 +763,9 @@ __global__ void __launch_bounds__(256) k_solve_single(NodeBufs nb, StepArgs a, i
             const float m = A0[h].x;
             float4 F = A1[h];
             // gravity enters here as m_node * g (Extrapolation.cpp:226-228)
-            F.x += m * a.sc.gravity[0];
-            F.y += m * a.sc.gravity[1];
-            F.z += m * a.sc.gravity[2];
+            F.x += m * grx;
+            F.y += m * gry;
+            F.z += m * grz;
             float vc[3] = {0.f, 0.f, 0.f}, v1[3] = {0.f, 0.f, 0.f}, a1[3] = {0.f, 0.f, 0.f};
             if (m != 0.0f) {
                 count++;
@@ -773,7 +775,7 @@ __global__ void __launch_bounds__(256) k_solve_single(NodeBufs nb, StepArgs a, i
             // grid BC, phase 2 (phase 1 is overwritten by the solve for every node the
             // particles read; phase 3 repeats phase 2)
             if (bt[h]) {
-                BCApply bc{bt[h], nb.bc_val[nd[h]], a.sc.fixed_grid_bcs};
+                BCApply bc{bt[h], nb.bc_val[nd[h]], fixed_bcs};
                 bool set[3];
                 float val[3];
                 bc.comps(set, val);
@@ -847,7 +849,7 @@ void launch_solve(const NodeBufs &nb, const StepArgs &a, bool keep_node_fields, 
     note_launch(1);
     long long grid = std::min<long long>((a.g.nnb + 7) / 8, (long long)sms * 16);  // 8 warps per CTA
     if (grid < 1) grid = 1;
-    if (a.sc.multi_body) k_solve_list<true><<<(unsigned)grid, 256, 0, s>>>(nb, a, keep_node_fields ? 1 : 0);
+    if (a.multi_body) k_solve_list<true><<<(unsigned)grid, 256, 0, s>>>(nb, a, keep_node_fields ? 1 : 0);
     else k_solve_single<<<(unsigned)grid, 256, 0, s>>>(nb, a, keep_node_fields ? 1 : 0);
     note_launch(1);
 }
@@ -899,7 +901,7 @@ __device__ __forceinline__ void update_after_g2p(PState &st, const int c0[3], fl
                                                  const float L[3][3], const StepArgs &a, bool check_finite)
 {
     const GridGeom &g = a.g;
-    const StepScalars &sc = a.sc;
+    const StepScalars sc = *a.sc;
     Constit c;
     c.r[0] = L[0][0];
     c.r[1] = L[1][1];
@@ -1275,7 +1277,7 @@ void launch_g2p_update(const PView &src, const PView &dst, const int *perm, cons
     if (n == 0) return;
     const unsigned grid = (unsigned)((n + 255) / 256);
     const int tn = track_normals ? 1 : 0, cf = check_finite ? 1 : 0;
-    if (a.sc.multi_body) {
+    if (a.multi_body) {
         if (has_dp) k_g2p_update<true, true><<<grid, 256, 0, s>>>(src, dst, perm, n, nb, a, tn, cf);
         else k_g2p_update<true, false><<<grid, 256, 0, s>>>(src, dst, perm, n, nb, a, tn, cf);
     } else {

@@ -42,7 +42,8 @@ struct NodeBufs {
 
 struct StepArgs {
     GridGeom g;
-    StepScalars sc;
+    const StepScalars *sc;   // per-step scalars in device memory (one small copy per step)
+    int multi_body;          // host-side launch choice, fixed per handle
     const DevMaterial *mats;
     const float4 *pbc_val;   // particle BC values by pid
     int *status;

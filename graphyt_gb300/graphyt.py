@@ -527,7 +527,7 @@ class Solver:
         self.nds.t = t
 
     def iterate_GPU_steps(self, nsteps: int, mpmParameters: Optional[Parameters] = None, step0: int = 0,
-                          t0: float = 0.0, use_graph: bool = False):
+                          t0: float = 0.0, use_graph: bool = True):
         """nsteps consecutive steps from step0 (iterate_CPU_steps, Solver.cpp:75-84)."""
         if mpmParameters is not None:
             prm = mpmParameters._ctype()

@@ -77,7 +77,9 @@ typedef struct gy_options {
     int sort_every;     /* reorder particle state by cell every n steps (>= 1) */
     int full_sort;      /* 1: every sort is a full radix sort; 0: after the first, an incremental
                            re-sort of the particles that changed cell (same permutation) */
-    int reserved;       /* must be 0 */
+    int use_graph;      /* 1 (default): each step replays a captured CUDA graph of its kernels,
+                           the step's scalars reaching the device in one small copy; 0: the
+                           kernels are launched one by one */
     int track_normals;  /* 1: keep per-particle contact normals (getNormalsArr) */
     int check_finite;   /* 1: flag NaN/Inf in particle state every step */
     int keep_node_fields; /* 1: keep centre-of-mass node velocity/force for node getters */
@@ -166,7 +168,7 @@ gy_status gy_get_options(const gy_solver *h, gy_options *opt);
 gy_status gy_step(gy_solver *h, double t, int step);
 
 /* Solver::iterate_CPU_steps (Solver.cpp:75-84) on the GPU: nsteps steps from step0/t0,
- * t advancing by dt.  use_graph = 1 replays the steps as a captured CUDA graph. */
+ * t advancing by dt.  use_graph overrides gy_options.use_graph for these steps. */
 gy_status gy_steps(gy_solver *h, double t0, int step0, int nsteps, int use_graph);
 
 /* Waits for all queued work, then reports device error flags (GY_ERR_RANGE /

@@ -204,6 +204,7 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sort-every", type=int, default=1)
+    ap.add_argument("--full-sort", action="store_true", help="full radix sort every step (no incremental re-sort)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
@@ -220,7 +221,7 @@ def main():
     dist = Dist(world, local)
     sc = scenes.dam_break(scale=args.scale)
     n = sc.n
-    solver = graphyt.from_scene(sc, device=local, options=dict(sort_every=args.sort_every))
+    solver = graphyt.from_scene(sc, device=local, options=dict(sort_every=args.sort_every, full_sort=int(args.full_sort)))
     lib, h = solver.lib, solver.h
     dt = solver.dt
     for k in range(args.warmup):
@@ -293,7 +294,7 @@ def main():
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "dam_break_3d_newtonian", "particles": n, "nodes": sc.num_nodes(),
                        "active_nodes": n_active, "cellsize": sc.cellsize, "psep": sc.psep, "model": "newtonian",
-                       "sort_every": args.sort_every, "l2": "state larger than L2 (no flush needed)",
+                       "sort_every": args.sort_every, "sort": "full" if args.full_sort else "incremental", "l2": "state larger than L2 (no flush needed)",
                        "parallelism": "replicas" if world > 1 else "single"},
             "phase_ms_per_step": dict(zip(names, per_step)),
             "roofline": roofline,

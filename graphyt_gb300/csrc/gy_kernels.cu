@@ -268,24 +268,33 @@ __global__ void __launch_bounds__(P2G_CH) k_p2g_tiled(PView P, const int *perm, 
         const int tox = bx * CB, toy = by * CB, toz = g.is3d ? bz * CB : 0;
         for (int t = tid; t < P2G_FIELDS * PT_NODES; t += P2G_CH) tile[t] = 0.f;
         for (long long base = start;; base += P2G_CH) {
-            int cnt;
+            int cnt, kcur = -1, kprev = -1;
+            long long j = 0;
+            const long long i = base + tid;
             if (sorted) {
                 // sorted keys: the segment's particles in this chunk are a prefix of it; the
-                // barrier also ends the previous chunk's use of the staging arrays
-                const long long i = base + tid;
-                cnt = __syncthreads_count(i < n && (skey[i] >> CB_SHIFT) == blk);
+                // barrier also ends the previous chunk's use of the staging arrays.  The
+                // particle's slot and its predecessor's key load with its own key.
+                const bool inr = i < n;
+                kcur = inr ? skey[i] : -1;
+                kprev = (inr && tid > 0) ? skey[i - 1] : -1;
+                j = inr ? perm[i] : 0;
+                cnt = __syncthreads_count(inr && (kcur >> CB_SHIFT) == blk);
             } else {
                 cnt = (int)min((long long)P2G_CH, segment_chunk_end(skey, n, blk, base, P2G_CH, &s_end) - base);
+                if (tid < cnt) {
+                    kcur = skey[i];
+                    kprev = tid > 0 ? skey[i - 1] : -1;
+                }
+                j = i;
             }
             if (cnt <= 0) break;
             // ---- stage weights and payload, natural (coalesced) order ----
             bool head = false;
             if (tid < cnt) {
-                const long long i = base + tid;
-                const int cell = skey[i] & 63;  // cell inside the block: (lz*4 + ly)*4 + lx
-                head = tid == 0 || (skey[i - 1] & 63) != cell;
+                const int cell = kcur & 63;  // cell inside the block: (lz*4 + ly)*4 + lx
+                head = tid == 0 || (kprev & 63) != cell;
                 cellof[tid] = cell;
-                const long long j = perm ? perm[i] : i;
                 const int m = tid >> 1, hf = tid & 1;
                 float S[3], G[3];
                 gimp_axis(P.f(PF_OX, j), g, S, G);
@@ -1130,34 +1139,51 @@ __global__ void __launch_bounds__(GY_G2P_THREADS, GY_G2P_MINB) k_g2p_tiled(PView
         int bx, by, bz;
         decode_block(blk, g, bx, by, bz);
         const int tox = bx * CB, toy = by * CB, toz = g.is3d ? bz * CB : 0;
-        __syncthreads();  // the previous segment's particles are done with the tile
-        for (int t = tid; t < PT_NODES; t += blockDim.x) {
+        // the solved node tile, loaded into registers before anything waits on it
+        constexpr int TILE_ITERS = (PT_NODES + GY_G2P_THREADS - 1) / GY_G2P_THREADS;
+        float4 TVr[TILE_ITERS], TAr[TILE_ITERS];
+#pragma unroll
+        for (int h = 0; h < TILE_ITERS; h++) {
+            const int t = tid + h * GY_G2P_THREADS;
+            TVr[h] = z4;
+            TAr[h] = z4;
             const int ni = tox + t % PT, nj = toy + (t / PT) % PT, nk = toz + t / (PT * PT);
-            float4 V = z4, A = z4;
-            if (ni < g.nx && nj < g.ny && nk < g.nz) {
+            if (t < PT_NODES && ni < g.nx && nj < g.ny && nk < g.nz) {
                 const int nd = node_index(ni, nj, nk, g);
-                V = nb.gv[nd];
-                A = nb.ga[nd];
-                if (V.x == 0.0f) { V = z4; A = z4; }
+                TVr[h] = __ldg(&nb.gv[nd]);
+                TAr[h] = __ldg(&nb.ga[nd]);
             }
+        }
+        __syncthreads();  // the previous segment's particles are done with the tile
+#pragma unroll
+        for (int h = 0; h < TILE_ITERS; h++) {
+            const int t = tid + h * GY_G2P_THREADS;
+            if (t >= PT_NODES) break;
+            float4 V = TVr[h], A = TAr[h];
+            if (V.x == 0.0f) { V = z4; A = z4; }
             TV[t] = make_float4(V.y, V.z, V.w, A.z);
             TA[t] = make_float2(A.x, A.y);
         }
         for (long long base = start;; base += blockDim.x) {
-            int cnt;
+            int cnt, key = 0;
+            long long j = 0;
+            const long long i = base + tid;
             if (sorted) {
-                // the barrier also publishes the tile
-                const long long i = base + tid;
-                cnt = __syncthreads_count(i < n && (skey[i] >> CB_SHIFT) == blk);
+                // the particle's key and slot are loaded together; the barrier also publishes
+                // the tile.  skey[i] is the key of particle perm[i].
+                const bool inr = i < n;
+                key = inr ? skey[i] : -1;
+                j = inr ? perm[i] : 0;
+                cnt = __syncthreads_count(inr && (key >> CB_SHIFT) == blk);
             } else {
                 cnt = (int)min((long long)blockDim.x, segment_chunk_end(skey, n, blk, base, blockDim.x, &s_end) - base);
+                if (tid < cnt) key = skey[i];
+                j = i;
             }
             if (cnt <= 0) break;
             if (tid < cnt) {
-                const long long i = base + tid;
-                const long long j = perm ? perm[i] : i;
                 PState st;
-                st.key = src.ii(PF_KEY, j);
+                st.key = key;
 #pragma unroll
                 for (int k = 0; k < 3; k++) st.o[k] = src.f(PF_OX + k, j);
                 // the rest of the state travels to shared memory during the G2P sums

@@ -162,6 +162,14 @@ constexpr int P2G_FIELDS = 7;           // m, px, py, pz, fx, fy, fz
 #ifndef GY_P2G_CH
 #define GY_P2G_CH 128
 #endif
+#ifndef GY_P2G_MINB
+#define GY_P2G_MINB 0  // 0: registers left to the compiler
+#endif
+#if GY_P2G_MINB > 0
+#define GY_P2G_BOUNDS __launch_bounds__(P2G_CH, GY_P2G_MINB)
+#else
+#define GY_P2G_BOUNDS __launch_bounds__(P2G_CH)
+#endif
 constexpr int P2G_CH = GY_P2G_CH;       // particles per chunk = threads per CTA
 constexpr int P2G_NP = P2G_CH / 2 + 1;  // pairs per staged row; the odd row length (in float4)
                                         // puts the three rows one load reads in different banks
@@ -241,7 +249,7 @@ __device__ __forceinline__ void p2g_single(P2GAcc &A, const float4 (*W)[P2G_NP],
     A.fz.x = fmaf(gx, s5, fmaf(gy, s4, fmaf(gz, s2, A.fz.x)));
 }
 
-__global__ void __launch_bounds__(P2G_CH) k_p2g_tiled(PView P, const int *perm, const int *skey, long long n,
+__global__ void GY_P2G_BOUNDS k_p2g_tiled(PView P, const int *perm, const int *skey, long long n,
                                                        const int *seg_start, const int *nseg_ptr, int sorted,
                                                        NodeBufs nb, GridGeom g)
 {
@@ -1088,10 +1096,10 @@ __global__ void __launch_bounds__(256, 3) k_g2p_update(PView src, PView dst, con
 
 // G2P CTA size and the resident CTAs per SM it is register-limited to (64 registers)
 #ifndef GY_G2P_MINB
-#define GY_G2P_MINB 8
+#define GY_G2P_MINB 16
 #endif
 #ifndef GY_G2P_THREADS
-#define GY_G2P_THREADS 128
+#define GY_G2P_THREADS 64
 #endif
 
 // 4-byte asynchronous global -> shared copy (no register holds the value in flight)

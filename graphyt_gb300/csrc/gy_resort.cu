@@ -204,9 +204,11 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_place_stayers(const int *key,
     const long long wstride = ((long long)gridDim.x * blockDim.x) >> 5;
     for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nw; w += wstride) {
         const long long i = w * 32 + lane;
+        const int kv = i < n ? key[i] : 0;  // independent of the chain below: issued first
         const unsigned m = wmask[w];
         const long long rbase = w * 32 - wpref[w];  // rank of the warp's first stayer
         const long long gw0 = rbase >> 5;
+        const int gbase = gwpref[gw0];
         int c0 = 0, c1 = 0;
         if (gwcnt[gw0] | gwcnt[gw0 + 1]) {  // movers in these gaps: per-gap counts, prefix-summed
             c0 = gapcnt[gw0 * 32 + lane];
@@ -226,8 +228,8 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_place_stayers(const int *key,
         const int rr = (int)(r - gw0 * 32);  // 0..62 for a stayer
         const int in0 = __shfl_sync(0xffffffffu, c0, rr & 31), in1 = __shfl_sync(0xffffffffu, c1, rr & 31);
         if (!stay) continue;
-        const long long pos = r + gwpref[gw0] + (rr < 32 ? in0 : tot0 + in1);
-        skey_out[pos] = key[i];
+        const long long pos = r + gbase + (rr < 32 ? in0 : tot0 + in1);
+        skey_out[pos] = kv;
         perm_out[pos] = (int)i;
     }
 }

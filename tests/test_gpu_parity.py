@@ -42,7 +42,7 @@ def test_sort_presorted_and_reversed(gpu_lib):
 
 # ---- the incremental re-sort: the same permutation as the full stable sort --------------
 @pytest.mark.parametrize("n", [1, 2, 31, 32, 33, 2049, 100_003, 1_000_000])
-@pytest.mark.parametrize("frac", [0.0, 0.001, 0.1, 1.0])
+@pytest.mark.parametrize("frac", [0.0, 0.001, 0.004, 0.1, 1.0])
 def test_resort_matches_full_stable_sort(gpu_lib, n, frac):
     """Previous sorted keys (with long runs of equal keys, like cells), a fraction of the
     particles moved to nearby or arbitrary keys: the re-sort returns the stable order."""

@@ -41,6 +41,14 @@ G2P_BYTES_PER_NODE = 24            # v(3), a(3) read per active node
 SOLVE_BYTES_PER_NODE = 52          # m, p, f read; v, a written
 STEP_BYTES_PER_PARTICLE = 168
 STEP_BYTES_PER_NODE = 104
+# multi-body Drucker-Prager + Grady-Kipp (the Brazilian disc): the plastic strain, eqps,
+# damage and smax fields add 68 B per particle; per active node the centre-of-mass fields
+# plus two body slots (accumulated, solved, read back)
+DP_BYTES_PER_PARTICLE = 236
+MB_P2G_BYTES_PER_NODE = 84           # COM + two body slots, 28 B each
+MB_SOLVE_BYTES_PER_NODE = 156
+MB_G2P_BYTES_PER_NODE = 72
+MB_STEP_BYTES_PER_NODE = 312
 
 
 def dist_env():
@@ -202,6 +210,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--workload", default="dam_break", choices=["dam_break", "brazilian_disc"],
+                    help="dam_break: the headline 3D Newtonian dam break; brazilian_disc: the multi-body "
+                         "Drucker-Prager + Grady-Kipp disc between rigid platens")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sort-every", type=int, default=1)
     ap.add_argument("--full-sort", action="store_true", help="full radix sort every step (no incremental re-sort)")
@@ -219,7 +230,7 @@ def main():
     from graphyt_gb300 import graphyt, scenes
 
     dist = Dist(world, local)
-    sc = scenes.dam_break(scale=args.scale)
+    sc = scenes.dam_break(scale=args.scale) if args.workload == "dam_break" else scenes.brazilian_disc(scale=args.scale)
     n = sc.n
     solver = graphyt.from_scene(sc, device=local, options=dict(sort_every=args.sort_every, full_sort=int(args.full_sort)))
     lib, h = solver.lib, solver.h
@@ -229,24 +240,31 @@ def main():
     solver.Synchronise()
     dist.barrier()
 
+    # the timed region: K steps as the library runs them (graph replay), CUDA events on the
+    # handle's stream around them
     sampler = ClockSampler(local)
     if rank == 0:
         sampler.start()
-    L.check(lib.gy_set_phase_timing(h, 1), h)
     launches0 = lib.gy_kernel_launches()
     ms = C.c_float()
     step0 = args.warmup
     L.check(lib.gy_time_steps(h, step0 * dt, step0, args.steps, C.byref(ms)), h, "timed steps")
     launches = lib.gy_kernel_launches() - launches0
-    phase = (C.c_float * 5)()
-    nph = C.c_int64()
-    L.check(lib.gy_get_phase_times(h, phase, C.byref(nph)), h)
-    L.check(lib.gy_set_phase_timing(h, 0), h)
     clocks = sampler.stop() if rank == 0 else None
     solver.Synchronise()
     ms_max = dist.max(ms.value)
     ms_per_step = ms_max / args.steps
     value = n * args.steps * world / (ms_max / 1e3)
+
+    # phase breakdown, separately: events between the phases need kernel-by-kernel launches
+    L.check(lib.gy_set_phase_timing(h, 1), h)
+    step0 += args.steps
+    L.check(lib.gy_steps(h, step0 * dt, step0, args.steps, 0), h, "phase-timed steps")
+    solver.Synchronise()
+    phase = (C.c_float * 5)()
+    nph = C.c_int64()
+    L.check(lib.gy_get_phase_times(h, phase, C.byref(nph)), h)
+    L.check(lib.gy_set_phase_timing(h, 0), h)
 
     st = solver.stats()
     n_active = int(st["active_nodes"])
@@ -266,20 +284,23 @@ def main():
     # roofline of the dominant kernel
     names = ["sort", "p2g", "grid", "g2p_update"]
     per_step = [phase[k] / max(nph.value, 1) for k in range(4)]
+    multi = args.workload == "brazilian_disc"
     algo = {
         "sort": 0.0,
-        "p2g": P2G_BYTES_PER_PARTICLE * n + P2G_BYTES_PER_NODE * n_active,
-        "grid": SOLVE_BYTES_PER_NODE * n_active,
-        "g2p_update": G2P_BYTES_PER_PARTICLE * n + G2P_BYTES_PER_NODE * n_active,
+        "p2g": P2G_BYTES_PER_PARTICLE * n + (MB_P2G_BYTES_PER_NODE if multi else P2G_BYTES_PER_NODE) * n_active,
+        "grid": (MB_SOLVE_BYTES_PER_NODE if multi else SOLVE_BYTES_PER_NODE) * n_active,
+        "g2p_update": (DP_BYTES_PER_PARTICLE if multi else G2P_BYTES_PER_PARTICLE) * n
+                      + (MB_G2P_BYTES_PER_NODE if multi else G2P_BYTES_PER_NODE) * n_active,
     }
     dom = max(range(4), key=lambda k: per_step[k] if names[k] != "sort" else -1)
     peak, peak_kind = measured_peak()
     achieved = algo[names[dom]] / (per_step[dom] / 1e3) / 1e9
-    traffic = profiled_traffic().get(names[dom])
+    traffic = profiled_traffic().get(names[dom]) if not multi else None
     roofline = {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
                 "algorithmic_bytes": algo[names[dom]]}
-    step_bytes = STEP_BYTES_PER_PARTICLE * n + STEP_BYTES_PER_NODE * n_active
+    step_bytes = ((DP_BYTES_PER_PARTICLE if multi else STEP_BYTES_PER_PARTICLE) * n
+                  + (MB_STEP_BYTES_PER_NODE if multi else STEP_BYTES_PER_NODE) * n_active)
     whole = step_bytes / (ms_per_step / 1e3) / 1e9
 
     cpu = None
@@ -292,8 +313,10 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "dam_break_3d_newtonian", "particles": n, "nodes": sc.num_nodes(),
-                       "active_nodes": n_active, "cellsize": sc.cellsize, "psep": sc.psep, "model": "newtonian",
+            "config": {"workload": "dam_break_3d_newtonian" if not multi else "brazilian_disc_dp_gk_rigid_platens",
+                       "particles": n, "nodes": sc.num_nodes(),
+                       "active_nodes": n_active, "cellsize": sc.cellsize, "psep": sc.psep,
+                       "model": "newtonian" if not multi else "drucker_prager+grady_kipp, 3 bodies",
                        "sort_every": args.sort_every, "sort": "full" if args.full_sort else "incremental", "l2": "state larger than L2 (no flush needed)",
                        "parallelism": "replicas" if world > 1 else "single"},
             "phase_ms_per_step": dict(zip(names, per_step)),

@@ -456,12 +456,200 @@ __global__ void __launch_bounds__(256) k_p2g_multi(PView P, const int *perm, lon
             }
 }
 
+// Multi-body P2G through a shared-memory node tile: the tiled scheme of k_p2g_tiled with one
+// particle at a time per warp and, per node, the centre-of-mass fields plus the two body
+// slots (mass, momentum, force, normal).  A lane's body slot for a particle follows the node's
+// body pair (Extrapolation.cpp:191-198) read once per segment into shared memory.
+constexpr int MB_FIELDS = 27;                 // COM m, p(3), f(3); slot s: m, p(3), f(3), n(3)
+constexpr int MB_NP = P2G_CH + 1;             // staged row length; odd, so rows fall in other banks
+
+__global__ void __launch_bounds__(P2G_CH) k_p2g_multi_tiled(PView P, const int *perm, const int *skey, long long n,
+                                                            const int *seg_start, const int *nseg_ptr, int sorted,
+                                                            NodeBufs nb, StepArgs a)
+{
+    __shared__ float tile[MB_FIELDS * PT_NODES];
+    __shared__ int2 tbody[PT_NODES];
+    __shared__ float2 W[9][MB_NP];    // (S, G) per axis/stencil node and particle
+    __shared__ float4 Q0[P2G_CH];     // m, m v
+    __shared__ float4 Q1[P2G_CH];     // V sigma / h: xx, yy, zz, xy
+    __shared__ float4 Q2[P2G_CH];     // V sigma / h: yz, xz; normal volume / h; object | rigid << 16
+    __shared__ int cellof[P2G_CH];
+    __shared__ int run_start[P2G_CH + 1];
+    __shared__ int wcount[P2G_CH / 32];
+    __shared__ long long s_end;
+    const GridGeom &g = a.g;
+    const int nseg = *nseg_ptr;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int ii = lane % 3, jj = (lane / 3) % 3, kk = min(lane / 9, 2);
+    const bool scatter_lane = lane < 27;
+    const float grx = a.sc->gravity[0], gry = a.sc->gravity[1], grz = a.sc->gravity[2];
+    const float init_vol = a.sc->init_volume;
+    for (int sgi = blockIdx.x; sgi < nseg; sgi += gridDim.x) {
+        const long long start = seg_start[sgi];
+        const int blk = seg_block(skey, start);
+        int bx, by, bz;
+        decode_block(blk, g, bx, by, bz);
+        const int tox = bx * CB, toy = by * CB, toz = g.is3d ? bz * CB : 0;
+        __syncthreads();  // the previous segment's flush is done with the tile
+        for (int t = tid; t < MB_FIELDS * PT_NODES; t += P2G_CH) tile[t] = 0.f;
+        for (int t = tid; t < PT_NODES; t += P2G_CH) {
+            const int ni = tox + t % PT, nj = toy + (t / PT) % PT, nk = toz + t / (PT * PT);
+            tbody[t] = (ni < g.nx && nj < g.ny && nk < g.nz) ? nb.body[node_index(ni, nj, nk, g)] : make_int2(-1, -1);
+        }
+        for (long long base = start;; base += P2G_CH) {
+            int cnt, kcur = -1, kprev = -1;
+            long long j = 0;
+            const long long i = base + tid;
+            if (sorted) {
+                const bool inr = i < n;
+                kcur = inr ? skey[i] : -1;
+                kprev = (inr && tid > 0) ? skey[i - 1] : -1;
+                j = inr ? perm[i] : 0;
+                cnt = __syncthreads_count(tid < P2G_CH && inr && (kcur >> CB_SHIFT) == blk);
+            } else {
+                cnt = (int)min((long long)P2G_CH, segment_chunk_end(skey, n, blk, base, P2G_CH, &s_end) - base);
+                if (tid < cnt) {
+                    kcur = skey[i];
+                    kprev = tid > 0 ? skey[i - 1] : -1;
+                }
+                j = i;
+            }
+            if (cnt <= 0) break;
+            bool head = false;
+            if (tid < cnt) {
+                const int cell = kcur & 63;
+                head = tid == 0 || (kprev & 63) != cell;
+                cellof[tid] = cell;
+                float S[3], G[3];
+                gimp_axis(P.f(PF_OX, j), g, S, G);
+#pragma unroll
+                for (int k = 0; k < 3; k++) W[0 + k][tid] = make_float2(S[k], G[k]);
+                gimp_axis(P.f(PF_OY, j), g, S, G);
+#pragma unroll
+                for (int k = 0; k < 3; k++) W[3 + k][tid] = make_float2(S[k], G[k]);
+                if (g.is3d) {
+                    gimp_axis(P.f(PF_OZ, j), g, S, G);
+                } else {
+                    S[0] = 1.f; S[1] = 0.f; S[2] = 0.f; G[0] = 0.f; G[1] = 0.f; G[2] = 0.f;
+                }
+#pragma unroll
+                for (int k = 0; k < 3; k++) W[6 + k][tid] = make_float2(S[k], G[k]);
+                const uint32_t info = (uint32_t)P.ii(PF_INFO, j);
+                const bool rigid = (info & INFO_RIGID) != 0;
+                const float smass = P.f(PF_MASS, j), rho = P.f(PF_RHO, j);
+                // a rigid particle's P2G mass is 1 (Extrapolation.cpp:183); its stored mass still
+                // sets the volume the normals use
+                const float m = rigid ? 1.0f : smass;
+                const float sc = (m / rho) * g.inv_h;
+                const float vol_n = ((info & INFO_INIT_VOL) ? init_vol : smass / rho) * g.inv_h;
+                Q0[tid] = make_float4(m, m * P.f(PF_VX, j), m * P.f(PF_VY, j), m * P.f(PF_VZ, j));
+                Q1[tid] = make_float4(P.f(PF_S0, j) * sc, P.f(PF_S0 + 1, j) * sc, P.f(PF_S0 + 2, j) * sc,
+                                      P.f(PF_S0 + 3, j) * sc);
+                Q2[tid] = make_float4(P.f(PF_S0 + 4, j) * sc, P.f(PF_S0 + 5, j) * sc, vol_n,
+                                      __int_as_float(info_obj(info) | (rigid ? 1 << 16 : 0)));
+            }
+            const unsigned hm = __ballot_sync(0xffffffffu, head);
+            if (lane == 0) wcount[warp] = __popc(hm);
+            __syncthreads();
+            int wbase = 0, R = 0;
+#pragma unroll
+            for (int w2 = 0; w2 < P2G_CH / 32; w2++) {
+                const int c = wcount[w2];
+                wbase += (w2 < warp) ? c : 0;
+                R += c;
+            }
+            if (head) run_start[wbase + __popc(hm & ((1u << lane) - 1u))] = tid;
+            if (tid == 0) run_start[R] = cnt;
+            __syncthreads();
+            for (int r = warp; r < R; r += P2G_CH / 32) {
+                const int p0 = run_start[r], p1 = run_start[r + 1];
+                const int cell = cellof[p0];
+                const int li = cell & 3, lj = (cell >> 2) & 3, lk = cell >> 4;
+                const int t = ((lk + kk) * PT + (lj + jj)) * PT + (li + ii);
+                const int2 bp = tbody[t];
+                float c[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+                float b0[10] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+                float b1[10] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+                for (int p = p0; p < p1; p++) {
+                    const float2 X = W[ii][p], Y = W[3 + jj][p], Z = W[6 + kk][p];
+                    const float4 q0 = Q0[p], q1 = Q1[p], q2 = Q2[p];
+                    const float syz = Y.x * Z.x;
+                    const float w = X.x * syz, gx = X.y * syz, gy = X.x * Y.y * Z.x, gz = X.x * Y.x * Z.y;
+                    const float wm = w * q0.x;
+                    const float fx = -(gx * q1.x + gy * q1.w + gz * q2.y);
+                    const float fy = -(gx * q1.w + gy * q1.y + gz * q2.x);
+                    const float fz = -(gx * q2.y + gy * q2.x + gz * q1.z);
+                    const float gfx = wm * grx, gfy = wm * gry, gfz = wm * grz;
+                    c[0] += wm; c[1] += w * q0.y; c[2] += w * q0.z; c[3] += w * q0.w;
+                    c[4] += fx + gfx; c[5] += fy + gfy; c[6] += fz + gfz;
+                    const int of = __float_as_int(q2.w);
+                    const int obj = of & 0xFFFF;
+                    const float gr = (of >> 16) ? 0.f : 1.f;  // body fields: no gravity on rigid particles
+                    const int sel = (bp.x == obj) ? 0 : ((bp.y == obj) ? 1 : -1);
+                    if (sel == 0) {
+                        b0[0] += wm; b0[1] += w * q0.y; b0[2] += w * q0.z; b0[3] += w * q0.w;
+                        b0[4] += fx + gr * gfx; b0[5] += fy + gr * gfy; b0[6] += fz + gr * gfz;
+                        b0[7] += gx * q2.z; b0[8] += gy * q2.z; b0[9] += gz * q2.z;
+                    } else if (sel == 1) {
+                        b1[0] += wm; b1[1] += w * q0.y; b1[2] += w * q0.z; b1[3] += w * q0.w;
+                        b1[4] += fx + gr * gfx; b1[5] += fy + gr * gfy; b1[6] += fz + gr * gfz;
+                        b1[7] += gx * q2.z; b1[8] += gy * q2.z; b1[9] += gz * q2.z;
+                    }
+                }
+                if (!scatter_lane) continue;
+                if (c[0] != 0.f) {
+#pragma unroll
+                    for (int f = 0; f < 7; f++) atomicAdd(&tile[f * PT_NODES + t], c[f]);
+                }
+                if (b0[0] != 0.f) {
+#pragma unroll
+                    for (int f = 0; f < 10; f++) atomicAdd(&tile[(7 + f) * PT_NODES + t], b0[f]);
+                }
+                if (b1[0] != 0.f) {
+#pragma unroll
+                    for (int f = 0; f < 10; f++) atomicAdd(&tile[(17 + f) * PT_NODES + t], b1[f]);
+                }
+            }
+            if (cnt < P2G_CH) break;
+        }
+        __syncthreads();
+        // ---- flush: COM fields and the touched body slots, vector reductions ----
+        for (int t = tid; t < PT_NODES; t += P2G_CH) {
+            const int ni = tox + t % PT, nj = toy + (t / PT) % PT, nk = toz + t / (PT * PT);
+            if (ni >= g.nx || nj >= g.ny || nk >= g.nz) continue;
+            const float m = tile[t];
+            if (m == 0.f) continue;
+            const int nd = node_index(ni, nj, nk, g);
+            const float *f = tile + t;
+            red_add4(&nb.acc0[nd], f[0], f[PT_NODES], f[2 * PT_NODES], f[3 * PT_NODES]);
+            red_add4(&nb.acc1[nd], f[4 * PT_NODES], f[5 * PT_NODES], f[6 * PT_NODES], 0.f);
+#pragma unroll
+            for (int sl = 0; sl < 2; sl++) {
+                const float *b = f + (7 + 10 * sl) * PT_NODES;
+                if (b[0] == 0.f) continue;
+                red_add4(&nb.bacc0[sl][nd], b[0], b[PT_NODES], b[2 * PT_NODES], b[3 * PT_NODES]);
+                red_add4(&nb.bacc1[sl][nd], b[4 * PT_NODES], b[5 * PT_NODES], b[6 * PT_NODES], 0.f);
+                red_add4(&nb.bnrm[sl][nd], b[7 * PT_NODES], b[8 * PT_NODES], b[9 * PT_NODES], 0.f);
+            }
+            mark_node(nb, ni, nj, nk, g);
+        }
+    }
+}
+
 void launch_p2g(const PView &p, const int *perm, const int *skey, long long n, const int *seg_start,
                 const int *nseg, int persist_grid, const NodeBufs &nb, const StepArgs &a, cudaStream_t s)
 {
     if (n == 0) return;
     if (a.multi_body) {
-        k_p2g_multi<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p, perm, n, nb, a);
+        static int mgrid = 0;  // persistent grid of the multi-body kernel (its own occupancy)
+        if (mgrid == 0) {
+            int dev = 0, sms = 1, b = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_p2g_multi_tiled, P2G_CH, 0);
+            mgrid = sms * std::max(b, 1);
+        }
+        k_p2g_multi_tiled<<<mgrid, P2G_CH, 0, s>>>(p, perm, skey, n, seg_start, nseg, perm ? 1 : 0, nb, a);
     } else {
         k_p2g_tiled<<<persist_grid, P2G_CH, 0, s>>>(p, perm, skey, n, seg_start, nseg, perm ? 1 : 0, nb, a.g);
     }

@@ -780,9 +780,9 @@ __device__ __forceinline__ bool solve_node(const NodeBufs &nb, const StepArgs &a
     bool active = false;
     {
         const int lx = lnode & 3, ly = (lnode >> 2) & 3, lz = (lnode >> 4) & 3;
-        const int bx = (int)(blk % g.nnbx);
-        const long long tb = blk / g.nnbx;
-        const int by = (int)(tb % g.nnby), bz = (int)(tb / g.nnby);
+        const int b32 = (int)blk;  // node blocks < 2^31
+        const int bx = b32 % g.nnbx, tb = b32 / g.nnbx;
+        const int by = tb % g.nnby, bz = tb / g.nnby;
         const int i = bx * 4 + lx, j = by * 4 + ly, k = bz * 4 + lz;
         if (i < g.nx && j < g.ny && k < g.nz) {
             const int nd = node_index(i, j, k, g);
@@ -1021,8 +1021,8 @@ __global__ void k_compact_active(NodeBufs nb, int nnb)
     }
 }
 
-// One warp per active node block from the list P2G and the fold built; the block's 64
-// nodes take two passes of the warp, then its flag is cleared for the next step.
+// Multi-body nodal solve with contact: two warps per active node block from the list P2G
+// and the fold built (32 nodes each); the block's flag is cleared for the next step.
 template <bool MULTI>
 __global__ void __launch_bounds__(256) k_solve_list(NodeBufs nb, StepArgs a, int keep)
 {
@@ -1031,12 +1031,11 @@ __global__ void __launch_bounds__(256) k_solve_list(NodeBufs nb, StepArgs a, int
     const int nw = (int)((gridDim.x * blockDim.x) >> 5);
     const int nact = *nb.active_n;
     int count = 0;
-    for (int w = gw; w < nact; w += nw) {
-        const long long blk = nb.active_list[w];
-        count += solve_node<MULTI>(nb, a, keep, blk, lane) ? 1 : 0;
-        count += solve_node<MULTI>(nb, a, keep, blk, lane + 32) ? 1 : 0;
-        __syncwarp();
-        if (lane == 0) nb.flags[blk] = 0;
+    // one warp per half block (32 nodes), so the two halves' loads are in flight together
+    for (int w = gw; w < 2 * nact; w += nw) {
+        const long long blk = nb.active_list[w >> 1];
+        count += solve_node<MULTI>(nb, a, keep, blk, lane + 32 * (w & 1)) ? 1 : 0;
+        if (lane == 0 && (w & 1) == 0) nb.flags[blk] = 0;
     }
     if (nb.active_count) {
         for (int off = 16; off > 0; off >>= 1) count += __shfl_down_sync(0xffffffffu, count, off);
@@ -1484,6 +1483,171 @@ __global__ void __launch_bounds__(GY_G2P_THREADS, GY_G2P_MINB) k_g2p_tiled(PView
     }
 }
 
+// Multi-body G2P + update through a shared-memory node tile: per node the body pair (or
+// none when the node has no mass, so it is skipped, Extrapolation.cpp:301-303) and both body
+// slots' solved fields; each particle reads the slot of its own object (Extrapolation.cpp:
+// 311-355), with the weight zeroed where the node holds neither of its bodies.
+template <bool HAS_DP, bool NRM>
+__global__ void __launch_bounds__(GY_G2P_THREADS) k_g2p_multi_tiled(PView src, PView dst, const int *perm,
+                                                                    const int *skey, long long n,
+                                                                    const int *seg_start, const int *nseg_ptr,
+                                                                    int sorted, NodeBufs nb, StepArgs a,
+                                                                    int check_finite)
+{
+    constexpr int NST = G2P_NBASE + (HAS_DP ? G2P_NDP : 0);
+    __shared__ int2 TP[PT_NODES];
+    __shared__ float4 TVb[2][PT_NODES];  // (m, v1) per body slot
+    __shared__ float4 TAb[2][PT_NODES];  // (a1, -) per body slot
+    __shared__ float4 TN[NRM ? 2 : 1][NRM ? PT_NODES : 1];
+    __shared__ float stage[NST][GY_G2P_THREADS];
+    __shared__ long long s_end;
+    const GridGeom &g = a.g;
+    const int nseg = *nseg_ptr;
+    const int tid = threadIdx.x;
+    for (int sgi = blockIdx.x; sgi < nseg; sgi += gridDim.x) {
+        const long long start = seg_start[sgi];
+        const int blk = seg_block(skey, start);
+        int bx, by, bz;
+        decode_block(blk, g, bx, by, bz);
+        const int tox = bx * CB, toy = by * CB, toz = g.is3d ? bz * CB : 0;
+        __syncthreads();  // the previous segment's particles are done with the tile
+        for (int t = tid; t < PT_NODES; t += blockDim.x) {
+            const int ni = tox + t % PT, nj = toy + (t / PT) % PT, nk = toz + t / (PT * PT);
+            int2 pr = make_int2(-1, -1);
+            const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+            float4 v0 = z4, v1 = z4, a0 = z4, a1 = z4, n0 = z4, n1 = z4;
+            if (ni < g.nx && nj < g.ny && nk < g.nz) {
+                const int nd = node_index(ni, nj, nk, g);
+                if (__ldg(&nb.gv[nd].x) != 0.0f) {
+                    pr = __ldg(&nb.body[nd]);
+                    v0 = __ldg(&nb.bgv[0][nd]);
+                    v1 = __ldg(&nb.bgv[1][nd]);
+                    a0 = __ldg(&nb.bga[0][nd]);
+                    a1 = __ldg(&nb.bga[1][nd]);
+                    if (NRM) {
+                        n0 = __ldg(&nb.nrm_out[0][nd]);
+                        n1 = __ldg(&nb.nrm_out[1][nd]);
+                    }
+                }
+            }
+            TP[t] = pr;
+            TVb[0][t] = v0;
+            TVb[1][t] = v1;
+            TAb[0][t] = a0;
+            TAb[1][t] = a1;
+            if (NRM) {
+                TN[0][t] = n0;
+                TN[1][t] = n1;
+            }
+        }
+        for (long long base = start;; base += blockDim.x) {
+            int cnt, key = 0;
+            long long j = 0;
+            const long long i = base + tid;
+            if (sorted) {
+                const bool inr = i < n;
+                key = inr ? skey[i] : -1;
+                j = inr ? perm[i] : 0;
+                cnt = __syncthreads_count(inr && (key >> CB_SHIFT) == blk);
+            } else {
+                cnt = (int)min((long long)blockDim.x, segment_chunk_end(skey, n, blk, base, blockDim.x, &s_end) - base);
+                if (tid < cnt) key = skey[i];
+                j = i;
+            }
+            if (cnt <= 0) break;
+            if (tid < cnt) {
+                PState st;
+                st.key = key;
+#pragma unroll
+                for (int k = 0; k < 3; k++) st.o[k] = src.f(PF_OX + k, j);
+                const int obj = info_obj((uint32_t)src.ii(PF_INFO, j));
+#pragma unroll
+                for (int f = 0; f < NST; f++) cp_async4(&stage[f][tid], &src.f(g2p_stage_field(f), j));
+                cp_async_commit();
+                float S[3][3], G[3][3];
+                gimp_axis(st.o[0], g, S[0], G[0]);
+                gimp_axis(st.o[1], g, S[1], G[1]);
+                if (g.is3d) {
+                    gimp_axis(st.o[2], g, S[2], G[2]);
+                } else {
+                    S[2][0] = 1.f; S[2][1] = 0.f; S[2][2] = 0.f; G[2][0] = 0.f; G[2][1] = 0.f; G[2][2] = 0.f;
+                }
+                const int lc = st.key & 63;
+                const int t0 = ((lc >> 4) * PT + ((lc >> 2) & 3)) * PT + (lc & 3);
+                float acc[3] = {0.f, 0.f, 0.f}, vg[3] = {0.f, 0.f, 0.f};
+                float L[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+                float nrm[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+                for (int kk = 0; kk < 3; kk++) {
+                    if (kk > 0 && !g.is3d) break;
+#pragma unroll
+                    for (int jj = 0; jj < 3; jj++) {
+                        const float syz = S[1][jj] * S[2][kk];
+                        const float gyz = G[1][jj] * S[2][kk] * g.inv_h, syg = S[1][jj] * G[2][kk] * g.inv_h;
+#pragma unroll
+                        for (int ii = 0; ii < 3; ii++) {
+                            const int t = t0 + (kk * PT + jj) * PT + ii;
+                            const int2 pr = TP[t];
+                            const int slot = (pr.x == obj) ? 0 : ((pr.y == obj) ? 1 : -1);
+                            const int sl = slot > 0 ? 1 : 0;
+                            const float on = slot >= 0 ? 1.f : 0.f;  // a third body sees nothing here
+                            const float4 Vb = TVb[sl][t], Ab = TAb[sl][t];
+                            const float wgt = S[0][ii] * syz * on;
+                            const float gx = G[0][ii] * syz * g.inv_h * on, gy = S[0][ii] * gyz * on;
+                            const float gz = S[0][ii] * syg * on;
+                            acc[0] += wgt * Ab.x; acc[1] += wgt * Ab.y; acc[2] += wgt * Ab.z;
+                            vg[0] += wgt * Vb.y; vg[1] += wgt * Vb.z; vg[2] += wgt * Vb.w;
+                            L[0][0] += Vb.y * gx; L[0][1] += Vb.y * gy; L[0][2] += Vb.y * gz;
+                            L[1][0] += Vb.z * gx; L[1][1] += Vb.z * gy; L[1][2] += Vb.z * gz;
+                            L[2][0] += Vb.w * gx; L[2][1] += Vb.w * gy; L[2][2] += Vb.w * gz;
+                            if (NRM) {
+                                const float4 N = TN[sl][t];
+                                nrm[0] += wgt * N.x; nrm[1] += wgt * N.y; nrm[2] += wgt * N.z;
+                            }
+                        }
+                    }
+                }
+                cp_async_wait_all();
+#pragma unroll
+                for (int k = 0; k < 3; k++) st.v[k] = stage[k][tid];
+#pragma unroll
+                for (int k = 0; k < 6; k++) {
+                    st.s[k] = stage[3 + k][tid];
+                    st.e[k] = stage[9 + k][tid];
+                }
+                st.rho = stage[15][tid];
+                st.mass = stage[16][tid];
+                st.info = __float_as_uint(stage[17][tid]);
+                st.pid = __float_as_int(stage[18][tid]);
+                if (HAS_DP) {
+                    st.eqps = stage[G2P_NBASE + (HAS_DP ? 0 : 0)][tid];
+#pragma unroll
+                    for (int k = 0; k < 6; k++) st.ep[k] = stage[G2P_NBASE + (HAS_DP ? 1 + k : 0)][tid];
+                    st.dmg = stage[G2P_NBASE + (HAS_DP ? 7 : 0)][tid];
+                    st.smax = stage[G2P_NBASE + (HAS_DP ? 8 : 0)][tid];
+                } else {
+                    st.eqps = 0.f;
+#pragma unroll
+                    for (int k = 0; k < 6; k++) st.ep[k] = 0.f;
+                    st.dmg = 0.f;
+                    st.smax = 0.f;
+                }
+                int c0[3];
+                decode_key(st.key, g, c0[0], c0[1], c0[2]);
+                if (!g.is3d) c0[2] = 0;
+                update_after_g2p<HAS_DP>(st, c0, acc, vg, L, a, check_finite != 0);
+                store_state<HAS_DP>(dst, i, st);
+                if (NRM) {
+                    dst.f(PF_NX, i) = nrm[0];
+                    dst.f(PF_NY, i) = nrm[1];
+                    dst.f(PF_NZ, i) = nrm[2];
+                }
+            }
+            if (cnt < (int)blockDim.x) break;
+        }
+    }
+}
+
 int g2p_blocks_per_sm(bool has_dp)
 {
     int b = 0;
@@ -1500,8 +1664,30 @@ void launch_g2p_update(const PView &src, const PView &dst, const int *perm, cons
     const unsigned grid = (unsigned)((n + 255) / 256);
     const int tn = track_normals ? 1 : 0, cf = check_finite ? 1 : 0;
     if (a.multi_body) {
-        if (has_dp) k_g2p_update<true, true><<<grid, 256, 0, s>>>(src, dst, perm, n, nb, a, tn, cf);
-        else k_g2p_update<true, false><<<grid, 256, 0, s>>>(src, dst, perm, n, nb, a, tn, cf);
+        const int srt = perm ? 1 : 0;
+        (void)grid;
+        static int mgrid[4] = {0, 0, 0, 0};  // persistent grids of the four multi-body variants
+        const int vi = (has_dp ? 2 : 0) + (tn ? 1 : 0);
+        if (mgrid[vi] == 0) {
+            int dev = 0, sms = 1, b = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            const void *k = vi == 3 ? (const void *)k_g2p_multi_tiled<true, true>
+                          : vi == 2 ? (const void *)k_g2p_multi_tiled<true, false>
+                          : vi == 1 ? (const void *)k_g2p_multi_tiled<false, true>
+                                    : (const void *)k_g2p_multi_tiled<false, false>;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, GY_G2P_THREADS, 0);
+            mgrid[vi] = sms * std::max(b, 1);
+        }
+        const unsigned mg = (unsigned)mgrid[vi];
+        if (has_dp && tn)
+            k_g2p_multi_tiled<true, true><<<mg, GY_G2P_THREADS, 0, s>>>(src, dst, perm, skey, n, seg_start, nseg, srt, nb, a, cf);
+        else if (has_dp)
+            k_g2p_multi_tiled<true, false><<<mg, GY_G2P_THREADS, 0, s>>>(src, dst, perm, skey, n, seg_start, nseg, srt, nb, a, cf);
+        else if (tn)
+            k_g2p_multi_tiled<false, true><<<mg, GY_G2P_THREADS, 0, s>>>(src, dst, perm, skey, n, seg_start, nseg, srt, nb, a, cf);
+        else
+            k_g2p_multi_tiled<false, false><<<mg, GY_G2P_THREADS, 0, s>>>(src, dst, perm, skey, n, seg_start, nseg, srt, nb, a, cf);
     } else {
         const int srt = perm ? 1 : 0;
         if (has_dp)

@@ -789,6 +789,22 @@ __device__ __forceinline__ bool solve_node(const NodeBufs &nb, const StepArgs &a
             const float4 A0 = nb.acc0[nd];
             float4 A1 = nb.acc1[nd];
             const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+            // every load of the node is issued before the first store (the accumulators are
+            // cleared after they were read)
+            float4 B0[2], B1[2], BN[2];
+            int2 body = make_int2(-1, -1);
+            unsigned char hr = 0;
+            if (MULTI) {
+#pragma unroll
+                for (int b = 0; b < 2; b++) {
+                    B0[b] = nb.bacc0[b][nd];
+                    B1[b] = nb.bacc1[b][nd];
+                    BN[b] = nb.bnrm[b][nd];
+                }
+                body = nb.body[nd];
+                hr = nb.has_rigid[nd];
+            }
+            const int bt = nb.bc_type ? nb.bc_type[nd] : 0;
             nb.acc0[nd] = z4;
             nb.acc1[nd] = z4;
             const float m = A0.x;
@@ -810,11 +826,8 @@ __device__ __forceinline__ bool solve_node(const NodeBufs &nb, const StepArgs &a
                     body_update(m, A0, A1, dtn, v1, a1);
                 }
             } else {
-                float4 B0[2], B1[2], BN[2];
+#pragma unroll
                 for (int b = 0; b < 2; b++) {
-                    B0[b] = nb.bacc0[b][nd];
-                    B1[b] = nb.bacc1[b][nd];
-                    BN[b] = nb.bnrm[b][nd];
                     nb.bacc0[b][nd] = z4;
                     nb.bacc1[b][nd] = z4;
                     nb.bnrm[b][nd] = z4;
@@ -825,8 +838,6 @@ __device__ __forceinline__ bool solve_node(const NodeBufs &nb, const StepArgs &a
                     if (mag1 > 1e-8f) { n1[0] = BN[0].x / mag1; n1[1] = BN[0].y / mag1; n1[2] = BN[0].z / mag1; }
                     const float n2[3] = {-n1[0], -n1[1], -n1[2]};  // Grid.cpp:45-47
                     const float m1 = B0[0].x, m2 = B0[1].x;
-                    const int2 body = nb.body[nd];
-                    const unsigned char hr = nb.has_rigid[nd];
                     if (body.y != -1) {
                         float ap1 = 0.f, ap2 = 0.f, rv1[3] = {0.f, 0.f, 0.f}, rv2[3] = {0.f, 0.f, 0.f};
                         if (m1 != 0.0f) {
@@ -892,7 +903,6 @@ __device__ __forceinline__ bool solve_node(const NodeBufs &nb, const StepArgs &a
             }
             // grid BC, phase 2 (phase 1 is overwritten by the solve for every node the
             // particles read; phase 3 repeats phase 2)
-            const int bt = nb.bc_type ? nb.bc_type[nd] : 0;
             if (bt) {
                 BCApply bc{bt, nb.bc_val[nd], a.sc->fixed_grid_bcs};
                 bool set[3];

@@ -6,14 +6,15 @@
 //   fold      periodic node-layer fold of the accumulated P2G fields (Grid.cpp:310-795);
 //   P2G       one CTA per segment: particles of a run of equal cell are summed in registers
 //             by one warp (lane = stencil node) into a shared-memory node tile, flushed with
-//             vector reductions (Extrapolation.cpp:166-286); multi-body problems scatter per
-//             particle into the centre-of-mass and body-slot fields;
+//             vector reductions (Extrapolation.cpp:166-286); multi-body problems keep the
+//             centre-of-mass and both body-slot fields in the tile;
 //   solve     nodal momentum update + grid BCs over the active 4x4x4 node blocks only
 //             (Grid.cpp:9-245, 862-1094); it also clears the accumulators it read;
-//   G2P       one pass over the particles in sorted order: G2P (Extrapolation.cpp:127-163,
-//             288-367), particle BCs (TimeIntegration.cpp:177-296), update + constitutive +
-//             damage + wrap (TimeIntegration.cpp:11-117), the state written to the other
-//             slab in sorted order.
+//   G2P       one CTA per segment over a shared-memory tile of the solved nodes, a thread
+//             per particle in sorted order: G2P (Extrapolation.cpp:127-163, 288-367), particle
+//             BCs (TimeIntegration.cpp:177-296), update + constitutive + damage + wrap
+//             (TimeIntegration.cpp:11-117), the state written to the other slab in sorted
+//             order.
 //
 // P2G is a particle-centric scatter: the reference gathers per node over a 4x4x4 cell
 // window (Extrapolation.cpp:31-125), but a particle contributes exactly to the nodes of its
@@ -56,39 +57,6 @@ struct PState {
 };
 
 template <bool HAS_DP>
-__device__ __forceinline__ void load_state(const PView &P, long long j, PState &st)
-{
-    st.key = P.ii(PF_KEY, j);
-    st.info = (uint32_t)P.ii(PF_INFO, j);
-    st.pid = P.ii(PF_PID, j);
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-        st.o[k] = P.f(PF_OX + k, j);
-        st.v[k] = P.f(PF_VX + k, j);
-    }
-#pragma unroll
-    for (int k = 0; k < 6; k++) {
-        st.s[k] = P.f(PF_S0 + k, j);
-        st.e[k] = P.f(PF_E0 + k, j);
-    }
-    st.rho = P.f(PF_RHO, j);
-    st.mass = P.f(PF_MASS, j);
-    if (HAS_DP) {
-        st.eqps = P.f(PF_EQPS, j);
-#pragma unroll
-        for (int k = 0; k < 6; k++) st.ep[k] = P.f(PF_EP0 + k, j);
-        st.dmg = P.f(PF_DMG, j);
-        st.smax = P.f(PF_SMAX, j);
-    } else {
-        st.eqps = 0.f;
-#pragma unroll
-        for (int k = 0; k < 6; k++) st.ep[k] = 0.f;
-        st.dmg = 0.f;
-        st.smax = 0.f;
-    }
-}
-
-template <bool HAS_DP>
 __device__ __forceinline__ void store_state(const PView &P, long long i, const PState &st)
 {
     P.ii(PF_KEY, i) = st.key;
@@ -115,33 +83,6 @@ __device__ __forceinline__ void store_state(const PView &P, long long i, const P
     }
 }
 
-// register-array element with a run-time index, without spilling the array to local memory
-__device__ __forceinline__ float sel3(const float a[3], int i) { return i == 0 ? a[0] : (i == 1 ? a[1] : a[2]); }
-
-// GIMP weights of a particle: S/G per axis and how many stencil nodes carry weight
-struct Stencil {
-    int c[3];
-    float S[3][3], G[3][3];
-    int cnt[3];
-};
-
-__device__ __forceinline__ void make_stencil(const PState &st, const GridGeom &g, Stencil &w)
-{
-    decode_key(st.key, g, w.c[0], w.c[1], w.c[2]);
-    gimp_axis(st.o[0], g, w.S[0], w.G[0]);
-    gimp_axis(st.o[1], g, w.S[1], w.G[1]);
-    w.cnt[0] = (st.o[0] < 1.0f - g.lp) ? 2 : 3;
-    w.cnt[1] = (st.o[1] < 1.0f - g.lp) ? 2 : 3;
-    if (g.is3d) {
-        gimp_axis(st.o[2], g, w.S[2], w.G[2]);
-        w.cnt[2] = (st.o[2] < 1.0f - g.lp) ? 2 : 3;
-    } else {
-        w.c[2] = 0;
-        w.S[2][0] = 1.f; w.S[2][1] = 0.f; w.S[2][2] = 0.f;
-        w.G[2][0] = 0.f; w.G[2][1] = 0.f; w.G[2][2] = 0.f;
-        w.cnt[2] = 1;
-    }
-}
 
 // ---------------------------------------------------------------------------------------
 // Single-body P2G through a shared-memory node tile.  Gravity is added per node in the
@@ -400,60 +341,6 @@ __global__ void GY_P2G_BOUNDS k_p2g_tiled(PView P, const int *perm, const int *s
         }
         __syncthreads();
     }
-}
-
-// Multi-body P2G: centre-of-mass fields plus the particle's body slot (Extrapolation.cpp:
-// 191-256): per-body gravity skips rigid particles, normals use the stored volume.
-__global__ void __launch_bounds__(256) k_p2g_multi(PView P, const int *perm, long long n, NodeBufs nb, StepArgs a)
-{
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const GridGeom &g = a.g;
-    PState st;
-    load_state<false>(P, perm ? perm[i] : i, st);
-    Stencil w;
-    make_stencil(st, g, w);
-    const bool rigid = (st.info & INFO_RIGID) != 0;
-    // P2G takes a rigid particle's mass as 1 in 2D and 3D (Extrapolation.cpp:183); in 2D the
-    // stored mass stays rho psep^2 (Solver.cpp:58-66) and still sets the stored volume
-    const float m = rigid ? 1.0f : st.mass;
-    const float Vf = m / st.rho;
-    const float sc = Vf * g.inv_h;
-    const float s0 = st.s[0] * sc, s1 = st.s[1] * sc, s2 = st.s[2] * sc;
-    const float s3 = st.s[3] * sc, s4 = st.s[4] * sc, s5 = st.s[5] * sc;
-    const float mgx = m * a.sc->gravity[0], mgy = m * a.sc->gravity[1], mgz = m * a.sc->gravity[2];
-    const int obj = info_obj(st.info);
-    const float vol_n = ((st.info & INFO_INIT_VOL) ? a.sc->init_volume : st.mass / st.rho) * g.inv_h;
-#pragma unroll
-    for (int kk = 0; kk < 3; kk++)
-#pragma unroll
-        for (int jj = 0; jj < 3; jj++)
-#pragma unroll
-            for (int ii = 0; ii < 3; ii++) {
-                if (kk >= w.cnt[2] || jj >= w.cnt[1] || ii >= w.cnt[0]) continue;
-                const float syz = w.S[1][jj] * w.S[2][kk];
-                const float wgt = w.S[0][ii] * syz;
-                const float gx = w.G[0][ii] * syz;
-                const float gy = w.S[0][ii] * w.G[1][jj] * w.S[2][kk];
-                const float gz = w.S[0][ii] * w.S[1][jj] * w.G[2][kk];
-                const int ni = w.c[0] + ii, nj = w.c[1] + jj, nk = w.c[2] + kk;
-                const int nd = node_index(ni, nj, nk, g);
-                const float wm = wgt * m;
-                const float fx = -(gx * s0 + gy * s3 + gz * s5);
-                const float fy = -(gx * s3 + gy * s1 + gz * s4);
-                const float fz = -(gx * s5 + gy * s4 + gz * s2);
-                red_add4(&nb.acc0[nd], wm, wm * st.v[0], wm * st.v[1], wm * st.v[2]);
-                red_add4(&nb.acc1[nd], fx + wgt * mgx, fy + wgt * mgy, fz + wgt * mgz, 0.0f);
-                const int2 b = nb.body[nd];
-                const int slot = (b.x == obj) ? 0 : ((b.y == obj) ? 1 : -1);
-                if (slot >= 0) {
-                    red_add4(&nb.bacc0[slot][nd], wm, wm * st.v[0], wm * st.v[1], wm * st.v[2]);
-                    if (rigid) red_add4(&nb.bacc1[slot][nd], fx, fy, fz, 0.0f);
-                    else red_add4(&nb.bacc1[slot][nd], fx + wgt * mgx, fy + wgt * mgy, fz + wgt * mgz, 0.0f);
-                    red_add4(&nb.bnrm[slot][nd], gx * vol_n, gy * vol_n, gz * vol_n, 0.0f);
-                }
-                mark_node(nb, ni, nj, nk, g);
-            }
 }
 
 // Multi-body P2G through a shared-memory node tile: the tiled scheme of k_p2g_tiled with one
@@ -1216,81 +1103,6 @@ __device__ __forceinline__ void update_after_g2p(PState &st, const int c0[3], fl
     st.info &= ~INFO_INIT_VOL;
 }
 
-template <bool MULTI, bool HAS_DP>
-__device__ __forceinline__ void g2p_update_one(PState &st, const NodeBufs &nb, const StepArgs &a, bool track_normals,
-                                               bool check_finite, float nrm[3])
-{
-    const GridGeom &g = a.g;
-    Stencil w;
-    make_stencil(st, g, w);
-    const int obj = info_obj(st.info);
-
-    // ---- G2P (Extrapolation.cpp:288-367) ----
-    float acc[3] = {0.f, 0.f, 0.f}, vg[3] = {0.f, 0.f, 0.f};
-    float L[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};  // L[a][b] = sum v_a dW/dx_b
-    nrm[0] = nrm[1] = nrm[2] = 0.f;
-#pragma unroll
-    for (int kk = 0; kk < 3; kk++)
-#pragma unroll
-        for (int jj = 0; jj < 3; jj++) {
-            if (kk >= w.cnt[2] || jj >= w.cnt[1]) continue;
-            const float syz = w.S[1][jj] * w.S[2][kk];
-            const float gyz = w.G[1][jj] * w.S[2][kk] * g.inv_h, syg = w.S[1][jj] * w.G[2][kk] * g.inv_h;
-#pragma unroll
-            for (int ii = 0; ii < 3; ii++) {
-                if (ii >= w.cnt[0]) continue;
-                const int nd = node_index(w.c[0] + ii, w.c[1] + jj, w.c[2] + kk, g);
-                const float4 V = __ldg(&nb.gv[nd]);
-                if (V.x == 0.0f) continue;  // nodes without mass are skipped
-                float4 Vb, Ab;
-                int slot = 0;
-                if (!MULTI) {
-                    Vb = V;
-                    Ab = __ldg(&nb.ga[nd]);
-                } else {
-                    const int2 b = __ldg(&nb.body[nd]);
-                    slot = (b.x == obj) ? 0 : ((b.y == obj) ? 1 : -1);
-                    if (slot < 0) continue;  // a third body sees nothing from this node
-                    Vb = __ldg(&nb.bgv[slot][nd]);
-                    Ab = __ldg(&nb.bga[slot][nd]);
-                }
-                const float wgt = w.S[0][ii] * syz;
-                const float gx = w.G[0][ii] * syz * g.inv_h, gy = w.S[0][ii] * gyz, gz = w.S[0][ii] * syg;
-                acc[0] += wgt * Ab.x; acc[1] += wgt * Ab.y; acc[2] += wgt * Ab.z;
-                vg[0] += wgt * Vb.y; vg[1] += wgt * Vb.z; vg[2] += wgt * Vb.w;
-                L[0][0] += Vb.y * gx; L[0][1] += Vb.y * gy; L[0][2] += Vb.y * gz;
-                L[1][0] += Vb.z * gx; L[1][1] += Vb.z * gy; L[1][2] += Vb.z * gz;
-                L[2][0] += Vb.w * gx; L[2][1] += Vb.w * gy; L[2][2] += Vb.w * gz;
-                if (MULTI && track_normals) {
-                    const float4 N = __ldg(&nb.nrm_out[slot][nd]);
-                    nrm[0] += wgt * N.x; nrm[1] += wgt * N.y; nrm[2] += wgt * N.z;
-                }
-            }
-        }
-
-    update_after_g2p<HAS_DP>(st, w.c, acc, vg, L, a, check_finite);
-}
-
-// Unfused G2P + update: one thread per particle in sorted order, state read through perm
-// and written to the other slab.
-template <bool MULTI, bool HAS_DP>
-__global__ void __launch_bounds__(256, 3) k_g2p_update(PView src, PView dst, const int *perm, long long n, NodeBufs nb,
-                                                    StepArgs a, int track_normals, int check_finite)
-{
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    PState st;
-    load_state<HAS_DP>(src, perm ? perm[i] : i, st);
-    float nrm[3];
-    g2p_update_one<MULTI, HAS_DP>(st, nb, a, track_normals != 0, check_finite != 0, nrm);
-    store_state<HAS_DP>(dst, i, st);
-    if (track_normals) {
-        dst.f(PF_NX, i) = nrm[0];
-        dst.f(PF_NY, i) = nrm[1];
-        dst.f(PF_NZ, i) = nrm[2];
-    }
-}
-
 // G2P CTA size and the resident CTAs per SM it is register-limited to (64 registers)
 #ifndef GY_G2P_MINB
 #define GY_G2P_MINB 16
@@ -1671,11 +1483,9 @@ void launch_g2p_update(const PView &src, const PView &dst, const int *perm, cons
                        bool track_normals, bool check_finite, bool has_dp, cudaStream_t s)
 {
     if (n == 0) return;
-    const unsigned grid = (unsigned)((n + 255) / 256);
     const int tn = track_normals ? 1 : 0, cf = check_finite ? 1 : 0;
     if (a.multi_body) {
         const int srt = perm ? 1 : 0;
-        (void)grid;
         static int mgrid[4] = {0, 0, 0, 0};  // persistent grids of the four multi-body variants
         const int vi = (has_dp ? 2 : 0) + (tn ? 1 : 0);
         if (mgrid[vi] == 0) {

@@ -300,14 +300,20 @@ __global__ void GY_P2G_BOUNDS k_p2g_tiled(PView P, const int *perm, const int *s
                 const int cell = cellof[p0];
                 P2GAcc A;
                 A.m = A.px = A.py = A.pz = A.fx = A.fy = A.fz = make_float2(0.f, 0.f);
-                int p = p0;
-                if (p & 1) {  // an odd start: the second particle of its pair alone
-                    p2g_single<1>(A, W, Q, p >> 1, ii, jj, kk);
-                    p++;
-                }
+                if (p1 - p0 == 8 && !(p0 & 1)) {
+                    // a full cell (psep = cellsize / 2) on a pair boundary: four pairs, unrolled
+#pragma unroll
+                    for (int k = 0; k < 4; k++) p2g_pair(A, W, Q, (p0 >> 1) + k, ii, jj, kk);
+                } else {
+                    int p = p0;
+                    if (p & 1) {  // an odd start: the second particle of its pair alone
+                        p2g_single<1>(A, W, Q, p >> 1, ii, jj, kk);
+                        p++;
+                    }
 #pragma unroll 2
-                for (; p + 1 < p1; p += 2) p2g_pair(A, W, Q, p >> 1, ii, jj, kk);
-                if (p < p1) p2g_single<0>(A, W, Q, p >> 1, ii, jj, kk);
+                    for (; p + 1 < p1; p += 2) p2g_pair(A, W, Q, p >> 1, ii, jj, kk);
+                    if (p < p1) p2g_single<0>(A, W, Q, p >> 1, ii, jj, kk);
+                }
                 const float am = A.m.x + A.m.y, apx = A.px.x + A.px.y, apy = A.py.x + A.py.y;
                 const float apz = A.pz.x + A.pz.y;
                 const float afx = -(A.fx.x + A.fx.y), afy = -(A.fy.x + A.fy.y), afz = -(A.fz.x + A.fz.y);

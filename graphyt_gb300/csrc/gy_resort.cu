@@ -49,19 +49,31 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_mask(const int *key, const in
     }
 }
 
-// movers (key, slot) in slot order
+// movers (key, slot) in slot order.  A warp takes 32 words at once (one mask per lane) and
+// visits only the words that hold movers.
 __global__ void __launch_bounds__(RS_THREADS) k_rs_compact(const int *key, const unsigned *wmask, const int *wpref,
                                                              long long nw, int *bkey, int *bidx)
 {
     const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
     const long long wstride = ((long long)gridDim.x * blockDim.x) >> 5;
-    for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nw; w += wstride) {
-        const unsigned m = wmask[w];
-        if (!((m >> lane) & 1u)) continue;
-        const long long i = w * 32 + lane;
-        const int pos = wpref[w] + __popc(m & ((1u << lane) - 1u));
-        bkey[pos] = key[i];
-        bidx[pos] = (int)i;
+    for (long long w0 = (((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; w0 < nw; w0 += wstride * 32) {
+        const long long wl = w0 + lane;
+        const unsigned mk = wl < nw ? wmask[wl] : 0u;
+        const int pref = mk ? wpref[wl] : 0;
+        unsigned nz = __ballot_sync(0xffffffffu, mk != 0u);
+        while (nz) {
+            const int u = __ffs(nz) - 1;
+            nz &= nz - 1u;
+            const unsigned m = __shfl_sync(0xffffffffu, mk, u);
+            const int base = __shfl_sync(0xffffffffu, pref, u);
+            if ((m >> lane) & 1u) {
+                const long long i = (w0 + u) * 32 + lane;
+                const int pos = base + __popc(m & lt);
+                bkey[pos] = key[i];
+                bidx[pos] = (int)i;
+            }
+        }
     }
 }
 
@@ -193,44 +205,68 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_place_movers(const int *prev,
     }
 }
 
-// stayer r lands at r + (movers with gap <= r).  The stayer ranks of one warp's 32 slots lie
-// in at most two consecutive 32-gap words, whose counts the warp loads and prefix-sums.
+// stayer r lands at r + (movers with gap <= r).  A warp takes 32 words at once: their masks,
+// prefixes and gap-word data load one per lane; the keys load eight words ahead.  The stayer
+// ranks of one word lie in at most two consecutive 32-gap words, whose counts the warp loads
+// and prefix-sums only when they hold movers.
 __global__ void __launch_bounds__(RS_THREADS) k_rs_place_stayers(const int *key, long long n, const unsigned *wmask,
                                                                    const int *wpref, long long nw, const int *gapcnt,
                                                                    const int *gwcnt, const int *gwpref, int *skey_out,
                                                                    int *perm_out)
 {
     const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
     const long long wstride = ((long long)gridDim.x * blockDim.x) >> 5;
-    for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nw; w += wstride) {
-        const long long i = w * 32 + lane;
-        const int kv = i < n ? key[i] : 0;  // independent of the chain below: issued first
-        const unsigned m = wmask[w];
-        const long long rbase = w * 32 - wpref[w];  // rank of the warp's first stayer
-        const long long gw0 = rbase >> 5;
-        const int gbase = gwpref[gw0];
-        int c0 = 0, c1 = 0;
-        if (gwcnt[gw0] | gwcnt[gw0 + 1]) {  // movers in these gaps: per-gap counts, prefix-summed
-            c0 = gapcnt[gw0 * 32 + lane];
-            c1 = gapcnt[gw0 * 32 + 32 + lane];
+    for (long long w0 = (((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; w0 < nw; w0 += wstride * 32) {
+        const long long wl = w0 + lane;
+        const bool wv = wl < nw;
+        const unsigned mk = wv ? wmask[wl] : 0u;
+        const long long rb = wv ? wl * 32 - wpref[wl] : 0;  // rank of the word's first stayer
+        const long long gwl = rb >> 5;
+        const int gb = wv ? gwpref[gwl] : 0;
+        const int gc = wv ? (gwcnt[gwl] | gwcnt[gwl + 1]) : 0;
+        const int nwords = (int)min((long long)32, nw - w0);
+        for (int u0 = 0; u0 < nwords; u0 += 8) {
+            int kv[8];
 #pragma unroll
-            for (int off = 1; off < 32; off <<= 1) {
-                const int y0 = __shfl_up_sync(0xffffffffu, c0, off), y1 = __shfl_up_sync(0xffffffffu, c1, off);
-                if (lane >= off) {
-                    c0 += y0;
-                    c1 += y1;
+            for (int v = 0; v < 8; v++) {
+                const long long i = (w0 + u0 + v) * 32 + lane;
+                kv[v] = (u0 + v < nwords && i < n) ? key[i] : 0;
+            }
+#pragma unroll
+            for (int v = 0; v < 8; v++) {
+                const int u = u0 + v;
+                if (u >= nwords) break;  // warp-uniform
+                const unsigned m = __shfl_sync(0xffffffffu, mk, u);
+                const long long rbase = __shfl_sync(0xffffffffu, rb, u);
+                const long long gw0 = rbase >> 5;
+                int c0 = 0, c1 = 0;
+                if (__shfl_sync(0xffffffffu, gc, u)) {
+                    c0 = gapcnt[gw0 * 32 + lane];
+                    c1 = gapcnt[gw0 * 32 + 32 + lane];
+#pragma unroll
+                    for (int off = 1; off < 32; off <<= 1) {
+                        const int y0 = __shfl_up_sync(0xffffffffu, c0, off), y1 = __shfl_up_sync(0xffffffffu, c1, off);
+                        if (lane >= off) {
+                            c0 += y0;
+                            c1 += y1;
+                        }
+                    }
+                }
+                const int gbase = __shfl_sync(0xffffffffu, gb, u);
+                const int tot0 = __shfl_sync(0xffffffffu, c0, 31);
+                const long long i = (w0 + u) * 32 + lane;
+                const bool stay = i < n && !((m >> lane) & 1u);
+                const long long r = rbase + lane - __popc(m & lt);
+                const int rr = (int)(r - gw0 * 32);  // 0..62 for a stayer
+                const int in0 = __shfl_sync(0xffffffffu, c0, rr & 31), in1 = __shfl_sync(0xffffffffu, c1, rr & 31);
+                if (stay) {
+                    const long long pos = r + gbase + (rr < 32 ? in0 : tot0 + in1);
+                    skey_out[pos] = kv[v];
+                    perm_out[pos] = (int)i;
                 }
             }
         }
-        const int tot0 = __shfl_sync(0xffffffffu, c0, 31);
-        const bool stay = i < n && !((m >> lane) & 1u);
-        const long long r = rbase + lane - __popc(m & ((1u << lane) - 1u));
-        const int rr = (int)(r - gw0 * 32);  // 0..62 for a stayer
-        const int in0 = __shfl_sync(0xffffffffu, c0, rr & 31), in1 = __shfl_sync(0xffffffffu, c1, rr & 31);
-        if (!stay) continue;
-        const long long pos = r + gbase + (rr < 32 ? in0 : tot0 + in1);
-        skey_out[pos] = kv;
-        perm_out[pos] = (int)i;
     }
 }
 
@@ -292,11 +328,13 @@ void resort_keys(const int *key, const int *prev_skey, int *skey_out, int *perm_
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long long nw = (n + 31) / 32;
     const unsigned wgrid = (unsigned)std::min<long long>((nw + RS_WARPS - 1) / RS_WARPS, (long long)sms * 16);
+    const long long nw32 = (nw + 31) / 32;  // 32-word batches (compaction, stayer placement)
+    const unsigned bgrid = (unsigned)std::max<long long>(1, std::min<long long>((nw32 + RS_WARPS - 1) / RS_WARPS, (long long)sms * 16));
     const unsigned qgrid = (unsigned)std::min<long long>((n + RS_THREADS - 1) / RS_THREADS, (long long)sms * 8);
     k_rs_mask<<<wgrid, RS_THREADS, 0, s>>>(key, prev_skey, n, rs.wmask, rs.wcnt, nw);
     cudaMemsetAsync(rs.wcnt + nw, 0, sizeof(int), s);
     exclusive_scan_int(rs.wcnt, rs.wpref, nw + 1, rs.wscan_tmp, s);
-    k_rs_compact<<<wgrid, RS_THREADS, 0, s>>>(key, rs.wmask, rs.wpref, nw, rs.bkey, rs.bidx);
+    k_rs_compact<<<bgrid, RS_THREADS, 0, s>>>(key, rs.wmask, rs.wpref, nw, rs.bkey, rs.bidx);
     note_launch(2);
     // stable sort of the movers by key; their count is wpref[nw]
     const int G = std::min(2 * sms, RS_MAX_CTAS);
@@ -315,7 +353,7 @@ void resort_keys(const int *key, const int *prev_skey, int *skey_out, int *perm_
     k_rs_place_movers<<<qgrid, RS_THREADS, 0, s>>>(prev_skey, n, rs.wmask, rs.wpref, nw, kin, vin, rs.gap, rs.gapcnt,
                                                    rs.gwcnt, skey_out, perm_out);
     exclusive_scan_int(rs.gwcnt, rs.gwpref, rs.ngw + 1, rs.gscan_tmp, s);
-    k_rs_place_stayers<<<wgrid, RS_THREADS, 0, s>>>(key, n, rs.wmask, rs.wpref, nw, rs.gapcnt, rs.gwcnt, rs.gwpref,
+    k_rs_place_stayers<<<bgrid, RS_THREADS, 0, s>>>(key, n, rs.wmask, rs.wpref, nw, rs.gapcnt, rs.gwcnt, rs.gwpref,
                                                     skey_out, perm_out);
     k_rs_clear<<<qgrid, RS_THREADS, 0, s>>>(rs.gap, rs.wpref, nw, rs.gapcnt, rs.gwcnt);
     note_launch(3);

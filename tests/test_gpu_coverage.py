@@ -1,0 +1,80 @@
+"""GPU parity on paths the main parity file does not reach: the periodic node fold, the
+turbulent-liquid model, contact normals, the particle BC family, and multi-body problems
+between sorts.  Same tolerances as test_gpu_parity.py (FP32 GPU against the FP64 oracle)."""
+import numpy as np
+import pytest
+
+from graphyt_gb300 import scenes
+from tests.helpers import rel_l2, run_gpu, run_oracle
+
+pytestmark = pytest.mark.gpu
+
+ONE_STEP_TOL = 1e-5
+MANY_STEP_TOL = 1e-3
+
+
+def _compare(gpu, ref, fields, tol):
+    for f in fields:
+        a, b = gpu._get_particles(f), ref.pfield(f)
+        if np.linalg.norm(b) == 0:
+            assert np.max(np.abs(a)) < 1e-9, f
+        else:
+            assert rel_l2(a, b) <= tol, (f, rel_l2(a, b))
+
+
+def test_periodic_fold_seam(gpu_lib, oracle_built):
+    """A block whose stencils reach the last three node layers on every axis: their sums are
+    folded onto the first three (Grid.cpp:310-795) and read back by G2P.  The block stays
+    below the wrap threshold L - 2 cellsize, so no particle wraps (a wrapped particle is
+    invisible to the reference's P2G until its next sort)."""
+    sc = scenes.tiny_block(model=1, n_side=6)
+    sc.pos += np.array([0.35, 0.40, 0.40])
+    assert sc.pos.max() < sc.L[0] - 2 * sc.cellsize - 0.02
+    for steps, tol in ((2, ONE_STEP_TOL), (20, MANY_STEP_TOL)):
+        _compare(run_gpu(sc, steps), run_oracle(sc, steps), ("vel", "stress", "pos"), tol)
+
+
+def test_turbulent_liquid(gpu_lib, oracle_built):
+    """Material model 5, turbulentLiquid (ConstitutiveModels.cpp:66-126)."""
+    sc = scenes.tiny_block(model=5)
+    for steps, tol in ((2, ONE_STEP_TOL), (30, MANY_STEP_TOL)):
+        _compare(run_gpu(sc, steps), run_oracle(sc, steps), ("vel", "stress", "density"), tol)
+
+
+def test_contact_normals(gpu_lib, oracle_built):
+    """Two bodies in contact with per-particle contact normals kept (getNormalsArr,
+    Extrapolation.cpp:311-355)."""
+    sc = scenes.two_blocks()
+    gpu = run_gpu(sc, 12, options=dict(track_normals=1))
+    ref = run_oracle(sc, 12)
+    _compare(gpu, ref, ("vel", "stress"), MANY_STEP_TOL)
+    a, b = gpu._get_particles("normals"), ref.pfield("normals")
+    assert np.linalg.norm(b) > 0
+    assert rel_l2(a, b) <= MANY_STEP_TOL
+
+
+def test_particle_bc_family(gpu_lib, oracle_built):
+    """Velocity, force, sine-ramped and stress particle BCs (TimeIntegration.cpp:177-296) on
+    disjoint slices of one block."""
+    sc = scenes.tiny_block(model=1, n_side=8, gravity=(0.0, 0.0, -9.81))
+    x = sc.pos[:, 0]
+    edges = np.quantile(x, np.linspace(0, 1, 9))
+    kinds = [("mp_vx", (0.2, 0, 0, 0)), ("mp_vy", (-0.1, 0, 0, 0)), ("mp_fx", (3e-3, 0, 0, 0)),
+             ("mp_fz", (-2e-3, 0, 0, 0)), ("mp_vxsin", (0.1, 5.0, 0, 0)), ("mp_vx_vy", (0.05, -0.05, 0, 0)),
+             ("mp_fx_fy", (1e-3, 2e-3, 0, 0)), ("none", (0, 0, 0, 0))]
+    for k, (name, val) in enumerate(kinds):
+        sel = (x >= edges[k]) & (x <= edges[k + 1]) if k == len(kinds) - 1 else (x >= edges[k]) & (x < edges[k + 1])
+        sc.pbc_type[sel] = scenes.BC[name]
+        sc.pbc_val[sel] = val
+    for steps, tol in ((2, ONE_STEP_TOL), (15, MANY_STEP_TOL)):
+        _compare(run_gpu(sc, steps), run_oracle(sc, steps), ("vel", "stress", "pos"), tol)
+
+
+def test_multibody_between_sorts(gpu_lib):
+    """Multi-body contact with the particles re-ordered only every fourth step agrees with
+    sorting every step (the order is a performance choice)."""
+    sc = scenes.two_blocks()
+    a = run_gpu(sc, 14, options=dict(sort_every=1))
+    b = run_gpu(sc, 14, options=dict(sort_every=4))
+    for f in ("vel", "stress"):
+        assert rel_l2(a._get_particles(f), b._get_particles(f)) < 1e-5, f

@@ -78,3 +78,47 @@ def test_multibody_between_sorts(gpu_lib):
     b = run_gpu(sc, 14, options=dict(sort_every=4))
     for f in ("vel", "stress"):
         assert rel_l2(a._get_particles(f), b._get_particles(f)) < 1e-5, f
+
+
+def test_nonfinite_state_is_reported(gpu_lib):
+    """A particle whose velocity is not finite makes the step report GY_ERR_NONFINITE at the
+    next synchronisation (check_finite); the kernels' own clamps keep every index in range."""
+    from graphyt_gb300 import _lib, graphyt
+    sc = scenes.tiny_block(model=1)
+    sc.vel[0] = np.nan
+    with pytest.raises(_lib.GraphytGPUError) as e:
+        s = graphyt.from_scene(sc, options=dict(check_finite=1))
+        for k in range(3):
+            s.iterate_GPU(k * s.dt, k)
+        s.Synchronise()
+    assert e.value.code in (_lib.GY_ERR_NONFINITE, _lib.GY_ERR_ARG)
+
+
+def test_full_size_dam_break_mirror_symmetry(gpu_lib):
+    """Size-independent property at the benchmark's full size (11,995,200 particles): the dam
+    break is mirror-symmetric about the domain's mid-plane in y, so after ten steps every
+    particle's velocity mirrors its partner's to FP32 summation noise."""
+    sc = scenes.dam_break(scale=1.0)
+    s = run_gpu(sc, 10)
+    v = s._get_particles("vel")
+    p0 = sc.pos
+    psep = sc.psep
+    ix = np.floor(p0 / psep).astype(np.int64)  # lattice points sit at (k + 1/2) psep
+    iy_m = ix[:, 1].min() + ix[:, 1].max() - ix[:, 1]
+    ny = ix[:, 1].max() + 2
+    nz = ix[:, 2].max() + 2
+    key = (ix[:, 0] * ny + ix[:, 1]) * nz + ix[:, 2]
+    mkey = (ix[:, 0] * ny + iy_m) * nz + ix[:, 2]
+    order = np.argsort(key)
+    pos_in_sorted = np.searchsorted(key[order], mkey)
+    mate = order[pos_in_sorted]
+    assert np.array_equal(key[mate], mkey)
+    assert np.linalg.norm(v) > 0
+    # v_x, v_z equal and v_y opposite on mirror pairs
+    scale = np.linalg.norm(v)
+    assert np.linalg.norm(v[:, 0] - v[mate, 0]) <= 1e-4 * scale
+    assert np.linalg.norm(v[:, 2] - v[mate, 2]) <= 1e-4 * scale
+    assert np.linalg.norm(v[:, 1] + v[mate, 1]) <= 1e-4 * scale
+    st = s.stats()
+    m = s._get_particles("mass").sum()
+    assert abs(st["mass"] - m) <= 1e-9 * m

@@ -95,7 +95,9 @@ struct gy_solver {
     int *d_refkey0 = nullptr;
     DevMaterial *d_mats = nullptr;
     int *d_status = nullptr;
-    double *d_stats = nullptr;
+    double *d_stats = nullptr;              // STATS_SLOTS x 8 conservation partials
+    bool stats_fresh = false;               // d_stats holds the sums of the current state
+    double mass_total = 0.0;                // FP64 total mass (no step changes a mass)
 
     // device node state
     NodeBufs nb{};
@@ -499,6 +501,19 @@ static gy_status alloc_nodes(gy_solver *h)
     return GY_OK;
 }
 
+// Full conservation sums of the state as set (initialisation, state load): the total mass
+// is kept on the host, since steps leave it unchanged and their G2P sums only the rest.
+static gy_status sum_state(gy_solver *h)
+{
+    launch_stats(pview(h, h->cur), h->n, h->d_stats, h->stream);
+    double v0 = 0.0;
+    CK(h, cudaMemcpyAsync(&v0, h->d_stats, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->mass_total = v0;
+    h->stats_fresh = true;
+    return GY_OK;
+}
+
 gy_status gy_initialize(gy_solver *h, const gy_material *mats, int nmat, const gy_params *prm)
 {
     if (!h || !mats || nmat <= 0 || !prm) return GY_ERR_ARG;
@@ -623,7 +638,7 @@ gy_status gy_initialize(gy_solver *h, const gy_material *mats, int nmat, const g
     CK(h, cudaMemcpyAsync(h->d_mats, dm.data(), nmat * sizeof(DevMaterial), cudaMemcpyHostToDevice, h->stream));
     if ((st = dalloc(h, &h->d_status, 4))) return st;
     CK(h, cudaMemsetAsync(h->d_status, 0, 4 * sizeof(int), h->stream));
-    if ((st = dalloc(h, &h->d_stats, 8))) return st;
+    if ((st = dalloc(h, &h->d_stats, STATS_SLOTS * 8))) return st;
     CK(h, cudaMalloc(&h->d_sc, sizeof(StepScalars)));
     CK(h, cudaMallocHost(&h->h_ring, gy_solver::kRing * sizeof(StepScalars)));
     for (int k = 0; k < gy_solver::kRing; k++) CK(h, cudaEventCreateWithFlags(&h->ring_ev[k], cudaEventDisableTiming));
@@ -673,7 +688,7 @@ gy_status gy_initialize(gy_solver *h, const gy_material *mats, int nmat, const g
     h->since_sort = 1 << 30;
     h->tables_valid = false;
     h->resort_valid = false;
-    return GY_OK;
+    return sum_state(h);
 }
 
 gy_status gy_set_dt(gy_solver *h, double dt)
@@ -743,6 +758,7 @@ static StepArgs make_args(gy_solver *h)
     a.mats = h->d_mats;
     a.pbc_val = h->d_pbc_val;
     a.status = h->d_status;
+    a.stats = h->d_stats;
     return a;
 }
 
@@ -788,7 +804,9 @@ static void issue_step(gy_solver *h, const StepVariant &v, cudaEvent_t *tev)
     launch_fold(h->nb, a, s);
     launch_solve(h->nb, a, h->opt.keep_node_fields != 0, s);
     if (tev) cudaEventRecord(tev[3], s);
-    // (d) G2P + particle BCs + update + constitutive + damage, written in sorted order
+    // (d) G2P + particle BCs + update + constitutive + damage, written in sorted order, with
+    // the conservation sums of the updated state
+    cudaMemsetAsync(h->d_stats, 0, STATS_SLOTS * 8 * sizeof(double), s);
     launch_g2p_update(src, dst, perm, skey, h->n, h->d_seg, h->d_nseg, h->g2p_grid, h->nb, a,
                       h->opt.track_normals != 0, h->opt.check_finite != 0, h->has_dp, s);
     if (tev) cudaEventRecord(tev[4], s);
@@ -797,6 +815,7 @@ static void issue_step(gy_solver *h, const StepVariant &v, cudaEvent_t *tev)
 static gy_status enqueue_step(gy_solver *h, double t, int step)
 {
     cudaStream_t s = h->stream;
+    h->stats_fresh = false;
     const bool timing = h->phase_timing && h->tev_used < kMaxTimedSteps;
     cudaEvent_t *tev = nullptr;
     if (timing) {
@@ -863,6 +882,7 @@ static gy_status enqueue_step(gy_solver *h, double t, int step)
     h->cur ^= 1;
     h->t_prev = t;
     h->steps++;
+    h->stats_fresh = true;
     return GY_OK;
 }
 
@@ -1077,12 +1097,20 @@ gy_status gy_get_stats(gy_solver *h, gy_stats *out)
     std::memset(out, 0, sizeof(*out));
     if (!h->initialized) return GY_OK;
     cudaSetDevice(h->device);
-    launch_stats(pview(h, h->cur), h->n, h->d_stats, h->stream);
-    double v[8];
+    // the last step's G2P summed the state it wrote (all but the mass, which is summed when
+    // the state is set); otherwise sum it here
+    if (!h->stats_fresh) {
+        gy_status st = sum_state(h);
+        if (st) return st;
+    }
+    double part[STATS_SLOTS * 8], v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     int flags[4];
-    CK(h, cudaMemcpyAsync(v, h->d_stats, sizeof(v), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaMemcpyAsync(part, h->d_stats, sizeof(part), cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaMemcpyAsync(flags, h->d_status, sizeof(flags), cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
+    for (int q = 0; q < STATS_SLOTS; q++)
+        for (int k = 1; k < 8; k++) v[k] += part[q * 8 + k];
+    v[0] = h->mass_total;
     out->mass = v[0];
     out->momentum[0] = v[1];
     out->momentum[1] = v[2];
@@ -1229,7 +1257,7 @@ gy_status gy_state_load(gy_solver *h, const void *buf, int64_t bytes)
     h->tables_valid = hd.tables_valid != 0;
     h->since_sort = 1 << 30;
     h->resort_valid = false;
-    return GY_OK;
+    return sum_state(h);
 }
 
 gy_status gy_sort_keys(const int *keys, int64_t n, int *perm_out, int device)

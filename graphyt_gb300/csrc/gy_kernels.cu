@@ -1142,6 +1142,38 @@ constexpr int G2P_NBASE = 19, G2P_NDP = 9;
 // massless nodes zeroed (they are skipped, Extrapolation.cpp:301-303), then runs one thread
 // per particle in sorted order.  The G2P sums are separable per axis: for every (j, k) node
 // row the three x nodes are contracted first, then weighted by the y/z factors.
+// Conservation sums of the updated particles, fused into G2P: each thread adds its particles'
+// momentum, kinetic and strain energy into its own shared-memory column (FP32, a few dozen
+// particles per thread), and the CTA adds its columns in FP64 into one of STATS_SLOTS global
+// partials at the end; the host adds the partials.  The total mass does not change in a step
+// and is summed when the state is set.
+constexpr int NSTAT = 5;
+
+__device__ __forceinline__ void particle_stats(float (*col)[GY_G2P_THREADS], const PState &st)
+{
+    const int t = threadIdx.x;
+    col[0][t] += st.mass * st.v[0];
+    col[1][t] += st.mass * st.v[1];
+    col[2][t] += st.mass * st.v[2];
+    col[3][t] += 0.5f * st.mass * (st.v[0] * st.v[0] + st.v[1] * st.v[1] + st.v[2] * st.v[2]);
+    float se = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; k++) se += st.s[k] * st.e[k];
+#pragma unroll
+    for (int k = 3; k < 6; k++) se += 2.f * st.s[k] * st.e[k];
+    col[4][t] += 0.5f * __fdividef(st.mass, st.rho) * se;  // volume m / rho (diagnostic precision)
+}
+
+__device__ __forceinline__ void stats_cta_flush(double *out, float (*col)[GY_G2P_THREADS])
+{
+    __syncthreads();
+    if (threadIdx.x < NSTAT) {
+        double v = 0.0;
+        for (int t = 0; t < GY_G2P_THREADS; t++) v += (double)col[threadIdx.x][t];
+        atomicAdd(&out[(blockIdx.x % STATS_SLOTS) * 8 + 1 + threadIdx.x], v);
+    }
+}
+
 template <bool HAS_DP>
 __global__ void __launch_bounds__(GY_G2P_THREADS, GY_G2P_MINB) k_g2p_tiled(PView src, PView dst, const int *perm, const int *skey,
                                                       long long n, const int *seg_start, const int *nseg_ptr,
@@ -1151,11 +1183,14 @@ __global__ void __launch_bounds__(GY_G2P_THREADS, GY_G2P_MINB) k_g2p_tiled(PView
     __shared__ float4 TV[PT_NODES];  // (v1x, v1y, v1z, a1z), zero for massless nodes
     __shared__ float2 TA[PT_NODES];  // (a1x, a1y)
     __shared__ float stage[NST][GY_G2P_THREADS];
+    __shared__ float s_st[NSTAT][GY_G2P_THREADS];
     __shared__ long long s_end;
     const GridGeom &g = a.g;
     const int nseg = *nseg_ptr;
     const int tid = threadIdx.x;
     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < NSTAT; k++) s_st[k][tid] = 0.f;  // each thread's own column
     for (int sgi = blockIdx.x; sgi < nseg; sgi += gridDim.x) {
         const long long start = seg_start[sgi];
         const int blk = seg_block(skey, start);
@@ -1305,10 +1340,12 @@ __global__ void __launch_bounds__(GY_G2P_THREADS, GY_G2P_MINB) k_g2p_tiled(PView
                 if (!g.is3d) c0[2] = 0;
                 update_after_g2p<HAS_DP>(st, c0, acc, vg, L, a, check_finite != 0);
                 store_state<HAS_DP>(dst, i, st);
+                if (a.stats) particle_stats(s_st, st);
             }
             if (cnt < (int)blockDim.x) break;
         }
     }
+    if (a.stats) stats_cta_flush(a.stats, s_st);
 }
 
 // Multi-body G2P + update through a shared-memory node tile: per node the body pair (or
@@ -1328,10 +1365,13 @@ __global__ void __launch_bounds__(GY_G2P_THREADS) k_g2p_multi_tiled(PView src, P
     __shared__ float4 TAb[2][PT_NODES];  // (a1, -) per body slot
     __shared__ float4 TN[NRM ? 2 : 1][NRM ? PT_NODES : 1];
     __shared__ float stage[NST][GY_G2P_THREADS];
+    __shared__ float s_st[NSTAT][GY_G2P_THREADS];
     __shared__ long long s_end;
     const GridGeom &g = a.g;
     const int nseg = *nseg_ptr;
     const int tid = threadIdx.x;
+#pragma unroll
+    for (int k = 0; k < NSTAT; k++) s_st[k][tid] = 0.f;  // each thread's own column
     for (int sgi = blockIdx.x; sgi < nseg; sgi += gridDim.x) {
         const long long start = seg_start[sgi];
         const int blk = seg_block(skey, start);
@@ -1470,10 +1510,12 @@ __global__ void __launch_bounds__(GY_G2P_THREADS) k_g2p_multi_tiled(PView src, P
                     dst.f(PF_NY, i) = nrm[1];
                     dst.f(PF_NZ, i) = nrm[2];
                 }
+                if (a.stats) particle_stats(s_st, st);
             }
             if (cnt < (int)blockDim.x) break;
         }
     }
+    if (a.stats) stats_cta_flush(a.stats, s_st);
 }
 
 int g2p_blocks_per_sm(bool has_dp)
@@ -1629,9 +1671,11 @@ void launch_body_assign(const NodeBufs &nb, const StepArgs &a, const int *cell_m
 }
 
 // ---------------------------------------------------------------------------------------
-// Conservation sums: mass, momentum, kinetic energy, strain energy.  Each thread sums its
-// few particles in FP32 (the state's own precision), the mass in FP64 so that its total is
-// exact to FP64 rounding; warps, CTAs and the grid add in FP64.
+// Conservation sums: mass, momentum, kinetic energy, strain energy, of a state that no step
+// has summed (after initialisation or a state load; a step's G2P sums its own output).
+// Each thread sums its few particles in FP32 (the state's own precision), the mass in FP64
+// so that its total is exact to FP64 rounding; warps, CTAs and the grid add in FP64 into the
+// first partial slot.
 
 __global__ void k_stats(PView P, long long n, double *out)
 {
@@ -1670,7 +1714,7 @@ __global__ void k_stats(PView P, long long n, double *out)
 
 void launch_stats(const PView &p, long long n, double *out8, cudaStream_t s)
 {
-    cudaMemsetAsync(out8, 0, 8 * sizeof(double), s);
+    cudaMemsetAsync(out8, 0, STATS_SLOTS * 8 * sizeof(double), s);
     if (n == 0) return;
     long long blocks = (n + 255) / 256;
     if (blocks > 2048) blocks = 2048;

@@ -47,7 +47,12 @@ struct StepArgs {
     const DevMaterial *mats;
     const float4 *pbc_val;   // particle BC values by pid
     int *status;
+    double *stats;           // STATS_SLOTS x 8 conservation partials written by G2P, or null
 };
+
+// partials of the conservation sums (mass, momentum, kinetic and strain energy); the host
+// adds the slots
+constexpr int STATS_SLOTS = 16;
 
 // process-wide count of kernel launches (for the benchmark's launch accounting)
 void note_launch(int k);

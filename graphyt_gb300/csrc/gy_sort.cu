@@ -9,6 +9,7 @@
 // from a block-local rank: warps walk their elements in order, peers with the same digit
 // are found with __match_any_sync, and per-warp digit counters are prefix-summed across
 // warps.  The result is bit-identical to a CPU stable sort of the same keys.
+#include <algorithm>
 #include <mutex>
 
 #include "../../include/graphyt_gpu.h"
@@ -197,27 +198,43 @@ const int *sort_pairs(const int *keys_in, int *perm_out, long long n, int key_bi
     return kin;
 }
 
-// Segments: starts of the runs of equal cell block in key order (the list is unordered).
-__global__ void k_block_heads(const int *skey, long long n, int *seg_start, int *nseg)
+// Segments: starts of the runs of equal cell block in key order (the list is unordered).  A
+// grid of a few CTAs per SM strides over the keys, four per thread, all loads issued first.
+__global__ void __launch_bounds__(256) k_block_heads(const int *skey, long long n, int *seg_start, int *nseg)
 {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const bool head = (i == 0) || ((skey[i] >> CB_SHIFT) != (skey[i - 1] >> CB_SHIFT));
-    const unsigned mask = __ballot_sync(__activemask(), head);
-    if (!mask) return;
     const int lane = threadIdx.x & 31;
-    const int leader = __ffs(mask) - 1;
-    int base = 0;
-    if (lane == leader) base = atomicAdd(nseg, __popc(mask));
-    base = __shfl_sync(__activemask(), base, leader);
-    if (head) seg_start[base + __popc(mask & ((1u << lane) - 1u))] = (int)i;
+    const long long stride = 4LL * gridDim.x * blockDim.x;
+    for (long long b0 = 4LL * blockIdx.x * blockDim.x; b0 < n; b0 += stride) {
+        int kc[4], kp[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const long long i = b0 + (long long)u * blockDim.x + threadIdx.x;
+            kc[u] = i < n ? skey[i] : 0;
+            kp[u] = (i < n && i > 0) ? skey[i - 1] : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const long long i = b0 + (long long)u * blockDim.x + threadIdx.x;
+            const bool head = i < n && (i == 0 || (kc[u] >> CB_SHIFT) != (kp[u] >> CB_SHIFT));
+            const unsigned mask = __ballot_sync(0xffffffffu, head);
+            if (!mask) continue;
+            int base = 0;
+            if (lane == 0) base = atomicAdd(nseg, __popc(mask));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (head) seg_start[base + __popc(mask & ((1u << lane) - 1u))] = (int)i;
+        }
+    }
 }
 
 void launch_block_heads(const int *skey, long long n, int *seg_start, int *nseg, cudaStream_t s)
 {
     cudaMemsetAsync(nseg, 0, sizeof(int), s);
     if (n > 0) {
-        k_block_heads<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(skey, n, seg_start, nseg);
+        int dev = 0, sms = 1;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const long long grid = std::min<long long>((n + 1023) / 1024, (long long)sms * 8);
+        k_block_heads<<<(unsigned)grid, 256, 0, s>>>(skey, n, seg_start, nseg);
         note_launch(1);
     }
 }

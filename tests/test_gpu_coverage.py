@@ -122,3 +122,39 @@ def test_full_size_dam_break_mirror_symmetry(gpu_lib):
     st = s.stats()
     m = s._get_particles("mass").sum()
     assert abs(st["mass"] - m) <= 1e-9 * m
+
+
+def _fp64_stats(s):
+    m = s._get_particles("mass")
+    v = s._get_particles("vel").reshape(-1, 3)
+    sig = s._get_particles("stress").reshape(-1, 6)
+    eps = s._get_particles("strain").reshape(-1, 6)
+    rho = s._get_particles("density")
+    se = (sig[:, :3] * eps[:, :3]).sum(1) + 2.0 * (sig[:, 3:] * eps[:, 3:]).sum(1)
+    return dict(mass=m.sum(), momentum=(m[:, None] * v).sum(0), kinetic=0.5 * (m * (v * v).sum(1)).sum(),
+                strain_energy=0.5 * (m / rho * se).sum(), pscale=(m * np.abs(v).sum(1)).sum(),
+                sscale=0.5 * (m / rho * np.abs(se)).sum())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("scene", ["dam_break", "two_blocks", "brazilian_disc"])
+def test_step_fused_stats_match_separate_sum(gpu_lib, tmp_path, scene):
+    """The conservation sums a step's G2P accumulates equal a separate pass over the state it
+    wrote (the pass a state load forces) and FP64 sums of the fetched fields."""
+    sc = {"dam_break": lambda: scenes.dam_break(scale=0.125),
+          "two_blocks": lambda: scenes.two_blocks(),
+          "brazilian_disc": lambda: scenes.brazilian_disc(scale=0.25)}[scene]()
+    s = run_gpu(sc, 7)
+    fused = s.stats()
+    path = str(tmp_path / "state.bin")
+    s.save(path)
+    s.load(path)
+    full = s.stats()
+    ref = _fp64_stats(s)
+    for st in (fused, full):
+        assert abs(st["mass"] - ref["mass"]) <= 1e-12 * ref["mass"]
+        assert np.max(np.abs(np.array(st["momentum"]) - ref["momentum"])) <= 1e-5 * ref["pscale"]
+        assert abs(st["kinetic"] - ref["kinetic"]) <= 1e-5 * ref["kinetic"] + 1e-30
+        assert abs(st["strain_energy"] - ref["strain_energy"]) <= 1e-5 * ref["sscale"] + 1e-30
+        assert st["steps"] == 7
+    assert ref["kinetic"] > 0

@@ -5,16 +5,17 @@
 //             list of non-empty 4x4x4 cell blocks ("segments");
 //   fold      periodic node-layer fold of the accumulated P2G fields (Grid.cpp:310-795);
 //   P2G       one CTA per segment: particles of a run of equal cell are summed in registers
-//             by one warp (lane = stencil node) into a shared-memory node tile, flushed with
-//             vector reductions (Extrapolation.cpp:166-286); multi-body problems keep the
-//             centre-of-mass and both body-slot fields in the tile;
+//             (nine lanes per run, a lane per x column of three stencil nodes) into a
+//             shared-memory node tile, flushed with vector reductions (Extrapolation.cpp:
+//             166-286); multi-body problems keep the centre-of-mass and both body-slot
+//             fields in the tile (a lane per stencil node);
 //   solve     nodal momentum update + grid BCs over the active 4x4x4 node blocks only
 //             (Grid.cpp:9-245, 862-1094); it also clears the accumulators it read;
 //   G2P       one CTA per segment over a shared-memory tile of the solved nodes, a thread
 //             per particle in sorted order: G2P (Extrapolation.cpp:127-163, 288-367), particle
 //             BCs (TimeIntegration.cpp:177-296), update + constitutive + damage + wrap
 //             (TimeIntegration.cpp:11-117), the state written to the other slab in sorted
-//             order.
+//             order, with the momentum and energy sums of that state.
 //
 // P2G is a particle-centric scatter: the reference gathers per node over a 4x4x4 cell
 // window (Extrapolation.cpp:31-125), but a particle contributes exactly to the nodes of its
@@ -89,31 +90,17 @@ __device__ __forceinline__ void store_state(const PView &P, long long i, const P
 // solve as m_node * g, which equals sum_p w m_p g (Extrapolation.cpp:226-278).
 //
 // A CTA owns one segment (the particles of one 4x4x4 cell block), whose stencils lie in the
-// 6x6x6 node tile [4b, 4b+6).  Each chunk of P2G_CH particles is loaded in natural
-// (coalesced) order and its GIMP weights and payload are staged in shared memory as pairs of
-// neighbouring particles.  The particles of one cell share their 27 stencil nodes, so a warp
-// takes one run of equal cell at a time with lane k owning stencil node k: each lane sums the
-// run's contributions to its node in registers, two particles per packed FP32x2 instruction,
-// and adds the sum into the tile once -- seven shared atomics per node per cell instead of
-// per particle, and the 27 lanes of one instruction hit 27 different nodes.
+// 6x6x6 node tile [4b, 4b+6).  Each chunk of particles is loaded in natural (coalesced)
+// order and its GIMP weights and payload are staged in shared memory as pairs of
+// neighbouring particles.  The particles of one cell share their 27 stencil nodes, so their
+// sums are formed in registers, two particles per packed FP32x2 instruction, and added into
+// the tile once per node and cell -- seven shared atomics per node per cell instead of per
+// particle.
 
 constexpr int PT = 6;                   // tile edge in nodes
 constexpr int PT_NODES = PT * PT * PT;  // 216
 constexpr int P2G_FIELDS = 7;           // m, px, py, pz, fx, fy, fz
-#ifndef GY_P2G_CH
-#define GY_P2G_CH 128
-#endif
-#ifndef GY_P2G_MINB
-#define GY_P2G_MINB 0  // 0: registers left to the compiler
-#endif
-#if GY_P2G_MINB > 0
-#define GY_P2G_BOUNDS __launch_bounds__(P2G_CH, GY_P2G_MINB)
-#else
-#define GY_P2G_BOUNDS __launch_bounds__(P2G_CH)
-#endif
-constexpr int P2G_CH = GY_P2G_CH;       // particles per chunk = threads per CTA
-constexpr int P2G_NP = P2G_CH / 2 + 1;  // pairs per staged row; the odd row length (in float4)
-                                        // puts the three rows one load reads in different banks
+constexpr int P2G_CH = 128;             // multi-body P2G: particles per chunk = threads per CTA
 
 // Segment bounds when the keys are not freshly sorted: runs of one block can repeat, so
 // the run ends at the first index after `base` whose block differs (per chunk).
@@ -139,202 +126,255 @@ __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a
 __device__ __forceinline__ float2 lo2(float4 v) { return make_float2(v.x, v.y); }
 __device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); }
 
-// per-lane sums of one run: m, m v, and sum V sigma . grad N (the force with its sign flipped)
-struct P2GAcc {
-    float2 m, px, py, pz, fx, fy, fz;
+// Single-body P2G kernel.  A lane owns a column of three x nodes (jj, kk) of a run's stencil
+// and a warp takes three runs at once (lanes 0-8, 9-17, 18-26), so one shared load of a
+// staged pair serves the nine lanes of its run and the y/z factors multiply the payload once
+// per column: per pair and lane the three x nodes each add S_x (m, m v) syz and
+// G_x B + S_x C, with B = sigma_.x syz and C = sigma_.y G_y S_z + sigma_.z S_y G_z (the
+// separable form of the stencil sums).  A CTA of PC_THREADS stages PC_CH particles, one pair
+// per thread, about four full cells per warp and chunk.
+#ifndef GY_PC_MINB
+#define GY_PC_MINB 5  // 96 registers: five CTAs per SM
+#endif
+#ifndef GY_PC_UNROLL
+#define GY_PC_UNROLL 1
+#endif
+constexpr int PC_UNROLL = GY_PC_UNROLL;
+constexpr int PC_THREADS = 128;
+constexpr int PC_CH = 2 * PC_THREADS;
+// staged pair m sits at slot m + m / 8 of its row: the pairs the three groups of a warp read
+// in one load (runs about a third of a chunk apart) then fall in different banks
+__device__ __forceinline__ int pslot(int m) { return m + (m >> 3); }
+constexpr int PC_NP = PC_THREADS + (PC_THREADS - 1) / 8;  // 143 float4, odd
+constexpr int PC_WARPS = PC_THREADS / 32;
+
+// segment bounds of an unsorted chunk with two positions per thread
+__device__ __forceinline__ long long segment_chunk_end2(const int *skey, long long n, int blk, long long base,
+                                                        long long *s_end)
+{
+    if (threadIdx.x == 0) *s_end = base + PC_CH;
+    __syncthreads();
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const long long i = base + 2 * threadIdx.x + h;
+        if (!(i < n && (skey[i] >> CB_SHIFT) == blk)) atomicMin((unsigned long long *)s_end, (unsigned long long)i);
+    }
+    __syncthreads();
+    const long long e = *s_end;
+    __syncthreads();
+    return e;
+}
+
+struct ColAcc {
+    float2 m[3], px[3], py[3], pz[3], fx[3], fy[3], fz[3];
 };
 
-// Staged pair m: W[a][m] = (S, S', G, G') for axis/node a = 3*axis + node of particles 2m and
-// 2m+1; Q[0..4][m] = (m, m'), (m vx, ..'), then (m vy), (m vz), (s_xx), (s_yy), (s_zz),
-// (s_xy), (s_yz), (s_xz) of V sigma / h, two per float4 in that order.
-__device__ __forceinline__ void p2g_pair(P2GAcc &A, const float4 (*W)[P2G_NP], const float4 (*Q)[P2G_NP], int m,
-                                         int ii, int jj, int kk)
+// staged pair mp of the run, halves selected by mk (1 = the particle belongs to the run)
+template <bool MASKED>
+__device__ __forceinline__ void col_pair(ColAcc &A, const float4 (*W)[PC_NP], const float4 (*Q)[PC_NP], int mp,
+                                         int jj, int kk, float2 mk)
 {
-    const float4 X = W[ii][m], Y = W[3 + jj][m], Z = W[6 + kk][m];
-    const float4 q0 = Q[0][m], q1 = Q[1][m], q2 = Q[2][m], q3 = Q[3][m], q4 = Q[4][m];
-    const float2 Sx = lo2(X), Gx = hi2(X), Sy = lo2(Y), Gy = hi2(Y), Sz = lo2(Z), Gz = hi2(Z);
-    const float2 syz = mul2(Sy, Sz);
-    const float2 w = mul2(Sx, syz);
-    const float2 gx = mul2(Gx, syz);
-    const float2 gy = mul2(mul2(Sx, Sz), Gy);
-    const float2 gz = mul2(mul2(Sx, Sy), Gz);
-    A.m = fma2(w, lo2(q0), A.m);
-    A.px = fma2(w, hi2(q0), A.px);
-    A.py = fma2(w, lo2(q1), A.py);
-    A.pz = fma2(w, hi2(q1), A.pz);
+    const int sl = pslot(mp);
+    const float4 Y = W[3 + jj][sl], Z = W[6 + kk][sl];
+    const float4 q0 = Q[0][sl], q1 = Q[1][sl], q2 = Q[2][sl], q3 = Q[3][sl], q4 = Q[4][sl];
+    float2 syz = mul2(lo2(Y), lo2(Z)), gyz = mul2(hi2(Y), lo2(Z)), syg = mul2(lo2(Y), hi2(Z));
+    if (MASKED) {
+        syz = mul2(syz, mk);
+        gyz = mul2(gyz, mk);
+        syg = mul2(syg, mk);
+    }
+    const float2 mS = mul2(syz, lo2(q0)), pX = mul2(syz, hi2(q0)), pY = mul2(syz, lo2(q1)), pZ = mul2(syz, hi2(q1));
     const float2 s0 = lo2(q2), s1 = hi2(q2), s2 = lo2(q3), s3 = hi2(q3), s4 = lo2(q4), s5 = hi2(q4);
-    A.fx = fma2(gx, s0, fma2(gy, s3, fma2(gz, s5, A.fx)));
-    A.fy = fma2(gx, s3, fma2(gy, s1, fma2(gz, s4, A.fy)));
-    A.fz = fma2(gx, s5, fma2(gy, s4, fma2(gz, s2, A.fz)));
+    const float2 Bx = mul2(s0, syz), By = mul2(s3, syz), Bz = mul2(s5, syz);
+    const float2 Cx = fma2(s3, gyz, mul2(s5, syg)), Cy = fma2(s1, gyz, mul2(s4, syg));
+    const float2 Cz = fma2(s4, gyz, mul2(s2, syg));
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const float4 X = W[i][sl];
+        const float2 Sx = lo2(X), Gx = hi2(X);
+        A.m[i] = fma2(Sx, mS, A.m[i]);
+        A.px[i] = fma2(Sx, pX, A.px[i]);
+        A.py[i] = fma2(Sx, pY, A.py[i]);
+        A.pz[i] = fma2(Sx, pZ, A.pz[i]);
+        A.fx[i] = fma2(Gx, Bx, fma2(Sx, Cx, A.fx[i]));
+        A.fy[i] = fma2(Gx, By, fma2(Sx, Cy, A.fy[i]));
+        A.fz[i] = fma2(Gx, Bz, fma2(Sx, Cz, A.fz[i]));
+    }
 }
 
-// one particle: half H (0: particle 2m, 1: particle 2m+1) of staged pair m
-template <int H>
-__device__ __forceinline__ void p2g_single(P2GAcc &A, const float4 (*W)[P2G_NP], const float4 (*Q)[P2G_NP], int m,
-                                           int ii, int jj, int kk)
-{
-    const float4 X = W[ii][m], Y = W[3 + jj][m], Z = W[6 + kk][m];
-    const float4 q0 = Q[0][m], q1 = Q[1][m], q2 = Q[2][m], q3 = Q[3][m], q4 = Q[4][m];
-    const float Sx = H ? X.y : X.x, Gx = H ? X.w : X.z, Sy = H ? Y.y : Y.x, Gy = H ? Y.w : Y.z;
-    const float Sz = H ? Z.y : Z.x, Gz = H ? Z.w : Z.z;
-    const float syz = Sy * Sz;
-    const float w = Sx * syz, gx = Gx * syz, gy = Sx * Sz * Gy, gz = Sx * Sy * Gz;
-    A.m.x = fmaf(w, H ? q0.y : q0.x, A.m.x);
-    A.px.x = fmaf(w, H ? q0.w : q0.z, A.px.x);
-    A.py.x = fmaf(w, H ? q1.y : q1.x, A.py.x);
-    A.pz.x = fmaf(w, H ? q1.w : q1.z, A.pz.x);
-    const float s0 = H ? q2.y : q2.x, s1 = H ? q2.w : q2.z, s2 = H ? q3.y : q3.x;
-    const float s3 = H ? q3.w : q3.z, s4 = H ? q4.y : q4.x, s5 = H ? q4.w : q4.z;
-    A.fx.x = fmaf(gx, s0, fmaf(gy, s3, fmaf(gz, s5, A.fx.x)));
-    A.fy.x = fmaf(gx, s3, fmaf(gy, s1, fmaf(gz, s4, A.fy.x)));
-    A.fz.x = fmaf(gx, s5, fmaf(gy, s4, fmaf(gz, s2, A.fz.x)));
-}
-
-__global__ void GY_P2G_BOUNDS k_p2g_tiled(PView P, const int *perm, const int *skey, long long n,
-                                                       const int *seg_start, const int *nseg_ptr, int sorted,
-                                                       NodeBufs nb, GridGeom g)
+__global__ void __launch_bounds__(PC_THREADS, GY_PC_MINB) k_p2g_cols(PView P, const int *perm, const int *skey, long long n,
+                                                         const int *seg_start, const int *nseg_ptr, int sorted,
+                                                         NodeBufs nb, GridGeom g)
 {
     __shared__ float tile[P2G_FIELDS * PT_NODES];
-    __shared__ float4 W[9][P2G_NP];
-    __shared__ float4 Q[5][P2G_NP];
-    __shared__ int cellof[P2G_CH];
-    __shared__ int run_start[P2G_CH + 1];
-    __shared__ int wcount[P2G_CH / 32];
+    __shared__ float4 W[9][PC_NP];    // pair m: (S, S', G, G') per axis/stencil node
+    __shared__ float4 Q[5][PC_NP];    // pair m: (m, m'), (m vx, ..'), (m vy), (m vz), V sigma / h x6
+    __shared__ int run_start[PC_CH + 1];
+    __shared__ int run_cell[PC_CH];
+    __shared__ int wcount[PC_WARPS];
     __shared__ long long s_end;
     const int nseg = *nseg_ptr;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    // lane -> stencil node (ii, jj, kk); lanes 27..31 shadow valid nodes (kk clamped) so the
-    // scatter loop runs without divergence, and skip the atomics
-    const int ii = lane % 3, jj = (lane / 3) % 3, kk = min(lane / 9, 2);
+    const unsigned lt = (1u << lane) - 1u;
+    // lane -> (run group, jj, kk); lanes 27..31 shadow lane 26 and skip the atomics
+    const int grp = lane < 27 ? lane / 9 : 2, jk = lane < 27 ? lane % 9 : 8;
+    const int jj = jk % 3, kk = jk / 3;
     const bool scatter_lane = lane < 27;
-    float *Wf = reinterpret_cast<float *>(&W[0][0]);
-    float *Qf = reinterpret_cast<float *>(&Q[0][0]);
+    const float2 z2 = make_float2(0.f, 0.f);
     for (int sgi = blockIdx.x; sgi < nseg; sgi += gridDim.x) {
         const long long start = seg_start[sgi];
         const int blk = seg_block(skey, start);
         int bx, by, bz;
         decode_block(blk, g, bx, by, bz);
         const int tox = bx * CB, toy = by * CB, toz = g.is3d ? bz * CB : 0;
-        for (int t = tid; t < P2G_FIELDS * PT_NODES; t += P2G_CH) tile[t] = 0.f;
-        for (long long base = start;; base += P2G_CH) {
-            int cnt, kcur = -1, kprev = -1;
-            long long j = 0;
-            const long long i = base + tid;
+        for (int t = tid; t < P2G_FIELDS * PT_NODES; t += PC_THREADS) tile[t] = 0.f;
+        for (long long base = start;; base += PC_CH) {
+            const long long ia = base + 2 * tid, ib = ia + 1;
+            int cnt, ka = -1, kb = -1, kp = -1;
+            long long ja = 0, jb = 0;
             if (sorted) {
-                // sorted keys: the segment's particles in this chunk are a prefix of it; the
-                // barrier also ends the previous chunk's use of the staging arrays.  The
-                // particle's slot and its predecessor's key load with its own key.
-                const bool inr = i < n;
-                kcur = inr ? skey[i] : -1;
-                kprev = (inr && tid > 0) ? skey[i - 1] : -1;
-                j = inr ? perm[i] : 0;
-                cnt = __syncthreads_count(inr && (kcur >> CB_SHIFT) == blk);
+                // the segment's particles in this chunk are a prefix of it; the barriers also
+                // end the previous chunk's use of the staging arrays
+                ka = ia < n ? skey[ia] : -1;
+                kb = ib < n ? skey[ib] : -1;
+                kp = (ia < n && tid > 0) ? skey[ia - 1] : -1;
+                ja = ia < n ? perm[ia] : 0;
+                jb = ib < n ? perm[ib] : 0;
+                cnt = __syncthreads_count(ia < n && (ka >> CB_SHIFT) == blk);
+                cnt += __syncthreads_count(ib < n && (kb >> CB_SHIFT) == blk);
             } else {
-                cnt = (int)min((long long)P2G_CH, segment_chunk_end(skey, n, blk, base, P2G_CH, &s_end) - base);
-                if (tid < cnt) {
-                    kcur = skey[i];
-                    kprev = tid > 0 ? skey[i - 1] : -1;
+                cnt = (int)min((long long)PC_CH, segment_chunk_end2(skey, n, blk, base, &s_end) - base);
+                if (2 * tid < cnt) {
+                    ka = skey[ia];
+                    kp = tid > 0 ? skey[ia - 1] : -1;
                 }
-                j = i;
+                if (2 * tid + 1 < cnt) kb = skey[ib];
+                ja = ia;
+                jb = ib;
             }
             if (cnt <= 0) break;
-            // ---- stage weights and payload, natural (coalesced) order ----
-            bool head = false;
-            if (tid < cnt) {
-                const int cell = kcur & 63;  // cell inside the block: (lz*4 + ly)*4 + lx
-                head = tid == 0 || (kprev & 63) != cell;
-                cellof[tid] = cell;
-                const int m = tid >> 1, hf = tid & 1;
-                float S[3], G[3];
-                gimp_axis(P.f(PF_OX, j), g, S, G);
+            // ---- stage the pair (2 tid, 2 tid + 1); a particle past the chunk stages zeros ----
+            const int st = pslot(tid);
+            const bool va = 2 * tid < cnt, vb = 2 * tid + 1 < cnt;
+            const int ca = ka & 63, cb = kb & 63;  // cell inside the block: (lz*4 + ly)*4 + lx
+            const bool ha = va && (tid == 0 || (kp & 63) != ca);
+            const bool hb = vb && cb != ca;
+            if (va) {
+                float Sa[3], Ga[3], Sb[3] = {0.f, 0.f, 0.f}, Gb[3] = {0.f, 0.f, 0.f};
+                gimp_axis(P.f(PF_OX, ja), g, Sa, Ga);
+                if (vb) gimp_axis(P.f(PF_OX, jb), g, Sb, Gb);
 #pragma unroll
-                for (int k = 0; k < 3; k++) {
-                    Wf[((0 + k) * P2G_NP + m) * 4 + hf] = S[k];
-                    Wf[((0 + k) * P2G_NP + m) * 4 + 2 + hf] = G[k];
-                }
-                gimp_axis(P.f(PF_OY, j), g, S, G);
+                for (int k = 0; k < 3; k++) W[k][st] = make_float4(Sa[k], Sb[k], Ga[k], Gb[k]);
+                gimp_axis(P.f(PF_OY, ja), g, Sa, Ga);
+                if (vb) gimp_axis(P.f(PF_OY, jb), g, Sb, Gb);
 #pragma unroll
-                for (int k = 0; k < 3; k++) {
-                    Wf[((3 + k) * P2G_NP + m) * 4 + hf] = S[k];
-                    Wf[((3 + k) * P2G_NP + m) * 4 + 2 + hf] = G[k];
-                }
+                for (int k = 0; k < 3; k++) W[3 + k][st] = make_float4(Sa[k], Sb[k], Ga[k], Gb[k]);
                 if (g.is3d) {
-                    gimp_axis(P.f(PF_OZ, j), g, S, G);
+                    gimp_axis(P.f(PF_OZ, ja), g, Sa, Ga);
+                    if (vb) gimp_axis(P.f(PF_OZ, jb), g, Sb, Gb);
                 } else {
-                    S[0] = 1.f; S[1] = 0.f; S[2] = 0.f; G[0] = 0.f; G[1] = 0.f; G[2] = 0.f;
+                    Sa[0] = 1.f; Sa[1] = 0.f; Sa[2] = 0.f; Ga[0] = 0.f; Ga[1] = 0.f; Ga[2] = 0.f;
+                    if (vb) {
+                        Sb[0] = 1.f; Sb[1] = 0.f; Sb[2] = 0.f; Gb[0] = 0.f; Gb[1] = 0.f; Gb[2] = 0.f;
+                    }
                 }
 #pragma unroll
-                for (int k = 0; k < 3; k++) {
-                    Wf[((6 + k) * P2G_NP + m) * 4 + hf] = S[k];
-                    Wf[((6 + k) * P2G_NP + m) * 4 + 2 + hf] = G[k];
-                }
-                const float mass = P.f(PF_MASS, j);
-                const float sc = (mass / P.f(PF_RHO, j)) * g.inv_h;  // V sigma with the gradient's 1/h
-                Qf[(0 * P2G_NP + m) * 4 + hf] = mass;
-                Qf[(0 * P2G_NP + m) * 4 + 2 + hf] = mass * P.f(PF_VX, j);
-                Qf[(1 * P2G_NP + m) * 4 + hf] = mass * P.f(PF_VY, j);
-                Qf[(1 * P2G_NP + m) * 4 + 2 + hf] = mass * P.f(PF_VZ, j);
+                for (int k = 0; k < 3; k++) W[6 + k][st] = make_float4(Sa[k], Sb[k], Ga[k], Gb[k]);
+                const float ma = P.f(PF_MASS, ja), mb = vb ? P.f(PF_MASS, jb) : 0.f;
+                const float sca = (ma / P.f(PF_RHO, ja)) * g.inv_h;  // V sigma with the gradient's 1/h
+                const float scb = vb ? (mb / P.f(PF_RHO, jb)) * g.inv_h : 0.f;
+                const float vxb = vb ? P.f(PF_VX, jb) : 0.f, vyb = vb ? P.f(PF_VY, jb) : 0.f;
+                const float vzb = vb ? P.f(PF_VZ, jb) : 0.f;
+                Q[0][st] = make_float4(ma, mb, ma * P.f(PF_VX, ja), mb * vxb);
+                Q[1][st] = make_float4(ma * P.f(PF_VY, ja), mb * vyb, ma * P.f(PF_VZ, ja), mb * vzb);
 #pragma unroll
                 for (int k = 0; k < 3; k++) {
-                    Qf[((2 + k) * P2G_NP + m) * 4 + hf] = P.f(PF_S0 + 2 * k, j) * sc;
-                    Qf[((2 + k) * P2G_NP + m) * 4 + 2 + hf] = P.f(PF_S0 + 2 * k + 1, j) * sc;
+                    const float a0 = P.f(PF_S0 + 2 * k, ja) * sca, a1 = P.f(PF_S0 + 2 * k + 1, ja) * sca;
+                    const float b0 = vb ? P.f(PF_S0 + 2 * k, jb) * scb : 0.f;
+                    const float b1 = vb ? P.f(PF_S0 + 2 * k + 1, jb) * scb : 0.f;
+                    Q[2 + k][st] = make_float4(a0, b0, a1, b1);
                 }
+            } else {
+                const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+                for (int k = 0; k < 9; k++) W[k][st] = z4;
+#pragma unroll
+                for (int k = 0; k < 5; k++) Q[k][st] = z4;
             }
             // ---- runs of equal cell, in order: run r is [run_start[r], run_start[r+1]) ----
-            const unsigned hm = __ballot_sync(0xffffffffu, head);
-            if (lane == 0) wcount[warp] = __popc(hm);
+            const unsigned ba = __ballot_sync(0xffffffffu, ha), bb = __ballot_sync(0xffffffffu, hb);
+            if (lane == 0) wcount[warp] = __popc(ba) + __popc(bb);
             __syncthreads();
             int wbase = 0, R = 0;
 #pragma unroll
-            for (int w2 = 0; w2 < P2G_CH / 32; w2++) {
+            for (int w2 = 0; w2 < PC_WARPS; w2++) {
                 const int c = wcount[w2];
                 wbase += (w2 < warp) ? c : 0;
                 R += c;
             }
-            if (head) run_start[wbase + __popc(hm & ((1u << lane) - 1u))] = tid;
+            int ri = wbase + __popc(ba & lt) + __popc(bb & lt);
+            if (ha) {
+                run_start[ri] = 2 * tid;
+                run_cell[ri] = ca;
+                ri++;
+            }
+            if (hb) {
+                run_start[ri] = 2 * tid + 1;
+                run_cell[ri] = cb;
+            }
             if (tid == 0) run_start[R] = cnt;
             __syncthreads();
-            // ---- warp per run: lane = stencil node; sums in registers, one atomic per field ----
-            for (int r = warp; r < R; r += P2G_CH / 32) {
-                const int p0 = run_start[r], p1 = run_start[r + 1];
-                const int cell = cellof[p0];
-                P2GAcc A;
-                A.m = A.px = A.py = A.pz = A.fx = A.fy = A.fz = make_float2(0.f, 0.f);
-                if (p1 - p0 == 8 && !(p0 & 1)) {
-                    // a full cell (psep = cellsize / 2) on a pair boundary: four pairs, unrolled
+            // ---- three runs per warp, lane = x column (jj, kk) of its run.  Triple t holds
+            // runs t, t + T, t + 2T: cells a third of the chunk apart, whose stencils overlap
+            // little, so the groups' shared atomics seldom meet on one node ----
+            const int T = (R + 2) / 3;
+            for (int t3 = warp; t3 < T; t3 += PC_WARPS) {
+                const int r = t3 + grp * T;
+                const bool rv = r < R;
+                const int p0 = rv ? run_start[r] : 0, p1 = rv ? run_start[r + 1] : 0;
+                ColAcc A;
 #pragma unroll
-                    for (int k = 0; k < 4; k++) p2g_pair(A, W, Q, (p0 >> 1) + k, ii, jj, kk);
+                for (int i = 0; i < 3; i++) A.m[i] = A.px[i] = A.py[i] = A.pz[i] = A.fx[i] = A.fy[i] = A.fz[i] = z2;
+                const bool full = rv && p1 - p0 == 8 && !(p0 & 1);
+                if (__all_sync(0xffffffffu, full)) {
+                    // three full cells (psep = cellsize / 2) on pair boundaries: four pairs each
+#pragma unroll PC_UNROLL
+                    for (int k = 0; k < 4; k++) col_pair<false>(A, W, Q, (p0 >> 1) + k, jj, kk, z2);
                 } else {
-                    int p = p0;
-                    if (p & 1) {  // an odd start: the second particle of its pair alone
-                        p2g_single<1>(A, W, Q, p >> 1, ii, jj, kk);
-                        p++;
+                    const int m0 = p0 >> 1, np = rv ? ((p1 + 1) >> 1) - m0 : 0;
+                    const int maxp = __reduce_max_sync(0xffffffffu, np);
+                    for (int k = 0; k < maxp; k++) {
+                        const int mp = m0 + min(k, max(np - 1, 0));
+                        const int q = 2 * mp;
+                        const float2 mk = make_float2(k < np && q >= p0 && q < p1 ? 1.f : 0.f,
+                                                      k < np && q + 1 >= p0 && q + 1 < p1 ? 1.f : 0.f);
+                        col_pair<true>(A, W, Q, mp, jj, kk, mk);
                     }
-#pragma unroll 2
-                    for (; p + 1 < p1; p += 2) p2g_pair(A, W, Q, p >> 1, ii, jj, kk);
-                    if (p < p1) p2g_single<0>(A, W, Q, p >> 1, ii, jj, kk);
                 }
-                const float am = A.m.x + A.m.y, apx = A.px.x + A.px.y, apy = A.py.x + A.py.y;
-                const float apz = A.pz.x + A.pz.y;
-                const float afx = -(A.fx.x + A.fx.y), afy = -(A.fy.x + A.fy.y), afz = -(A.fz.x + A.fz.y);
-                // a node outside every particle's support has am == 0 and then no weight and
-                // no gradient either (an axis with S = 0 has G = 0)
-                if (!scatter_lane || am == 0.f) continue;
+                if (!scatter_lane || !rv) continue;
+                const int cell = run_cell[r];
                 const int li = cell & 3, lj = (cell >> 2) & 3, lk = cell >> 4;
-                const int t = ((lk + kk) * PT + (lj + jj)) * PT + (li + ii);
-                atomicAdd(&tile[0 * PT_NODES + t], am);
-                atomicAdd(&tile[1 * PT_NODES + t], apx);
-                atomicAdd(&tile[2 * PT_NODES + t], apy);
-                atomicAdd(&tile[3 * PT_NODES + t], apz);
-                atomicAdd(&tile[4 * PT_NODES + t], afx);
-                atomicAdd(&tile[5 * PT_NODES + t], afy);
-                atomicAdd(&tile[6 * PT_NODES + t], afz);
+                const int t0 = ((lk + kk) * PT + (lj + jj)) * PT + li;
+#pragma unroll
+                for (int i = 0; i < 3; i++) {
+                    const float am = A.m[i].x + A.m[i].y;
+                    // a node outside every particle's support has no weight and no gradient
+                    if (am == 0.f) continue;
+                    const int t = t0 + i;
+                    atomicAdd(&tile[0 * PT_NODES + t], am);
+                    atomicAdd(&tile[1 * PT_NODES + t], A.px[i].x + A.px[i].y);
+                    atomicAdd(&tile[2 * PT_NODES + t], A.py[i].x + A.py[i].y);
+                    atomicAdd(&tile[3 * PT_NODES + t], A.pz[i].x + A.pz[i].y);
+                    atomicAdd(&tile[4 * PT_NODES + t], -(A.fx[i].x + A.fx[i].y));
+                    atomicAdd(&tile[5 * PT_NODES + t], -(A.fy[i].x + A.fy[i].y));
+                    atomicAdd(&tile[6 * PT_NODES + t], -(A.fz[i].x + A.fz[i].y));
+                }
             }
-            if (cnt < P2G_CH) break;
+            if (cnt < PC_CH) break;
         }
         __syncthreads();
         // ---- flush the tile: two vector reductions per touched node ----
-        for (int t = tid; t < PT_NODES; t += P2G_CH) {
+        for (int t = tid; t < PT_NODES; t += PC_THREADS) {
             const float m = tile[t], px = tile[PT_NODES + t], py = tile[2 * PT_NODES + t], pz = tile[3 * PT_NODES + t];
             const float fx = tile[4 * PT_NODES + t], fy = tile[5 * PT_NODES + t], fz = tile[6 * PT_NODES + t];
             if (m == 0.f && px == 0.f && py == 0.f && pz == 0.f && fx == 0.f && fy == 0.f && fz == 0.f) continue;
@@ -349,8 +389,9 @@ __global__ void GY_P2G_BOUNDS k_p2g_tiled(PView P, const int *perm, const int *s
     }
 }
 
-// Multi-body P2G through a shared-memory node tile: the tiled scheme of k_p2g_tiled with one
-// particle at a time per warp and, per node, the centre-of-mass fields plus the two body
+// Multi-body P2G through a shared-memory node tile: segments, staging and runs of equal cell
+// as in the single-body kernel, with a warp taking one run at a time (lane k = stencil node
+// k), one particle per step, and, per node, the centre-of-mass fields plus the two body
 // slots (mass, momentum, force, normal).  A lane's body slot for a particle follows the node's
 // body pair (Extrapolation.cpp:191-198) read once per segment into shared memory.
 constexpr int MB_FIELDS = 27;                 // COM m, p(3), f(3); slot s: m, p(3), f(3), n(3)
@@ -544,7 +585,7 @@ void launch_p2g(const PView &p, const int *perm, const int *skey, long long n, c
         }
         k_p2g_multi_tiled<<<mgrid, P2G_CH, 0, s>>>(p, perm, skey, n, seg_start, nseg, perm ? 1 : 0, nb, a);
     } else {
-        k_p2g_tiled<<<persist_grid, P2G_CH, 0, s>>>(p, perm, skey, n, seg_start, nseg, perm ? 1 : 0, nb, a.g);
+        k_p2g_cols<<<persist_grid, PC_THREADS, 0, s>>>(p, perm, skey, n, seg_start, nseg, perm ? 1 : 0, nb, a.g);
     }
     note_launch(1);
 }
@@ -552,7 +593,7 @@ void launch_p2g(const PView &p, const int *perm, const int *skey, long long n, c
 int p2g_blocks_per_sm()
 {
     int b = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_p2g_tiled, P2G_CH, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_p2g_cols, PC_THREADS, 0);
     return b > 0 ? b : 1;
 }
 

@@ -65,6 +65,7 @@ class Scene:
     hold: Optional[np.ndarray] = None      # (N,) bool
     node_bc_type: Optional[np.ndarray] = None  # (Nn,)
     node_bc_val: Optional[np.ndarray] = None   # (Nn, 4)
+    temp: Optional[np.ndarray] = None          # (N,) temperature (MaterialPoints::setTemp)
 
     @property
     def is3D(self) -> bool:
@@ -126,6 +127,8 @@ def _finish(scene: Scene, seed: int) -> Scene:
         scene.pbc_val = np.zeros((n, 4))
     if scene.hold is None:
         scene.hold = np.zeros(n, bool)
+    if scene.temp is None:
+        scene.temp = np.zeros(n)
     nn = scene.num_nodes()
     if scene.node_bc_type is None:
         scene.node_bc_type = np.zeros(nn, np.int32)
@@ -133,7 +136,7 @@ def _finish(scene: Scene, seed: int) -> Scene:
         scene.node_bc_val = np.zeros((nn, 4))
     if seed is not None:
         perm = np.random.default_rng(seed).permutation(n)
-        for f in ("pos", "mat", "obj", "vel", "stress", "pbc_type", "pbc_val", "hold"):
+        for f in ("pos", "mat", "obj", "vel", "stress", "pbc_type", "pbc_val", "hold", "temp"):
             setattr(scene, f, np.ascontiguousarray(getattr(scene, f)[perm]))
     scene.pos = np.ascontiguousarray(scene.pos, np.float64)
     scene.mat = np.ascontiguousarray(scene.mat, np.int32)
@@ -379,4 +382,29 @@ def block_2d(seed: int = 0, model: int = 1, platen: bool = True, shift: bool = T
     if platen:
         v[sc.obj == 2, 1] = -0.2
     sc.vel = v
+    return _finish(sc, seed)
+
+
+def thermal_block(seed: int = 0, n_side: int = 10, cellsize: float = 0.05, model: int = 1,
+                  T_cold: float = 50.0, T_hot: float = 100.0) -> Scene:
+    """Heat conduction in a 3D block at rest (the pattern of Examples/thermalTest.py): the
+    particles of the lowest fifth in y start at T_cold, the highest fifth at T_hot, the rest
+    at 0.  Copper thermal properties (the material defaults, k 391, c 385.2) on an elastic
+    body of density 1000; no gravity.  The node temperature is the reference's unnormalised
+    sum S T m c (Extrapolation.cpp:281-283)."""
+    h = cellsize
+    psep = h / 2
+    side = n_side * psep
+    L = [side + 8 * h, side + 8 * h, side + 8 * h]
+    lo = [4 * h + 0.013 * psep, 4 * h + 0.021 * psep, 4 * h + 0.017 * psep]
+    pos = lattice_box(lo, [lo[0] + side, lo[1] + side, lo[2] + side], psep)
+    n = pos.shape[0]
+    y = (pos[:, 1] - lo[1]) / side
+    temp = np.zeros(n)
+    temp[y < 0.2] = T_cold
+    temp[y > 0.8] = T_hot
+    sc = Scene(name="thermal_block", L=L, cellsize=h, psep=psep, pos=pos,
+               mat=np.zeros(n, np.int32), obj=np.zeros(n, np.int32),
+               materials=[material(model=model, bulkMod=1e7, shearMod=5000.0, density=1000.0)],
+               gravity=[0.0, 0.0, 0.0], CFL=0.1, temp=temp)
     return _finish(sc, seed)

@@ -12,9 +12,11 @@
  *  - Sort (Extrapolation.cpp:370-503): the reference uses std::sort, whose order among
  *    particles of one cell is unspecified.  Here the order is fixed as (cellID, particle id),
  *    which the GPU body-slot rule uses too.
- *  - Thermal terms (Extrapolation.cpp:281-283, 358-362; TimeIntegration.cpp:50) are
- *    identically zero unless a temperature is set; no temperature setter is exposed, so
- *    they are omitted.
+ *  - Thermal terms (Extrapolation.cpp:281-283, 358-362; TimeIntegration.cpp:50): the
+ *    sort moves each particle's temperature gradient with the particle.  The reference's
+ *    sort copies one of its three components per slot (Extrapolation.cpp:446, 485), which
+ *    corrupts the gradients the P2G right after each sort uses; that copy depends on the
+ *    reference's own array order and is not restated.
  *  - 3x3 symmetric eigen-solve (eig3.cpp:258-267, JAMA tred2+tql2) is replaced by a
  *    cyclic Jacobi rotation method; the damaged stress V diag(s') V^T depends only on the
  *    eigenpairs, so the two agree to rounding.
@@ -49,6 +51,7 @@ struct gyo {
 
     /* node fields (Nodes.hpp:22-55): COM, body 1, body 2 */
     double *m0, *m1, *m2;
+    double *Tn, *Rn; /* node temperature (sum S T m c) and temperature rate (Nodes.hpp:47-48) */
     double *p0, *p1, *p2;
     double *f0, *f1, *f2;
     double *v0, *v1, *v2;
@@ -64,6 +67,7 @@ struct gyo {
     int N, cap;
     double psep, t;
     double *x, *x0, *u, *v, *gv, *a, *er, *dr, *s, *e, *ep, *eqp, *D, *smax, *m, *rho, *V, *nrm;
+    double *T, *gT, *Tr; /* temperature, its gradient, its rate (MaterialPoints.hpp:103-105) */
     int *cell, *mat, *obj, *bct, *pid;
     double *bcv;
     unsigned char *hold;
@@ -134,6 +138,7 @@ gyo *gyo_create(double Lx, double Ly, double Lz, double h, double psep)
     }
     size_t Nn = (size_t)o->Nn;
     o->m0 = dalloc(Nn); o->m1 = dalloc(Nn); o->m2 = dalloc(Nn);
+    o->Tn = dalloc(Nn); o->Rn = dalloc(Nn);
     o->p0 = dalloc(3 * Nn); o->p1 = dalloc(3 * Nn); o->p2 = dalloc(3 * Nn);
     o->f0 = dalloc(3 * Nn); o->f1 = dalloc(3 * Nn); o->f2 = dalloc(3 * Nn);
     o->v0 = dalloc(3 * Nn); o->v1 = dalloc(3 * Nn); o->v2 = dalloc(3 * Nn);
@@ -152,7 +157,8 @@ gyo *gyo_create(double Lx, double Ly, double Lz, double h, double psep)
 static void free_particles(gyo *o)
 {
     double **d[] = {&o->x, &o->x0, &o->u, &o->v, &o->gv, &o->a, &o->er, &o->dr, &o->s, &o->e,
-                    &o->ep, &o->eqp, &o->D, &o->smax, &o->m, &o->rho, &o->V, &o->nrm, &o->bcv};
+                    &o->ep, &o->eqp, &o->D, &o->smax, &o->m, &o->rho, &o->V, &o->nrm, &o->bcv,
+                    &o->T, &o->gT, &o->Tr};
     for (size_t i = 0; i < sizeof(d) / sizeof(d[0]); i++) { free(*d[i]); *d[i] = NULL; }
     int **ii[] = {&o->cell, &o->mat, &o->obj, &o->bct, &o->pid};
     for (size_t i = 0; i < sizeof(ii) / sizeof(ii[0]); i++) { free(*ii[i]); *ii[i] = NULL; }
@@ -162,7 +168,7 @@ static void free_particles(gyo *o)
 void gyo_destroy(gyo *o)
 {
     if (!o) return;
-    double *d[] = {o->m0, o->m1, o->m2, o->p0, o->p1, o->p2, o->f0, o->f1, o->f2, o->v0,
+    double *d[] = {o->m0, o->m1, o->m2, o->Tn, o->Rn, o->p0, o->p1, o->p2, o->f0, o->f1, o->f2, o->v0,
                    o->v1, o->v2, o->a0, o->a1, o->a2, o->n1, o->n2, o->nbcv};
     for (size_t i = 0; i < sizeof(d) / sizeof(d[0]); i++) free(d[i]);
     free(o->body); free(o->rigid); free(o->nbct); free(o->cells); free(o->ccount);
@@ -184,6 +190,7 @@ int gyo_add_particles(gyo *o, int n, const double *pos, const int *mat, const in
         GROW(o->s, double, 6); GROW(o->e, double, 6); GROW(o->ep, double, 6); GROW(o->eqp, double, 1);
         GROW(o->D, double, 1); GROW(o->smax, double, 1); GROW(o->m, double, 1); GROW(o->rho, double, 1);
         GROW(o->V, double, 1); GROW(o->nrm, double, 3); GROW(o->bcv, double, 4);
+        GROW(o->T, double, 1); GROW(o->gT, double, 3); GROW(o->Tr, double, 1);
         GROW(o->cell, int, 1); GROW(o->mat, int, 1); GROW(o->obj, int, 1); GROW(o->bct, int, 1);
         GROW(o->pid, int, 1);
         o->hold = (unsigned char *)realloc(o->hold, (size_t)cap);
@@ -196,7 +203,9 @@ int gyo_add_particles(gyo *o, int n, const double *pos, const int *mat, const in
             o->x0[3 * p + k] = pos[3 * q + k];
             o->u[3 * p + k] = o->v[3 * p + k] = o->gv[3 * p + k] = o->a[3 * p + k] = 0.0;
             o->nrm[3 * p + k] = 0.0;
+            o->gT[3 * p + k] = 0.0;
         }
+        o->T[p] = o->Tr[p] = 0.0;
         for (int k = 0; k < 6; k++) o->er[6 * p + k] = o->s[6 * p + k] = o->e[6 * p + k] = o->ep[6 * p + k] = 0.0;
         for (int k = 0; k < 4; k++) o->bcv[4 * p + k] = 0.0;
         o->dr[p] = o->eqp[p] = o->D[p] = o->smax[p] = o->m[p] = o->rho[p] = o->V[p] = 0.0;
@@ -229,6 +238,14 @@ void gyo_set_particle_bc(gyo *o, int p, int type, const double *val, int nval)
 {
     o->bct[p] = type;
     for (int i = 0; i < nval && i < 4; i++) o->bcv[4 * p + i] = val[i];
+}
+void gyo_set_particle_temps(gyo *o, int count, const int *ids, const double *T)
+{
+    int *at = ialloc((size_t)o->N);
+    for (int q = 0; q < o->N; q++) at[o->pid[q]] = q;
+    for (int q = 0; q < count; q++)
+        if (ids[q] >= 0 && ids[q] < o->N) o->T[at[ids[q]]] = T[q];
+    free(at);
 }
 void gyo_set_node_bc(gyo *o, int n, int type, const double *val, int nval)
 {
@@ -314,7 +331,7 @@ static void sort_particles(gyo *o)
     PERM(o->eqp, double, 1); PERM(o->D, double, 1); PERM(o->smax, double, 1); PERM(o->m, double, 1);
     PERM(o->rho, double, 1); PERM(o->obj, int, 1); PERM(o->V, double, 1); PERM(o->nrm, double, 3);
     PERM(o->bcv, double, 4); PERM(o->mat, int, 1); PERM(o->cell, int, 1); PERM(o->hold, unsigned char, 1);
-    PERM(o->bct, int, 1); PERM(o->pid, int, 1);
+    PERM(o->bct, int, 1); PERM(o->pid, int, 1); PERM(o->T, double, 1); PERM(o->gT, double, 3);
     o->cap = N;
     free(order);
     /* cell start table: exclusive scan with cells[0] = 0 (Extrapolation.cpp:494-501) */
@@ -333,6 +350,7 @@ static void reset_nodes(gyo *o)
 {
     size_t Nn = (size_t)o->Nn;
     memset(o->m0, 0, Nn * 8); memset(o->m1, 0, Nn * 8); memset(o->m2, 0, Nn * 8);
+    memset(o->Tn, 0, Nn * 8); memset(o->Rn, 0, Nn * 8);
     double *z3[] = {o->p0, o->p1, o->p2, o->f0, o->f1, o->f2, o->v0, o->v1, o->v2,
                     o->a0, o->a1, o->a2, o->n1, o->n2};
     for (size_t i = 0; i < sizeof(z3) / sizeof(z3[0]); i++) memset(z3[i], 0, 3 * Nn * 8);
@@ -343,6 +361,7 @@ static void reset_rates(gyo *o)
 {
     for (int p = 0; p < o->N; p++) {
         o->dr[p] = 0.0;
+        o->Tr[p] = 0.0;
         for (int k = 0; k < 3; k++) { o->a[3 * p + k] = 0.0; o->gv[3 * p + k] = 0.0; }
         for (int k = 0; k < 6; k++) o->er[6 * p + k] = 0.0;
     }
@@ -409,6 +428,13 @@ static void p2g_pair(gyo *o, int mp, int n, const double *np)
     o->f0[3 * n + 0] += w * mass * g[0];
     o->f0[3 * n + 1] += w * mass * g[1];
     o->f0[3 * n + 2] += w * mass * g[2];
+    /* thermal (Extrapolation.cpp:280-283): node temperature sum S T m c, not normalised;
+     * the rate from the particle's temperature gradient of the previous G2P */
+    const gyo_material *M = &o->mats[mid];
+    const double *gT = o->gT + 3 * mp;
+    o->Tn[n] += w * o->T[mp] * mass * M->specificHeatCapacity;
+    o->Rn[n] -= (mass / rho) * M->thermalConductivity *
+                ((gx * sy * sz * gT[0]) + (sx * gy * sz * gT[1]) + (sx * sy * gz * gT[2]));
 }
 
 static void p2g(gyo *o)
@@ -611,6 +637,8 @@ static void g2p(gyo *o)
         int ob = o->obj[mp];
         double rho = o->rho[mp];
         double *acc = o->a + 3 * mp, *gv = o->gv + 3 * mp, *er = o->er + 6 * mp, *nr = o->nrm + 3 * mp;
+        double *gT = o->gT + 3 * mp;
+        gT[0] = gT[1] = gT[2] = 0.0; /* Extrapolation.cpp:132-134 */
         for (int k = 0; k < kn; k++)
             for (int j = 0; j < 3; j++)
                 for (int i = 0; i < 3; i++) {
@@ -626,6 +654,11 @@ static void g2p(gyo *o)
                     double gy = gyo_gimp_grad(np[1] - xp[1], h, lp, xp[1]);
                     double gz = gyo_gimp_grad(np[2] - xp[2], h, lp, xp[2]);
                     if (!o->is3D) { sz = 1.0; gz = 0.0; }
+                    /* thermal, every node with mass, whatever its bodies (Extrapolation.cpp:358-362) */
+                    gT[0] += (gx * sy * sz) * o->Tn[n];
+                    gT[1] += (sx * gy * sz) * o->Tn[n];
+                    gT[2] += (sx * sy * gz) * o->Tn[n];
+                    o->Tr[mp] += sx * sy * sz * o->Rn[n];
                     const double *vb, *ab, *nb;
                     if (o->body[2 * n + 0] == ob) { vb = o->v1 + 3 * n; ab = o->a1 + 3 * n; nb = o->n1 + 3 * n; }
                     else if (o->body[2 * n + 1] == ob) { vb = o->v2 + 3 * n; ab = o->a2 + 3 * n; nb = o->n2 + 3 * n; }
@@ -1027,6 +1060,7 @@ static void update_particles(gyo *o)
             if (o->is3D) x[2] += o->gv[3 * p + 2] * dt;
         }
         for (int k = 0; k < 3; k++) o->u[3 * p + k] = x[k] - o->x0[3 * p + k];
+        o->T[p] += o->Tr[p] * dt; /* TimeIntegration.cpp:49-50 */
         for (int k = 0; k < 6; k++) o->e[6 * p + k] += o->er[6 * p + k] * dt;
         const gyo_material *M = &o->mats[o->mat[p]];
         if (!M->isRigid) {
@@ -1090,12 +1124,12 @@ int gyo_num_particles(const gyo *o) { return o->N; }
 int gyo_num_nodes(const gyo *o) { return o->Nn; }
 void gyo_dims(const gyo *o, int *nxyz) { nxyz[0] = o->Nx; nxyz[1] = o->Ny; nxyz[2] = o->Nz; }
 
-static const int pwidth[GYO_P_NFIELDS] = {3, 3, 3, 3, 3, 3, 6, 6, 6, 6, 1, 1, 1, 1, 1, 1, 3, 1};
+static const int pwidth[GYO_P_NFIELDS] = {3, 3, 3, 3, 3, 3, 6, 6, 6, 6, 1, 1, 1, 1, 1, 1, 3, 1, 1, 3};
 int gyo_particle_width(int f) { return (f >= 0 && f < GYO_P_NFIELDS) ? pwidth[f] : 0; }
 int gyo_node_width(int f)
 {
     switch (f) {
-    case GYO_N_MASS: case GYO_N_MASS1: case GYO_N_MASS2: return 1;
+    case GYO_N_MASS: case GYO_N_MASS1: case GYO_N_MASS2: case GYO_N_TEMP: case GYO_N_TEMPRATE: return 1;
     default: return (f > GYO_N_MASS2 && f <= GYO_N_NORMAL2) ? 3 : 0;
     }
 }
@@ -1103,7 +1137,8 @@ int gyo_node_width(int f)
 int gyo_get_particle_field(const gyo *o, int f, double *out)
 {
     const double *src[GYO_P_NFIELDS] = {o->x, o->x0, o->u, o->v, o->gv, o->a, o->er, o->s, o->e, o->ep,
-                                        o->eqp, o->D, o->smax, o->m, o->rho, o->V, o->nrm, o->dr};
+                                        o->eqp, o->D, o->smax, o->m, o->rho, o->V, o->nrm, o->dr,
+                                        o->T, o->gT};
     int w = gyo_particle_width(f);
     if (!w) return -1;
     memcpy(out, src[f], sizeof(double) * (size_t)w * (size_t)o->N);
@@ -1121,7 +1156,7 @@ int gyo_get_particle_ifield(const gyo *o, int f, int *out)
 int gyo_get_node_field(const gyo *o, int f, double *out)
 {
     const double *src[] = {o->m0, o->m1, o->m2, o->p0, o->p1, o->p2, o->f0, o->f1, o->f2,
-                           o->v0, o->v1, o->v2, o->a1, o->a2, o->n1, o->n2};
+                           o->v0, o->v1, o->v2, o->a1, o->a2, o->n1, o->n2, o->Tn, o->Rn};
     int w = gyo_node_width(f);
     if (!w) return -1;
     memcpy(out, src[f], sizeof(double) * (size_t)w * (size_t)o->Nn);

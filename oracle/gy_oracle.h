@@ -51,6 +51,9 @@ void gyo_set_particle_damage(gyo *o, int p, double D);
 void gyo_hold_particle(gyo *o, int p);
 void gyo_set_particle_bc(gyo *o, int p, int type, const double *val, int nval);
 void gyo_set_node_bc(gyo *o, int n, int type, const double *val, int nval);
+/* MaterialPoints::setTemp (MaterialPoints.cpp:319-322) for `count` particles given by their
+ * original index; valid before and between steps. */
+void gyo_set_particle_temps(gyo *o, int count, const int *ids, const double *T);
 
 /* Solver(nds, mpts, params, materials): dt from CFL and initialize() (Solver.cpp:7-69). */
 int gyo_init_solver(gyo *o, const gyo_params *prm, int nmat, const gyo_material *mats);
@@ -67,14 +70,14 @@ int gyo_step(gyo *o, double t, int step);
 enum gyo_pfield {
     GYO_P_POS = 0, GYO_P_POS0, GYO_P_DISP, GYO_P_VEL, GYO_P_GVEL, GYO_P_ACC, GYO_P_STRAINRATE,
     GYO_P_STRESS, GYO_P_STRAIN, GYO_P_PSTRAIN, GYO_P_EQPS, GYO_P_DAMAGE, GYO_P_SMAX, GYO_P_MASS,
-    GYO_P_DENSITY, GYO_P_VOLUME, GYO_P_NORMALS, GYO_P_DENSITYRATE,
+    GYO_P_DENSITY, GYO_P_VOLUME, GYO_P_NORMALS, GYO_P_DENSITYRATE, GYO_P_TEMP, GYO_P_TEMPGRAD,
     GYO_P_NFIELDS
 };
 enum gyo_pifield { GYO_PI_CELL = 0, GYO_PI_MAT, GYO_PI_OBJ, GYO_PI_PID };
 enum gyo_nfield {
     GYO_N_MASS = 0, GYO_N_MASS1, GYO_N_MASS2, GYO_N_MOM, GYO_N_MOM1, GYO_N_MOM2, GYO_N_FORCE,
     GYO_N_FORCE1, GYO_N_FORCE2, GYO_N_VEL, GYO_N_VEL1, GYO_N_VEL2, GYO_N_ACC1, GYO_N_ACC2,
-    GYO_N_NORMAL1, GYO_N_NORMAL2
+    GYO_N_NORMAL1, GYO_N_NORMAL2, GYO_N_TEMP, GYO_N_TEMPRATE
 };
 enum gyo_nifield { GYO_NI_BODY = 0, GYO_NI_RIGID, GYO_NI_CELLS, GYO_NI_CELLCOUNT };
 

@@ -23,13 +23,13 @@ REF_LIB = os.path.join(HERE, "_ref", "libgyref.so")
 
 P_FIELDS = dict(pos=0, pos0=1, disp=2, vel=3, gvel=4, acc=5, strainrate=6, stress=7, strain=8,
                 pstrain=9, eqps=10, damage=11, smax=12, mass=13, density=14, volume=15, normals=16,
-                densityrate=17)
+                densityrate=17, temp=18, tempgrad=19)
 P_WIDTH = dict(pos=3, pos0=3, disp=3, vel=3, gvel=3, acc=3, strainrate=6, stress=6, strain=6,
                pstrain=6, eqps=1, damage=1, smax=1, mass=1, density=1, volume=1, normals=3,
-               densityrate=1)
+               densityrate=1, temp=1, tempgrad=3)
 PI_FIELDS = dict(cell=0, mat=1, obj=2, pid=3)
 N_FIELDS = dict(mass=0, mass1=1, mass2=2, mom=3, mom1=4, mom2=5, force=6, force1=7, force2=8,
-                vel=9, vel1=10, vel2=11, acc1=12, acc2=13, normal1=14, normal2=15)
+                vel=9, vel1=10, vel2=11, acc1=12, acc2=13, normal1=14, normal2=15, temp=16, temprate=17)
 NI_FIELDS = dict(body=0, rigid=1, cells=2, cellcount=3)
 
 MAT_DOUBLE_FIELDS = ["bulkMod", "shearMod", "density", "viscosity", "thermalConductivity",
@@ -83,6 +83,7 @@ def _lib(kind: str):
         "hold_particle": (None, [vp, C.c_int]),
         "set_particle_bc": (None, [vp, C.c_int, C.c_int, dp, C.c_int]),
         "set_node_bc": (None, [vp, C.c_int, C.c_int, dp, C.c_int]),
+        "set_particle_temps": (None, [vp, C.c_int, ip, dp]),
         "init_solver": (C.c_int, [vp, C.POINTER(Params), C.c_int, C.POINTER(Material)]),
         "get_dt": (C.c_double, [vp]),
         "set_dt": (None, [vp, C.c_double]),
@@ -175,6 +176,9 @@ class Oracle:
         for p in np.nonzero(scene.pbc_type)[0]:
             v = np.ascontiguousarray(scene.pbc_val[p], np.float64)
             self._call("set_particle_bc", self.h, int(p), int(scene.pbc_type[p]), _dp(v), 4)
+        temp = getattr(scene, "temp", None)
+        if temp is not None and np.any(temp != 0.0):
+            self.set_temps(np.nonzero(temp)[0], temp[temp != 0.0])
         for n in np.nonzero(scene.node_bc_type)[0]:
             v = np.ascontiguousarray(scene.node_bc_val[n], np.float64)
             self._call("set_node_bc", self.h, int(n), int(scene.node_bc_type[n]), _dp(v), 4)
@@ -188,6 +192,12 @@ class Oracle:
         self.dt = self._call("get_dt", self.h)
         self.step_index = 0
         self.t = 0.0
+
+    def set_temps(self, ids, T) -> None:
+        """MaterialPoints::setTemp for particles given by their original index."""
+        ids = np.ascontiguousarray(ids, np.int32)
+        T = np.ascontiguousarray(T, np.float64)
+        self._call("set_particle_temps", self.h, int(ids.size), _ip(ids), _dp(T))
 
     def _call(self, name, *args):
         return getattr(self.lib, self.pre + name)(*args)
@@ -242,7 +252,7 @@ class Oracle:
 
     def nfield(self, name: str) -> np.ndarray:
         nn = self._call("num_nodes", self.h)
-        w = 1 if name.startswith("mass") else 3
+        w = 1 if name.startswith("mass") or name.startswith("temp") else 3
         out = np.empty((nn, w), np.float64)
         self._call("get_node_field", self.h, N_FIELDS[name], _dp(out))
         return out if w > 1 else out[:, 0]

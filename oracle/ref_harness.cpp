@@ -26,10 +26,13 @@
 
 static int pwidth(int f)
 {
-    static const int w[GYO_P_NFIELDS] = {3, 3, 3, 3, 3, 3, 6, 6, 6, 6, 1, 1, 1, 1, 1, 1, 3, 1};
+    static const int w[GYO_P_NFIELDS] = {3, 3, 3, 3, 3, 3, 6, 6, 6, 6, 1, 1, 1, 1, 1, 1, 3, 1, 1, 3};
     return (f >= 0 && f < GYO_P_NFIELDS) ? w[f] : 0;
 }
-static int nwidth(int f) { return (f == GYO_N_MASS || f == GYO_N_MASS1 || f == GYO_N_MASS2) ? 1 : 3; }
+static int nwidth(int f)
+{
+    return (f == GYO_N_MASS || f == GYO_N_MASS1 || f == GYO_N_MASS2 || f == GYO_N_TEMP || f == GYO_N_TEMPRATE) ? 1 : 3;
+}
 
 struct gyr {
     Nodes *nds;
@@ -94,6 +97,13 @@ int gyr_add_particles(gyr *r, int n, const double *pos, const int *mat, const in
 }
 
 void gyr_set_particle_vel(gyr *r, int p, double vx, double vy, double vz) { r->mpts->setVel(p, vx, vy, vz); }
+void gyr_set_particle_temps(gyr *r, int count, const int *ids, const double *T)
+{
+    std::vector<int> at(r->pid.size());
+    for (size_t q = 0; q < r->pid.size(); q++) at[r->pid[q]] = (int)q;
+    for (int q = 0; q < count; q++)
+        if (ids[q] >= 0 && ids[q] < (int)at.size()) r->mpts->setTemp(at[ids[q]], T[q]);
+}
 void gyr_set_particle_stress(gyr *r, int p, const double *s)
 {
     r->mpts->setStress(p, s[0], s[1], s[2], s[3], s[4], s[5]);
@@ -169,6 +179,7 @@ static void harness_sort(gyr *r)
     permute(m->damage, order, 1); permute(m->smax, order, 1); permute(m->mass, order, 1);
     permute(m->density, order, 1); permute(m->objID, order, 1); permute(m->volume, order, 1);
     permute(m->normals, order, 3); permute(m->temperature, order, 1); permute(m->BCVAL, order, 4);
+    permute(m->temperatureGrad, order, 3);  /* with its particle (the reference's sort garbles it) */
     permute(m->material, order, 1); permute(m->cellID, order, 1); permute(m->hold, order, 1);
     permute(m->BCTYPE, order, 1); permute(r->pid, order, 1);
     int cur = 0;
@@ -270,6 +281,8 @@ int gyr_get_particle_field(const gyr *r, int f, double *out)
     case GYO_P_VOLUME: src = m->volume.data(); break;
     case GYO_P_NORMALS: src = m->normals.data(); break;
     case GYO_P_DENSITYRATE: src = m->densityRate.data(); break;
+    case GYO_P_TEMP: src = m->temperature.data(); break;
+    case GYO_P_TEMPGRAD: src = m->temperatureGrad.data(); break;
     default: return -1;
     }
     std::memcpy(out, src, sizeof(double) * (size_t)w * (size_t)N);
@@ -313,6 +326,8 @@ int gyr_get_node_field(const gyr *r, int f, double *out)
     case GYO_N_ACC2: src = n->acceleration_body2; break;
     case GYO_N_NORMAL1: src = n->normals_body1; break;
     case GYO_N_NORMAL2: src = n->normals_body2; break;
+    case GYO_N_TEMP: src = n->temperature; break;
+    case GYO_N_TEMPRATE: src = n->temperatureRate; break;
     default: return -1;
     }
     std::memcpy(out, src, sizeof(double) * (size_t)nwidth(f) * (size_t)n->numNodes);

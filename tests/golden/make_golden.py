@@ -5,7 +5,7 @@ from the reference tree) on the seeded scenes of graphyt_gb300.scenes and stores
 particle state by particle id.  The fixtures let tests pin the oracle and the GPU path on
 machines where the reference tree is absent.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]
 """
 import os
 import sys
@@ -20,6 +20,7 @@ from graphyt_gb300 import scenes  # noqa: E402
 from oracle import oracle  # noqa: E402
 
 FIELDS = ["pos", "vel", "stress", "density", "strain", "eqps", "pstrain", "damage", "disp"]
+THERMAL_FIELDS = ["temp", "tempgrad"]
 
 # name -> (scene factory, steps, max stored particles)
 CASES = {
@@ -37,7 +38,12 @@ CASES = {
     "two_blocks_rigid": (lambda: scenes.two_blocks(rigid_second=True), 40, None),
     "block_2d_elastic": (lambda: scenes.block_2d(model=1), 200, None),
     "block_2d_dp": (lambda: scenes.block_2d(model=4), 200, None),
+    "thermal_block": (lambda: scenes.thermal_block(), 30, None),
 }
+
+
+def fields_for(name):
+    return FIELDS + (THERMAL_FIELDS if name.startswith("thermal") else [])
 
 
 def generate(name, kind="ref"):
@@ -49,19 +55,19 @@ def generate(name, kind="ref"):
     if cap is not None and sc.n > cap:
         ids = np.linspace(0, sc.n - 1, cap).astype(np.int64)
     out = {"ids": ids, "steps": np.int64(steps), "dt": np.float64(o.dt), "n": np.int64(sc.n)}
-    for f in FIELDS:
+    for f in fields_for(name):
         out[f] = o.pfield(f)[ids]
     return out
 
 
-def main():
+def main(names=None):
     if not oracle.available("ref"):
         oracle.build()
-    for name in CASES:
+    for name in names or CASES:
         data = generate(name, "ref")
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **data)
         print(name, int(data["n"]), "particles,", int(data["steps"]), "steps")
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -23,7 +23,7 @@ def test_port_matches_reference_goldens(oracle_built, name):
     path = os.path.join(GOLDEN, name + ".npz")
     gold = np.load(path)
     got = make_golden.generate(name, kind="port")
-    for f in make_golden.FIELDS:
+    for f in make_golden.fields_for(name):
         a, b = got[f], gold[f]
         if np.linalg.norm(b) == 0:
             assert np.array_equal(a, b), f
@@ -173,3 +173,32 @@ def test_scene_counts():
     assert scenes.elastic_cube("particle").n == 8000
     pts = scenes.lattice_box([0.02, 0.02, 0.02], [1.02, 1.98, 0.785], 0.005)
     assert len(pts) == 200 * 392 * 153
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(GOLDEN), "..", "oracle", "_ref", "libgyref.so"))
+                    and not os.path.isdir("/root/reference"), reason="reference tree not available")
+def test_thermal_harness_matches_literal_between_sorts(oracle_built):
+    """Heat conduction: the harness sequence and the restatement equal Solver::iterate_CPU
+    while no sort has moved a temperature gradient (steps 1-9: the step-1 sort sees the
+    all-zero initial gradients).  A run through step 1's sort of step 0's gradients differs,
+    since the reference's sort copies one gradient component per slot
+    (Extrapolation.cpp:446, 485)."""
+    from oracle.oracle import Oracle, available
+    if not available("ref"):
+        pytest.skip("reference library not built")
+    sc = scenes.thermal_block()
+
+    def temp_after(kind, mode, steps):
+        o = Oracle(sc, kind, mode=mode)
+        for k in steps:
+            o.step(step=k)
+        return o.pfield("temp")
+
+    clean = range(1, 10)
+    lit, har, port = temp_after("ref", 0, clean), temp_after("ref", 1, clean), temp_after("port", 1, clean)
+    dT = np.linalg.norm(har - sc.temp)
+    assert dT > 1.0
+    assert np.linalg.norm(lit - har) <= 1e-12 * dT
+    assert np.linalg.norm(port - har) <= 1e-12 * dT
+    garbled = range(0, 9)
+    assert np.linalg.norm(temp_after("ref", 0, garbled) - temp_after("ref", 1, garbled)) > 1e-3 * dT

@@ -21,9 +21,9 @@ STATUS_NAMES = {0: "GY_OK", -1: "GY_ERR_ARG", -2: "GY_ERR_CUDA", -3: "GY_ERR_STA
                 -5: "GY_ERR_UNSUPPORTED", -6: "GY_ERR_NONFINITE", -7: "GY_ERR_NOMEM"}
 
 P_FIELDS = dict(pos=0, pos0=1, disp=2, vel=3, stress=4, strain=5, pstrain=6, eqps=7, damage=8, smax=9,
-                mass=10, density=11, volume=12, normals=13)
+                mass=10, density=11, volume=12, normals=13, temp=14, tempgrad=15)
 P_WIDTH = dict(pos=3, pos0=3, disp=3, vel=3, stress=6, strain=6, pstrain=6, eqps=1, damage=1, smax=1,
-               mass=1, density=1, volume=1, normals=3)
+               mass=1, density=1, volume=1, normals=3, temp=1, tempgrad=3)
 PI_FIELDS = dict(cellid=0, material=1, object=2, device_slot=3)
 N_FIELDS = dict(mass=0, vel=1, force=2, vel1=3, acc1=4)
 
@@ -71,6 +71,7 @@ SIGNATURES = {
     "gy_set_particle_vel": (C.c_int, [_vp, C.c_int64, _i64p, _dp]),
     "gy_set_particle_stress": (C.c_int, [_vp, C.c_int64, _i64p, _dp]),
     "gy_set_particle_damage": (C.c_int, [_vp, C.c_int64, _i64p, _dp]),
+    "gy_set_particle_temp": (C.c_int, [_vp, C.c_int64, _i64p, _dp]),
     "gy_hold_particles": (C.c_int, [_vp, C.c_int64, _i64p]),
     "gy_set_particle_bc": (C.c_int, [_vp, C.c_int64, _i64p, _ip, _dp]),
     "gy_set_node_bc": (C.c_int, [_vp, C.c_int64, _i64p, _ip, _dp]),

@@ -49,7 +49,7 @@ struct gy_solver {
     std::vector<int> nidx[3];
 
     // host staging, insertion order (MaterialPoints)
-    std::vector<double> pos, vel, stress, dmg;
+    std::vector<double> pos, vel, stress, dmg, temp;
     std::vector<int> mat, obj, pbc_type;
     std::vector<double> pbc_val;
     std::vector<unsigned char> hold;
@@ -96,6 +96,9 @@ struct gy_solver {
     DevMaterial *d_mats = nullptr;
     int *d_status = nullptr;
     double *d_stats = nullptr;              // STATS_SLOTS x 8 conservation partials
+    float4 *d_therm = nullptr;              // (T, grad T) by insertion index, once a temperature is set
+    float2 *d_tnode = nullptr;              // node (T sum, T rate), zero between steps
+    bool thermal = false;                   // run the heat conduction kernels
     bool stats_fresh = false;               // d_stats holds the sums of the current state
     double mass_total = 0.0;                // FP64 total mass (no step changes a mass)
 
@@ -165,10 +168,13 @@ void free_device(gy_solver *h)
     }
     void *ptrs[] = {h->slab[0], h->slab[1], h->d_perm, h->d_seg, h->d_nseg, h->sort_mem, h->resort_mem, h->d_pbc_val,
                     h->d_refkey0, h->d_mats, h->d_status, h->d_stats, h->node_mem, h->d_cell_min,
-                    h->d_nidx[0], h->d_nidx[1], h->d_nidx[2], h->d_sc};
+                    h->d_nidx[0], h->d_nidx[1], h->d_nidx[2], h->d_sc, h->d_therm, h->d_tnode};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     h->d_sc = nullptr;
+    h->d_therm = nullptr;
+    h->d_tnode = nullptr;
+    h->thermal = false;
     h->slab[0] = h->slab[1] = nullptr;
     h->d_perm = h->d_seg = h->d_nseg = nullptr;
     h->sort_mem = nullptr;
@@ -310,6 +316,7 @@ gy_status gy_add_particles(gy_solver *h, int64_t n, const double *pos3, const in
         }
         for (int k = 0; k < 6; k++) h->stress.push_back(0.0);
         h->dmg.push_back(0.0);
+        h->temp.push_back(0.0);
         h->mat.push_back(mat ? mat[i] : 0);
         h->obj.push_back(obj ? obj[i] : 0);
         h->pbc_type.push_back(0);
@@ -377,6 +384,66 @@ gy_status gy_set_particle_bc(gy_solver *h, int64_t count, const int64_t *idx, co
     return GY_OK;
 }
 
+// Device buffers of the heat conduction terms; T starts from the host values.
+static gy_status enable_thermal(gy_solver *h)
+{
+    if (h->d_therm) return GY_OK;
+    gy_status st;
+    if ((st = dalloc(h, &h->d_therm, h->cap))) return st;
+    if ((st = dalloc(h, &h->d_tnode, h->nn))) return st;
+    std::vector<float4> th((size_t)h->cap, make_float4(0.f, 0.f, 0.f, 0.f));
+    for (long long i = 0; i < h->n; i++) th[i].x = (float)h->temp[i];
+    CK(h, cudaMemcpyAsync(h->d_therm, th.data(), (size_t)h->cap * sizeof(float4), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaMemsetAsync(h->d_tnode, 0, (size_t)h->nn * sizeof(float2), h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return GY_OK;
+}
+
+gy_status gy_set_particle_temp(gy_solver *h, int64_t count, const int64_t *idx, const double *T)
+{
+    if (!h || count < 0 || (count > 0 && (!idx || !T))) return GY_ERR_ARG;
+    bool any = false;
+    for (int64_t q = 0; q < count; q++) {
+        if (!valid_index(h, idx[q])) return fail(h, GY_ERR_ARG, "particle index out of range");
+        any = any || T[q] != 0.0;
+    }
+    if (!h->initialized) {
+        for (int64_t q = 0; q < count; q++) h->temp[idx[q]] = T[q];
+        return GY_OK;
+    }
+    // between steps: the device copy is authoritative once it exists
+    if (!h->d_therm && !any) return GY_OK;  // every temperature is still zero
+    cudaSetDevice(h->device);
+    gy_status st;
+    if ((st = enable_thermal(h))) return st;
+    if (count == 0) return GY_OK;
+    std::vector<int> ids((size_t)count);
+    std::vector<float> tv((size_t)count);
+    for (int64_t q = 0; q < count; q++) {
+        ids[q] = (int)idx[q];
+        tv[q] = (float)T[q];
+    }
+    int *d_ids = nullptr;
+    float *d_t = nullptr;
+    if ((st = dalloc(h, &d_ids, (size_t)count))) return st;
+    if ((st = dalloc(h, &d_t, (size_t)count))) {
+        cudaFree(d_ids);
+        return st;
+    }
+    cudaMemcpyAsync(d_ids, ids.data(), (size_t)count * sizeof(int), cudaMemcpyHostToDevice, h->stream);
+    cudaMemcpyAsync(d_t, tv.data(), (size_t)count * sizeof(float), cudaMemcpyHostToDevice, h->stream);
+    launch_thermal_set(h->d_therm, d_ids, d_t, (int)count, h->n, h->stream);
+    const cudaError_t e = cudaStreamSynchronize(h->stream);
+    cudaFree(d_ids);
+    cudaFree(d_t);
+    if (e != cudaSuccess) return fail(h, GY_ERR_CUDA, std::string("temperature upload: ") + cudaGetErrorString(e));
+    if (!h->thermal) {
+        h->thermal = true;
+        drop_graphs(h);  // the step now carries the thermal kernels
+    }
+    return GY_OK;
+}
+
 gy_status gy_set_node_bc(gy_solver *h, int64_t count, const int64_t *nodes, const int *type, const double *val4)
 {
     PRE_INIT(h);
@@ -417,6 +484,8 @@ static DevMaterial to_dev(const gy_material &m)
     d.gk_rate_coef = (float)(((mm + 3.0) / 3.0) * std::pow(alpha, 1.0 / 3.0));
     d.gk_logk = (float)std::log(m.damageK > 0 ? m.damageK : 1e-300);
     d.turb_stress = (float)m.turbStress;
+    d.k_th = (float)m.thermalConductivity;
+    d.c_th = (float)m.specificHeatCapacity;
     d.model = m.model;
     d.rigid = m.isRigid ? 1 : 0;
     d.damage = m.isDamage ? 1 : 0;
@@ -681,6 +750,8 @@ gy_status gy_initialize(gy_solver *h, const gy_material *mats, int nmat, const g
         h->g2p_grid = sms * g2p_blocks_per_sm(h->has_dp);
     }
     if ((st = alloc_nodes(h))) return st;
+    for (long long i = 0; i < n && !h->thermal; i++) h->thermal = h->temp[i] != 0.0;
+    if (h->thermal && (st = enable_thermal(h))) return st;
     CK(h, cudaStreamSynchronize(h->stream));
     h->initialized = true;
     h->steps = 0;
@@ -799,6 +870,7 @@ static void issue_step(gy_solver *h, const StepVariant &v, cudaEvent_t *tev)
     cudaMemsetAsync(h->nb.active_n, 0, sizeof(int), s);
     // (b) P2G
     launch_p2g(src, perm, skey, h->n, h->d_seg, h->d_nseg, h->persist_grid, h->nb, a, s);
+    if (h->thermal) launch_thermal_p2g(src, h->d_therm, perm, skey, h->n, h->d_seg, h->d_nseg, h->d_tnode, a, s);
     if (tev) cudaEventRecord(tev[2], s);
     // (c) periodic fold, nodal solve, grid BCs
     launch_fold(h->nb, a, s);
@@ -809,6 +881,8 @@ static void issue_step(gy_solver *h, const StepVariant &v, cudaEvent_t *tev)
     cudaMemsetAsync(h->d_stats, 0, STATS_SLOTS * 8 * sizeof(double), s);
     launch_g2p_update(src, dst, perm, skey, h->n, h->d_seg, h->d_nseg, h->g2p_grid, h->nb, a,
                       h->opt.track_normals != 0, h->opt.check_finite != 0, h->has_dp, s);
+    if (h->thermal)
+        launch_thermal_g2p(src, h->d_therm, perm, skey, h->n, h->d_seg, h->d_nseg, h->d_tnode, h->nb, a, s);
     if (tev) cudaEventRecord(tev[4], s);
 }
 
@@ -939,7 +1013,7 @@ static gy_status fetch_slab(gy_solver *h, std::vector<float> &hs)
     return GY_OK;
 }
 
-static const int kPWidth[GY_P_NFIELDS] = {3, 3, 3, 3, 6, 6, 6, 1, 1, 1, 1, 1, 1, 3};
+static const int kPWidth[GY_P_NFIELDS] = {3, 3, 3, 3, 6, 6, 6, 1, 1, 1, 1, 1, 1, 3, 1, 3};
 
 gy_status gy_get_particles(gy_solver *h, int field, double *out, int64_t count)
 {
@@ -957,9 +1031,31 @@ gy_status gy_get_particles(gy_solver *h, int field, double *out, int64_t count)
                 case GY_P_VEL: v = h->vel[3 * i + k]; break;
                 case GY_P_STRESS: v = h->stress[6 * i + k]; break;
                 case GY_P_DAMAGE: v = h->dmg[i]; break;
+                case GY_P_TEMP: v = h->temp[i]; break;
                 default: v = 0.0;
                 }
                 out[(size_t)i * w + k] = v;
+            }
+        }
+        return GY_OK;
+    }
+    if (field == GY_P_TEMP || field == GY_P_TEMPGRAD) {
+        // kept by insertion index; without a device copy every temperature is the host value
+        // and every gradient zero
+        std::vector<float4> th;
+        if (h->d_therm) {
+            th.resize((size_t)n);
+            cudaSetDevice(h->device);
+            CK(h, cudaStreamSynchronize(h->stream));
+            CK(h, cudaMemcpy(th.data(), h->d_therm, (size_t)n * sizeof(float4), cudaMemcpyDeviceToHost));
+        }
+        for (long long i = 0; i < n; i++) {
+            if (field == GY_P_TEMP) {
+                out[i] = h->d_therm ? (double)th[i].x : h->temp[i];
+            } else {
+                out[3 * i] = h->d_therm ? (double)th[i].y : 0.0;
+                out[3 * i + 1] = h->d_therm ? (double)th[i].z : 0.0;
+                out[3 * i + 2] = h->d_therm ? (double)th[i].w : 0.0;
             }
         }
         return GY_OK;
@@ -1177,14 +1273,14 @@ struct StateHeader {
     int32_t nbody, multi, has_dp, track_normals;
     int64_t steps;
     double t_prev, dt;
-    int32_t tables_valid, pad;
+    int32_t tables_valid, thermal;
 };
 
 size_t state_table_ints(const gy_solver *h) { return h->multi ? (size_t)h->g.nc * (h->nbody + 1) : 0; }
-size_t state_bytes(const gy_solver *h)
+size_t state_bytes(const gy_solver *h, bool thermal)
 {
     return sizeof(StateHeader) + (size_t)PF_COUNT * h->n * sizeof(float) + state_table_ints(h) * sizeof(int) +
-           (h->multi ? (size_t)h->nn * (sizeof(int2) + 1) : 0);
+           (h->multi ? (size_t)h->nn * (sizeof(int2) + 1) : 0) + (thermal ? (size_t)h->n * sizeof(float4) : 0);
 }
 }  // namespace
 
@@ -1192,7 +1288,7 @@ gy_status gy_state_size(const gy_solver *h, int64_t *bytes)
 {
     if (!h || !bytes) return GY_ERR_ARG;
     if (!h->initialized) return GY_ERR_STATE;
-    *bytes = (int64_t)state_bytes(h);
+    *bytes = (int64_t)state_bytes(h, h->d_therm != nullptr);
     return GY_OK;
 }
 
@@ -1200,7 +1296,8 @@ gy_status gy_state_save(gy_solver *h, void *buf, int64_t bytes)
 {
     if (!h || !buf) return GY_ERR_ARG;
     if (!h->initialized) return fail(h, GY_ERR_STATE, "nothing to save before gy_initialize");
-    if (bytes < (int64_t)state_bytes(h)) return fail(h, GY_ERR_ARG, "buffer smaller than gy_state_size");
+    if (bytes < (int64_t)state_bytes(h, h->d_therm != nullptr))
+        return fail(h, GY_ERR_ARG, "buffer smaller than gy_state_size");
     cudaSetDevice(h->device);
     CK(h, cudaStreamSynchronize(h->stream));
     StateHeader hd{};
@@ -1208,6 +1305,7 @@ gy_status gy_state_save(gy_solver *h, void *buf, int64_t bytes)
     hd.n = h->n; hd.cap = h->cap; hd.nn = h->nn; hd.nc = h->g.nc;
     hd.nbody = h->nbody; hd.multi = h->multi; hd.has_dp = h->has_dp; hd.track_normals = h->opt.track_normals;
     hd.steps = h->steps; hd.t_prev = h->t_prev; hd.dt = h->dt; hd.tables_valid = h->tables_valid;
+    hd.thermal = h->d_therm ? 1 : 0;
     char *p = static_cast<char *>(buf);
     std::memcpy(p, &hd, sizeof(hd));
     p += sizeof(hd);
@@ -1221,7 +1319,9 @@ gy_status gy_state_save(gy_solver *h, void *buf, int64_t bytes)
         CK(h, cudaMemcpy(p, h->nb.body, (size_t)h->nn * sizeof(int2), cudaMemcpyDeviceToHost));
         p += (size_t)h->nn * sizeof(int2);
         CK(h, cudaMemcpy(p, h->nb.has_rigid, (size_t)h->nn, cudaMemcpyDeviceToHost));
+        p += (size_t)h->nn;
     }
+    if (h->d_therm) CK(h, cudaMemcpy(p, h->d_therm, (size_t)h->n * sizeof(float4), cudaMemcpyDeviceToHost));
     return GY_OK;
 }
 
@@ -1236,7 +1336,7 @@ gy_status gy_state_load(gy_solver *h, const void *buf, int64_t bytes)
     if (hd.n != h->n || hd.nn != h->nn || hd.nc != h->g.nc || hd.nbody != h->nbody || hd.multi != (int)h->multi ||
         hd.has_dp != (int)h->has_dp || hd.track_normals != h->opt.track_normals)
         return fail(h, GY_ERR_ARG, "state belongs to a different model (grid, particles, bodies or options differ)");
-    if (bytes < (int64_t)state_bytes(h)) return fail(h, GY_ERR_ARG, "buffer shorter than the state");
+    if (bytes < (int64_t)state_bytes(h, hd.thermal != 0)) return fail(h, GY_ERR_ARG, "buffer shorter than the state");
     cudaSetDevice(h->device);
     CK(h, cudaStreamSynchronize(h->stream));
     const char *p = static_cast<const char *>(buf) + sizeof(hd);
@@ -1250,6 +1350,17 @@ gy_status gy_state_load(gy_solver *h, const void *buf, int64_t bytes)
         CK(h, cudaMemcpy(h->nb.body, p, (size_t)h->nn * sizeof(int2), cudaMemcpyHostToDevice));
         p += (size_t)h->nn * sizeof(int2);
         CK(h, cudaMemcpy(h->nb.has_rigid, p, (size_t)h->nn, cudaMemcpyHostToDevice));
+        p += (size_t)h->nn;
+    }
+    if (hd.thermal) {
+        gy_status st = enable_thermal(h);
+        if (st) return st;
+        CK(h, cudaMemcpy(h->d_therm, p, (size_t)h->n * sizeof(float4), cudaMemcpyHostToDevice));
+        CK(h, cudaMemset(h->d_tnode, 0, (size_t)h->nn * sizeof(float2)));
+        if (!h->thermal) {
+            h->thermal = true;
+            drop_graphs(h);
+        }
     }
     h->steps = hd.steps;
     h->t_prev = hd.t_prev;

@@ -58,6 +58,7 @@ struct DevMaterial {
     float gk_m, gk_rate_coef;   // Grady-Kipp m and ((m+3)/3) * alpha^(1/3)
     float gk_logk;              // log(k) for e_min = (V k)^(-1/m)
     float turb_stress;
+    float k_th, c_th;           // thermal conductivity, specific heat capacity
     int model, rigid, damage, damage_model;
 };
 constexpr int MAX_MATERIALS = 32;

@@ -74,6 +74,14 @@ void launch_body_assign(const NodeBufs &nb, const StepArgs &a, const int *cell_m
                         const int *nidx_x, const int *nidx_y, const int *nidx_z, cudaStream_t s);
 void launch_stats(const PView &p, long long n, double *out8, cudaStream_t s);
 
+// heat conduction (gy_thermal.cu): therm = (T, grad T) per insertion index, tnode = (T, rate)
+void launch_thermal_p2g(const PView &p, const float4 *therm, const int *perm, const int *skey, long long n,
+                        const int *seg_start, const int *nseg, float2 *tnode, const StepArgs &a, cudaStream_t s);
+void launch_thermal_g2p(const PView &p, float4 *therm, const int *perm, const int *skey, long long n,
+                        const int *seg_start, const int *nseg, const float2 *tnode, const NodeBufs &nb,
+                        const StepArgs &a, cudaStream_t s);
+void launch_thermal_set(float4 *therm, const int *ids, const float *T, int count, long long n, cudaStream_t s);
+
 // sort (gy_sort.cu): stable LSD radix sort of (key, index) pairs
 struct SortScratch {
     int *keys[2], *vals[2];

@@ -135,6 +135,7 @@ class MaterialPoints:
         self._vel = {}
         self._stress = {}
         self._damage = {}
+        self._temp = {}
         self._hold = set()
         self._bc = {}
         self._solver: Optional["Solver"] = None
@@ -197,6 +198,20 @@ class MaterialPoints:
     def setDamage(self, p, D):
         self._damage[int(p)] = float(D)
 
+    def setTemp(self, p, T):
+        """MaterialPoints::setTemp (MaterialPoints.cpp:319-322); also between steps."""
+        self.setTemps([p], [T])
+
+    def setTemps(self, idx, T):
+        """setTemp for many particles at once."""
+        idx = np.asarray(idx, np.int64).ravel()
+        T = np.broadcast_to(np.asarray(T, np.float64).ravel(), idx.shape)
+        if self._solver is None:
+            for p, t in zip(idx.tolist(), T.tolist()):
+                self._temp[int(p)] = float(t)
+        else:
+            self._solver._set_temps(idx, T)
+
     def holdParticle(self, p):
         self._hold.add(int(p))
 
@@ -234,6 +249,9 @@ class MaterialPoints:
 
     def getPlasticStrainArr(self):
         return self._field("pstrain").ravel()
+
+    def getTemperatureArr(self):
+        return self._field("temp").ravel()
 
     def getAccPlasticStrainArr(self):
         return self._field("eqps").ravel()
@@ -325,12 +343,13 @@ class MaterialPoints:
         v = self._field("vel")
         s = self._field("stress")
         rho = self._field("density").ravel()
+        T = self._field("temp").ravel()
         vm = np.sqrt(s[:, 0] ** 2 + s[:, 1] ** 2 + s[:, 2] ** 2 + (2 * s[:, 3]) ** 2 + (2 * s[:, 4]) ** 2 + (2 * s[:, 5]) ** 2)
         P = 0.33 * (s[:, 0] + s[:, 1] + s[:, 2])
         with open(f"output/{filename}_mpts_{step}.csv", "w") as f:
             f.write("x,y,z,vm,P,T,vx,vy,vz,rho\n")
             for i in range(len(x)):
-                f.write("%f,%f,%f,%f,%f,%f,%f,%f,%f,%f\n" % (x[i, 0], x[i, 1], x[i, 2], vm[i], P[i], 0.0,
+                f.write("%f,%f,%f,%f,%f,%f,%f,%f,%f,%f\n" % (x[i, 0], x[i, 1], x[i, 2], vm[i], P[i], T[i],
                                                            v[i, 0], v[i, 1], v[i, 2], rho[i]))
 
 
@@ -481,6 +500,10 @@ class Solver:
             idx = np.fromiter(mp._damage.keys(), np.int64)
             d = np.ascontiguousarray(np.array(list(mp._damage.values()), np.float64))
             L.check(lib.gy_set_particle_damage(h, len(idx), L.i64ptr(idx), L.dptr(d)), h, "setDamage")
+        if mp._temp:
+            idx = np.fromiter(mp._temp.keys(), np.int64)
+            t = np.ascontiguousarray(np.fromiter(mp._temp.values(), np.float64))
+            L.check(lib.gy_set_particle_temp(h, len(idx), L.i64ptr(idx), L.dptr(t)), h, "setTemp")
         if mp._hold:
             idx = np.array(sorted(mp._hold), np.int64)
             L.check(lib.gy_hold_particles(h, len(idx), L.i64ptr(idx)), h, "holdParticle")
@@ -554,6 +577,11 @@ class Solver:
                 raise KeyError(k)
             setattr(o, k, int(v))
         L.check(self.lib.gy_set_options(self.h, C.byref(o)), self.h, "options")
+
+    def _set_temps(self, idx, T):
+        idx = np.ascontiguousarray(idx, np.int64)
+        T = np.ascontiguousarray(T, np.float64)
+        L.check(self.lib.gy_set_particle_temp(self.h, len(idx), L.i64ptr(idx), L.dptr(T)), self.h, "setTemp")
 
     def save(self, path: str):
         """Write a binary snapshot of the device state (checkpoint); resume with load()."""
@@ -629,6 +657,9 @@ def from_scene(scene, device: int = -1, options: Optional[dict] = None) -> Solve
     nzs = np.nonzero(np.any(scene.stress != 0, axis=1))[0]
     mp._stress = {int(p): tuple(scene.stress[p]) for p in nzs}
     mp._hold = set(np.nonzero(scene.hold)[0].tolist())
+    temp = getattr(scene, "temp", None)
+    if temp is not None:
+        mp._temp = {int(p): float(temp[p]) for p in np.nonzero(temp)[0]}
     nzb = np.nonzero(scene.pbc_type)[0]
     mp._bc = {int(p): (int(scene.pbc_type[p]), list(scene.pbc_val[p])) for p in nzb}
     nodes._bc_type = scene.node_bc_type.astype(np.int32).copy()

@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define GY_ABI_VERSION 2
+#define GY_ABI_VERSION 3
 
 typedef int gy_status;
 enum {
@@ -98,10 +98,13 @@ typedef struct gy_stats {
 
 /* Particle fields for gy_get_particles / gy_set_particles (double, insertion order).
  * Widths: POS 3, POS0 3, DISP 3, VEL 3, STRESS 6, STRAIN 6, PSTRAIN 6, EQPS 1, DAMAGE 1,
- * SMAX 1, MASS 1, DENSITY 1, VOLUME 1, NORMALS 3.  Stress/strain order xx yy zz xy yz xz. */
+ * SMAX 1, MASS 1, DENSITY 1, VOLUME 1, NORMALS 3, TEMP 1, TEMPGRAD 3.  Stress/strain order
+ * xx yy zz xy yz xz.  TEMP / TEMPGRAD: getTemperatureArr (MaterialPoints.cpp:265) and the
+ * particle temperature gradient of the last G2P (Extrapolation.cpp:358-361). */
 enum gy_pfield {
     GY_P_POS = 0, GY_P_POS0, GY_P_DISP, GY_P_VEL, GY_P_STRESS, GY_P_STRAIN, GY_P_PSTRAIN,
     GY_P_EQPS, GY_P_DAMAGE, GY_P_SMAX, GY_P_MASS, GY_P_DENSITY, GY_P_VOLUME, GY_P_NORMALS,
+    GY_P_TEMP, GY_P_TEMPGRAD,
     GY_P_NFIELDS
 };
 /* Integer particle fields: CELLID (the reference's binning key, TimeIntegration.cpp:110-115),
@@ -143,6 +146,12 @@ gy_status gy_set_particle_stress(gy_solver *h, int64_t count, const int64_t *idx
 gy_status gy_set_particle_damage(gy_solver *h, int64_t count, const int64_t *idx, const double *d);
 gy_status gy_hold_particles(gy_solver *h, int64_t count, const int64_t *idx);
 gy_status gy_set_particle_bc(gy_solver *h, int64_t count, const int64_t *idx, const int *type, const double *val4);
+
+/* MaterialPoints::setTemp (MaterialPoints.cpp:319-322) for many particles.  Unlike the other
+ * setters it also works between steps (the reference's scripts reset temperatures every step,
+ * Examples/thermalTest.py:110-117).  The heat conduction terms of the step run once any
+ * temperature is nonzero. */
+gy_status gy_set_particle_temp(gy_solver *h, int64_t count, const int64_t *idx, const double *T);
 
 /* Nodes::setBC (Nodes.cpp:155-163) for many nodes: node index, BCTypes value, 4 values. */
 gy_status gy_set_node_bc(gy_solver *h, int64_t count, const int64_t *nodes, const int *type, const double *val4);

@@ -1,0 +1,162 @@
+"""GPU parity of the heat conduction terms (P2G Extrapolation.cpp:280-283, G2P :358-362,
+update TimeIntegration.cpp:49-50) against the oracle and the reference's golden fixture."""
+import os
+
+import numpy as np
+import pytest
+
+from graphyt_gb300 import scenes
+from tests.golden import make_golden
+from tests.helpers import rel_l2, run_gpu, run_oracle
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+# FP32 temperature: the change of T over a run is compared relative to its own size
+STEP_TOL = 1e-4
+MANY_STEP_TOL = 1e-3
+
+
+def _dT(temp, scene):
+    return temp - scene.temp
+
+
+def test_thermal_one_step_parity(gpu_lib, oracle_built):
+    """After two steps the temperature change and the gradient of the last G2P agree with
+    the FP64 restatement."""
+    sc = scenes.thermal_block()
+    gpu = run_gpu(sc, 2)
+    ref = run_oracle(sc, 2)
+    assert rel_l2(_dT(gpu._get_particles("temp"), sc), _dT(ref.pfield("temp"), sc)) <= STEP_TOL
+    assert rel_l2(gpu._get_particles("tempgrad"), ref.pfield("tempgrad")) <= STEP_TOL
+
+
+def test_thermal_golden(gpu_lib):
+    """30 steps against the reference's own output (harness sequence)."""
+    gold = np.load(os.path.join(GOLDEN, "thermal_block.npz"))
+    make, steps, _ = make_golden.CASES["thermal_block"]
+    sc = make()
+    gpu = run_gpu(sc, int(gold["steps"]))
+    ids = gold["ids"]
+    got = gpu._get_particles("temp")[ids]
+    assert rel_l2(got - sc.temp[ids], gold["temp"] - sc.temp[ids]) <= MANY_STEP_TOL
+    assert rel_l2(gpu._get_particles("tempgrad")[ids], gold["tempgrad"]) <= MANY_STEP_TOL
+    for f in ("vel", "stress"):
+        a, b = gpu._get_particles(f)[ids], gold[f]
+        if np.linalg.norm(b) == 0:
+            assert np.max(np.abs(a)) < 1e-9
+        else:
+            assert rel_l2(a, b) <= MANY_STEP_TOL
+
+
+def test_thermal_temperatures_reset_between_steps(gpu_lib, oracle_built):
+    """The pattern of Examples/thermalTest.py: the script sets the hot and cold zones'
+    temperatures again after every step; the GPU takes the values between steps."""
+    from graphyt_gb300 import graphyt
+    from oracle.oracle import Oracle
+    sc = scenes.thermal_block()
+    hot = np.nonzero(sc.temp == 100.0)[0]
+    cold = np.nonzero(sc.temp == 50.0)[0]
+    gpu = graphyt.from_scene(sc)
+    ref = Oracle(sc, "port")
+    dt = gpu.dt
+    for k in range(20):
+        gpu.iterate_GPU(k * dt, k)
+        ref.step()
+        gpu.mpts.setTemps(hot, 100.0)
+        gpu.mpts.setTemps(cold, 50.0)
+        ref.set_temps(hot, np.full(hot.size, 100.0))
+        ref.set_temps(cold, np.full(cold.size, 50.0))
+    gpu.Synchronise()
+    a, b = gpu.mpts.getTemperatureArr(), ref.pfield("temp")
+    assert np.array_equal(a[hot], b[hot]) and np.array_equal(a[cold], b[cold])
+    assert rel_l2(a - sc.temp, b - sc.temp) <= MANY_STEP_TOL
+    assert np.abs(b - sc.temp).max() > 1.0
+
+
+def test_thermal_set_after_initialize_enables_conduction(gpu_lib, oracle_built):
+    """Temperatures first set after the solver exists start the conduction terms; until then
+    every temperature stays at zero and no gradient forms."""
+    from graphyt_gb300 import graphyt
+    from oracle.oracle import Oracle
+    sc = scenes.thermal_block()
+    T = sc.temp.copy()
+    sc.temp = np.zeros(sc.n)
+    gpu = graphyt.from_scene(sc)
+    ref = Oracle(sc, "port")
+    dt = gpu.dt
+    for k in range(3):
+        gpu.iterate_GPU(k * dt, k)
+        ref.step()
+    assert np.all(gpu.mpts.getTemperatureArr() == 0.0)
+    assert np.all(gpu._get_particles("tempgrad") == 0.0)
+    nz = np.nonzero(T)[0]
+    gpu.mpts.setTemps(nz, T[nz])
+    ref.set_temps(nz, T[nz])
+    for k in range(3, 12):
+        gpu.iterate_GPU(k * dt, k)
+        ref.step()
+    gpu.Synchronise()
+    assert rel_l2(gpu._get_particles("temp") - T, ref.pfield("temp") - T) <= MANY_STEP_TOL
+
+
+def test_thermal_two_bodies(gpu_lib, oracle_built):
+    """Conduction is body-agnostic (centre-of-mass nodes), rigid particles count with m = 1:
+    two blocks in contact, the second rigid, with a temperature on part of each."""
+    sc = scenes.two_blocks(rigid_second=True)
+    y = sc.pos[:, 1]
+    sc.temp = np.where(y > np.median(y), 80.0, 0.0) + np.where(sc.obj == sc.obj.max(), 20.0, 0.0)
+    gpu = run_gpu(sc, 15)
+    ref = run_oracle(sc, 15)
+    assert rel_l2(gpu._get_particles("temp") - sc.temp, ref.pfield("temp") - sc.temp) <= MANY_STEP_TOL
+    assert rel_l2(gpu._get_particles("vel"), ref.pfield("vel")) <= MANY_STEP_TOL
+
+
+def test_thermal_checkpoint_resume(gpu_lib, tmp_path):
+    """The snapshot carries the temperatures and gradients."""
+    from graphyt_gb300 import graphyt
+    sc = scenes.thermal_block()
+    a = graphyt.from_scene(sc)
+    dt = a.dt
+    for k in range(8):
+        a.iterate_GPU(k * dt, k)
+    path = str(tmp_path / "state.bin")
+    a.save(path)
+    for k in range(8, 16):
+        a.iterate_GPU(k * dt, k)
+    a.Synchronise()
+    b = graphyt.from_scene(sc)
+    b.load(path)
+    for k in range(8, 16):
+        b.iterate_GPU(k * dt, k)
+    b.Synchronise()
+    ta, tb = a._get_particles("temp"), b._get_particles("temp")
+    assert rel_l2(tb - sc.temp, ta - sc.temp) < 1e-5
+
+
+def test_no_temperature_no_conduction(gpu_lib):
+    """With every temperature zero the step runs without the thermal kernels and the
+    temperature getters report zeros; the first nonzero temperature adds the three thermal
+    launches (P2G, G2P + update, node clear) to every step."""
+    from graphyt_gb300 import graphyt
+    lib = gpu_lib
+    sc = scenes.tiny_block(model=1)
+    gpu = graphyt.from_scene(sc)
+    dt = gpu.dt
+
+    def launches(k0, k1):
+        gpu.Synchronise()
+        n0 = lib.gy_kernel_launches()
+        for k in range(k0, k1):
+            gpu.iterate_GPU(k * dt, k)
+        gpu.Synchronise()
+        return lib.gy_kernel_launches() - n0
+
+    launches(0, 3)
+    plain = launches(3, 6)
+    assert np.all(gpu._get_particles("temp") == 0.0)
+    assert np.all(gpu._get_particles("tempgrad") == 0.0)
+    gpu.mpts.setTemps(np.arange(sc.n // 2), 10.0)
+    warm = launches(6, 9)
+    assert warm == plain + 9
+    assert np.any(gpu._get_particles("tempgrad") != 0.0)

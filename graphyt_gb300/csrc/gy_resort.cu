@@ -32,19 +32,29 @@ __device__ __forceinline__ long long movers_before(long long P, const unsigned *
     return (long long)wpref[w] + (b ? __popc(wmask[w] & ((1u << b) - 1u)) : 0);
 }
 
-// one warp per 32 slots: mover mask and count
+// mover mask and count per 32 slots: a warp takes four words at a time, all loads first
 __global__ void __launch_bounds__(RS_THREADS) k_rs_mask(const int *key, const int *prev, long long n, unsigned *wmask,
                                                           int *wcnt, long long nw)
 {
     const int lane = threadIdx.x & 31;
     const long long wstride = ((long long)gridDim.x * blockDim.x) >> 5;
-    for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nw; w += wstride) {
-        const long long i = w * 32 + lane;
-        const bool f = i < n && key[i] != prev[i];
-        const unsigned m = __ballot_sync(0xffffffffu, f);
-        if (lane == 0) {
-            wmask[w] = m;
-            wcnt[w] = __popc(m);
+    for (long long w0 = (((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 4; w0 < nw; w0 += wstride * 4) {
+        int ka[4], kb[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const long long i = (w0 + u) * 32 + lane;
+            ka[u] = i < n ? key[i] : 0;
+            kb[u] = i < n ? prev[i] : 0;
+        }
+        unsigned mine = 0u;
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const unsigned m = __ballot_sync(0xffffffffu, ka[u] != kb[u]);
+            if (lane == u) mine = m;
+        }
+        if (lane < 4 && w0 + lane < nw) {
+            wmask[w0 + lane] = mine;
+            wcnt[w0 + lane] = __popc(mine);
         }
     }
 }
@@ -327,7 +337,7 @@ void resort_keys(const int *key, const int *prev_skey, int *skey_out, int *perm_
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long long nw = (n + 31) / 32;
-    const unsigned wgrid = (unsigned)std::min<long long>((nw + RS_WARPS - 1) / RS_WARPS, (long long)sms * 16);
+    const unsigned wgrid = (unsigned)std::min<long long>((nw + 4 * RS_WARPS - 1) / (4 * RS_WARPS), (long long)sms * 16);
     const long long nw32 = (nw + 31) / 32;  // 32-word batches (compaction, stayer placement)
     const unsigned bgrid = (unsigned)std::max<long long>(1, std::min<long long>((nw32 + RS_WARPS - 1) / RS_WARPS, (long long)sms * 16));
     const unsigned qgrid = (unsigned)std::min<long long>((n + RS_THREADS - 1) / RS_THREADS, (long long)sms * 8);

@@ -198,30 +198,54 @@ const int *sort_pairs(const int *keys_in, int *perm_out, long long n, int key_bi
     return kin;
 }
 
-// Segments: starts of the runs of equal cell block in key order (the list is unordered).  A
-// grid of a few CTAs per SM strides over the keys, four per thread, all loads issued first.
-__global__ void __launch_bounds__(256) k_block_heads(const int *skey, long long n, int *seg_start, int *nseg)
+// Segments: starts of the runs of equal cell block in key order (the list is unordered).
+// Each CTA walks a contiguous range in tiles of 1024 keys (four per thread, loads first) and
+// gathers its heads in shared memory; one global atomic per CTA flush reserves their places,
+// so the segment counter sees a few hundred atomics instead of one per warp with a head.
+constexpr int BH_THREADS = 256;
+constexpr int BH_TILE = 4 * BH_THREADS;
+constexpr int BH_BUF = 2 * BH_TILE;
+
+__global__ void __launch_bounds__(BH_THREADS) k_block_heads(const int *skey, long long n, int *seg_start, int *nseg)
 {
+    __shared__ int buf[BH_BUF];
+    __shared__ int bcount, bbase;
     const int lane = threadIdx.x & 31;
-    const long long stride = 4LL * gridDim.x * blockDim.x;
-    for (long long b0 = 4LL * blockIdx.x * blockDim.x; b0 < n; b0 += stride) {
+    const unsigned lt = (1u << lane) - 1u;
+    const long long tiles = (n + BH_TILE - 1) / BH_TILE;
+    const long long t0 = tiles * blockIdx.x / gridDim.x, t1 = tiles * (blockIdx.x + 1) / gridDim.x;
+    if (threadIdx.x == 0) bcount = 0;
+    __syncthreads();
+    for (long long t = t0; t < t1; t++) {
+        const long long b0 = t * BH_TILE;
         int kc[4], kp[4];
 #pragma unroll
         for (int u = 0; u < 4; u++) {
-            const long long i = b0 + (long long)u * blockDim.x + threadIdx.x;
+            const long long i = b0 + (long long)u * BH_THREADS + threadIdx.x;
             kc[u] = i < n ? skey[i] : 0;
             kp[u] = (i < n && i > 0) ? skey[i - 1] : 0;
         }
 #pragma unroll
         for (int u = 0; u < 4; u++) {
-            const long long i = b0 + (long long)u * blockDim.x + threadIdx.x;
+            const long long i = b0 + (long long)u * BH_THREADS + threadIdx.x;
             const bool head = i < n && (i == 0 || (kc[u] >> CB_SHIFT) != (kp[u] >> CB_SHIFT));
             const unsigned mask = __ballot_sync(0xffffffffu, head);
             if (!mask) continue;
             int base = 0;
-            if (lane == 0) base = atomicAdd(nseg, __popc(mask));
+            if (lane == 0) base = atomicAdd(&bcount, __popc(mask));
             base = __shfl_sync(0xffffffffu, base, 0);
-            if (head) seg_start[base + __popc(mask & ((1u << lane) - 1u))] = (int)i;
+            if (head) buf[base + __popc(mask & lt)] = (int)i;
+        }
+        __syncthreads();
+        const int c = bcount;
+        __syncthreads();  // every thread has read the count before the next tile adds to it
+        if (c > BH_BUF - BH_TILE || (t == t1 - 1 && c > 0)) {
+            if (threadIdx.x == 0) bbase = atomicAdd(nseg, c);
+            __syncthreads();
+            for (int q = threadIdx.x; q < c; q += BH_THREADS) seg_start[bbase + q] = buf[q];
+            __syncthreads();
+            if (threadIdx.x == 0) bcount = 0;
+            __syncthreads();
         }
     }
 }
@@ -233,8 +257,8 @@ void launch_block_heads(const int *skey, long long n, int *seg_start, int *nseg,
         int dev = 0, sms = 1;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        const long long grid = std::min<long long>((n + 1023) / 1024, (long long)sms * 8);
-        k_block_heads<<<(unsigned)grid, 256, 0, s>>>(skey, n, seg_start, nseg);
+        const long long grid = std::min<long long>((n + BH_TILE - 1) / BH_TILE, (long long)sms * 4);
+        k_block_heads<<<(unsigned)grid, BH_THREADS, 0, s>>>(skey, n, seg_start, nseg);
         note_launch(1);
     }
 }

@@ -631,7 +631,7 @@ gy_status gy_initialize(gy_solver *h, const gy_material *mats, int nmat, const g
             h->pbc_type[i] = 0;  // every other particle BC has no body in the reference
 
     // ---- particle slab ----
-    h->cap = std::max<long long>(n, 1);
+    h->cap = (std::max<long long>(n, 1) + 31) / 32 * 32;  // every field starts on a 128-byte boundary
     const size_t slab_floats = (size_t)PF_COUNT * h->cap;
     for (int s = 0; s < 2; s++) {
         gy_status st = dalloc(h, &h->slab[s], slab_floats);

@@ -135,6 +135,28 @@ __global__ void k_scan_add(int *out, long long n, const int *block_off)
     }
 }
 
+// the add pass when the tile sums fit one tile: each CTA sums the tile sums before its own
+// (at most SCAN_TILE of them), so the scan of the sums needs no launch of its own
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_add_self(int *out, long long n, const int *block_sums)
+{
+    __shared__ int red[SCAN_THREADS / 32];
+    if (blockIdx.x == 0) return;  // the first tile's prefix is zero
+    int part = 0;
+    for (int b = threadIdx.x; b < (int)blockIdx.x; b += SCAN_THREADS) part += block_sums[b];
+    for (int off = 16; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) red[warp] = part;
+    __syncthreads();
+    int add = 0;
+#pragma unroll
+    for (int w = 0; w < SCAN_THREADS / 32; w++) add += red[w];
+    const long long i = (long long)blockIdx.x * SCAN_TILE + threadIdx.x;
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        const long long e = i + (long long)k * SCAN_THREADS;
+        if (e < n) out[e] += add;
+    }
+}
+
 size_t scan_tmp_ints(long long n)
 {
     size_t total = 0;
@@ -158,6 +180,11 @@ void exclusive_scan_int(const int *in, int *out, long long n, int *tmp, cudaStre
     int *sums = tmp, *sums_scan = tmp + nb + 16;
     k_scan_tile<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, out, n, sums);
     note_launch(1);
+    if (nb <= SCAN_TILE) {
+        k_scan_add_self<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(out, n, sums);
+        note_launch(1);
+        return;
+    }
     exclusive_scan_int(sums, sums_scan, nb, tmp + 2 * nb + 32, s);
     k_scan_add<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(out, n, sums_scan);
     note_launch(1);
@@ -199,11 +226,11 @@ const int *sort_pairs(const int *keys_in, int *perm_out, long long n, int key_bi
 }
 
 // Segments: starts of the runs of equal cell block in key order (the list is unordered).
-// Each CTA walks a contiguous range in tiles of 1024 keys (four per thread, loads first) and
-// gathers its heads in shared memory; one global atomic per CTA flush reserves their places,
-// so the segment counter sees a few hundred atomics instead of one per warp with a head.
+// Each CTA walks a contiguous range in tiles of 4096 keys -- four 16-byte loads per thread,
+// all issued first; a key's predecessor is the previous thread's last key -- and gathers its
+// heads in shared memory; one global atomic per CTA flush reserves their places.
 constexpr int BH_THREADS = 256;
-constexpr int BH_TILE = 4 * BH_THREADS;
+constexpr int BH_TILE = 16 * BH_THREADS;
 constexpr int BH_BUF = 2 * BH_TILE;
 
 __global__ void __launch_bounds__(BH_THREADS) k_block_heads(const int *skey, long long n, int *seg_start, int *nseg)
@@ -214,27 +241,47 @@ __global__ void __launch_bounds__(BH_THREADS) k_block_heads(const int *skey, lon
     const unsigned lt = (1u << lane) - 1u;
     const long long tiles = (n + BH_TILE - 1) / BH_TILE;
     const long long t0 = tiles * blockIdx.x / gridDim.x, t1 = tiles * (blockIdx.x + 1) / gridDim.x;
+    const int4 *k4 = reinterpret_cast<const int4 *>(skey);
+    const bool vec = (reinterpret_cast<unsigned long long>(skey) & 15ull) == 0;  // 16-byte loads need it
     if (threadIdx.x == 0) bcount = 0;
     __syncthreads();
     for (long long t = t0; t < t1; t++) {
+        // element e of vector u of this thread: index b0 + u * 4 * BH_THREADS + 4 * tid + e
         const long long b0 = t * BH_TILE;
-        int kc[4], kp[4];
+        int4 kv[4];
+        int kprev[4];
 #pragma unroll
         for (int u = 0; u < 4; u++) {
-            const long long i = b0 + (long long)u * BH_THREADS + threadIdx.x;
-            kc[u] = i < n ? skey[i] : 0;
-            kp[u] = (i < n && i > 0) ? skey[i - 1] : 0;
+            const long long i = b0 + (long long)u * 4 * BH_THREADS + 4 * threadIdx.x;
+            if (vec && i + 3 < n) {
+                kv[u] = k4[i >> 2];
+            } else {
+                kv[u].x = i < n ? skey[i] : 0;
+                kv[u].y = i + 1 < n ? skey[i + 1] : 0;
+                kv[u].z = i + 2 < n ? skey[i + 2] : 0;
+                kv[u].w = i + 3 < n ? skey[i + 3] : 0;
+            }
+            kprev[u] = (lane == 0 && i > 0 && i <= n) ? skey[i - 1] : 0;
         }
 #pragma unroll
         for (int u = 0; u < 4; u++) {
-            const long long i = b0 + (long long)u * BH_THREADS + threadIdx.x;
-            const bool head = i < n && (i == 0 || (kc[u] >> CB_SHIFT) != (kp[u] >> CB_SHIFT));
-            const unsigned mask = __ballot_sync(0xffffffffu, head);
-            if (!mask) continue;
-            int base = 0;
-            if (lane == 0) base = atomicAdd(&bcount, __popc(mask));
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (head) buf[base + __popc(mask & lt)] = (int)i;
+            const long long i = b0 + (long long)u * 4 * BH_THREADS + 4 * threadIdx.x;
+            const int up = __shfl_up_sync(0xffffffffu, kv[u].w, 1);
+            const int before = lane == 0 ? kprev[u] : up;
+            const int e[4] = {kv[u].x, kv[u].y, kv[u].z, kv[u].w};
+            int pk = before;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const long long ie = i + q;
+                const bool head = ie < n && (ie == 0 || (e[q] >> CB_SHIFT) != (pk >> CB_SHIFT));
+                pk = e[q];
+                const unsigned mask = __ballot_sync(0xffffffffu, head);
+                if (!mask) continue;
+                int base = 0;
+                if (lane == 0) base = atomicAdd(&bcount, __popc(mask));
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (head) buf[base + __popc(mask & lt)] = (int)ie;
+            }
         }
         __syncthreads();
         const int c = bcount;

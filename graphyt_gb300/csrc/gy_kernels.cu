@@ -1178,11 +1178,6 @@ __device__ __forceinline__ constexpr int g2p_stage_field(int f)
 }
 constexpr int G2P_NBASE = 19, G2P_NDP = 9;
 
-// Single-body G2P + update through a shared-memory node tile.  A CTA owns one segment (the
-// particles of one 4x4x4 cell block): it loads the block's 6x6x6 solved node tile once, with
-// massless nodes zeroed (they are skipped, Extrapolation.cpp:301-303), then runs one thread
-// per particle in sorted order.  The G2P sums are separable per axis: for every (j, k) node
-// row the three x nodes are contracted first, then weighted by the y/z factors.
 // Conservation sums of the updated particles, fused into G2P: each thread adds its particles'
 // momentum, kinetic and strain energy into its own shared-memory column (FP32, a few dozen
 // particles per thread), and the CTA adds its columns in FP64 into one of STATS_SLOTS global
@@ -1215,6 +1210,11 @@ __device__ __forceinline__ void stats_cta_flush(double *out, float (*col)[GY_G2P
     }
 }
 
+// Single-body G2P + update through a shared-memory node tile.  A CTA owns one segment (the
+// particles of one 4x4x4 cell block): it loads the block's 6x6x6 solved node tile once, with
+// massless nodes zeroed (they are skipped, Extrapolation.cpp:301-303), then runs one thread
+// per particle in sorted order.  The G2P sums are separable per axis: for every (j, k) node
+// row the three x nodes are contracted first, then weighted by the y/z factors.
 template <bool HAS_DP>
 __global__ void __launch_bounds__(GY_G2P_THREADS, GY_G2P_MINB) k_g2p_tiled(PView src, PView dst, const int *perm, const int *skey,
                                                       long long n, const int *seg_start, const int *nseg_ptr,

@@ -408,3 +408,24 @@ def thermal_block(seed: int = 0, n_side: int = 10, cellsize: float = 0.05, model
                materials=[material(model=model, bulkMod=1e7, shearMod=5000.0, density=1000.0)],
                gravity=[0.0, 0.0, 0.0], CFL=0.1, temp=temp)
     return _finish(sc, seed)
+
+
+def thermal_2d(seed: int = 0, cellsize: float = 0.01) -> Scene:
+    """2D plate of Examples/thermalTest.py at a reduced size: particles below 30 % of the
+    plate height at 50, above 72 % at 100, the rest at 0; copper thermal properties, elastic
+    (K 1e7, G 1000) at density 1000 so that a step's temperature change is resolvable in
+    FP32; no gravity."""
+    h = cellsize
+    psep = h / 2
+    lo, hi = 6 * h + 0.0931 * psep, 24 * h + 0.0931 * psep
+    pos = lattice_box([lo, lo + 0.0517 * psep - 0.0931 * psep, 0.0], [hi, hi, 0.0], psep)
+    n = pos.shape[0]
+    y = (pos[:, 1] - pos[:, 1].min()) / (pos[:, 1].max() - pos[:, 1].min())
+    temp = np.zeros(n)
+    temp[y < 0.3] = 50.0
+    temp[y > 0.72] = 100.0
+    sc = Scene(name="thermal_2d", L=[30 * h, 30 * h, 0.0], cellsize=h, psep=psep, pos=pos,
+               mat=np.zeros(n, np.int32), obj=np.zeros(n, np.int32),
+               materials=[material(model=1, bulkMod=1e7, shearMod=1000.0, density=1000.0)],
+               gravity=[0.0, 0.0, 0.0], CFL=0.1, temp=temp)
+    return _finish(sc, seed)

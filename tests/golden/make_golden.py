@@ -39,6 +39,7 @@ CASES = {
     "block_2d_elastic": (lambda: scenes.block_2d(model=1), 200, None),
     "block_2d_dp": (lambda: scenes.block_2d(model=4), 200, None),
     "thermal_block": (lambda: scenes.thermal_block(), 30, None),
+    "thermal_2d": (lambda: scenes.thermal_2d(), 40, None),
 }
 
 

@@ -31,10 +31,11 @@ def test_thermal_one_step_parity(gpu_lib, oracle_built):
     assert rel_l2(gpu._get_particles("tempgrad"), ref.pfield("tempgrad")) <= STEP_TOL
 
 
-def test_thermal_golden(gpu_lib):
-    """30 steps against the reference's own output (harness sequence)."""
-    gold = np.load(os.path.join(GOLDEN, "thermal_block.npz"))
-    make, steps, _ = make_golden.CASES["thermal_block"]
+@pytest.mark.parametrize("name", ["thermal_block", "thermal_2d"])
+def test_thermal_golden(gpu_lib, name):
+    """30-40 steps against the reference's own output (harness sequence), 3D and 2D."""
+    gold = np.load(os.path.join(GOLDEN, name + ".npz"))
+    make, steps, _ = make_golden.CASES[name]
     sc = make()
     gpu = run_gpu(sc, int(gold["steps"]))
     ids = gold["ids"]

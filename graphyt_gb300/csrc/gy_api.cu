@@ -99,6 +99,8 @@ struct gy_solver {
     float4 *d_therm = nullptr;              // (T, grad T) by insertion index, once a temperature is set
     float2 *d_tnode = nullptr;              // node (T sum, T rate), zero between steps
     bool thermal = false;                   // run the heat conduction kernels
+    void *d_tset = nullptr;                 // scratch of gy_set_particle_temp between steps
+    size_t tset_bytes = 0;
     bool stats_fresh = false;               // d_stats holds the sums of the current state
     double mass_total = 0.0;                // FP64 total mass (no step changes a mass)
 
@@ -168,12 +170,14 @@ void free_device(gy_solver *h)
     }
     void *ptrs[] = {h->slab[0], h->slab[1], h->d_perm, h->d_seg, h->d_nseg, h->sort_mem, h->resort_mem, h->d_pbc_val,
                     h->d_refkey0, h->d_mats, h->d_status, h->d_stats, h->node_mem, h->d_cell_min,
-                    h->d_nidx[0], h->d_nidx[1], h->d_nidx[2], h->d_sc, h->d_therm, h->d_tnode};
+                    h->d_nidx[0], h->d_nidx[1], h->d_nidx[2], h->d_sc, h->d_therm, h->d_tnode, h->d_tset};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     h->d_sc = nullptr;
     h->d_therm = nullptr;
     h->d_tnode = nullptr;
+    h->d_tset = nullptr;
+    h->tset_bytes = 0;
     h->thermal = false;
     h->slab[0] = h->slab[1] = nullptr;
     h->d_perm = h->d_seg = h->d_nseg = nullptr;
@@ -423,19 +427,24 @@ gy_status gy_set_particle_temp(gy_solver *h, int64_t count, const int64_t *idx, 
         ids[q] = (int)idx[q];
         tv[q] = (float)T[q];
     }
-    int *d_ids = nullptr;
-    float *d_t = nullptr;
-    if ((st = dalloc(h, &d_ids, (size_t)count))) return st;
-    if ((st = dalloc(h, &d_t, (size_t)count))) {
-        cudaFree(d_ids);
-        return st;
+    // a scratch kept across calls (scripts reset temperatures every step); the copies are
+    // synchronous with respect to the host buffers, the kernel runs in stream order
+    const size_t need = (size_t)count * (sizeof(int) + sizeof(float));
+    if (need > h->tset_bytes) {
+        CK(h, cudaStreamSynchronize(h->stream));
+        if (h->d_tset) cudaFree(h->d_tset);
+        h->d_tset = nullptr;
+        h->tset_bytes = 0;
+        CK(h, cudaMalloc(&h->d_tset, need));
+        h->tset_bytes = need;
     }
-    cudaMemcpyAsync(d_ids, ids.data(), (size_t)count * sizeof(int), cudaMemcpyHostToDevice, h->stream);
-    cudaMemcpyAsync(d_t, tv.data(), (size_t)count * sizeof(float), cudaMemcpyHostToDevice, h->stream);
+    int *d_ids = static_cast<int *>(h->d_tset);
+    float *d_t = reinterpret_cast<float *>(d_ids + count);
+    CK(h, cudaMemcpyAsync(d_ids, ids.data(), (size_t)count * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaMemcpyAsync(d_t, tv.data(), (size_t)count * sizeof(float), cudaMemcpyHostToDevice, h->stream));
     launch_thermal_set(h->d_therm, d_ids, d_t, (int)count, h->n, h->stream);
+    // the host vectors die on return and the next call may rewrite the scratch
     const cudaError_t e = cudaStreamSynchronize(h->stream);
-    cudaFree(d_ids);
-    cudaFree(d_t);
     if (e != cudaSuccess) return fail(h, GY_ERR_CUDA, std::string("temperature upload: ") + cudaGetErrorString(e));
     if (!h->thermal) {
         h->thermal = true;

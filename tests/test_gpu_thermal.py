@@ -161,3 +161,12 @@ def test_no_temperature_no_conduction(gpu_lib):
     warm = launches(6, 9)
     assert warm == plain + 9
     assert np.any(gpu._get_particles("tempgrad") != 0.0)
+
+
+def test_thermal_between_sorts(gpu_lib, oracle_built):
+    """With the particles re-ordered only every third step, the thermal kernels walk the
+    unsorted runs of cell blocks and give the same temperatures."""
+    sc = scenes.thermal_block()
+    gpu = run_gpu(sc, 12, options=dict(sort_every=3))
+    ref = run_oracle(sc, 12)
+    assert rel_l2(_dT(gpu._get_particles("temp"), sc), _dT(ref.pfield("temp"), sc)) <= MANY_STEP_TOL

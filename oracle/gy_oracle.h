@@ -4,7 +4,7 @@
  * CPU oracle for Graphyt's explicit GIMP MPM step: an FP64 restatement, written from
  * scratch, of Solver::iterate_CPU (Solver.cpp:86-292) and every function it calls.
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs load this
- * library.  It is the checker, never the product: the GPU path does not link it.
+ * library.  It checks results and is never the product: the GPU path does not link it.
  */
 #ifndef GY_ORACLE_H
 #define GY_ORACLE_H

@@ -501,6 +501,36 @@ __global__ void __launch_bounds__(P2G_CH) k_p2g_multi_tiled(PView P, const int *
                 const int li = cell & 3, lj = (cell >> 2) & 3, lk = cell >> 4;
                 const int t = ((lk + kk) * PT + (lj + jj)) * PT + (li + ii);
                 const int2 bp = tbody[t];
+                // a run whose particles all belong to one deformable object, the node's first
+                // body: its slot-0 mass, momentum and force equal the centre-of-mass sums
+                // (gravity included), so only those and the normal are summed
+                const int of0 = __float_as_int(Q2[p0].w);
+                bool one = !(of0 >> 16);
+                for (int p = p0 + 1; p < p1; p++) one = one && __float_as_int(Q2[p].w) == of0;
+                if (one && bp.x == (of0 & 0xFFFF)) {
+                    float c[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, nr[3] = {0.f, 0.f, 0.f};
+                    for (int p = p0; p < p1; p++) {
+                        const float2 X = W[ii][p], Y = W[3 + jj][p], Z = W[6 + kk][p];
+                        const float4 q0 = Q0[p], q1 = Q1[p], q2 = Q2[p];
+                        const float syz = Y.x * Z.x;
+                        const float w = X.x * syz, gx = X.y * syz, gy = X.x * Y.y * Z.x, gz = X.x * Y.x * Z.y;
+                        const float wm = w * q0.x;
+                        c[0] += wm; c[1] += w * q0.y; c[2] += w * q0.z; c[3] += w * q0.w;
+                        c[4] += -(gx * q1.x + gy * q1.w + gz * q2.y) + wm * grx;
+                        c[5] += -(gx * q1.w + gy * q1.y + gz * q2.x) + wm * gry;
+                        c[6] += -(gx * q2.y + gy * q2.x + gz * q1.z) + wm * grz;
+                        nr[0] += gx * q2.z; nr[1] += gy * q2.z; nr[2] += gz * q2.z;
+                    }
+                    if (!scatter_lane || c[0] == 0.f) continue;
+#pragma unroll
+                    for (int f = 0; f < 7; f++) {
+                        atomicAdd(&tile[f * PT_NODES + t], c[f]);
+                        atomicAdd(&tile[(7 + f) * PT_NODES + t], c[f]);
+                    }
+#pragma unroll
+                    for (int f = 0; f < 3; f++) atomicAdd(&tile[(14 + f) * PT_NODES + t], nr[f]);
+                    continue;
+                }
                 float c[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
                 float b0[10] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
                 float b1[10] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};

@@ -218,6 +218,8 @@ def main():
                          "Drucker-Prager + Grady-Kipp disc between rigid platens")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sort-every", type=int, default=1)
+    ap.add_argument("--column-height", type=float, default=0.765,
+                    help="dam break water column height in m (1.5 gives the configuration's 24 M particles)")
     ap.add_argument("--full-sort", action="store_true", help="full radix sort every step (no incremental re-sort)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -233,7 +235,8 @@ def main():
     from graphyt_gb300 import graphyt, scenes
 
     dist = Dist(world, local)
-    sc = scenes.dam_break(scale=args.scale) if args.workload == "dam_break" else scenes.brazilian_disc(scale=args.scale)
+    sc = (scenes.dam_break(scale=args.scale, height=args.column_height) if args.workload == "dam_break"
+          else scenes.brazilian_disc(scale=args.scale))
     n = sc.n
     solver = graphyt.from_scene(sc, device=local, options=dict(sort_every=args.sort_every, full_sort=int(args.full_sort)))
     lib, h = solver.lib, solver.h
@@ -319,6 +322,7 @@ def main():
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "dam_break_3d_newtonian" if not multi else "brazilian_disc_dp_gk_rigid_platens",
                        "particles": n, "nodes": sc.num_nodes(),
+                       **({"column_height_m": args.column_height} if not multi else {}),
                        "active_nodes": n_active, "cellsize": sc.cellsize, "psep": sc.psep,
                        "model": "newtonian" if not multi else "drucker_prager+grady_kipp, 3 bodies",
                        "sort_every": args.sort_every, "sort": "full" if args.full_sort else "incremental", "l2": "state larger than L2 (no flush needed)",

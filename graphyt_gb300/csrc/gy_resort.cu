@@ -24,6 +24,7 @@ constexpr int RS_TILE = RS_THREADS * RS_ITEMS;       // 2048
 constexpr int RS_WARPS = RS_THREADS / 32;
 constexpr int RS_RADIX = 256;
 constexpr int RS_MAX_CTAS = 1024;                    // mover-sort CTAs (2 per SM)
+constexpr int RS_MAX_PASSES = 4;                     // 8-bit digits of a non-negative int key
 
 __device__ __forceinline__ long long movers_before(long long P, const unsigned *wmask, const int *wpref)
 {
@@ -32,12 +33,32 @@ __device__ __forceinline__ long long movers_before(long long P, const unsigned *
     return (long long)wpref[w] + (b ? __popc(wmask[w] & ((1u << b) - 1u)) : 0);
 }
 
-// mover mask and count per 32 slots: a warp takes four words at a time, all loads first
+// CTA c of the mover sort owns [m c / G, m (c+1) / G); the owner of position pos is the
+// largest c with floor(m c / G) <= pos
+__device__ __forceinline__ int owner_cta(int pos, int m, int G)
+{
+    const int c = (int)(((long long)(pos + 1) * G - 1) / m);
+    return c < G - 1 ? c : G - 1;
+}
+
+// mover mask and count per 32 slots: a warp takes four words at a time, all loads first.
+// The kernel also clears the gap counters the previous re-sort left (its m movers are still
+// listed in gap[] and wpref[nw]) and the digit histograms this re-sort accumulates.
 __global__ void __launch_bounds__(RS_THREADS) k_rs_mask(const int *key, const int *prev, long long n, unsigned *wmask,
-                                                          int *wcnt, long long nw)
+                                                          int *wcnt, long long nw, const int *gap, const int *wpref,
+                                                          int *gapcnt, int *gwcnt, int *hist, int hist_ints)
 {
     const int lane = threadIdx.x & 31;
     const long long wstride = ((long long)gridDim.x * blockDim.x) >> 5;
+    {
+        const int mprev = wpref[nw];
+        const int t = blockIdx.x * blockDim.x + threadIdx.x, tstride = gridDim.x * blockDim.x;
+        for (int q = t; q < mprev; q += tstride) {
+            gapcnt[gap[q]] = 0;
+            gwcnt[gap[q] >> 5] = 0;
+        }
+        for (int q = t; q < hist_ints; q += tstride) hist[q] = 0;
+    }
     for (long long w0 = (((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 4; w0 < nw; w0 += wstride * 4) {
         int ka[4], kb[4];
 #pragma unroll
@@ -62,8 +83,9 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_mask(const int *key, const in
 // movers (key, slot) in slot order.  A warp takes 32 words at once (one mask per lane) and
 // visits only the words that hold movers.
 __global__ void __launch_bounds__(RS_THREADS) k_rs_compact(const int *key, const unsigned *wmask, const int *wpref,
-                                                             long long nw, int *bkey, int *bidx)
+                                                             long long nw, int *bkey, int *bidx, int *hist0, int G)
 {
+    const int mtot = wpref[nw];
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     const long long wstride = ((long long)gridDim.x * blockDim.x) >> 5;
@@ -80,8 +102,10 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_compact(const int *key, const
             if ((m >> lane) & 1u) {
                 const long long i = (w0 + u) * 32 + lane;
                 const int pos = base + __popc(m & lt);
-                bkey[pos] = key[i];
+                const int k = key[i];
+                bkey[pos] = k;
                 bidx[pos] = (int)i;
+                atomicAdd(&hist0[(k & 0xFF) * G + owner_cta(pos, mtot, G)], 1);  // first pass's digit counts
             }
         }
     }
@@ -98,21 +122,11 @@ __device__ __forceinline__ void cta_range(int m, int &c0, int &c1)
     c1 = (int)((long long)m * (blockIdx.x + 1) / gridDim.x);
 }
 
-__global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const int *keys, const int *m_ptr, int shift, int *hist)
-{
-    __shared__ int cnt[RS_RADIX];
-    for (int d = threadIdx.x; d < RS_RADIX; d += RS_THREADS) cnt[d] = 0;
-    __syncthreads();
-    int c0, c1;
-    cta_range(*m_ptr, c0, c1);
-    for (int e = c0 + threadIdx.x; e < c1; e += RS_THREADS) atomicAdd(&cnt[(keys[e] >> shift) & 0xFF], 1);
-    __syncthreads();
-    for (int d = threadIdx.x; d < RS_RADIX; d += RS_THREADS) hist[d * gridDim.x + blockIdx.x] = cnt[d];
-}
-
+// hist_next (or null on the last pass) receives the next pass's digit counts per owner CTA of
+// each output position, so no separate histogram launch is needed
 __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const int *keys_in, const int *vals_in, int *keys_out,
                                                              int *vals_out, const int *m_ptr, int shift,
-                                                             const int *offsets)
+                                                             const int *offsets, int *hist_next)
 {
     __shared__ int wcnt[RS_WARPS][RS_RADIX];  // per-warp digit counts, then per-warp bases
     __shared__ int base[RS_RADIX];            // running per-digit base of this CTA
@@ -159,6 +173,8 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const int *keys_in, c
                 const int pos = wcnt[warp][d] + rnk[r];
                 keys_out[pos] = key[r];
                 vals_out[pos] = val[r];
+                if (hist_next)
+                    atomicAdd(&hist_next[((key[r] >> (shift + 8)) & 0xFF) * gridDim.x + owner_cta(pos, *m_ptr, gridDim.x)], 1);
             }
         }
         __syncthreads();  // wcnt is reused by the next tile
@@ -280,17 +296,6 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_place_stayers(const int *key,
     }
 }
 
-// leave the gap counters zero for the next call
-__global__ void __launch_bounds__(RS_THREADS) k_rs_clear(const int *gap, const int *wpref, long long nw, int *gapcnt,
-                                                           int *gwcnt)
-{
-    const int m = wpref[nw];
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < m; q += gridDim.x * blockDim.x) {
-        gapcnt[gap[q]] = 0;
-        gwcnt[gap[q] >> 5] = 0;
-    }
-}
-
 // ---- scratch and driver ---------------------------------------------------------------
 
 size_t resort_scratch_ints(long long cap)
@@ -299,7 +304,7 @@ size_t resort_scratch_ints(long long cap)
     const long long ngw = (cap + 2 + 63) / 32 + 2;  // 32-gap words, one spare word past the end
     const long long hist = (long long)RS_RADIX * RS_MAX_CTAS;
     return (size_t)(3 * (nw + 1) + scan_tmp_ints(nw + 1) + 5 * cap + ngw * 32 + 2 * (ngw + 1) +
-                    scan_tmp_ints(ngw + 1) + 2 * hist + scan_tmp_ints(hist) + 64);
+                    scan_tmp_ints(ngw + 1) + (RS_MAX_PASSES + 1) * hist + scan_tmp_ints(hist) + 64);
 }
 
 void resort_bind(ResortScratch &rs, int *mem, long long cap)
@@ -321,14 +326,14 @@ void resort_bind(ResortScratch &rs, int *mem, long long cap)
     rs.gwcnt = p; p += ngw + 1;
     rs.gwpref = p; p += ngw + 1;
     rs.gscan_tmp = p; p += scan_tmp_ints(ngw + 1);
-    rs.hist = p; p += 2 * hist;
+    rs.hist = p; p += (RS_MAX_PASSES + 1) * hist;  // a digit histogram per pass, then the offsets
     rs.hscan_tmp = p;
     rs.cap = cap;
     rs.ngw = ngw;
 }
 
-// gapcnt, gwcnt and wcnt[nw] must be zero on entry (the memory is zeroed once); they are
-// left zero on return.
+// The scratch must be zero before the first call (it is zeroed once); each call clears the
+// gap counters its predecessor left and the digit histograms it uses.
 void resort_keys(const int *key, const int *prev_skey, int *skey_out, int *perm_out, long long n, int key_bits,
                  ResortScratch &rs, cudaStream_t s)
 {
@@ -341,22 +346,25 @@ void resort_keys(const int *key, const int *prev_skey, int *skey_out, int *perm_
     const long long nw32 = (nw + 31) / 32;  // 32-word batches (compaction, stayer placement)
     const unsigned bgrid = (unsigned)std::max<long long>(1, std::min<long long>((nw32 + RS_WARPS - 1) / RS_WARPS, (long long)sms * 16));
     const unsigned qgrid = (unsigned)std::min<long long>((n + RS_THREADS - 1) / RS_THREADS, (long long)sms * 8);
-    k_rs_mask<<<wgrid, RS_THREADS, 0, s>>>(key, prev_skey, n, rs.wmask, rs.wcnt, nw);
+    const int G = std::min(2 * sms, RS_MAX_CTAS);
+    const int passes = std::min(RS_MAX_PASSES, std::max(1, (key_bits + 7) / 8));
+    const int hg = RS_RADIX * G;                                    // one pass's histogram
+    int *offsets = rs.hist + (long long)RS_MAX_PASSES * RS_RADIX * RS_MAX_CTAS;
+    k_rs_mask<<<wgrid, RS_THREADS, 0, s>>>(key, prev_skey, n, rs.wmask, rs.wcnt, nw, rs.gap, rs.wpref, rs.gapcnt,
+                                           rs.gwcnt, rs.hist, passes * hg);
     cudaMemsetAsync(rs.wcnt + nw, 0, sizeof(int), s);
     exclusive_scan_int(rs.wcnt, rs.wpref, nw + 1, rs.wscan_tmp, s);
-    k_rs_compact<<<bgrid, RS_THREADS, 0, s>>>(key, rs.wmask, rs.wpref, nw, rs.bkey, rs.bidx);
+    // movers in slot order, with the first pass's digit counts per mover-sort CTA
+    k_rs_compact<<<bgrid, RS_THREADS, 0, s>>>(key, rs.wmask, rs.wpref, nw, rs.bkey, rs.bidx, rs.hist, G);
     note_launch(2);
     // stable sort of the movers by key; their count is wpref[nw]
-    const int G = std::min(2 * sms, RS_MAX_CTAS);
-    const long long hist = (long long)RS_RADIX * RS_MAX_CTAS;
     const int *m_ptr = rs.wpref + nw;
     int *kin = rs.bkey, *vin = rs.bidx, *kout = rs.tkey, *vout = rs.tidx;
-    const int passes = std::max(1, (key_bits + 7) / 8);
     for (int p = 0; p < passes; p++) {
-        k_rs_hist<<<G, RS_THREADS, 0, s>>>(kin, m_ptr, 8 * p, rs.hist);
-        exclusive_scan_int(rs.hist, rs.hist + hist, (long long)RS_RADIX * G, rs.hscan_tmp, s);
-        k_rs_scatter<<<G, RS_THREADS, 0, s>>>(kin, vin, kout, vout, m_ptr, 8 * p, rs.hist + hist);
-        note_launch(2);
+        exclusive_scan_int(rs.hist + (long long)p * hg, offsets, hg, rs.hscan_tmp, s);
+        k_rs_scatter<<<G, RS_THREADS, 0, s>>>(kin, vin, kout, vout, m_ptr, 8 * p, offsets,
+                                              p + 1 < passes ? rs.hist + (long long)(p + 1) * hg : nullptr);
+        note_launch(1);
         std::swap(kin, kout);
         std::swap(vin, vout);
     }
@@ -365,8 +373,7 @@ void resort_keys(const int *key, const int *prev_skey, int *skey_out, int *perm_
     exclusive_scan_int(rs.gwcnt, rs.gwpref, rs.ngw + 1, rs.gscan_tmp, s);
     k_rs_place_stayers<<<bgrid, RS_THREADS, 0, s>>>(key, n, rs.wmask, rs.wpref, nw, rs.gapcnt, rs.gwcnt, rs.gwpref,
                                                     skey_out, perm_out);
-    k_rs_clear<<<qgrid, RS_THREADS, 0, s>>>(rs.gap, rs.wpref, nw, rs.gapcnt, rs.gwcnt);
-    note_launch(3);
+    note_launch(2);
 }
 
 }  // namespace gy

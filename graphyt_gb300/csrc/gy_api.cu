@@ -87,6 +87,10 @@ struct gy_solver {
     StepScalars *d_sc = nullptr;            // this step's scalars (device)
     static constexpr int kRing = 32;        // pinned staging slots for the per-step scalars
     StepScalars *h_ring = nullptr;
+    struct Readback {
+        double part[STATS_SLOTS * 8];
+        int flags[4];
+    } *h_rb = nullptr;                      // pinned: the step's sums and status words
     cudaEvent_t ring_ev[kRing] = {};
     bool ring_busy[kRing] = {};
     long long ring_pos = 0;
@@ -163,6 +167,8 @@ void free_device(gy_solver *h)
     drop_graphs(h);
     if (h->h_ring) cudaFreeHost(h->h_ring);
     h->h_ring = nullptr;
+    if (h->h_rb) cudaFreeHost(h->h_rb);
+    h->h_rb = nullptr;
     for (int k = 0; k < gy_solver::kRing; k++) {
         if (h->ring_ev[k]) cudaEventDestroy(h->ring_ev[k]);
         h->ring_ev[k] = nullptr;
@@ -719,6 +725,7 @@ gy_status gy_initialize(gy_solver *h, const gy_material *mats, int nmat, const g
     if ((st = dalloc(h, &h->d_stats, STATS_SLOTS * 8))) return st;
     CK(h, cudaMalloc(&h->d_sc, sizeof(StepScalars)));
     CK(h, cudaMallocHost(&h->h_ring, gy_solver::kRing * sizeof(StepScalars)));
+    CK(h, cudaMallocHost(&h->h_rb, sizeof(gy_solver::Readback)));
     for (int k = 0; k < gy_solver::kRing; k++) CK(h, cudaEventCreateWithFlags(&h->ring_ev[k], cudaEventDisableTiming));
     // sort scratch
     h->sort_mem = nullptr;
@@ -1208,10 +1215,11 @@ gy_status gy_get_stats(gy_solver *h, gy_stats *out)
         gy_status st = sum_state(h);
         if (st) return st;
     }
-    double part[STATS_SLOTS * 8], v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    int flags[4];
-    CK(h, cudaMemcpyAsync(part, h->d_stats, sizeof(part), cudaMemcpyDeviceToHost, h->stream));
-    CK(h, cudaMemcpyAsync(flags, h->d_status, sizeof(flags), cudaMemcpyDeviceToHost, h->stream));
+    double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const double *part = h->h_rb->part;
+    const int *flags = h->h_rb->flags;
+    CK(h, cudaMemcpyAsync(h->h_rb->part, h->d_stats, sizeof(h->h_rb->part), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaMemcpyAsync(h->h_rb->flags, h->d_status, sizeof(h->h_rb->flags), cudaMemcpyDeviceToHost, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
     for (int q = 0; q < STATS_SLOTS; q++)
         for (int k = 1; k < 8; k++) v[k] += part[q * 8 + k];

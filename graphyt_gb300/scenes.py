@@ -429,3 +429,37 @@ def thermal_2d(seed: int = 0, cellsize: float = 0.01) -> Scene:
                materials=[material(model=1, bulkMod=1e7, shearMod=1000.0, density=1000.0)],
                gravity=[0.0, 0.0, 0.0], CFL=0.1, temp=temp)
     return _finish(sc, seed)
+
+
+def disk_impact_2d(seed: int = 0) -> Scene:
+    """Two elastic disks colliding in 2D, the setting of the reference's
+    test/test_2d_impact_elastic.py: domain 0.1 x 0.1 m, cellsize 5e-4, psep half of it, a
+    lattice offset by a quarter cell; disk 1 (objectID 1, material 0) centred at
+    (0.05, 0.03), disk 2 (objectID 2, material 1) three cells above it, radius 0.005, both
+    K 1000, G 500, density 10, moving towards each other at 1.5 m/s; CFL 0.1, gravity off.
+    The lattice follows this module's convention, not pyck's, so particle indices differ
+    from the reference test's."""
+    h = 0.0005
+    psep = h / 2
+    r = 0.005
+    c1 = (0.050, 0.03)
+    c2 = (0.050, 0.03 + 0.01 + 3 * h)
+    parts, obj, mat = [], [], []
+    for k, c in enumerate((c1, c2)):
+        lo = [c[0] - r + 0.25 * h, c[1] - r + 0.25 * h, 0.0]
+        pts = lattice_box(lo, [c[0] + r + 0.25 * h, c[1] + r + 0.25 * h, 0.0], psep)
+        pts = pts[(pts[:, 0] - c[0]) ** 2 + (pts[:, 1] - c[1]) ** 2 <= r * r]
+        parts.append(pts)
+        obj.append(np.full(len(pts), k + 1))
+        mat.append(np.full(len(pts), k))
+    pos = np.concatenate(parts)
+    mats = [material(bulkMod=1000.0, shearMod=500.0, density=10.0, model=1) for _ in range(2)]
+    sc = Scene("disk_impact_2d", [0.10, 0.10, 0.0], h, psep, pos, np.concatenate(mat).astype(np.int32),
+               np.concatenate(obj).astype(np.int32), mats)
+    sc.CFL = 0.1
+    sc.tmax = 5e-3
+    v = np.zeros((len(pos), 3))
+    v[sc.obj == 1, 1] = 1.5
+    v[sc.obj == 2, 1] = -1.5
+    sc.vel = v
+    return _finish(sc, seed)

@@ -40,6 +40,7 @@ CASES = {
     "block_2d_dp": (lambda: scenes.block_2d(model=4), 200, None),
     "thermal_block": (lambda: scenes.thermal_block(), 30, None),
     "thermal_2d": (lambda: scenes.thermal_2d(), 40, None),
+    "disk_impact_2d": (lambda: scenes.disk_impact_2d(), 300, None),
 }
 
 

@@ -768,13 +768,29 @@ gy_status gy_initialize(gy_solver *h, const gy_material *mats, int nmat, const g
     if ((st = alloc_nodes(h))) return st;
     for (long long i = 0; i < n && !h->thermal; i++) h->thermal = h->temp[i] != 0.0;
     if (h->thermal && (st = enable_thermal(h))) return st;
+    // the slab goes to the device in insertion order; put it in cell-key order now, so the
+    // first step reads it coalesced and re-sorts only the particles that move
+    h->resort_valid = false;
+    if (n > 0) {
+        int key_bits = 1;
+        const long long maxkey = (long long)h->g.nbx * h->g.nby * h->g.nbz * 64;
+        while ((1LL << key_bits) < maxkey) key_bits++;
+        const int *keys = reinterpret_cast<const int *>(h->slab[0]) + (size_t)PF_KEY * h->cap;
+        const int *sorted = sort_pairs(keys, h->d_perm, n, key_bits, h->ws, h->stream);
+        launch_gather_slab(h->slab[0], h->slab[1], h->d_perm, n, h->cap, PF_COUNT, h->stream);
+        if (h->skey_buf[0])
+            CK(h, cudaMemcpyAsync(h->skey_buf[0], sorted, (size_t)n * sizeof(int), cudaMemcpyDeviceToDevice, h->stream));
+        h->cur = 1;
+        h->sk = 0;
+        h->resort_valid = h->skey_buf[0] != nullptr;
+    }
     CK(h, cudaStreamSynchronize(h->stream));
+    CK(h, cudaGetLastError());
     h->initialized = true;
     h->steps = 0;
     h->t_prev = 0.0;
     h->since_sort = 1 << 30;
     h->tables_valid = false;
-    h->resort_valid = false;
     return sum_state(h);
 }
 

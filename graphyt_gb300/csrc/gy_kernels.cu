@@ -1742,6 +1742,32 @@ void launch_body_assign(const NodeBufs &nb, const StepArgs &a, const int *cell_m
 }
 
 // ---------------------------------------------------------------------------------------
+// Slab reorder: dst field f slot i = src field f slot perm[i], 32-bit words (every field).
+
+__global__ void __launch_bounds__(256) k_gather_slab(const float *src, float *dst, const int *perm, long long n,
+                                                     long long cap, int nfields)
+{
+    const long long total = n * nfields;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < total;
+         q += (long long)gridDim.x * blockDim.x) {
+        const long long f = q / n, i = q - f * n;
+        dst[f * cap + i] = src[f * cap + perm[i]];
+    }
+}
+
+void launch_gather_slab(const float *src, float *dst, const int *perm, long long n, long long cap, int nfields,
+                        cudaStream_t s)
+{
+    if (n <= 0) return;
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long grid = std::min<long long>((n * nfields + 255) / 256, (long long)sms * 16);
+    k_gather_slab<<<(unsigned)grid, 256, 0, s>>>(src, dst, perm, n, cap, nfields);
+    note_launch(1);
+}
+
+// ---------------------------------------------------------------------------------------
 // Conservation sums: mass, momentum, kinetic energy, strain energy, of a state that no step
 // has summed (after initialisation or a state load; a step's G2P sums its own output).
 // Each thread sums its few particles in FP32 (the state's own precision), the mass in FP64

@@ -73,6 +73,8 @@ void launch_body_tables(const PView &p, long long n, const StepArgs &a, int *cel
 void launch_body_assign(const NodeBufs &nb, const StepArgs &a, const int *cell_min, int nbody,
                         const int *nidx_x, const int *nidx_y, const int *nidx_z, cudaStream_t s);
 void launch_stats(const PView &p, long long n, double *out8, cudaStream_t s);
+void launch_gather_slab(const float *src, float *dst, const int *perm, long long n, long long cap, int nfields,
+                        cudaStream_t s);
 
 // heat conduction (gy_thermal.cu): therm = (T, grad T) per insertion index, tnode = (T, rate)
 void launch_thermal_p2g(const PView &p, const float4 *therm, const int *perm, const int *skey, long long n,

@@ -901,8 +901,12 @@ static void issue_step(gy_solver *h, const StepVariant &v, cudaEvent_t *tev)
     if (tev) cudaEventRecord(tev[1], s);
     cudaMemsetAsync(h->nb.active_n, 0, sizeof(int), s);
     // (b) P2G
-    launch_p2g(src, perm, skey, h->n, h->d_seg, h->d_nseg, h->persist_grid, h->nb, a, s);
-    if (h->thermal) launch_thermal_p2g(src, h->d_therm, perm, skey, h->n, h->d_seg, h->d_nseg, h->d_tnode, a, s);
+    // heat conduction: fused into the single-body P2G, a separate pass for body slots
+    const bool fused_thermal = h->thermal && !h->multi;
+    launch_p2g(src, perm, skey, h->n, h->d_seg, h->d_nseg, h->persist_grid, h->nb, a, s,
+               fused_thermal ? h->d_therm : nullptr, fused_thermal ? h->d_tnode : nullptr);
+    if (h->thermal && h->multi)
+        launch_thermal_p2g(src, h->d_therm, perm, skey, h->n, h->d_seg, h->d_nseg, h->d_tnode, a, s);
     if (tev) cudaEventRecord(tev[2], s);
     // (c) periodic fold, nodal solve, grid BCs
     launch_fold(h->nb, a, s);

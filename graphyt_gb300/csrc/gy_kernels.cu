@@ -168,11 +168,16 @@ __device__ __forceinline__ long long segment_chunk_end2(const int *skey, long lo
 struct ColAcc {
     float2 m[3], px[3], py[3], pz[3], fx[3], fy[3], fz[3];
 };
+// heat conduction sums of a column (only with THERMAL): node temperature sum S T m c and
+// sum grad S . ((m / rho) k grad T) (the node rate with its sign flipped)
+struct ColTh {
+    float2 t[3], r[3];
+};
 
 // staged pair mp of the run, halves selected by mk (1 = the particle belongs to the run)
-template <bool MASKED>
+template <bool MASKED, bool THERMAL>
 __device__ __forceinline__ void col_pair(ColAcc &A, const float4 (*W)[PC_NP], const float4 (*Q)[PC_NP], int mp,
-                                         int jj, int kk, float2 mk)
+                                         int jj, int kk, float2 mk, ColTh &T, const float4 (*QT)[PC_NP])
 {
     const int sl = pslot(mp);
     const float4 Y = W[3 + jj][sl], Z = W[6 + kk][sl];
@@ -200,13 +205,33 @@ __device__ __forceinline__ void col_pair(ColAcc &A, const float4 (*W)[PC_NP], co
         A.fy[i] = fma2(Gx, By, fma2(Sx, Cy, A.fy[i]));
         A.fz[i] = fma2(Gx, Bz, fma2(Sx, Cz, A.fz[i]));
     }
+    if (THERMAL) {
+        // QT[0] = (T m c, T m c', g_x, g_x'), QT[1] = (g_y, g_y', g_z, g_z') with g = (m/rho) k grad T / h
+        const float4 t0 = QT[0][sl], t1 = QT[1][sl];
+        const float2 tS = mul2(syz, lo2(t0)), Bt = mul2(hi2(t0), syz);
+        const float2 Ct = fma2(lo2(t1), gyz, mul2(hi2(t1), syg));
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            const float4 X = W[i][sl];
+            T.t[i] = fma2(lo2(X), tS, T.t[i]);
+            T.r[i] = fma2(hi2(X), Bt, fma2(lo2(X), Ct, T.r[i]));
+        }
+    }
 }
 
+// THERMAL adds the heat conduction terms of Extrapolation.cpp:280-283 (single body: no rigid
+// particles): two more node fields in the tile, flushed into tnode, from the particle
+// temperature and gradient kept by insertion index in therm.
+template <bool THERMAL>
 __global__ void __launch_bounds__(PC_THREADS, GY_PC_MINB) k_p2g_cols(PView P, const int *perm, const int *skey, long long n,
                                                          const int *seg_start, const int *nseg_ptr, int sorted,
-                                                         NodeBufs nb, GridGeom g)
+                                                         NodeBufs nb, GridGeom g, const float4 *therm, float2 *tnode,
+                                                         const DevMaterial *mats)
 {
-    __shared__ float tile[P2G_FIELDS * PT_NODES];
+    constexpr int NF = P2G_FIELDS + (THERMAL ? 2 : 0);
+    __shared__ float tile[NF * PT_NODES];
+    __shared__ float4 QTs[THERMAL ? 2 * PC_NP : 1];
+    float4 (*QT)[PC_NP] = reinterpret_cast<float4 (*)[PC_NP]>(QTs);  // used only with THERMAL
     __shared__ float4 W[9][PC_NP];    // pair m: (S, S', G, G') per axis/stencil node
     __shared__ float4 Q[5][PC_NP];    // pair m: (m, m'), (m vx, ..'), (m vy), (m vz), V sigma / h x6
     __shared__ int run_start[PC_CH + 1];
@@ -227,7 +252,7 @@ __global__ void __launch_bounds__(PC_THREADS, GY_PC_MINB) k_p2g_cols(PView P, co
         int bx, by, bz;
         decode_block(blk, g, bx, by, bz);
         const int tox = bx * CB, toy = by * CB, toz = g.is3d ? bz * CB : 0;
-        for (int t = tid; t < P2G_FIELDS * PT_NODES; t += PC_THREADS) tile[t] = 0.f;
+        for (int t = tid; t < NF * PT_NODES; t += PC_THREADS) tile[t] = 0.f;
         for (long long base = start;; base += PC_CH) {
             const long long ia = base + 2 * tid, ib = ia + 1;
             int cnt, ka = -1, kb = -1, kp = -1;
@@ -294,12 +319,31 @@ __global__ void __launch_bounds__(PC_THREADS, GY_PC_MINB) k_p2g_cols(PView P, co
                     const float b1 = vb ? P.f(PF_S0 + 2 * k + 1, jb) * scb : 0.f;
                     Q[2 + k][st] = make_float4(a0, b0, a1, b1);
                 }
+                if (THERMAL) {
+                    const DevMaterial &Ma = mats[info_mat((uint32_t)P.ii(PF_INFO, ja))];
+                    const float4 tha = therm[P.ii(PF_PID, ja)];
+                    const float vka = (ma / P.f(PF_RHO, ja)) * Ma.k_th * g.inv_h;
+                    float4 thb = make_float4(0.f, 0.f, 0.f, 0.f);
+                    float cb = 0.f, vkb = 0.f;
+                    if (vb) {
+                        const DevMaterial &Mb = mats[info_mat((uint32_t)P.ii(PF_INFO, jb))];
+                        thb = therm[P.ii(PF_PID, jb)];
+                        cb = Mb.c_th;
+                        vkb = (mb / P.f(PF_RHO, jb)) * Mb.k_th * g.inv_h;
+                    }
+                    QT[0][st] = make_float4(tha.x * ma * Ma.c_th, thb.x * mb * cb, vka * tha.y, vkb * thb.y);
+                    QT[1][st] = make_float4(vka * tha.z, vkb * thb.z, vka * tha.w, vkb * thb.w);
+                }
             } else {
                 const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
                 for (int k = 0; k < 9; k++) W[k][st] = z4;
 #pragma unroll
                 for (int k = 0; k < 5; k++) Q[k][st] = z4;
+                if (THERMAL) {
+                    QT[0][st] = z4;
+                    QT[1][st] = z4;
+                }
             }
             // ---- runs of equal cell, in order: run r is [run_start[r], run_start[r+1]) ----
             const unsigned ba = __ballot_sync(0xffffffffu, ha), bb = __ballot_sync(0xffffffffu, hb);
@@ -333,13 +377,17 @@ __global__ void __launch_bounds__(PC_THREADS, GY_PC_MINB) k_p2g_cols(PView P, co
                 const bool rv = r < R;
                 const int p0 = rv ? run_start[r] : 0, p1 = rv ? run_start[r + 1] : 0;
                 ColAcc A;
+                ColTh TH;
 #pragma unroll
-                for (int i = 0; i < 3; i++) A.m[i] = A.px[i] = A.py[i] = A.pz[i] = A.fx[i] = A.fy[i] = A.fz[i] = z2;
+                for (int i = 0; i < 3; i++) {
+                    A.m[i] = A.px[i] = A.py[i] = A.pz[i] = A.fx[i] = A.fy[i] = A.fz[i] = z2;
+                    TH.t[i] = TH.r[i] = z2;
+                }
                 const bool full = rv && p1 - p0 == 8 && !(p0 & 1);
                 if (__all_sync(0xffffffffu, full)) {
                     // three full cells (psep = cellsize / 2) on pair boundaries: four pairs each
 #pragma unroll PC_UNROLL
-                    for (int k = 0; k < 4; k++) col_pair<false>(A, W, Q, (p0 >> 1) + k, jj, kk, z2);
+                    for (int k = 0; k < 4; k++) col_pair<false, THERMAL>(A, W, Q, (p0 >> 1) + k, jj, kk, z2, TH, QT);
                 } else {
                     const int m0 = p0 >> 1, np = rv ? ((p1 + 1) >> 1) - m0 : 0;
                     const int maxp = __reduce_max_sync(0xffffffffu, np);
@@ -348,7 +396,7 @@ __global__ void __launch_bounds__(PC_THREADS, GY_PC_MINB) k_p2g_cols(PView P, co
                         const int q = 2 * mp;
                         const float2 mk = make_float2(k < np && q >= p0 && q < p1 ? 1.f : 0.f,
                                                       k < np && q + 1 >= p0 && q + 1 < p1 ? 1.f : 0.f);
-                        col_pair<true>(A, W, Q, mp, jj, kk, mk);
+                        col_pair<true, THERMAL>(A, W, Q, mp, jj, kk, mk, TH, QT);
                     }
                 }
                 if (!scatter_lane || !rv) continue;
@@ -368,6 +416,10 @@ __global__ void __launch_bounds__(PC_THREADS, GY_PC_MINB) k_p2g_cols(PView P, co
                     atomicAdd(&tile[4 * PT_NODES + t], -(A.fx[i].x + A.fx[i].y));
                     atomicAdd(&tile[5 * PT_NODES + t], -(A.fy[i].x + A.fy[i].y));
                     atomicAdd(&tile[6 * PT_NODES + t], -(A.fz[i].x + A.fz[i].y));
+                    if (THERMAL) {
+                        atomicAdd(&tile[7 * PT_NODES + t], TH.t[i].x + TH.t[i].y);
+                        atomicAdd(&tile[8 * PT_NODES + t], -(TH.r[i].x + TH.r[i].y));
+                    }
                 }
             }
             if (cnt < PC_CH) break;
@@ -383,6 +435,10 @@ __global__ void __launch_bounds__(PC_THREADS, GY_PC_MINB) k_p2g_cols(PView P, co
             const int nd = node_index(ni, nj, nk, g);
             red_add4(&nb.acc0[nd], m, px, py, pz);
             red_add4(&nb.acc1[nd], fx, fy, fz, 0.f);
+            if (THERMAL) {
+                atomicAdd(&tnode[nd].x, tile[7 * PT_NODES + t]);
+                atomicAdd(&tnode[nd].y, tile[8 * PT_NODES + t]);
+            }
             mark_node(nb, ni, nj, nk, g);
         }
         __syncthreads();
@@ -601,7 +657,8 @@ __global__ void __launch_bounds__(P2G_CH) k_p2g_multi_tiled(PView P, const int *
 }
 
 void launch_p2g(const PView &p, const int *perm, const int *skey, long long n, const int *seg_start,
-                const int *nseg, int persist_grid, const NodeBufs &nb, const StepArgs &a, cudaStream_t s)
+                const int *nseg, int persist_grid, const NodeBufs &nb, const StepArgs &a, cudaStream_t s,
+                const float4 *therm, float2 *tnode)
 {
     if (n == 0) return;
     if (a.multi_body) {
@@ -615,7 +672,21 @@ void launch_p2g(const PView &p, const int *perm, const int *skey, long long n, c
         }
         k_p2g_multi_tiled<<<mgrid, P2G_CH, 0, s>>>(p, perm, skey, n, seg_start, nseg, perm ? 1 : 0, nb, a);
     } else {
-        k_p2g_cols<<<persist_grid, PC_THREADS, 0, s>>>(p, perm, skey, n, seg_start, nseg, perm ? 1 : 0, nb, a.g);
+        if (therm) {
+            static int tgrid = 0;  // persistent grid of the variant with heat conduction
+            if (tgrid == 0) {
+                int dev = 0, sms = 1, b = 0;
+                cudaGetDevice(&dev);
+                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_p2g_cols<true>, PC_THREADS, 0);
+                tgrid = sms * std::max(b, 1);
+            }
+            k_p2g_cols<true><<<tgrid, PC_THREADS, 0, s>>>(p, perm, skey, n, seg_start, nseg, perm ? 1 : 0, nb, a.g,
+                                                           therm, tnode, a.mats);
+        } else {
+            k_p2g_cols<false><<<persist_grid, PC_THREADS, 0, s>>>(p, perm, skey, n, seg_start, nseg, perm ? 1 : 0, nb,
+                                                                   a.g, nullptr, nullptr, nullptr);
+        }
     }
     note_launch(1);
 }
@@ -623,7 +694,7 @@ void launch_p2g(const PView &p, const int *perm, const int *skey, long long n, c
 int p2g_blocks_per_sm()
 {
     int b = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_p2g_cols, PC_THREADS, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_p2g_cols<false>, PC_THREADS, 0);
     return b > 0 ? b : 1;
 }
 

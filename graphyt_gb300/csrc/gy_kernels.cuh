@@ -59,8 +59,11 @@ void note_launch(int k);
 long long launch_count();
 
 // launchers (gy_kernels.cu)
+// therm / tnode non-null: the single-body kernel also sums the heat conduction node fields
+// (multi-body problems run launch_thermal_p2g instead)
 void launch_p2g(const PView &p, const int *perm, const int *skey, long long n, const int *seg_start,
-                const int *nseg, int persist_grid, const NodeBufs &nb, const StepArgs &a, cudaStream_t s);
+                const int *nseg, int persist_grid, const NodeBufs &nb, const StepArgs &a, cudaStream_t s,
+                const float4 *therm = nullptr, float2 *tnode = nullptr);
 void launch_fold(const NodeBufs &nb, const StepArgs &a, cudaStream_t s);
 void launch_solve(const NodeBufs &nb, const StepArgs &a, bool keep_node_fields, cudaStream_t s);
 void launch_g2p_update(const PView &src, const PView &dst, const int *perm, const int *skey, long long n,

@@ -218,6 +218,8 @@ def main():
                          "Drucker-Prager + Grady-Kipp disc between rigid platens")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sort-every", type=int, default=1)
+    ap.add_argument("--temperature", type=float, default=0.0,
+                    help="initial temperature of every particle; nonzero runs the heat conduction terms")
     ap.add_argument("--column-height", type=float, default=0.765,
                     help="dam break water column height in m (1.5 gives the configuration's 24 M particles)")
     ap.add_argument("--full-sort", action="store_true", help="full radix sort every step (no incremental re-sort)")
@@ -237,6 +239,10 @@ def main():
     dist = Dist(world, local)
     sc = (scenes.dam_break(scale=args.scale, height=args.column_height) if args.workload == "dam_break"
           else scenes.brazilian_disc(scale=args.scale))
+    if args.temperature:
+        # a linear profile along x, so the conduction terms have gradients to carry
+        x = sc.pos[:, 0]
+        sc.temp = args.temperature * (1.0 + (x - x.min()) / max(x.max() - x.min(), 1e-30))
     n = sc.n
     solver = graphyt.from_scene(sc, device=local, options=dict(sort_every=args.sort_every, full_sort=int(args.full_sort)))
     lib, h = solver.lib, solver.h
@@ -323,6 +329,7 @@ def main():
             "config": {"workload": "dam_break_3d_newtonian" if not multi else "brazilian_disc_dp_gk_rigid_platens",
                        "particles": n, "nodes": sc.num_nodes(),
                        **({"column_height_m": args.column_height} if not multi else {}),
+                       **({"heat_conduction": True} if args.temperature else {}),
                        "active_nodes": n_active, "cellsize": sc.cellsize, "psep": sc.psep,
                        "model": "newtonian" if not multi else "drucker_prager+grady_kipp, 3 bodies",
                        "sort_every": args.sort_every, "sort": "full" if args.full_sort else "incremental", "l2": "state larger than L2 (no flush needed)",

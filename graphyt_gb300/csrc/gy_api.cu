@@ -916,9 +916,12 @@ static void issue_step(gy_solver *h, const StepVariant &v, cudaEvent_t *tev)
     // the conservation sums of the updated state
     cudaMemsetAsync(h->d_stats, 0, STATS_SLOTS * 8 * sizeof(double), s);
     launch_g2p_update(src, dst, perm, skey, h->n, h->d_seg, h->d_nseg, h->g2p_grid, h->nb, a,
-                      h->opt.track_normals != 0, h->opt.check_finite != 0, h->has_dp, s);
-    if (h->thermal)
+                      h->opt.track_normals != 0, h->opt.check_finite != 0, h->has_dp, s,
+                      fused_thermal ? h->d_therm : nullptr, fused_thermal ? h->d_tnode : nullptr);
+    if (h->thermal && h->multi)
         launch_thermal_g2p(src, h->d_therm, perm, skey, h->n, h->d_seg, h->d_nseg, h->d_tnode, h->nb, a, s);
+    else if (h->thermal)
+        launch_thermal_clear(h->nb, a, h->d_tnode, s);
     if (tev) cudaEventRecord(tev[4], s);
 }
 

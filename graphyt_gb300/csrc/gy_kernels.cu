@@ -1258,6 +1258,7 @@ __device__ __forceinline__ void update_after_g2p(PState &st, const int c0[3], fl
 #ifndef GY_G2P_THREADS
 #define GY_G2P_THREADS 64
 #endif
+#define GY_G2P_MINB_TH 12  // the variant with heat conduction: 80 registers
 
 // 4-byte asynchronous global -> shared copy (no register holds the value in flight)
 __device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
@@ -1316,14 +1317,19 @@ __device__ __forceinline__ void stats_cta_flush(double *out, float (*col)[GY_G2P
 // massless nodes zeroed (they are skipped, Extrapolation.cpp:301-303), then runs one thread
 // per particle in sorted order.  The G2P sums are separable per axis: for every (j, k) node
 // row the three x nodes are contracted first, then weighted by the y/z factors.
-template <bool HAS_DP>
-__global__ void __launch_bounds__(GY_G2P_THREADS, GY_G2P_MINB) k_g2p_tiled(PView src, PView dst, const int *perm, const int *skey,
-                                                      long long n, const int *seg_start, const int *nseg_ptr,
-                                                      int sorted, NodeBufs nb, StepArgs a, int check_finite)
+// THERMAL adds the heat conduction terms (Extrapolation.cpp:132-134, 358-362 and
+// TimeIntegration.cpp:49-50): the node (T, rate) tile, the particle's temperature gradient and
+// rate summed with the same weights, and its temperature update, in therm by insertion index.
+template <bool HAS_DP, bool THERMAL>
+__global__ void __launch_bounds__(GY_G2P_THREADS, THERMAL ? GY_G2P_MINB_TH : GY_G2P_MINB)
+    k_g2p_tiled(PView src, PView dst, const int *perm, const int *skey, long long n, const int *seg_start,
+                const int *nseg_ptr, int sorted, NodeBufs nb, StepArgs a, int check_finite, float4 *therm,
+                const float2 *tnode)
 {
     constexpr int NST = G2P_NBASE + (HAS_DP ? G2P_NDP : 0);
     __shared__ float4 TV[PT_NODES];  // (v1x, v1y, v1z, a1z), zero for massless nodes
     __shared__ float2 TA[PT_NODES];  // (a1x, a1y)
+    __shared__ float2 TN[THERMAL ? PT_NODES : 1];  // node (T sum, T rate)
     __shared__ float stage[NST][GY_G2P_THREADS];
     __shared__ float s_st[NSTAT][GY_G2P_THREADS];
     __shared__ long long s_end;
@@ -1342,16 +1348,19 @@ __global__ void __launch_bounds__(GY_G2P_THREADS, GY_G2P_MINB) k_g2p_tiled(PView
         // the solved node tile, loaded into registers before anything waits on it
         constexpr int TILE_ITERS = (PT_NODES + GY_G2P_THREADS - 1) / GY_G2P_THREADS;
         float4 TVr[TILE_ITERS], TAr[TILE_ITERS];
+        float2 TNr[THERMAL ? TILE_ITERS : 1];
 #pragma unroll
         for (int h = 0; h < TILE_ITERS; h++) {
             const int t = tid + h * GY_G2P_THREADS;
             TVr[h] = z4;
             TAr[h] = z4;
+            if (THERMAL) TNr[h] = make_float2(0.f, 0.f);
             const int ni = tox + t % PT, nj = toy + (t / PT) % PT, nk = toz + t / (PT * PT);
             if (t < PT_NODES && ni < g.nx && nj < g.ny && nk < g.nz) {
                 const int nd = node_index(ni, nj, nk, g);
                 TVr[h] = __ldg(&nb.gv[nd]);
                 TAr[h] = __ldg(&nb.ga[nd]);
+                if (THERMAL) TNr[h] = __ldg(&tnode[nd]);
             }
         }
         __syncthreads();  // the previous segment's particles are done with the tile
@@ -1363,6 +1372,7 @@ __global__ void __launch_bounds__(GY_G2P_THREADS, GY_G2P_MINB) k_g2p_tiled(PView
             if (V.x == 0.0f) { V = z4; A = z4; }
             TV[t] = make_float4(V.y, V.z, V.w, A.z);
             TA[t] = make_float2(A.x, A.y);
+            if (THERMAL) TN[t] = TNr[h];
         }
         for (long long base = start;; base += blockDim.x) {
             int cnt, key = 0;
@@ -1411,6 +1421,7 @@ __global__ void __launch_bounds__(GY_G2P_THREADS, GY_G2P_MINB) k_g2p_tiled(PView
                 float2 vg01 = z2, acc01 = z2, vz_az = z2;       // (vg_x, vg_y), (a_x, a_y), (vg_z, a_z)
                 float2 Lc0 = z2, Lc1 = z2, Lc2 = z2;            // (L[0][b], L[1][b]) for b = x, y, z
                 float L20 = 0.f, L21 = 0.f, L22 = 0.f;           // L[2][b]
+                float gtx = 0.f, gty = 0.f, gtz = 0.f, trate = 0.f;  // heat conduction (THERMAL)
                 float2 Sx2[3], Gx2[3];
 #pragma unroll
                 for (int k = 0; k < 3; k++) {
@@ -1448,6 +1459,21 @@ __global__ void __launch_bounds__(GY_G2P_THREADS, GY_G2P_MINB) k_g2p_tiled(PView
                         L21 = fmaf(gyz, xv2a2.x, L21);
                         Lc2 = fma2(syg2, xv01, Lc2);
                         L22 = fmaf(syg, xv2a2.x, L22);
+                        if (THERMAL) {
+                            const float2 *tn = TN + t0 + (kk * PT + jj) * PT;
+                            float xT = 0.f, xgT = 0.f, xR = 0.f;
+#pragma unroll
+                            for (int ii = 0; ii < 3; ii++) {
+                                const float2 q = tn[ii];
+                                xT = fmaf(Sx[ii], q.x, xT);
+                                xgT = fmaf(Gx[ii], q.x, xgT);
+                                xR = fmaf(Sx[ii], q.y, xR);
+                            }
+                            gtx = fmaf(syz, xgT, gtx);
+                            gty = fmaf(gyz, xT, gty);
+                            gtz = fmaf(syg, xT, gtz);
+                            trate = fmaf(syz, xR, trate);
+                        }
                     }
                 }
                 float acc[3] = {acc01.x, acc01.y, vz_az.y}, vg[3] = {vg01.x, vg01.y, vz_az.x};
@@ -1477,11 +1503,14 @@ __global__ void __launch_bounds__(GY_G2P_THREADS, GY_G2P_MINB) k_g2p_tiled(PView
                     st.dmg = 0.f;
                     st.smax = 0.f;
                 }
+                float4 th = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (THERMAL) th = therm[st.pid];  // loads while the update runs
                 int c0[3];
                 decode_key(st.key, g, c0[0], c0[1], c0[2]);
                 if (!g.is3d) c0[2] = 0;
                 update_after_g2p<HAS_DP>(st, c0, acc, vg, L, a, check_finite != 0);
                 store_state<HAS_DP>(dst, i, st);
+                if (THERMAL) therm[st.pid] = make_float4(th.x + trate * a.sc->dt, gtx, gty, gtz);
                 if (a.stats) particle_stats(s_st, st);
             }
             if (cnt < (int)blockDim.x) break;
@@ -1663,14 +1692,15 @@ __global__ void __launch_bounds__(GY_G2P_THREADS) k_g2p_multi_tiled(PView src, P
 int g2p_blocks_per_sm(bool has_dp)
 {
     int b = 0;
-    if (has_dp) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_g2p_tiled<true>, GY_G2P_THREADS, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_g2p_tiled<false>, GY_G2P_THREADS, 0);
+    if (has_dp) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_g2p_tiled<true, false>, GY_G2P_THREADS, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_g2p_tiled<false, false>, GY_G2P_THREADS, 0);
     return b > 0 ? b : 1;
 }
 
 void launch_g2p_update(const PView &src, const PView &dst, const int *perm, const int *skey, long long n,
                        const int *seg_start, const int *nseg, int g2p_grid, const NodeBufs &nb, const StepArgs &a,
-                       bool track_normals, bool check_finite, bool has_dp, cudaStream_t s)
+                       bool track_normals, bool check_finite, bool has_dp, cudaStream_t s, float4 *therm,
+                       const float2 *tnode)
 {
     if (n == 0) return;
     const int tn = track_normals ? 1 : 0, cf = check_finite ? 1 : 0;
@@ -1700,10 +1730,29 @@ void launch_g2p_update(const PView &src, const PView &dst, const int *perm, cons
             k_g2p_multi_tiled<false, false><<<mg, GY_G2P_THREADS, 0, s>>>(src, dst, perm, skey, n, seg_start, nseg, srt, nb, a, cf);
     } else {
         const int srt = perm ? 1 : 0;
-        if (has_dp)
-            k_g2p_tiled<true><<<g2p_grid, GY_G2P_THREADS, 0, s>>>(src, dst, perm, skey, n, seg_start, nseg, srt, nb, a, cf);
-        else
-            k_g2p_tiled<false><<<g2p_grid, GY_G2P_THREADS, 0, s>>>(src, dst, perm, skey, n, seg_start, nseg, srt, nb, a, cf);
+        if (therm) {
+            static int tgrid[2] = {0, 0};  // persistent grids of the variants with heat conduction
+            if (tgrid[has_dp] == 0) {
+                int dev = 0, sms = 1, b = 0;
+                cudaGetDevice(&dev);
+                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+                if (has_dp) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_g2p_tiled<true, true>, GY_G2P_THREADS, 0);
+                else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_g2p_tiled<false, true>, GY_G2P_THREADS, 0);
+                tgrid[has_dp] = sms * std::max(b, 1);
+            }
+            if (has_dp)
+                k_g2p_tiled<true, true><<<tgrid[1], GY_G2P_THREADS, 0, s>>>(src, dst, perm, skey, n, seg_start, nseg, srt,
+                                                                             nb, a, cf, therm, tnode);
+            else
+                k_g2p_tiled<false, true><<<tgrid[0], GY_G2P_THREADS, 0, s>>>(src, dst, perm, skey, n, seg_start, nseg, srt,
+                                                                              nb, a, cf, therm, tnode);
+        } else if (has_dp) {
+            k_g2p_tiled<true, false><<<g2p_grid, GY_G2P_THREADS, 0, s>>>(src, dst, perm, skey, n, seg_start, nseg, srt, nb,
+                                                                          a, cf, nullptr, nullptr);
+        } else {
+            k_g2p_tiled<false, false><<<g2p_grid, GY_G2P_THREADS, 0, s>>>(src, dst, perm, skey, n, seg_start, nseg, srt, nb,
+                                                                           a, cf, nullptr, nullptr);
+        }
     }
     note_launch(1);
 }

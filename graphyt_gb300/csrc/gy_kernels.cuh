@@ -66,9 +66,12 @@ void launch_p2g(const PView &p, const int *perm, const int *skey, long long n, c
                 const float4 *therm = nullptr, float2 *tnode = nullptr);
 void launch_fold(const NodeBufs &nb, const StepArgs &a, cudaStream_t s);
 void launch_solve(const NodeBufs &nb, const StepArgs &a, bool keep_node_fields, cudaStream_t s);
+// therm / tnode non-null: the single-body kernel also runs the heat conduction G2P and the
+// temperature update (multi-body problems run launch_thermal_g2p instead)
 void launch_g2p_update(const PView &src, const PView &dst, const int *perm, const int *skey, long long n,
                        const int *seg_start, const int *nseg, int g2p_grid, const NodeBufs &nb, const StepArgs &a,
-                       bool track_normals, bool check_finite, bool has_dp, cudaStream_t s);
+                       bool track_normals, bool check_finite, bool has_dp, cudaStream_t s, float4 *therm = nullptr,
+                       const float2 *tnode = nullptr);
 int g2p_blocks_per_sm(bool has_dp);
 int p2g_blocks_per_sm();
 void launch_body_tables(const PView &p, long long n, const StepArgs &a, int *cell_min, int nbody,
@@ -85,6 +88,7 @@ void launch_thermal_p2g(const PView &p, const float4 *therm, const int *perm, co
 void launch_thermal_g2p(const PView &p, float4 *therm, const int *perm, const int *skey, long long n,
                         const int *seg_start, const int *nseg, const float2 *tnode, const NodeBufs &nb,
                         const StepArgs &a, cudaStream_t s);
+void launch_thermal_clear(const NodeBufs &nb, const StepArgs &a, float2 *tnode, cudaStream_t s);
 void launch_thermal_set(float4 *therm, const int *ids, const float *T, int count, long long n, cudaStream_t s);
 
 // sort (gy_sort.cu): stable LSD radix sort of (key, index) pairs

@@ -300,8 +300,14 @@ void launch_thermal_g2p(const PView &p, float4 *therm, const int *perm, const in
         grid = grid_of((long long)1 << 40, 1, std::max(b, 1));
     }
     k_thermal_g2p<<<grid, TH_THREADS, 0, s>>>(p, therm, perm, skey, n, seg_start, nseg, perm ? 1 : 0, tnode, a);
-    k_thermal_clear<<<grid_of(64LL * a.g.nnb, 256, 8), 256, 0, s>>>(nb, a.g, const_cast<float2 *>(tnode));
-    note_launch(2);
+    note_launch(1);
+    launch_thermal_clear(nb, a, const_cast<float2 *>(tnode), s);
+}
+
+void launch_thermal_clear(const NodeBufs &nb, const StepArgs &a, float2 *tnode, cudaStream_t s)
+{
+    k_thermal_clear<<<grid_of(64LL * a.g.nnb, 256, 8), 256, 0, s>>>(nb, a.g, tnode);
+    note_launch(1);
 }
 
 void launch_thermal_set(float4 *therm, const int *ids, const float *T, int count, long long n, cudaStream_t s)

@@ -175,6 +175,16 @@ __device__ __forceinline__ int node_index(int i, int j, int k, const GridGeom &g
 }
 
 // device error bits
+// Programmatic dependent launch (the re-sort's chain of short kernels): a kernel first lets
+// the next kernel of its stream start launching (once all of this grid's CTAs are resident)
+// and then waits until its own predecessor has completed and its writes are visible.
+// Launched without the attribute, both instructions return at once.
+__device__ __forceinline__ void pdl_prologue()
+{
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 constexpr int ERR_RANGE = 1;
 constexpr int ERR_NONFINITE = 2;
 

@@ -1,6 +1,8 @@
 // gy_kernels.cuh -- launch interface between the host runtime (gy_api.cu) and the kernels.
 #pragma once
 
+#include <utility>
+
 #include "gy_common.cuh"
 
 namespace gy {
@@ -53,6 +55,24 @@ struct StepArgs {
 // partials of the conservation sums (mass, momentum, kinetic and strain energy); the host
 // adds the slots
 constexpr int STATS_SLOTS = 16;
+
+// launch with programmatic stream serialization (the kernel starts with pdl_prologue), so the
+// launch of a kernel overlaps the tail of the one before it in the stream or graph
+template <typename... P, typename... A>
+inline void launch_pdl(void (*kernel)(P...), dim3 grid, dim3 block, cudaStream_t s, A &&... args)
+{
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t c{};
+    c.gridDim = grid;
+    c.blockDim = block;
+    c.dynamicSmemBytes = 0;
+    c.stream = s;
+    c.attrs = at;
+    c.numAttrs = 1;
+    cudaLaunchKernelEx(&c, kernel, std::forward<A>(args)...);
+}
 
 // process-wide count of kernel launches (for the benchmark's launch accounting)
 void note_launch(int k);

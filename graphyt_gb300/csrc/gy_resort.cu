@@ -48,6 +48,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_mask(const int *key, const in
                                                           int *wcnt, long long nw, const int *gap, const int *wpref,
                                                           int *gapcnt, int *gwcnt, int *hist, int hist_ints)
 {
+    pdl_prologue();
     const int lane = threadIdx.x & 31;
     const long long wstride = ((long long)gridDim.x * blockDim.x) >> 5;
     {
@@ -85,6 +86,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_mask(const int *key, const in
 __global__ void __launch_bounds__(RS_THREADS) k_rs_compact(const int *key, const unsigned *wmask, const int *wpref,
                                                              long long nw, int *bkey, int *bidx, int *hist0, int G)
 {
+    pdl_prologue();
     const int mtot = wpref[nw];
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
@@ -128,6 +130,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const int *keys_in, c
                                                              int *vals_out, const int *m_ptr, int shift,
                                                              const int *offsets, int *hist_next)
 {
+    pdl_prologue();
     __shared__ int wcnt[RS_WARPS][RS_RADIX];  // per-warp digit counts, then per-warp bases
     __shared__ int base[RS_RADIX];            // running per-digit base of this CTA
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -189,6 +192,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_place_movers(const int *prev,
                                                                   const int *sidx, int *gap, int *gapcnt, int *gwcnt,
                                                                   int *skey_out, int *perm_out)
 {
+    pdl_prologue();
     const int m = wpref[nw];
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < m; q += gridDim.x * blockDim.x) {
         const int k = skey[q], i = sidx[q];
@@ -240,6 +244,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_place_stayers(const int *key,
                                                                    const int *gwcnt, const int *gwpref, int *skey_out,
                                                                    int *perm_out)
 {
+    pdl_prologue();
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     const long long wstride = ((long long)gridDim.x * blockDim.x) >> 5;
@@ -350,28 +355,28 @@ void resort_keys(const int *key, const int *prev_skey, int *skey_out, int *perm_
     const int passes = std::min(RS_MAX_PASSES, std::max(1, (key_bits + 7) / 8));
     const int hg = RS_RADIX * G;                                    // one pass's histogram
     int *offsets = rs.hist + (long long)RS_MAX_PASSES * RS_RADIX * RS_MAX_CTAS;
-    k_rs_mask<<<wgrid, RS_THREADS, 0, s>>>(key, prev_skey, n, rs.wmask, rs.wcnt, nw, rs.gap, rs.wpref, rs.gapcnt,
+    launch_pdl(k_rs_mask, wgrid, RS_THREADS, s, key, prev_skey, n, rs.wmask, rs.wcnt, nw, rs.gap, rs.wpref, rs.gapcnt,
                                            rs.gwcnt, rs.hist, passes * hg);
     cudaMemsetAsync(rs.wcnt + nw, 0, sizeof(int), s);
     exclusive_scan_int(rs.wcnt, rs.wpref, nw + 1, rs.wscan_tmp, s);
     // movers in slot order, with the first pass's digit counts per mover-sort CTA
-    k_rs_compact<<<bgrid, RS_THREADS, 0, s>>>(key, rs.wmask, rs.wpref, nw, rs.bkey, rs.bidx, rs.hist, G);
+    launch_pdl(k_rs_compact, bgrid, RS_THREADS, s, key, rs.wmask, rs.wpref, nw, rs.bkey, rs.bidx, rs.hist, G);
     note_launch(2);
     // stable sort of the movers by key; their count is wpref[nw]
     const int *m_ptr = rs.wpref + nw;
     int *kin = rs.bkey, *vin = rs.bidx, *kout = rs.tkey, *vout = rs.tidx;
     for (int p = 0; p < passes; p++) {
         exclusive_scan_int(rs.hist + (long long)p * hg, offsets, hg, rs.hscan_tmp, s);
-        k_rs_scatter<<<G, RS_THREADS, 0, s>>>(kin, vin, kout, vout, m_ptr, 8 * p, offsets,
+        launch_pdl(k_rs_scatter, G, RS_THREADS, s, kin, vin, kout, vout, m_ptr, 8 * p, offsets,
                                               p + 1 < passes ? rs.hist + (long long)(p + 1) * hg : nullptr);
         note_launch(1);
         std::swap(kin, kout);
         std::swap(vin, vout);
     }
-    k_rs_place_movers<<<qgrid, RS_THREADS, 0, s>>>(prev_skey, n, rs.wmask, rs.wpref, nw, kin, vin, rs.gap, rs.gapcnt,
+    launch_pdl(k_rs_place_movers, qgrid, RS_THREADS, s, prev_skey, n, rs.wmask, rs.wpref, nw, kin, vin, rs.gap, rs.gapcnt,
                                                    rs.gwcnt, skey_out, perm_out);
     exclusive_scan_int(rs.gwcnt, rs.gwpref, rs.ngw + 1, rs.gscan_tmp, s);
-    k_rs_place_stayers<<<bgrid, RS_THREADS, 0, s>>>(key, n, rs.wmask, rs.wpref, nw, rs.gapcnt, rs.gwcnt, rs.gwpref,
+    launch_pdl(k_rs_place_stayers, bgrid, RS_THREADS, s, key, n, rs.wmask, rs.wpref, nw, rs.gapcnt, rs.gwcnt, rs.gwpref,
                                                     skey_out, perm_out);
     note_launch(2);
 }

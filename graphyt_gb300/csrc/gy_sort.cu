@@ -25,6 +25,7 @@ constexpr int RADIX = 256;
 
 __global__ void __launch_bounds__(SORT_THREADS) k_radix_hist(const int *keys, long long n, int shift, int *hist, int nblocks)
 {
+    pdl_prologue();
     __shared__ int cnt[RADIX];
     for (int d = threadIdx.x; d < RADIX; d += SORT_THREADS) cnt[d] = 0;
     __syncthreads();
@@ -41,6 +42,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_scatter(const int *keys_
                                                                  int *vals_out, long long n, int shift,
                                                                  const int *offsets, int nblocks)
 {
+    pdl_prologue();
     __shared__ int wcnt[SORT_WARPS][RADIX];   // per-warp digit counts, then per-warp bases
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int d = lane; d < RADIX; d += 32) wcnt[warp][d] = 0;
@@ -93,6 +95,7 @@ constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_tile(const int *in, int *out, long long n, int *block_sums)
 {
+    pdl_prologue();
     __shared__ int wsum[SCAN_THREADS / 32];
     const long long base = (long long)blockIdx.x * SCAN_TILE + (long long)threadIdx.x * SCAN_ITEMS;
     int v[SCAN_ITEMS], tsum = 0;
@@ -127,6 +130,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_tile(const int *in, int *
 
 __global__ void k_scan_add(int *out, long long n, const int *block_off)
 {
+    pdl_prologue();
     const long long i = (long long)blockIdx.x * SCAN_TILE + threadIdx.x;
     const int add = block_off[blockIdx.x];
     for (int k = 0; k < SCAN_ITEMS; k++) {
@@ -139,6 +143,7 @@ __global__ void k_scan_add(int *out, long long n, const int *block_off)
 // (at most SCAN_TILE of them), so the scan of the sums needs no launch of its own
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_add_self(int *out, long long n, const int *block_sums)
 {
+    pdl_prologue();
     __shared__ int red[SCAN_THREADS / 32];
     if (blockIdx.x == 0) return;  // the first tile's prefix is zero
     int part = 0;
@@ -173,20 +178,20 @@ void exclusive_scan_int(const int *in, int *out, long long n, int *tmp, cudaStre
     if (n <= 0) return;
     const long long nb = (n + SCAN_TILE - 1) / SCAN_TILE;
     if (nb == 1) {
-        k_scan_tile<<<1, SCAN_THREADS, 0, s>>>(in, out, n, nullptr);
+        launch_pdl(k_scan_tile, 1, SCAN_THREADS, s, in, out, n, nullptr);
         note_launch(1);
         return;
     }
     int *sums = tmp, *sums_scan = tmp + nb + 16;
-    k_scan_tile<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, out, n, sums);
+    launch_pdl(k_scan_tile, (unsigned)nb, SCAN_THREADS, s, in, out, n, sums);
     note_launch(1);
     if (nb <= SCAN_TILE) {
-        k_scan_add_self<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(out, n, sums);
+        launch_pdl(k_scan_add_self, (unsigned)nb, SCAN_THREADS, s, out, n, sums);
         note_launch(1);
         return;
     }
     exclusive_scan_int(sums, sums_scan, nb, tmp + 2 * nb + 32, s);
-    k_scan_add<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(out, n, sums_scan);
+    launch_pdl(k_scan_add, (unsigned)nb, SCAN_THREADS, s, out, n, sums_scan);
     note_launch(1);
 }
 
@@ -212,10 +217,10 @@ const int *sort_pairs(const int *keys_in, int *perm_out, long long n, int key_bi
         const int shift = 8 * p;
         int *kout = ws.keys[cur];
         int *vout = (p == passes - 1) ? perm_out : ws.vals[cur];
-        k_radix_hist<<<nblocks, SORT_THREADS, 0, s>>>(kin, n, shift, ws.hist, nblocks);
+        launch_pdl(k_radix_hist, nblocks, SORT_THREADS, s, kin, n, shift, ws.hist, nblocks);
         note_launch(1);
         exclusive_scan_int(ws.hist, ws.hist + (long long)RADIX * nblocks, (long long)RADIX * nblocks, ws.scan_tmp, s);
-        k_radix_scatter<<<nblocks, SORT_THREADS, 0, s>>>(kin, vin, kout, vout, n, shift,
+        launch_pdl(k_radix_scatter, nblocks, SORT_THREADS, s, kin, vin, kout, vout, n, shift,
                                                          ws.hist + (long long)RADIX * nblocks, nblocks);
         note_launch(1);
         kin = kout;
@@ -235,6 +240,7 @@ constexpr int BH_BUF = 2 * BH_TILE;
 
 __global__ void __launch_bounds__(BH_THREADS) k_block_heads(const int *skey, long long n, int *seg_start, int *nseg)
 {
+    pdl_prologue();
     __shared__ int buf[BH_BUF];
     __shared__ int bcount, bbase;
     const int lane = threadIdx.x & 31;
@@ -305,7 +311,7 @@ void launch_block_heads(const int *skey, long long n, int *seg_start, int *nseg,
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         const long long grid = std::min<long long>((n + BH_TILE - 1) / BH_TILE, (long long)sms * 4);
-        k_block_heads<<<(unsigned)grid, BH_THREADS, 0, s>>>(skey, n, seg_start, nseg);
+        launch_pdl(k_block_heads, (unsigned)grid, BH_THREADS, s, skey, n, seg_start, nseg);
         note_launch(1);
     }
 }

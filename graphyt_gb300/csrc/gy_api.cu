@@ -871,7 +871,6 @@ static void issue_step(gy_solver *h, const StepVariant &v, cudaEvent_t *tev)
     const StepArgs a = make_args(h);
     cudaStream_t s = h->stream;
     if (tev) cudaEventRecord(tev[0], s);
-    cudaMemsetAsync(h->nb.active_count, 0, sizeof(int), s);
     // (a) stable counting sort of the cell keys; the particle kernels read through perm
     const int *perm = nullptr;
     const int *skey = reinterpret_cast<const int *>(h->slab[v.cur]) + (size_t)PF_KEY * h->cap;
@@ -891,7 +890,8 @@ static void issue_step(gy_solver *h, const StepVariant &v, cudaEvent_t *tev)
         skey = out;
         perm = h->d_perm;
     }
-    launch_block_heads(skey, h->n, h->d_seg, h->d_nseg, s);
+    // block heads also zero the active node-block count and list length of this step
+    launch_block_heads(skey, h->n, h->d_seg, h->d_nseg, s, h->nb.active_n, h->nb.active_count);
     PView src = pview(h, v.cur), dst = pview(h, v.cur ^ 1);
     // body slots from the sort table of the reference's cadence (Solver.cpp:91)
     if (v.tables) {
@@ -899,7 +899,6 @@ static void issue_step(gy_solver *h, const StepVariant &v, cudaEvent_t *tev)
         launch_body_assign(h->nb, a, h->d_cell_min, h->nbody, h->d_nidx[0], h->d_nidx[1], h->d_nidx[2], s);
     }
     if (tev) cudaEventRecord(tev[1], s);
-    cudaMemsetAsync(h->nb.active_n, 0, sizeof(int), s);
     // (b) P2G
     // heat conduction: fused into the single-body P2G, a separate pass for body slots
     const bool fused_thermal = h->thermal && !h->multi;
@@ -913,8 +912,7 @@ static void issue_step(gy_solver *h, const StepVariant &v, cudaEvent_t *tev)
     launch_solve(h->nb, a, h->opt.keep_node_fields != 0, s);
     if (tev) cudaEventRecord(tev[3], s);
     // (d) G2P + particle BCs + update + constitutive + damage, written in sorted order, with
-    // the conservation sums of the updated state
-    cudaMemsetAsync(h->d_stats, 0, STATS_SLOTS * 8 * sizeof(double), s);
+    // the conservation sums of the updated state (their partials zeroed by the compaction)
     launch_g2p_update(src, dst, perm, skey, h->n, h->d_seg, h->d_nseg, h->g2p_grid, h->nb, a,
                       h->opt.track_normals != 0, h->opt.check_finite != 0, h->has_dp, s,
                       fused_thermal ? h->d_therm : nullptr, fused_thermal ? h->d_tnode : nullptr);

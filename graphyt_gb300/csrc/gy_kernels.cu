@@ -1051,9 +1051,12 @@ __global__ void __launch_bounds__(256) k_solve_single(NodeBufs nb, StepArgs a, i
 }
 
 // The flagged node blocks, appended to the solve's list: one ballot and one atomic per warp.
-__global__ void k_compact_active(NodeBufs nb, int nnb)
+// It also zeroes the conservation partials the step's G2P adds into (stats, may be null).
+__global__ void k_compact_active(NodeBufs nb, int nnb, double *stats)
 {
     const int lane = threadIdx.x & 31;
+    if (stats && blockIdx.x == 0)
+        for (int q = threadIdx.x; q < STATS_SLOTS * 8; q += blockDim.x) stats[q] = 0.0;
     for (int b0 = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; b0 < nnb; b0 += gridDim.x * blockDim.x) {
         const int b = b0 + lane;
         const bool f = b < nnb && nb.flags[b] != 0;
@@ -1094,7 +1097,7 @@ void launch_solve(const NodeBufs &nb, const StepArgs &a, bool keep_node_fields, 
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long long cgrid = std::min<long long>((a.g.nnb + 255) / 256, (long long)sms * 8);
-    k_compact_active<<<(unsigned)std::max<long long>(cgrid, 1), 256, 0, s>>>(nb, (int)a.g.nnb);
+    k_compact_active<<<(unsigned)std::max<long long>(cgrid, 1), 256, 0, s>>>(nb, (int)a.g.nnb, a.stats);
     note_launch(1);
     long long grid = std::min<long long>((a.g.nnb + 7) / 8, (long long)sms * 16);  // 8 warps per CTA
     if (grid < 1) grid = 1;

@@ -59,6 +59,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_mask(const int *key, const in
             gwcnt[gap[q] >> 5] = 0;
         }
         for (int q = t; q < hist_ints; q += tstride) hist[q] = 0;
+        if (t == 0) wcnt[nw] = 0;  // the scan's last entry, so that wpref[nw] is the mover count
     }
     for (long long w0 = (((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 4; w0 < nw; w0 += wstride * 4) {
         int ka[4], kb[4];
@@ -357,7 +358,6 @@ void resort_keys(const int *key, const int *prev_skey, int *skey_out, int *perm_
     int *offsets = rs.hist + (long long)RS_MAX_PASSES * RS_RADIX * RS_MAX_CTAS;
     launch_pdl(k_rs_mask, wgrid, RS_THREADS, s, key, prev_skey, n, rs.wmask, rs.wcnt, nw, rs.gap, rs.wpref, rs.gapcnt,
                                            rs.gwcnt, rs.hist, passes * hg);
-    cudaMemsetAsync(rs.wcnt + nw, 0, sizeof(int), s);
     exclusive_scan_int(rs.wcnt, rs.wpref, nw + 1, rs.wscan_tmp, s);
     // movers in slot order, with the first pass's digit counts per mover-sort CTA
     launch_pdl(k_rs_compact, bgrid, RS_THREADS, s, key, rs.wmask, rs.wpref, nw, rs.bkey, rs.bidx, rs.hist, G);

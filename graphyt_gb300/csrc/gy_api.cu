@@ -74,7 +74,7 @@ struct gy_solver {
     float *slab[2] = {nullptr, nullptr};
     int cur = 0;
     int *d_perm = nullptr;
-    int *d_seg = nullptr, *d_nseg = nullptr;   // non-empty cell-block segments
+    int *d_seg = nullptr, *d_nseg = nullptr;   // non-empty cell-block segments; two counts, by slab parity
     int persist_grid = 1;
     int g2p_grid = 1;
     SortScratch ws{};
@@ -758,6 +758,7 @@ gy_status gy_initialize(gy_solver *h, const gy_material *mats, int nmat, const g
     if ((st = dalloc(h, &h->d_perm, h->cap))) return st;
     if ((st = dalloc(h, &h->d_seg, h->cap))) return st;
     if ((st = dalloc(h, &h->d_nseg, 4))) return st;
+    CK(h, cudaMemsetAsync(h->d_nseg, 0, 4 * sizeof(int), h->stream));
     {
         int dev = 0, sms = 1;
         cudaGetDevice(&dev);
@@ -890,8 +891,11 @@ static void issue_step(gy_solver *h, const StepVariant &v, cudaEvent_t *tev)
         skey = out;
         perm = h->d_perm;
     }
-    // block heads also zero the active node-block count and list length of this step
-    launch_block_heads(skey, h->n, h->d_seg, h->d_nseg, s, h->nb.active_n, h->nb.active_count);
+    // the segment count alternates between two counters by slab parity: this step's block
+    // heads fill one and zero the other for the next step, and zero this step's active
+    // node-block count and list length
+    int *nseg = h->d_nseg + v.cur;
+    launch_block_heads(skey, h->n, h->d_seg, nseg, s, h->nb.active_n, h->nb.active_count, h->d_nseg + (v.cur ^ 1));
     PView src = pview(h, v.cur), dst = pview(h, v.cur ^ 1);
     // body slots from the sort table of the reference's cadence (Solver.cpp:91)
     if (v.tables) {
@@ -902,10 +906,10 @@ static void issue_step(gy_solver *h, const StepVariant &v, cudaEvent_t *tev)
     // (b) P2G
     // heat conduction: fused into the single-body P2G, a separate pass for body slots
     const bool fused_thermal = h->thermal && !h->multi;
-    launch_p2g(src, perm, skey, h->n, h->d_seg, h->d_nseg, h->persist_grid, h->nb, a, s,
+    launch_p2g(src, perm, skey, h->n, h->d_seg, nseg, h->persist_grid, h->nb, a, s,
                fused_thermal ? h->d_therm : nullptr, fused_thermal ? h->d_tnode : nullptr);
     if (h->thermal && h->multi)
-        launch_thermal_p2g(src, h->d_therm, perm, skey, h->n, h->d_seg, h->d_nseg, h->d_tnode, a, s);
+        launch_thermal_p2g(src, h->d_therm, perm, skey, h->n, h->d_seg, nseg, h->d_tnode, a, s);
     if (tev) cudaEventRecord(tev[2], s);
     // (c) periodic fold, nodal solve, grid BCs
     launch_fold(h->nb, a, s);
@@ -913,11 +917,11 @@ static void issue_step(gy_solver *h, const StepVariant &v, cudaEvent_t *tev)
     if (tev) cudaEventRecord(tev[3], s);
     // (d) G2P + particle BCs + update + constitutive + damage, written in sorted order, with
     // the conservation sums of the updated state (their partials zeroed by the compaction)
-    launch_g2p_update(src, dst, perm, skey, h->n, h->d_seg, h->d_nseg, h->g2p_grid, h->nb, a,
+    launch_g2p_update(src, dst, perm, skey, h->n, h->d_seg, nseg, h->g2p_grid, h->nb, a,
                       h->opt.track_normals != 0, h->opt.check_finite != 0, h->has_dp, s,
                       fused_thermal ? h->d_therm : nullptr, fused_thermal ? h->d_tnode : nullptr);
     if (h->thermal && h->multi)
-        launch_thermal_g2p(src, h->d_therm, perm, skey, h->n, h->d_seg, h->d_nseg, h->d_tnode, h->nb, a, s);
+        launch_thermal_g2p(src, h->d_therm, perm, skey, h->n, h->d_seg, nseg, h->d_tnode, h->nb, a, s);
     else if (h->thermal)
         launch_thermal_clear(h->nb, a, h->d_tnode, s);
     if (tev) cudaEventRecord(tev[4], s);

@@ -135,9 +135,9 @@ void resort_bind(ResortScratch &rs, int *mem, long long cap);
 void resort_keys(const int *key, const int *prev_skey, int *skey_out, int *perm_out, long long n, int key_bits,
                  ResortScratch &rs, cudaStream_t s);
 const int *sort_pairs(const int *keys_in, int *perm_out, long long n, int key_bits, SortScratch &ws, cudaStream_t s);
-// clear0 / clear1 (may be null): counters the kernel zeroes on the way
+// nseg must be zero on entry; clear0..2 (may be null): counters the kernel zeroes on the way
 void launch_block_heads(const int *skey, long long n, int *seg_start, int *nseg, cudaStream_t s,
-                        int *clear0 = nullptr, int *clear1 = nullptr);
+                        int *clear0 = nullptr, int *clear1 = nullptr, int *clear2 = nullptr);
 void exclusive_scan_int(const int *in, int *out, long long n, int *tmp, cudaStream_t s);
 size_t scan_tmp_ints(long long n);
 

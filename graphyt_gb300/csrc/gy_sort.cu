@@ -238,15 +238,16 @@ constexpr int BH_THREADS = 256;
 constexpr int BH_TILE = 16 * BH_THREADS;
 constexpr int BH_BUF = 2 * BH_TILE;
 
-// also zeroes the step's two node-block counters (clear0, clear1; may be null), which nothing
-// reads between the previous step's G2P and this step's compaction
+// nseg must be zero on entry.  The kernel also zeroes up to three counters of the caller
+// (clear0..2, may be null) that nothing reads while it runs.
 __global__ void __launch_bounds__(BH_THREADS) k_block_heads(const int *skey, long long n, int *seg_start, int *nseg,
-                                                            int *clear0, int *clear1)
+                                                            int *clear0, int *clear1, int *clear2)
 {
     pdl_prologue();
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         if (clear0) *clear0 = 0;
         if (clear1) *clear1 = 0;
+        if (clear2) *clear2 = 0;
     }
     __shared__ int buf[BH_BUF];
     __shared__ int bcount, bbase;
@@ -311,19 +312,18 @@ __global__ void __launch_bounds__(BH_THREADS) k_block_heads(const int *skey, lon
 }
 
 void launch_block_heads(const int *skey, long long n, int *seg_start, int *nseg, cudaStream_t s, int *clear0,
-                        int *clear1)
+                        int *clear1, int *clear2)
 {
-    cudaMemsetAsync(nseg, 0, sizeof(int), s);
     if (n > 0) {
         int dev = 0, sms = 1;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         const long long grid = std::min<long long>((n + BH_TILE - 1) / BH_TILE, (long long)sms * 4);
-        launch_pdl(k_block_heads, (unsigned)grid, BH_THREADS, s, skey, n, seg_start, nseg, clear0, clear1);
+        launch_pdl(k_block_heads, (unsigned)grid, BH_THREADS, s, skey, n, seg_start, nseg, clear0, clear1, clear2);
         note_launch(1);
     } else {
-        if (clear0) cudaMemsetAsync(clear0, 0, sizeof(int), s);
-        if (clear1) cudaMemsetAsync(clear1, 0, sizeof(int), s);
+        for (int *c : {clear0, clear1, clear2})
+            if (c) cudaMemsetAsync(c, 0, sizeof(int), s);
     }
 }
 

@@ -164,21 +164,34 @@ def profiled_traffic():
         return {}
 
 
-def cpu_sample_scene():
-    """Bounded CPU sample of the same workload: a 0.14 m wide y-slab of the dam break at the
-    same resolution (200 x 20 x 153 = 612,000 particles, 1.2 M nodes)."""
+WORKLOADS = {
+    "dam_break": "dam_break_3d_newtonian",
+    "brazilian_disc": "brazilian_disc_dp_gk_rigid_platens",
+    "impact_batch": "impact_batch_sphere_on_dp_gk_slab",
+}
+
+
+def cpu_sample_scene(workload: str = "dam_break"):
+    """Bounded CPU sample of the same workload at the same resolution.  Dam break: a 0.14 m
+    wide y-slab (200 x 20 x 153 = 612,000 particles, 1.2 M nodes).  Brazilian disc: the disc
+    at a quarter of the resolution (about 160 k particles).  Impact batch: a batch of 16
+    instances drawn like the full one (about 0.8 M particles)."""
     from graphyt_gb300 import scenes
-    return scenes.dam_break(scale=1.0, width=0.14)
+    if workload == "brazilian_disc":
+        return scenes.brazilian_disc(scale=0.25), "Brazilian disc at cellsize 2e-3"
+    if workload == "impact_batch":
+        return scenes.impact_batch(n_inst=16, seed=0), "16-instance impact batch, cellsize 0.01"
+    return scenes.dam_break(scale=1.0, width=0.14), "dam break y-slab 4 x 0.14 x 2 m, cellsize 0.01"
 
 
-def run_cpu(nsteps: int, warmup: int, prefer_reference: bool = True):
+def run_cpu(nsteps: int, warmup: int, prefer_reference: bool = True, workload: str = "dam_break"):
     """Time the reference's CPU step (oracle/_ref when built, else the FP64 restatement) on
     the bounded sample.  Returns (particle-steps/s, kind, threads, sample description)."""
     from oracle import oracle as O
     kind = "ref" if (prefer_reference and O.available("ref")) else "port"
     if not O.available(kind):
         O.build()
-    sc = cpu_sample_scene()
+    sc, what = cpu_sample_scene(workload)
     o = O.Oracle(sc, kind, mode=1)
     o.run(warmup)
     t0 = time.perf_counter()
@@ -186,20 +199,19 @@ def run_cpu(nsteps: int, warmup: int, prefer_reference: bool = True):
     dt = time.perf_counter() - t0
     threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     o.close()
-    sample = (f"dam break y-slab 4 x 0.14 x 2 m, cellsize 0.01, {sc.n} particles, {sc.num_nodes()} nodes, "
-              f"{nsteps} timed steps after {warmup}")
+    sample = f"{what}, {sc.n} particles, {sc.num_nodes()} nodes, {nsteps} timed steps after {warmup}"
     return sc.n * nsteps / dt, ("reference" if kind == "ref" else "port"), threads, sample
 
 
 def bench_reference(args, rank):
     if rank != 0:
         return
-    value, kind, threads, sample = run_cpu(args.steps, args.warmup)
+    value, kind, threads, sample = run_cpu(args.steps, args.warmup, workload=args.workload)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "dam_break_3d_newtonian", "sample": sample},
+        "config": {"workload": WORKLOADS[args.workload], "sample": sample},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -213,9 +225,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--scale", type=float, default=1.0)
-    ap.add_argument("--workload", default="dam_break", choices=["dam_break", "brazilian_disc"],
+    ap.add_argument("--workload", default="dam_break", choices=list(WORKLOADS),
                     help="dam_break: the headline 3D Newtonian dam break; brazilian_disc: the multi-body "
-                         "Drucker-Prager + Grady-Kipp disc between rigid platens")
+                         "Drucker-Prager + Grady-Kipp disc between rigid platens; impact_batch: independent "
+                         "sphere-on-slab impacts of uneven sizes advanced as one grid")
+    ap.add_argument("--instances", type=int, default=256, help="impact_batch: number of instances")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sort-every", type=int, default=1)
     ap.add_argument("--temperature", type=float, default=0.0,
@@ -237,8 +251,12 @@ def main():
     from graphyt_gb300 import graphyt, scenes
 
     dist = Dist(world, local)
-    sc = (scenes.dam_break(scale=args.scale, height=args.column_height) if args.workload == "dam_break"
-          else scenes.brazilian_disc(scale=args.scale))
+    if args.workload == "dam_break":
+        sc = scenes.dam_break(scale=args.scale, height=args.column_height)
+    elif args.workload == "brazilian_disc":
+        sc = scenes.brazilian_disc(scale=args.scale)
+    else:
+        sc = scenes.impact_batch(n_inst=args.instances, seed=0)
     if args.temperature:
         # a linear profile along x, so the conduction terms have gradients to carry
         x = sc.pos[:, 0]
@@ -297,7 +315,7 @@ def main():
     # roofline of the dominant kernel
     names = ["sort", "p2g", "grid", "g2p_update"]
     per_step = [phase[k] / max(nph.value, 1) for k in range(4)]
-    multi = args.workload == "brazilian_disc"
+    multi = args.workload != "dam_break"
     algo = {
         "sort": 0.0,
         "p2g": P2G_BYTES_PER_PARTICLE * n + (MB_P2G_BYTES_PER_NODE if multi else P2G_BYTES_PER_NODE) * n_active,
@@ -318,7 +336,7 @@ def main():
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        v, kind, threads, sample = run_cpu(2, 1)
+        v, kind, threads, sample = run_cpu(2, 1, workload=args.workload)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample}
 
     if rank == 0:
@@ -326,12 +344,17 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "dam_break_3d_newtonian" if not multi else "brazilian_disc_dp_gk_rigid_platens",
+            "config": {"workload": WORKLOADS[args.workload],
                        "particles": n, "nodes": sc.num_nodes(),
+                       **({"instances": len(sc.instances), "instance_particles": [min(i.n for i in sc.instances),
+                                                                                 max(i.n for i in sc.instances)],
+                           "dt_shared": sc.dt} if sc.instances else {}),
                        **({"column_height_m": args.column_height} if not multi else {}),
                        **({"heat_conduction": True} if args.temperature else {}),
                        "active_nodes": n_active, "cellsize": sc.cellsize, "psep": sc.psep,
-                       "model": "newtonian" if not multi else "drucker_prager+grady_kipp, 3 bodies",
+                       "model": {"dam_break": "newtonian", "brazilian_disc": "drucker_prager+grady_kipp, 3 bodies",
+                                 "impact_batch": "drucker_prager+grady_kipp slab + elastic sphere per instance, "
+                                                 "2 bodies"}[args.workload],
                        "sort_every": args.sort_every, "sort": "full" if args.full_sort else "incremental", "l2": "state larger than L2 (no flush needed)",
                        "parallelism": "replicas" if world > 1 else "single"},
             "phase_ms_per_step": dict(zip(names, per_step)),

@@ -606,7 +606,7 @@ gy_status gy_initialize(gy_solver *h, const gy_material *mats, int nmat, const g
 {
     if (!h || !mats || nmat <= 0 || !prm) return GY_ERR_ARG;
     if (h->initialized) return fail(h, GY_ERR_STATE, "already initialized");
-    if (nmat > MAX_MATERIALS) return fail(h, GY_ERR_UNSUPPORTED, "more than 32 materials");
+    if (nmat > MAX_MATERIALS) return fail(h, GY_ERR_UNSUPPORTED, "more than 4096 materials");
     if ((prm->is3D != 0) != (h->g.is3d != 0))
         return fail(h, GY_ERR_ARG, "Parameters.is3D does not match the grid (L[2] == 0 means 2D)");
     cudaSetDevice(h->device);

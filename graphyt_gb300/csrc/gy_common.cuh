@@ -30,15 +30,15 @@ enum PField : int {
 };
 
 // PF_INFO bit layout
-constexpr uint32_t INFO_MAT_MASK = 0xFFu;          // bits 0-7   material index
-constexpr int INFO_OBJ_SHIFT = 8;                  // bits 8-15  object slot (dense)
+constexpr uint32_t INFO_MAT_MASK = 0xFFFu;         // bits 0-11  material index
+constexpr int INFO_OBJ_SHIFT = 12;                 // bits 12-15 object slot (dense, < MAX_BODIES)
 constexpr int INFO_BC_SHIFT = 16;                  // bits 16-23 BCTypes value (< 256)
 constexpr uint32_t INFO_HOLD = 1u << 24;           // holdParticle
 constexpr uint32_t INFO_RIGID = 1u << 25;          // material is rigid
 constexpr uint32_t INFO_INIT_VOL = 1u << 26;       // volume still psep^d (no update yet)
 
 __host__ __device__ inline int info_mat(uint32_t i) { return int(i & INFO_MAT_MASK); }
-__host__ __device__ inline int info_obj(uint32_t i) { return int((i >> INFO_OBJ_SHIFT) & 0xFFu); }
+__host__ __device__ inline int info_obj(uint32_t i) { return int((i >> INFO_OBJ_SHIFT) & 0xFu); }
 __host__ __device__ inline int info_bc(uint32_t i) { return int((i >> INFO_BC_SHIFT) & 0xFFu); }
 
 // BCTypes::function values (BoundaryConditions.hpp:6-77) the step acts on.
@@ -61,7 +61,7 @@ struct DevMaterial {
     float k_th, c_th;           // thermal conductivity, specific heat capacity
     int model, rigid, damage, damage_model;
 };
-constexpr int MAX_MATERIALS = 32;
+constexpr int MAX_MATERIALS = 4096;  // a batch of independent instances carries one per instance
 constexpr int MAX_BODIES = 16;
 
 // Grid geometry and per-step scalars, passed by value to every kernel.

@@ -578,6 +578,33 @@ class Solver:
             setattr(o, k, int(v))
         L.check(self.lib.gy_set_options(self.h, C.byref(o)), self.h, "options")
 
+    def autotune(self, step0: int = 0, steps: int = 6,
+                 candidates=((1, 0), (2, 0), (4, 0), (1, 1))) -> dict:
+        """Choose the fastest (sort_every, full_sort) pair for this problem and keep it.
+
+        Each candidate runs a few untimed steps (its CUDA graphs are captured there), then
+        ``steps`` steps timed with CUDA events.  These are real steps of the run, from step
+        ``step0`` on, since the knobs change speed and never results beyond summation order;
+        the returned ``next_step`` is where the caller continues.  The cell block (4^3 cells
+        and its 6^3-node shared-memory tile) and the work of a lane group (one run of equal
+        cell) are fixed by the kernels, so the sort cadence and the sort kind are what is
+        left to tune."""
+        ms = C.c_float()
+        dt = self.dt
+        step = int(step0)
+        times = {}
+        for sort_every, full_sort in candidates:
+            self.set_options(sort_every=int(sort_every), full_sort=int(full_sort))
+            warm = max(2, 2 * int(sort_every))
+            L.check(self.lib.gy_steps(self.h, step * dt, step, warm, 1), self.h, "autotune")
+            step += warm
+            L.check(self.lib.gy_time_steps(self.h, step * dt, step, int(steps), C.byref(ms)), self.h, "autotune")
+            step += int(steps)
+            times[(int(sort_every), int(full_sort))] = ms.value / max(int(steps), 1)
+        best = min(times, key=times.get)
+        self.set_options(sort_every=best[0], full_sort=best[1])
+        return dict(sort_every=best[0], full_sort=best[1], ms_per_step=times, next_step=step)
+
     def _set_temps(self, idx, T):
         idx = np.ascontiguousarray(idx, np.int64)
         T = np.ascontiguousarray(T, np.float64)

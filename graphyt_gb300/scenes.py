@@ -66,6 +66,8 @@ class Scene:
     node_bc_type: Optional[np.ndarray] = None  # (Nn,)
     node_bc_val: Optional[np.ndarray] = None   # (Nn, 4)
     temp: Optional[np.ndarray] = None          # (N,) temperature (MaterialPoints::setTemp)
+    inst: Optional[np.ndarray] = None          # (N,) instance index, for a batch of instances
+    instances: Optional[List["Instance"]] = None
 
     @property
     def is3D(self) -> bool:
@@ -136,8 +138,9 @@ def _finish(scene: Scene, seed: int) -> Scene:
         scene.node_bc_val = np.zeros((nn, 4))
     if seed is not None:
         perm = np.random.default_rng(seed).permutation(n)
-        for f in ("pos", "mat", "obj", "vel", "stress", "pbc_type", "pbc_val", "hold", "temp"):
-            setattr(scene, f, np.ascontiguousarray(getattr(scene, f)[perm]))
+        for f in ("pos", "mat", "obj", "vel", "stress", "pbc_type", "pbc_val", "hold", "temp", "inst"):
+            if getattr(scene, f) is not None:
+                setattr(scene, f, np.ascontiguousarray(getattr(scene, f)[perm]))
     scene.pos = np.ascontiguousarray(scene.pos, np.float64)
     scene.mat = np.ascontiguousarray(scene.mat, np.int32)
     scene.obj = np.ascontiguousarray(scene.obj, np.int32)
@@ -463,3 +466,169 @@ def disk_impact_2d(seed: int = 0) -> Scene:
     v[sc.obj == 2, 1] = -1.5
     sc.vel = v
     return _finish(sc, seed)
+
+
+# ------------------------------------------------------------------------------------------
+# a batch of independent instances in one grid
+
+@dataclasses.dataclass
+class Instance:
+    """One impact problem of a batch: a sphere (objectID 2, material 0) resting on a
+    Drucker-Prager + Grady-Kipp slab (objectID 1, material 1 + index) and moving down at the
+    impact speed.  Sizes are in cells of the batch's cellsize; ``box`` is the instance's own
+    domain (margin included) and ``origin`` its cell offset in the batch grid."""
+    index: int
+    target: int
+    side: int
+    thick: int
+    radius: float
+    box: tuple
+    origin: tuple = (0, 0, 0)
+    scale: tuple = (1.0, 1.0, 1.0, 1.0)   # K, G, cohesion, friction angle over the nominal rock
+    n: int = 0
+
+
+# the rock of the Brazilian disc workload: DP K 3e10, G 2e10, rho 2600, cohesion 1e7,
+# friction 30 deg, dilatancy 0, critical strain 0.01; GK m 9, k 5e32, Cg 0.4 x P-wave speed
+ROCK = dict(K=3e10, G=2e10, rho=2600.0, cohesion=1e7, phi=30.0)
+
+
+def _rock(K, G, cohesion, phi, rho=ROCK["rho"]) -> Dict:
+    cp = math.sqrt((K + 4.0 * G / 3.0) / rho)
+    return material(bulkMod=K, shearMod=G, density=rho, cohesion=cohesion, phi=phi, psi=0.0,
+                    criticalStrain=0.01, isDamage=1, damageModel=1, Cg=0.4 * cp, damageM=9.0,
+                    damageK=5e32, model=4)
+
+
+def _impact_count(side: int, thick: int, radius: float) -> int:
+    """Particles of a side x side x thick-cell slab (two per cell and axis) plus a sphere of
+    the given radius in cells, from the volumes."""
+    return 8 * side * side * thick + int(4.0 / 3.0 * math.pi * (2.0 * radius) ** 3)
+
+
+def _impact_shape(target: int, margin: int):
+    """Slab side and thickness (a quarter of the side) and sphere radius (0.15 of the side)
+    whose particle count is closest to target."""
+    best = None
+    for side in range(4, 400):
+        thick = max(2, int(round(side / 4)))
+        radius = max(1.5, 0.15 * side)
+        err = abs(_impact_count(side, thick, radius) - target)
+        if best is None or err < best[0]:
+            best = (err, side, thick, radius)
+    _, side, thick, radius = best
+    box = (side + 2 * margin, side + 2 * margin, thick + int(math.ceil(2 * radius)) + 1 + 2 * margin)
+    return side, thick, radius, box
+
+
+def impact_batch_layout(n_inst: int = 256, seed: int = 0, n_min: int = 2000, n_max: int = 200000,
+                        margin: int = 5, spread: float = 0.3):
+    """Instances and the batch grid (cells per axis) without particles.
+
+    Particle counts are drawn log-uniform in [n_min, n_max] and the slab's K, G, cohesion
+    and friction angle uniformly within +/-spread of the nominal rock, all from
+    numpy.random.default_rng(seed).  The instance boxes are shelf-packed on the x-y plane,
+    widest first, in rows along x about as long as the square root of their total area;
+    boxes touch, and each keeps ``margin`` empty cells around its content, so neighbouring
+    instances never reach a common node (GIMP support spans 1.25 cells) and the periodic
+    fold of the outermost three node layers sees no mass."""
+    rng = np.random.default_rng(seed)
+    targets = np.exp(rng.uniform(math.log(n_min), math.log(n_max), n_inst))
+    scales = rng.uniform(1.0 - spread, 1.0 + spread, (n_inst, 4))
+    insts = []
+    for i in range(n_inst):
+        side, thick, radius, box = _impact_shape(int(round(targets[i])), margin)
+        insts.append(Instance(i, int(round(targets[i])), side, thick, radius, box,
+                              scale=tuple(float(v) for v in scales[i])))
+    order = sorted(range(n_inst), key=lambda i: (-insts[i].box[0], i))
+    area = sum(insts[i].box[0] * insts[i].box[1] for i in order)
+    row_len = max(insts[order[0]].box[0], int(math.ceil(math.sqrt(area))))
+    x = y = depth = width = 0
+    for i in order:
+        b = insts[i].box
+        if x + b[0] > row_len:
+            y, x, depth = y + depth, 0, 0
+        insts[i].origin = (x, y, 0)
+        x += b[0]
+        depth = max(depth, b[1])
+        width = max(width, x)
+    dims = (width, y + depth, max(inst.box[2] for inst in insts))
+    return insts, dims
+
+
+def _impact_particles(inst: Instance, h: float, margin: int):
+    """Lattice points of the slab and the sphere in the instance's own frame (a shift of
+    (0.0931, 0.0517, 0.0713) psep keeps them off the quarter-cell binning boundaries).  The
+    sphere's lowest layer sits one psep above the slab's top layer."""
+    psep = h / 2
+    m = margin * h
+    side, thick = inst.side * h, inst.thick * h
+    slab = lattice_box([m, m, m], [m + side, m + side, m + thick], psep)
+    r = inst.radius * h
+    cx = cy = m + side / 2
+    z0 = m + thick
+    ball = lattice_box([cx - r, cy - r, z0], [cx + r, cy + r, z0 + 2 * r], psep)
+    cz = z0 + r
+    ball = ball[((ball[:, 0] - cx) ** 2 + (ball[:, 1] - cy) ** 2 + (ball[:, 2] - cz) ** 2) <= r * r]
+    shift = np.array([0.0931, 0.0517, 0.0713]) * psep
+    return slab + shift, ball + shift
+
+
+def impact_batch(n_inst: int = 256, seed: int = 0, n_min: int = 2000, n_max: int = 200000,
+                 cellsize: float = 0.01, speed: float = 5.0, margin: int = 5) -> Scene:
+    """A batch of independent 3D impact problems advanced as one grid: in each instance a
+    sphere dropped at ``speed`` onto a Drucker-Prager + Grady-Kipp slab (see
+    :func:`impact_batch_layout` for the draws and the packing).  The sphere is elastic with
+    the nominal rock's K, G and density; gravity -9.81 in z; every instance steps with the
+    batch's dt, the Solver's CFL 0.3 formula over all materials (Solver.cpp:15-32).  At the
+    defaults this is 256 instances and about 11 M particles.  ``scene.inst`` holds each
+    particle's instance and ``scene.instances`` the layout."""
+    h = cellsize
+    psep = h / 2
+    insts, dims = impact_batch_layout(n_inst, seed, n_min, n_max, margin)
+    materials = [material(bulkMod=ROCK["K"], shearMod=ROCK["G"], density=ROCK["rho"], model=1)]
+    pos, mat, obj, inst_of, vel = [], [], [], [], []
+    for inst in insts:
+        slab, ball = _impact_particles(inst, h, margin)
+        off = np.array(inst.origin, np.float64) * h
+        inst.n = len(slab) + len(ball)
+        sK, sG, sc_, sphi = inst.scale
+        materials.append(_rock(ROCK["K"] * sK, ROCK["G"] * sG, ROCK["cohesion"] * sc_, ROCK["phi"] * sphi))
+        pos += [slab + off, ball + off]
+        mat += [np.full(len(slab), 1 + inst.index), np.zeros(len(ball))]
+        obj += [np.full(len(slab), 1), np.full(len(ball), 2)]
+        inst_of.append(np.full(inst.n, inst.index))
+        v = np.zeros((inst.n, 3))
+        v[len(slab):, 2] = -speed
+        vel.append(v)
+    sc = Scene("impact_batch", [dims[0] * h, dims[1] * h, dims[2] * h], h, psep, np.concatenate(pos),
+               np.concatenate(mat).astype(np.int32), np.concatenate(obj).astype(np.int32), materials)
+    sc.gravity = [0.0, 0.0, -9.81]
+    sc.CFL = 0.3
+    sc.tmax = 1.0
+    maxK = max([1.0] + [m["bulkMod"] for m in materials])
+    minrho = min([1e15] + [m["density"] for m in materials])
+    sc.dt = sc.CFL * (h / math.sqrt(maxK / minrho))
+    sc.vel = np.concatenate(vel)
+    sc.inst = np.concatenate(inst_of).astype(np.int32)
+    sc.instances = insts
+    return _finish(sc, seed)
+
+
+def batch_instance(batch: Scene, index: int) -> Scene:
+    """Instance ``index`` of a batch as a problem of its own: its particles in the batch's
+    order, moved to the instance's own domain (the box at the origin), materials [sphere,
+    this slab], the batch's dt and gravity."""
+    inst = batch.instances[index]
+    sel = np.nonzero(batch.inst == index)[0]
+    h = batch.cellsize
+    pos = batch.pos[sel] - np.array(inst.origin, np.float64) * h
+    mat = np.where(batch.mat[sel] == 0, 0, 1).astype(np.int32)
+    sc = Scene(f"impact_instance_{index}", [b * h for b in inst.box], h, batch.psep, pos, mat,
+               batch.obj[sel].copy(), [batch.materials[0], batch.materials[1 + index]])
+    sc.gravity = list(batch.gravity)
+    sc.CFL = batch.CFL
+    sc.tmax = batch.tmax
+    sc.dt = batch.dt
+    sc.vel = batch.vel[sel].copy()
+    return _finish(sc, None)

@@ -1,0 +1,124 @@
+"""A batch of independent impact problems advanced as one grid: the layout keeps the
+instances apart, the batched step equals each instance's own step (FP64 restatement on CPU),
+and the GPU batch matches the FP64 restatement per instance on sampled instances."""
+import numpy as np
+import pytest
+
+from graphyt_gb300 import scenes
+from tests.helpers import rel_l2, run_gpu, run_oracle
+
+STEP_TOL = 1e-5
+MANY_STEP_TOL = 1e-3
+
+
+def test_batch_layout_256():
+    """256 instances: counts log-uniform in [2k, 200k], materials within +/-30 % of the
+    nominal rock, boxes inside the grid and disjoint on the x-y plane, every box as high as
+    its content plus the margins."""
+    insts, dims = scenes.impact_batch_layout(256, seed=0)
+    t = np.array([i.target for i in insts])
+    assert t.min() >= 2000 and t.max() <= 200000
+    lg = np.log(t)
+    assert abs(np.median(lg) - 0.5 * (np.log(2000) + np.log(200000))) < 0.5
+    sc = np.array([i.scale for i in insts])
+    assert sc.min() >= 0.7 and sc.max() <= 1.3
+    occ = np.zeros(dims[:2], np.int32)
+    for i in insts:
+        x, y, z = i.origin
+        bx, by, bz = i.box
+        assert z == 0 and x + bx <= dims[0] and y + by <= dims[1] and bz <= dims[2]
+        occ[x:x + bx, y:y + by] += 1
+        assert bz >= i.thick + 2 * i.radius + 10
+    assert occ.max() == 1
+
+
+def test_batch_particles_stay_in_their_boxes():
+    b = scenes.impact_batch(n_inst=5, seed=2, n_min=2000, n_max=8000)
+    h = b.cellsize
+    for i in b.instances:
+        p = b.pos[b.inst == i.index] / h - np.array(i.origin)
+        assert len(p) == i.n
+        assert p.min() >= 5.0 and np.all(p.max(axis=0) <= np.array(i.box) - 5.0)
+        assert abs(i.n - i.target) < 0.25 * i.target + 200
+    assert len(b.materials) == 1 + len(b.instances)
+    assert np.all(b.vel[b.obj == 2, 2] == -5.0) and np.all(b.vel[b.obj == 1] == 0.0)
+
+
+def test_batch_instances_do_not_couple(oracle_built):
+    """In the FP64 restatement, a batch of three instances gives each instance the same
+    state as its own run (instance domain, same dt), to rounding."""
+    b = scenes.impact_batch(n_inst=3, seed=1, n_min=2000, n_max=4000)
+    ob = run_oracle(b, 30)
+    for i in range(3):
+        own = run_oracle(scenes.batch_instance(b, i), 30)
+        sel = np.nonzero(b.inst == i)[0]
+        for f in ("vel", "stress", "eqps"):
+            assert rel_l2(ob.pfield(f)[sel], own.pfield(f)) < 1e-10, (i, f)
+
+
+@pytest.mark.gpu
+def test_batch_one_step(gpu_lib, oracle_built):
+    b = scenes.impact_batch(n_inst=6, seed=4, n_min=2000, n_max=10000)
+    gpu = run_gpu(b, 2)
+    for i in (0, 3):
+        own = run_oracle(scenes.batch_instance(b, i), 2)
+        sel = np.nonzero(b.inst == i)[0]
+        for f in ("vel", "stress"):
+            assert rel_l2(gpu._get_particles(f)[sel], own.pfield(f)) <= STEP_TOL, (i, f)
+
+
+@pytest.mark.gpu
+def test_batch_sampled_instances_vs_oracle(gpu_lib, oracle_built):
+    """Eight instances sampled from a 12-instance batch, 60 steps: per-instance relative L2
+    of velocity, stress and equivalent plastic strain against each instance's own FP64 run."""
+    b = scenes.impact_batch(n_inst=12, seed=3, n_min=2000, n_max=12000)
+    steps = 60
+    gpu = run_gpu(b, steps)
+    got = {f: gpu._get_particles(f) for f in ("vel", "stress", "eqps")}
+    pick = np.random.default_rng(0).choice(12, 8, replace=False)
+    worst = 0.0
+    for i in pick:
+        own = run_oracle(scenes.batch_instance(b, int(i)), steps)
+        sel = np.nonzero(b.inst == i)[0]
+        for f in got:
+            ref = own.pfield(f)
+            if np.linalg.norm(ref) == 0:
+                assert np.max(np.abs(got[f][sel])) < 1e-9
+                continue
+            e = rel_l2(got[f][sel], ref)
+            worst = max(worst, e)
+            assert e <= MANY_STEP_TOL, (int(i), f, e)
+    assert worst > 0.0
+
+
+@pytest.mark.gpu
+def test_batch_gpu_equals_standalone_gpu(gpu_lib):
+    """The GPU batch and the GPU run of one instance on its own grid agree to FP32
+    summation order."""
+    b = scenes.impact_batch(n_inst=4, seed=5, n_min=3000, n_max=9000)
+    gpu = run_gpu(b, 30)
+    for i in (1, 2):
+        own = run_gpu(scenes.batch_instance(b, i), 30)
+        sel = np.nonzero(b.inst == i)[0]
+        for f in ("vel", "stress"):
+            assert rel_l2(gpu._get_particles(f)[sel], own._get_particles(f)) <= 1e-4, (i, f)
+
+
+@pytest.mark.gpu
+def test_autotune_keeps_results(gpu_lib):
+    """The autotuner times real steps under each candidate and keeps the fastest; the run it
+    leaves behind equals an untuned run of the same number of steps, to summation order."""
+    from graphyt_gb300 import graphyt
+    b = scenes.impact_batch(n_inst=4, seed=6, n_min=3000, n_max=9000)
+    tuned = graphyt.from_scene(b)
+    res = tuned.autotune(step0=0, steps=3)
+    assert (res["sort_every"], res["full_sort"]) in res["ms_per_step"]
+    assert all(v > 0 for v in res["ms_per_step"].values())
+    nxt = res["next_step"]
+    dt = tuned.dt
+    for k in range(nxt, nxt + 5):
+        tuned.iterate_GPU(k * dt, k)
+    tuned.Synchronise()
+    plain = run_gpu(b, nxt + 5)
+    for f in ("vel", "stress"):
+        assert rel_l2(tuned._get_particles(f), plain._get_particles(f)) <= 1e-4, f

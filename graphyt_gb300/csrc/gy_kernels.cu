@@ -480,12 +480,21 @@ __global__ void __launch_bounds__(P2G_CH) k_p2g_multi_tiled(PView P, const int *
         int bx, by, bz;
         decode_block(blk, g, bx, by, bz);
         const int tox = bx * CB, toy = by * CB, toz = g.is3d ? bz * CB : 0;
+        // the object of the segment's first particle: while every particle met so far belongs
+        // to it and is deformable, and every tile node has it as first body (or no body), each
+        // particle's slot-0 sums equal its centre-of-mass sums, so the tile holds the latter
+        // (and the slot-0 normals) only
+        const int obj0 = info_obj((uint32_t)P.ii(PF_INFO, sorted ? perm[start] : start));
         __syncthreads();  // the previous segment's flush is done with the tile
         for (int t = tid; t < MB_FIELDS * PT_NODES; t += P2G_CH) tile[t] = 0.f;
+        bool tile_one = true;
         for (int t = tid; t < PT_NODES; t += P2G_CH) {
             const int ni = tox + t % PT, nj = toy + (t / PT) % PT, nk = toz + t / (PT * PT);
-            tbody[t] = (ni < g.nx && nj < g.ny && nk < g.nz) ? nb.body[node_index(ni, nj, nk, g)] : make_int2(-1, -1);
+            const int2 pr = (ni < g.nx && nj < g.ny && nk < g.nz) ? nb.body[node_index(ni, nj, nk, g)] : make_int2(-1, -1);
+            tbody[t] = pr;
+            tile_one = tile_one && (pr.x == obj0 || pr.x == -1);
         }
+        bool uni = __syncthreads_and(tile_one) != 0;
         for (long long base = start;; base += P2G_CH) {
             int cnt, kcur = -1, kprev = -1;
             long long j = 0;
@@ -505,7 +514,7 @@ __global__ void __launch_bounds__(P2G_CH) k_p2g_multi_tiled(PView P, const int *
                 j = i;
             }
             if (cnt <= 0) break;
-            bool head = false;
+            bool head = false, mine_one = true;
             if (tid < cnt) {
                 const int cell = kcur & 63;
                 head = tid == 0 || (kprev & 63) != cell;
@@ -537,10 +546,22 @@ __global__ void __launch_bounds__(P2G_CH) k_p2g_multi_tiled(PView P, const int *
                                       P.f(PF_S0 + 3, j) * sc);
                 Q2[tid] = make_float4(P.f(PF_S0 + 4, j) * sc, P.f(PF_S0 + 5, j) * sc, vol_n,
                                       __int_as_float(info_obj(info) | (rigid ? 1 << 16 : 0)));
+                mine_one = !rigid && info_obj(info) == obj0;
             }
             const unsigned hm = __ballot_sync(0xffffffffu, head);
             if (lane == 0) wcount[warp] = __popc(hm);
-            __syncthreads();
+            const bool chunk_one = __syncthreads_and(mine_one) != 0;
+            if (uni && !chunk_one) {
+                // from here on the slots are summed apart: slot 0 starts from what the
+                // centre-of-mass fields hold (all of it slot-0 sums), except at nodes
+                // without a body, whose slots receive nothing
+                for (int t = tid; t < PT_NODES; t += P2G_CH)
+                    if (tbody[t].x >= 0)
+#pragma unroll
+                        for (int f = 0; f < 7; f++) tile[(7 + f) * PT_NODES + t] = tile[f * PT_NODES + t];
+                __syncthreads();
+                uni = false;
+            }
             int wbase = 0, R = 0;
 #pragma unroll
             for (int w2 = 0; w2 < P2G_CH / 32; w2++) {
@@ -557,6 +578,28 @@ __global__ void __launch_bounds__(P2G_CH) k_p2g_multi_tiled(PView P, const int *
                 const int li = cell & 3, lj = (cell >> 2) & 3, lk = cell >> 4;
                 const int t = ((lk + kk) * PT + (lj + jj)) * PT + (li + ii);
                 const int2 bp = tbody[t];
+                if (uni) {
+                    float c[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, nr[3] = {0.f, 0.f, 0.f};
+                    for (int p = p0; p < p1; p++) {
+                        const float2 X = W[ii][p], Y = W[3 + jj][p], Z = W[6 + kk][p];
+                        const float4 q0 = Q0[p], q1 = Q1[p], q2 = Q2[p];
+                        const float syz = Y.x * Z.x;
+                        const float w = X.x * syz, gx = X.y * syz, gy = X.x * Y.y * Z.x, gz = X.x * Y.x * Z.y;
+                        const float wm = w * q0.x;
+                        c[0] += wm; c[1] += w * q0.y; c[2] += w * q0.z; c[3] += w * q0.w;
+                        c[4] += -(gx * q1.x + gy * q1.w + gz * q2.y) + wm * grx;
+                        c[5] += -(gx * q1.w + gy * q1.y + gz * q2.x) + wm * gry;
+                        c[6] += -(gx * q2.y + gy * q2.x + gz * q1.z) + wm * grz;
+                        nr[0] += gx * q2.z; nr[1] += gy * q2.z; nr[2] += gz * q2.z;
+                    }
+                    if (!scatter_lane || c[0] == 0.f) continue;
+#pragma unroll
+                    for (int f = 0; f < 7; f++) atomicAdd(&tile[f * PT_NODES + t], c[f]);
+                    if (bp.x >= 0)
+#pragma unroll
+                        for (int f = 0; f < 3; f++) atomicAdd(&tile[(14 + f) * PT_NODES + t], nr[f]);
+                    continue;
+                }
                 // a run whose particles all belong to one deformable object, the node's first
                 // body: its slot-0 mass, momentum and force equal the centre-of-mass sums
                 // (gravity included), so only those and the normal are summed
@@ -643,6 +686,15 @@ __global__ void __launch_bounds__(P2G_CH) k_p2g_multi_tiled(PView P, const int *
             const float *f = tile + t;
             red_add4(&nb.acc0[nd], f[0], f[PT_NODES], f[2 * PT_NODES], f[3 * PT_NODES]);
             red_add4(&nb.acc1[nd], f[4 * PT_NODES], f[5 * PT_NODES], f[6 * PT_NODES], 0.f);
+            if (uni) {
+                if (tbody[t].x >= 0) {
+                    red_add4(&nb.bacc0[0][nd], f[0], f[PT_NODES], f[2 * PT_NODES], f[3 * PT_NODES]);
+                    red_add4(&nb.bacc1[0][nd], f[4 * PT_NODES], f[5 * PT_NODES], f[6 * PT_NODES], 0.f);
+                    red_add4(&nb.bnrm[0][nd], f[14 * PT_NODES], f[15 * PT_NODES], f[16 * PT_NODES], 0.f);
+                }
+                mark_node(nb, ni, nj, nk, g);
+                continue;
+            }
 #pragma unroll
             for (int sl = 0; sl < 2; sl++) {
                 const float *b = f + (7 + 10 * sl) * PT_NODES;
@@ -1262,6 +1314,14 @@ __device__ __forceinline__ void update_after_g2p(PState &st, const int c0[3], fl
 #define GY_G2P_THREADS 64
 #endif
 #define GY_G2P_MINB_TH 12  // the variant with heat conduction: 80 registers
+// multi-body G2P: CTA size and resident CTAs per SM (the node tile holds two body slots, so
+// a larger CTA shares it among more particles)
+#ifndef GY_G2PM_THREADS
+#define GY_G2PM_THREADS 128
+#endif
+#ifndef GY_G2PM_MINB
+#define GY_G2PM_MINB 5
+#endif
 
 // 4-byte asynchronous global -> shared copy (no register holds the value in flight)
 __device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
@@ -1290,7 +1350,8 @@ constexpr int G2P_NBASE = 19, G2P_NDP = 9;
 // and is summed when the state is set.
 constexpr int NSTAT = 5;
 
-__device__ __forceinline__ void particle_stats(float (*col)[GY_G2P_THREADS], const PState &st)
+template <int NT>
+__device__ __forceinline__ void particle_stats(float (*col)[NT], const PState &st)
 {
     const int t = threadIdx.x;
     col[0][t] += st.mass * st.v[0];
@@ -1305,12 +1366,13 @@ __device__ __forceinline__ void particle_stats(float (*col)[GY_G2P_THREADS], con
     col[4][t] += 0.5f * __fdividef(st.mass, st.rho) * se;  // volume m / rho (diagnostic precision)
 }
 
-__device__ __forceinline__ void stats_cta_flush(double *out, float (*col)[GY_G2P_THREADS])
+template <int NT>
+__device__ __forceinline__ void stats_cta_flush(double *out, float (*col)[NT])
 {
     __syncthreads();
     if (threadIdx.x < NSTAT) {
         double v = 0.0;
-        for (int t = 0; t < GY_G2P_THREADS; t++) v += (double)col[threadIdx.x][t];
+        for (int t = 0; t < NT; t++) v += (double)col[threadIdx.x][t];
         atomicAdd(&out[(blockIdx.x % STATS_SLOTS) * 8 + 1 + threadIdx.x], v);
     }
 }
@@ -1527,7 +1589,7 @@ __global__ void __launch_bounds__(GY_G2P_THREADS, THERMAL ? GY_G2P_MINB_TH : GY_
 // slots' solved fields; each particle reads the slot of its own object (Extrapolation.cpp:
 // 311-355), with the weight zeroed where the node holds neither of its bodies.
 template <bool HAS_DP, bool NRM>
-__global__ void __launch_bounds__(GY_G2P_THREADS) k_g2p_multi_tiled(PView src, PView dst, const int *perm,
+__global__ void __launch_bounds__(GY_G2PM_THREADS, GY_G2PM_MINB) k_g2p_multi_tiled(PView src, PView dst, const int *perm,
                                                                     const int *skey, long long n,
                                                                     const int *seg_start, const int *nseg_ptr,
                                                                     int sorted, NodeBufs nb, StepArgs a,
@@ -1538,8 +1600,8 @@ __global__ void __launch_bounds__(GY_G2P_THREADS) k_g2p_multi_tiled(PView src, P
     __shared__ float4 TVb[2][PT_NODES];  // (m, v1) per body slot
     __shared__ float4 TAb[2][PT_NODES];  // (a1, -) per body slot
     __shared__ float4 TN[NRM ? 2 : 1][NRM ? PT_NODES : 1];
-    __shared__ float stage[NST][GY_G2P_THREADS];
-    __shared__ float s_st[NSTAT][GY_G2P_THREADS];
+    __shared__ float stage[NST][GY_G2PM_THREADS];
+    __shared__ float s_st[NSTAT][GY_G2PM_THREADS];
     __shared__ long long s_end;
     const GridGeom &g = a.g;
     const int nseg = *nseg_ptr;
@@ -1719,18 +1781,18 @@ void launch_g2p_update(const PView &src, const PView &dst, const int *perm, cons
                           : vi == 2 ? (const void *)k_g2p_multi_tiled<true, false>
                           : vi == 1 ? (const void *)k_g2p_multi_tiled<false, true>
                                     : (const void *)k_g2p_multi_tiled<false, false>;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, GY_G2P_THREADS, 0);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, GY_G2PM_THREADS, 0);
             mgrid[vi] = sms * std::max(b, 1);
         }
         const unsigned mg = (unsigned)mgrid[vi];
         if (has_dp && tn)
-            k_g2p_multi_tiled<true, true><<<mg, GY_G2P_THREADS, 0, s>>>(src, dst, perm, skey, n, seg_start, nseg, srt, nb, a, cf);
+            k_g2p_multi_tiled<true, true><<<mg, GY_G2PM_THREADS, 0, s>>>(src, dst, perm, skey, n, seg_start, nseg, srt, nb, a, cf);
         else if (has_dp)
-            k_g2p_multi_tiled<true, false><<<mg, GY_G2P_THREADS, 0, s>>>(src, dst, perm, skey, n, seg_start, nseg, srt, nb, a, cf);
+            k_g2p_multi_tiled<true, false><<<mg, GY_G2PM_THREADS, 0, s>>>(src, dst, perm, skey, n, seg_start, nseg, srt, nb, a, cf);
         else if (tn)
-            k_g2p_multi_tiled<false, true><<<mg, GY_G2P_THREADS, 0, s>>>(src, dst, perm, skey, n, seg_start, nseg, srt, nb, a, cf);
+            k_g2p_multi_tiled<false, true><<<mg, GY_G2PM_THREADS, 0, s>>>(src, dst, perm, skey, n, seg_start, nseg, srt, nb, a, cf);
         else
-            k_g2p_multi_tiled<false, false><<<mg, GY_G2P_THREADS, 0, s>>>(src, dst, perm, skey, n, seg_start, nseg, srt, nb, a, cf);
+            k_g2p_multi_tiled<false, false><<<mg, GY_G2PM_THREADS, 0, s>>>(src, dst, perm, skey, n, seg_start, nseg, srt, nb, a, cf);
     } else {
         const int srt = perm ? 1 : 0;
         if (therm) {

@@ -486,7 +486,10 @@ __global__ void __launch_bounds__(P2G_CH) k_p2g_multi_tiled(PView P, const int *
         // (and the slot-0 normals) only
         const int obj0 = info_obj((uint32_t)P.ii(PF_INFO, sorted ? perm[start] : start));
         __syncthreads();  // the previous segment's flush is done with the tile
-        for (int t = tid; t < MB_FIELDS * PT_NODES; t += P2G_CH) tile[t] = 0.f;
+        // the centre-of-mass fields and the slot-0 normals; the other slot fields are set
+        // when the segment stops being one object's
+        for (int t = tid; t < 7 * PT_NODES; t += P2G_CH) tile[t] = 0.f;
+        for (int t = tid; t < 3 * PT_NODES; t += P2G_CH) tile[14 * PT_NODES + t] = 0.f;
         bool tile_one = true;
         for (int t = tid; t < PT_NODES; t += P2G_CH) {
             const int ni = tox + t % PT, nj = toy + (t / PT) % PT, nk = toz + t / (PT * PT);
@@ -495,6 +498,13 @@ __global__ void __launch_bounds__(P2G_CH) k_p2g_multi_tiled(PView P, const int *
             tile_one = tile_one && (pr.x == obj0 || pr.x == -1);
         }
         bool uni = __syncthreads_and(tile_one) != 0;
+        if (!uni)
+            for (int t = tid; t < PT_NODES; t += P2G_CH) {
+#pragma unroll
+                for (int f = 7; f < 14; f++) tile[f * PT_NODES + t] = 0.f;
+#pragma unroll
+                for (int f = 17; f < MB_FIELDS; f++) tile[f * PT_NODES + t] = 0.f;
+            }
         for (long long base = start;; base += P2G_CH) {
             int cnt, kcur = -1, kprev = -1;
             long long j = 0;
@@ -555,10 +565,13 @@ __global__ void __launch_bounds__(P2G_CH) k_p2g_multi_tiled(PView P, const int *
                 // from here on the slots are summed apart: slot 0 starts from what the
                 // centre-of-mass fields hold (all of it slot-0 sums), except at nodes
                 // without a body, whose slots receive nothing
-                for (int t = tid; t < PT_NODES; t += P2G_CH)
-                    if (tbody[t].x >= 0)
+                for (int t = tid; t < PT_NODES; t += P2G_CH) {
+                    const bool has = tbody[t].x >= 0;
 #pragma unroll
-                        for (int f = 0; f < 7; f++) tile[(7 + f) * PT_NODES + t] = tile[f * PT_NODES + t];
+                    for (int f = 0; f < 7; f++) tile[(7 + f) * PT_NODES + t] = has ? tile[f * PT_NODES + t] : 0.f;
+#pragma unroll
+                    for (int f = 17; f < MB_FIELDS; f++) tile[f * PT_NODES + t] = 0.f;
+                }
                 __syncthreads();
                 uni = false;
             }
@@ -780,6 +793,9 @@ __global__ void k_fold(NodeBufs nb, GridGeom g, int axis)
     if (axis == 0) { pi = l; pj = a0; pk = a1; qi = g.nx - 3 + l; qj = a0; qk = a1; }
     else if (axis == 1) { pi = a0; pj = l; pk = a1; qi = a0; qj = g.ny - 3 + l; qk = a1; }
     else { pi = a0; pj = a1; pk = l; qi = a0; qj = a1; qk = g.nz - 3 + l; }
+    // the accumulators of a node block P2G (or an earlier axis' fold) did not flag are all
+    // zero: a pair of such nodes folds to zeros already in place
+    if (!nb.flags[node_block(pi, pj, pk, g)] && !nb.flags[node_block(qi, qj, qk, g)]) return;
     const long long p = node_index(pi, pj, pk, g), q = node_index(qi, qj, qk, g);
     bool any = fold4(nb.acc0, p, q);
     any |= fold4(nb.acc1, p, q);

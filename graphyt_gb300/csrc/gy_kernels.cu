@@ -1891,43 +1891,69 @@ void launch_body_tables(const PView &p, long long n, const StepArgs &a, int *cel
     note_launch(1);
 }
 
-__global__ void k_body_assign(NodeBufs nb, GridGeom g, const int *cell_min, int nbody, const int *nidx_x,
-                              const int *nidx_y, const int *nidx_z)
+// Body pair of every node (Extrapolation.cpp:191-208): the window of 4x4x4 cells from the
+// node's cell - 2 is scanned in k, j, i order; the first particle of the first occupied cell
+// names body 1, and the first particle of another object in that or a later cell names body
+// 2; the rigid flags are ORed over the whole window.  Cells are addressed by the linear cell
+// index as the reference forms it (an index outside [0, nc) is skipped, one outside a row
+// wraps into the neighbouring row).
+//
+// One CTA per 4x4x4 node block: the union of its nodes' windows (at most 8 cells per axis) is
+// summarised into shared memory once, one word per cell -- its first and second body by
+// particle order and its rigid bits -- so each node's 64-cell scan reads shared memory.  With
+// the first body b1 of the first occupied cell fixed, a later cell's "first particle of
+// another object" is its first body when that differs from b1, else its second.
+constexpr int BA_SPAN = 8;
+
+__device__ __forceinline__ int body_cell_summary(const int *row, int nbody)
 {
-    const long long nd = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (nd >= g.nn) return;
-    const int i = (int)(nd % g.nx);
-    const int j = (int)((nd / g.nx) % g.ny);
-    const int k = (int)(nd / ((long long)g.nx * g.ny));
-    const int cx = nidx_x[i], cy = nidx_y[j], cz = g.is3d ? nidx_z[k] : 0;
+    int f = -1, fp = NO_PARTICLE, s2 = -1, sp = NO_PARTICLE;
+    for (int b = 0; b < nbody; b++) {
+        const int pid = row[b];
+        if (pid == NO_PARTICLE) continue;
+        if (pid < fp) { s2 = f; sp = fp; f = b; fp = pid; }
+        else if (pid < sp) { s2 = b; sp = pid; }
+    }
+    return (f + 1) | ((s2 + 1) << 5) | (row[nbody] << 10);
+}
+
+__global__ void __launch_bounds__(64) k_body_assign(NodeBufs nb, GridGeom g, const int *cell_min, int nbody,
+                                                    const int *nidx_x, const int *nidx_y, const int *nidx_z)
+{
+    __shared__ int cs[BA_SPAN * BA_SPAN * BA_SPAN];
+    const long long blk = blockIdx.x;
+    const int bx = (int)(blk % g.nnbx), by = (int)((blk / g.nnbx) % g.nnby), bz = (int)(blk / ((long long)g.nnbx * g.nnby));
+    const int i0 = bx * 4, j0 = by * 4, k0 = bz * 4;
+    const int cx0 = nidx_x[i0] - 2, cy0 = nidx_y[j0] - 2, cz0 = g.is3d ? nidx_z[k0] - 2 : 0;
+    const int zspan = g.is3d ? BA_SPAN : 1;
     const int stride = nbody + 1;
+    const long long plane = (long long)g.ncx * g.ncy;
+    for (int q = threadIdx.x; q < BA_SPAN * BA_SPAN * zspan; q += blockDim.x) {
+        const int lx = q % BA_SPAN, ly = (q / BA_SPAN) % BA_SPAN, lz = q / (BA_SPAN * BA_SPAN);
+        const long long c = (long long)(cx0 + lx) + (long long)(cy0 + ly) * g.ncx + (long long)(cz0 + lz) * plane;
+        cs[q] = (c >= 0 && c < g.nc) ? body_cell_summary(cell_min + c * stride, nbody) : 0;
+    }
+    __syncthreads();
+    const int lx = threadIdx.x & 3, ly = (threadIdx.x >> 2) & 3, lz = threadIdx.x >> 4;
+    const int i = i0 + lx, j = j0 + ly, k = k0 + lz;
+    if (i >= g.nx || j >= g.ny || k >= g.nz) return;
+    const int ox = nidx_x[i] - cx0, oy = nidx_y[j] - cy0, oz = g.is3d ? nidx_z[k] - cz0 : 2;
     int b0 = -1, b1 = -1;
     int rig = 0;  // OR of rigid bits over the window
     const int kmin = g.is3d ? -2 : 0, kmax = g.is3d ? 2 : 1;
     for (int kk = kmin; kk < kmax; kk++)
         for (int jj = -2; jj < 2; jj++)
             for (int ii = -2; ii < 2; ii++) {
-                const long long c = (long long)(cx + ii) + (long long)(cy + jj) * g.ncx + (long long)(cz + kk) * g.ncx * g.ncy;
-                if (c >= g.nc || c < 0) continue;
-                const int *row = cell_min + c * stride;
-                rig |= row[nbody];
+                const int v = cs[((g.is3d ? oz + kk : 0) * BA_SPAN + (oy + jj)) * BA_SPAN + (ox + ii)];
+                rig |= v >> 10;
                 if (b1 != -1) continue;
-                // first particle of the cell, and first one whose object differs from b0
-                int first = -1, fpid = NO_PARTICLE, other = -1, opid = NO_PARTICLE;
-                for (int b = 0; b < nbody; b++) {
-                    const int pid = row[b];
-                    if (pid == NO_PARTICLE) continue;
-                    if (pid < fpid) { fpid = pid; first = b; }
-                }
+                const int first = (v & 31) - 1;
                 if (first < 0) continue;
                 if (b0 == -1) b0 = first;
-                for (int b = 0; b < nbody; b++) {
-                    const int pid = row[b];
-                    if (b == b0 || pid == NO_PARTICLE) continue;
-                    if (pid < opid) { opid = pid; other = b; }
-                }
+                const int other = first != b0 ? first : ((v >> 5) & 31) - 1;
                 if (other >= 0) b1 = other;
             }
+    const long long nd = node_index(i, j, k, g);
     nb.body[nd] = make_int2(b0, b1);
     unsigned char hr = 0;
     if (b0 >= 0 && (rig >> b0) & 1) hr |= 1;
@@ -1938,7 +1964,7 @@ __global__ void k_body_assign(NodeBufs nb, GridGeom g, const int *cell_min, int 
 void launch_body_assign(const NodeBufs &nb, const StepArgs &a, const int *cell_min, int nbody, const int *nidx_x,
                         const int *nidx_y, const int *nidx_z, cudaStream_t s)
 {
-    k_body_assign<<<(unsigned)((a.g.nn + 255) / 256), 256, 0, s>>>(nb, a.g, cell_min, nbody, nidx_x, nidx_y, nidx_z);
+    k_body_assign<<<(unsigned)a.g.nnb, 64, 0, s>>>(nb, a.g, cell_min, nbody, nidx_x, nidx_y, nidx_z);
     note_launch(1);
 }
 

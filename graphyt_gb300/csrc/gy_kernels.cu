@@ -1139,8 +1139,11 @@ __global__ void k_compact_active(NodeBufs nb, int nnb, double *stats)
 
 // Multi-body nodal solve with contact: two warps per active node block from the list P2G
 // and the fold built (32 nodes each); the block's flag is cleared for the next step.
+#ifndef GY_SOLVE_MINB
+#define GY_SOLVE_MINB 5  // resident 256-thread CTAs per SM the multi-body solve is register-capped to (48)
+#endif
 template <bool MULTI>
-__global__ void __launch_bounds__(256) k_solve_list(NodeBufs nb, StepArgs a, int keep)
+__global__ void __launch_bounds__(256, GY_SOLVE_MINB) k_solve_list(NodeBufs nb, StepArgs a, int keep)
 {
     const int lane = threadIdx.x & 31;
     const int gw = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);

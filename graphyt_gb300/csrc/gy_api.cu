@@ -94,10 +94,6 @@ struct gy_solver {
     cudaEvent_t ring_ev[kRing] = {};
     bool ring_busy[kRing] = {};
     long long ring_pos = 0;
-    StepScalars sc_last{};                  // the scalars the device holds, when sc_valid
-    bool sc_valid = false;
-    bool time_bcs = false;                  // a sine-ramped particle BC reads the step time
-    bool rb_fresh = false;                  // h_rb holds the last step's sums and status words
     std::vector<StepGraph> graphs;          // captured steps, one per StepVariant
     float4 *d_pbc_val = nullptr;
     int *d_refkey0 = nullptr;
@@ -648,11 +644,6 @@ gy_status gy_initialize(gy_solver *h, const gy_material *mats, int nmat, const g
             h->pbc_type[i] != BC_MP_FY && h->pbc_type[i] != BC_MP_FZ && h->pbc_type[i] != BC_MP_FX_FY &&
             h->pbc_type[i] != BC_MP_STRESS_XX_YY)
             h->pbc_type[i] = 0;  // every other particle BC has no body in the reference
-    h->time_bcs = false;
-    for (long long i = 0; i < n; i++)
-        if (h->pbc_type[i] == BC_MP_VXSIN || h->pbc_type[i] == BC_MP_VYSIN || h->pbc_type[i] == BC_MP_SYYSIN)
-            h->time_bcs = true;
-    h->sc_valid = false;
 
     // ---- particle slab ----
     h->cap = (std::max<long long>(n, 1) + 31) / 32 * 32;  // every field starts on a 128-byte boundary
@@ -959,20 +950,17 @@ static gy_status enqueue_step(gy_solver *h, double t, int step)
         v.sk = h->sk ^ 1;
     }
     if (h->multi && ((step % 10 == 0) || step == 1 || !h->tables_valid)) v.tables = h->steps == 0 ? 2 : 1;
-    // the step's scalars through a pinned ring slot, copied only when they differ from those
-    // the device holds; a slot is rewritten only after the copy that last read it has run
-    // (the host waits only when 32 copies are queued)
-    StepScalars sc = make_scalars(h, step);
-    if (!h->time_bcs) sc.t_bc = 0.0f;  // read only by the sine-ramped particle BCs
-    if (!h->sc_valid || std::memcmp(&sc, &h->sc_last, sizeof(sc)) != 0) {
+    // every step's scalars (dt, dt at the nodes, gravity, damping, friction, BC time) travel
+    // host-to-device through a pinned ring slot, ahead of the step's kernels on its stream; a
+    // slot is rewritten only after the copy that last read it has run (the host waits only
+    // when 32 steps are queued)
+    {
         const int slot = (int)(h->ring_pos++ % gy_solver::kRing);
         if (h->ring_busy[slot]) CK(h, cudaEventSynchronize(h->ring_ev[slot]));
-        h->h_ring[slot] = sc;
+        h->h_ring[slot] = make_scalars(h, step);
         CK(h, cudaMemcpyAsync(h->d_sc, &h->h_ring[slot], sizeof(StepScalars), cudaMemcpyHostToDevice, s));
         CK(h, cudaEventRecord(h->ring_ev[slot], s));
         h->ring_busy[slot] = true;
-        h->sc_last = sc;
-        h->sc_valid = true;
     }
     if (h->opt.use_graph && !timing) {
         StepGraph *gr = nullptr;

@@ -486,6 +486,7 @@ class Instance:
     origin: tuple = (0, 0, 0)
     scale: tuple = (1.0, 1.0, 1.0, 1.0)   # K, G, cohesion, friction angle over the nominal rock
     n: int = 0
+    mat: int = 0                          # the slab's material row in its batch
 
 
 # the rock of the Brazilian disc workload: DP K 3e10, G 2e10, rho 2600, cohesion 1e7,
@@ -522,7 +523,7 @@ def _impact_shape(target: int, margin: int):
 
 
 def impact_batch_layout(n_inst: int = 256, seed: int = 0, n_min: int = 2000, n_max: int = 200000,
-                        margin: int = 5, spread: float = 0.3):
+                        margin: int = 5, spread: float = 0.3, shard: Optional[tuple] = None):
     """Instances and the batch grid (cells per axis) without particles.
 
     Particle counts are drawn log-uniform in [n_min, n_max] and the slab's K, G, cohesion
@@ -531,16 +532,23 @@ def impact_batch_layout(n_inst: int = 256, seed: int = 0, n_min: int = 2000, n_m
     widest first, in rows along x about as long as the square root of their total area;
     boxes touch, and each keeps ``margin`` empty cells around its content, so neighbouring
     instances never reach a common node (GIMP support spans 1.25 cells) and the periodic
-    fold of the outermost three node layers sees no mass."""
+    fold of the outermost three node layers sees no mass.
+
+    shard = (rank, ranks) keeps the instances whose index is rank modulo ranks (the draws are
+    those of the whole batch), for one process per GPU each stepping its share."""
     rng = np.random.default_rng(seed)
     targets = np.exp(rng.uniform(math.log(n_min), math.log(n_max), n_inst))
     scales = rng.uniform(1.0 - spread, 1.0 + spread, (n_inst, 4))
     insts = []
     for i in range(n_inst):
+        if shard is not None and i % shard[1] != shard[0]:
+            continue
         side, thick, radius, box = _impact_shape(int(round(targets[i])), margin)
         insts.append(Instance(i, int(round(targets[i])), side, thick, radius, box,
                               scale=tuple(float(v) for v in scales[i])))
-    order = sorted(range(n_inst), key=lambda i: (-insts[i].box[0], i))
+    if not insts:
+        raise ValueError("the shard holds no instance")
+    order = sorted(range(len(insts)), key=lambda i: (-insts[i].box[0], i))
     area = sum(insts[i].box[0] * insts[i].box[1] for i in order)
     row_len = max(insts[order[0]].box[0], int(math.ceil(math.sqrt(area))))
     x = y = depth = width = 0
@@ -575,17 +583,19 @@ def _impact_particles(inst: Instance, h: float, margin: int):
 
 
 def impact_batch(n_inst: int = 256, seed: int = 0, n_min: int = 2000, n_max: int = 200000,
-                 cellsize: float = 0.01, speed: float = 5.0, margin: int = 5) -> Scene:
+                 cellsize: float = 0.01, speed: float = 5.0, margin: int = 5,
+                 shard: Optional[tuple] = None) -> Scene:
     """A batch of independent 3D impact problems advanced as one grid: in each instance a
     sphere dropped at ``speed`` onto a Drucker-Prager + Grady-Kipp slab (see
     :func:`impact_batch_layout` for the draws and the packing).  The sphere is elastic with
     the nominal rock's K, G and density; gravity -9.81 in z; every instance steps with the
     batch's dt, the Solver's CFL 0.3 formula over all materials (Solver.cpp:15-32).  At the
     defaults this is 256 instances and about 11 M particles.  ``scene.inst`` holds each
-    particle's instance and ``scene.instances`` the layout."""
+    particle's instance and ``scene.instances`` the layout; ``shard`` as in
+    :func:`impact_batch_layout`."""
     h = cellsize
     psep = h / 2
-    insts, dims = impact_batch_layout(n_inst, seed, n_min, n_max, margin)
+    insts, dims = impact_batch_layout(n_inst, seed, n_min, n_max, margin, shard=shard)
     materials = [material(bulkMod=ROCK["K"], shearMod=ROCK["G"], density=ROCK["rho"], model=1)]
     pos, mat, obj, inst_of, vel = [], [], [], [], []
     for inst in insts:
@@ -593,9 +603,10 @@ def impact_batch(n_inst: int = 256, seed: int = 0, n_min: int = 2000, n_max: int
         off = np.array(inst.origin, np.float64) * h
         inst.n = len(slab) + len(ball)
         sK, sG, sc_, sphi = inst.scale
+        inst.mat = len(materials)
         materials.append(_rock(ROCK["K"] * sK, ROCK["G"] * sG, ROCK["cohesion"] * sc_, ROCK["phi"] * sphi))
         pos += [slab + off, ball + off]
-        mat += [np.full(len(slab), 1 + inst.index), np.zeros(len(ball))]
+        mat += [np.full(len(slab), inst.mat), np.zeros(len(ball))]
         obj += [np.full(len(slab), 1), np.full(len(ball), 2)]
         inst_of.append(np.full(inst.n, inst.index))
         v = np.zeros((inst.n, 3))
@@ -606,26 +617,35 @@ def impact_batch(n_inst: int = 256, seed: int = 0, n_min: int = 2000, n_max: int
     sc.gravity = [0.0, 0.0, -9.81]
     sc.CFL = 0.3
     sc.tmax = 1.0
-    maxK = max([1.0] + [m["bulkMod"] for m in materials])
-    minrho = min([1e15] + [m["density"] for m in materials])
-    sc.dt = sc.CFL * (h / math.sqrt(maxK / minrho))
+    # the whole batch's dt (every shard steps with it): the nominal rock scaled by the
+    # largest K factor drawn, over the common density
+    maxK = ROCK["K"] * max(1.0, max(_batch_scales(n_inst, seed, n_min, n_max)[:, 0]))
+    sc.dt = sc.CFL * (h / math.sqrt(maxK / ROCK["rho"]))
     sc.vel = np.concatenate(vel)
     sc.inst = np.concatenate(inst_of).astype(np.int32)
     sc.instances = insts
     return _finish(sc, seed)
 
 
+def _batch_scales(n_inst, seed, n_min, n_max, spread: float = 0.3):
+    """The material factors of every instance of the whole batch (the draws of
+    :func:`impact_batch_layout`)."""
+    rng = np.random.default_rng(seed)
+    rng.uniform(math.log(n_min), math.log(n_max), n_inst)
+    return rng.uniform(1.0 - spread, 1.0 + spread, (n_inst, 4))
+
+
 def batch_instance(batch: Scene, index: int) -> Scene:
     """Instance ``index`` of a batch as a problem of its own: its particles in the batch's
     order, moved to the instance's own domain (the box at the origin), materials [sphere,
     this slab], the batch's dt and gravity."""
-    inst = batch.instances[index]
+    inst = next(i for i in batch.instances if i.index == index)
     sel = np.nonzero(batch.inst == index)[0]
     h = batch.cellsize
     pos = batch.pos[sel] - np.array(inst.origin, np.float64) * h
     mat = np.where(batch.mat[sel] == 0, 0, 1).astype(np.int32)
     sc = Scene(f"impact_instance_{index}", [b * h for b in inst.box], h, batch.psep, pos, mat,
-               batch.obj[sel].copy(), [batch.materials[0], batch.materials[1 + index]])
+               batch.obj[sel].copy(), [batch.materials[0], batch.materials[inst.mat]])
     sc.gravity = list(batch.gravity)
     sc.CFL = batch.CFL
     sc.tmax = batch.tmax

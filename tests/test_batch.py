@@ -144,3 +144,23 @@ def test_full_batch_largest_instances_match_their_own_runs(gpu_lib):
         assert rel_l2(vel[sel], own._get_particles("vel")) <= 1e-4
         assert rel_l2(stress[sel], own._get_particles("stress")) <= 1e-4
         own.close()
+
+
+@pytest.mark.gpu
+def test_batch_500_steps_per_instance(gpu_lib, oracle_built):
+    """Six instances over the configuration's 500 steps: per instance, velocity and stress
+    within 1e-3 of the FP64 restatement.  The equivalent plastic strain, the most sensitive
+    field (a 1e-7 relative change of the FP64 initial positions moves it by 1.6e-4 here), is
+    held to 5e-3."""
+    b = scenes.impact_batch(n_inst=6, seed=7, n_min=2000, n_max=6000)
+    steps = 500
+    gpu = run_gpu(b, steps)
+    ref = run_oracle(b, steps)
+    for f, tol in (("vel", MANY_STEP_TOL), ("stress", MANY_STEP_TOL), ("eqps", 5e-3)):
+        a, r = gpu._get_particles(f), ref.pfield(f)
+        for i in range(6):
+            sel = b.inst == i
+            if np.linalg.norm(r[sel]) == 0:
+                assert np.max(np.abs(a[sel])) < 1e-9
+                continue
+            assert rel_l2(a[sel], r[sel]) <= tol, (i, f, rel_l2(a[sel], r[sel]))

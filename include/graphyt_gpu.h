@@ -157,7 +157,8 @@ gy_status gy_set_particle_temp(gy_solver *h, int64_t count, const int64_t *idx, 
 gy_status gy_set_node_bc(gy_solver *h, int64_t count, const int64_t *nodes, const int *type, const double *val4);
 
 /* Solver::Solver (Solver.cpp:7-37): stores the materials and parameters, sets dt =
- * CFL*h/sqrt(maxK/minRho) and runs initialize() (Solver.cpp:40-69); uploads all state. */
+ * CFL*h/sqrt(maxK/minRho) and runs initialize() (Solver.cpp:40-69); uploads all state.
+ * Up to 4096 materials and 16 distinct objectIDs (GY_ERR_UNSUPPORTED beyond). */
 gy_status gy_initialize(gy_solver *h, const gy_material *mats, int nmat, const gy_params *prm);
 
 /* Solver::setDt (Solver.cpp:70-73) and the dt attribute (Solver.i:17). */

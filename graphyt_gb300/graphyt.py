@@ -216,15 +216,19 @@ class MaterialPoints:
         self._hold.add(int(p))
 
     def setBC(self, p, type, val):
-        v = list(val)[:4] + [0.0] * (4 - len(list(val)[:4]))
+        """MaterialPoints::setBC (MaterialPoints.cpp:88-93): writes the type and only the values
+        given; the others keep what an earlier call set (zero at first, :210-217)."""
+        v = list(self._bc.get(int(p), (0, [0.0] * 4))[1])
+        given = [float(x) for x in list(val)[:4]]
+        v[: len(given)] = given
         self._bc[int(p)] = (int(type), v)
 
     def setBCs(self, idx, type, val):
+        """setBC for many particles at once: idx (k,), type (k,) or scalar, val (k, <=4) or (<=4,)."""
         val = np.atleast_2d(np.asarray(val, np.float64))
         types = np.broadcast_to(np.asarray(type, np.int32), (len(idx),))
         for q, p in enumerate(np.asarray(idx).tolist()):
-            row = val[q if len(val) > 1 else 0].tolist()
-            self._bc[int(p)] = (int(types[q]), row + [0.0] * (4 - len(row)))
+            self.setBC(p, types[q], val[q if len(val) > 1 else 0].tolist())
 
     # ---- getters (MaterialPoints.cpp:238-273) --------------------------------------------
     def _field(self, name):

@@ -261,3 +261,35 @@ def test_dam_break_coarse_1000_steps(gpu_lib, oracle_built):
     for f in ("vel", "stress", "pos"):
         err = rel_l2(gpu._get_particles(f), ref.pfield(f))
         assert err <= MANY_STEP_TOL, (f, err)
+
+
+def test_brazilian_disc_coarse_200_steps(gpu_lib, oracle_built):
+    """The Brazilian disc at a tenth of the resolution (11,392 particles, disc and two rigid
+    platens) over 200 steps, through platen contact into Drucker-Prager yielding: velocity,
+    stress and equivalent plastic strain within 1e-3 of the FP64 restatement.  Over this
+    horizon a 1e-7 relative change of the FP64 initial positions moves velocity and stress by
+    3e-6 and the plastic strain by 2e-5; past the onset of yielding the reference itself
+    diverges (6e-3 at 400 steps, 0.35 in velocity at 1000), so no longer run can be held to a
+    fixed bound."""
+    sc = scenes.brazilian_disc(scale=0.1)
+    gpu = run_gpu(sc, 200)
+    ref = run_oracle(sc, 200)
+    assert np.linalg.norm(ref.pfield("eqps")) > 0  # the return mapping acted
+    for f in ("vel", "stress", "eqps"):
+        err = rel_l2(gpu._get_particles(f), ref.pfield(f))
+        assert err <= MANY_STEP_TOL, (f, err)
+
+
+def test_damage_block_100_steps(gpu_lib, oracle_built):
+    """Drucker-Prager + Grady-Kipp block of 1,728 particles over 100 steps, by which time
+    nearly every particle has grown damage: velocity, stress, damage and equivalent plastic
+    strain within 1e-3 of the FP64 restatement.  Over this horizon a 1e-7 relative change of
+    the FP64 initial positions moves the stress by 1.3e-5 and the damage by 7e-7; by 200 steps
+    the reference itself diverges (0.28 in stress)."""
+    sc = scenes.damage_block(n_side=12)
+    gpu = run_gpu(sc, 100)
+    ref = run_oracle(sc, 100)
+    assert (ref.pfield("damage") > 0).mean() > 0.9
+    for f in ("vel", "stress", "damage", "eqps"):
+        err = rel_l2(gpu._get_particles(f), ref.pfield(f))
+        assert err <= MANY_STEP_TOL, (f, err)

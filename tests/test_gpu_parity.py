@@ -125,7 +125,7 @@ def test_one_step_parity(gpu_lib, oracle_built, name):
     nsteps = 2  # steps 0 and 1 (step 1 uses the half-dt nodal update)
     gpu = run_gpu(sc, nsteps)
     ref = run_oracle(sc, nsteps)
-    for f in ("vel", "stress", "pos", "density"):
+    for f in ("vel", "stress", "pos", "density", "damage"):
         a = gpu._get_particles(f)
         b = ref.pfield(f)
         err = rel_l2(a, b)

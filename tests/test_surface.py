@@ -170,3 +170,10 @@ def test_particle_ids_and_getters_before_the_solver():
     assert mp.getMatID(1) == 2 and mp.getObjID(2) == 6
     with pytest.raises(RuntimeError):
         mp.getStressArr()
+
+
+def test_missing_library_fails_loudly(tmp_path, monkeypatch):
+    """Without the built CUDA library the package raises; there is no CPU path to fall to."""
+    monkeypatch.setattr(L, "_lib", None)
+    with pytest.raises(ImportError, match="no CPU fallback"):
+        L.load(str(tmp_path / "libgraphyt_gpu.so"))

@@ -25,3 +25,40 @@ def run_oracle(scene, nsteps, kind="port"):
     o = Oracle(scene, kind, mode=1)
     o.run(nsteps)
     return o
+
+
+AFFINE_A = np.array([[0.8, 0.3, -0.2], [0.1, -0.5, 0.4], [-0.3, 0.2, 0.6]])
+
+
+def affine_block(model):
+    """A 16^3-particle block with the affine velocity field v = A (x - c) + b and no gravity.
+    For particles 2.5 cells or more inside the block every node they read sees a full
+    lattice, so GIMP reproduces the linear field: their first-step strain rate is sym(A)
+    exactly.  Returns the scene and the mask of those particles."""
+    from graphyt_gb300 import scenes
+    sc = scenes.tiny_block(model=model, n_side=16, L=(2.5, 2.5, 2.5), gravity=(0.0, 0.0, 0.0))
+    sc.materials[0]["viscosity"] = 2e5
+    sc.vel = (sc.pos - sc.pos.mean(axis=0)) @ AFFINE_A.T + np.array([0.05, -0.02, 0.01])
+    lo, hi, d = sc.pos.min(axis=0), sc.pos.max(axis=0), 2.5 * sc.cellsize - 1e-9
+    inner = np.all((sc.pos > lo + d) & (sc.pos < hi - d), axis=1)
+    return sc, inner
+
+
+def affine_block_stress(model, mat, dt):
+    """Stress after one step from zero stress and zero strain under the strain rate sym(A):
+    elastic, ConstitutiveModels.cpp:12-28 (1/3 written 0.3333); Newtonian, :41-62 (1/3 written
+    0.33333, pressure K tr(strain), viscous terms multiplied by dt)."""
+    E = 0.5 * (AFFINE_A + AFFINE_A.T)
+    er = np.array([E[0, 0], E[1, 1], E[2, 2], E[0, 1], E[1, 2], E[0, 2]])
+    K, G, mu = mat["bulkMod"], mat["shearMod"], mat["viscosity"]
+    out = np.empty(6)
+    if model == 1:
+        vol = 0.3333 * er[:3].sum()
+        out[:3] = (2.0 * G * (er[:3] - vol) + 3.0 * K * vol) * dt
+        out[3:] = 2.0 * G * er[3:] * dt
+    else:
+        vol = 0.33333 * er[:3].sum()
+        P = K * er[:3].sum() * dt
+        out[:3] = P + mu * (2.0 - 2.0 / 3.0) * (er[:3] - vol) * dt
+        out[3:] = 2.0 * mu * er[3:] * dt
+    return out, er * dt

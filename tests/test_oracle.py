@@ -12,7 +12,7 @@ import pytest
 
 from graphyt_gb300 import scenes
 from tests.golden import make_golden
-from tests.helpers import rel_l2
+from tests.helpers import affine_block, affine_block_stress, rel_l2
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 
@@ -202,3 +202,19 @@ def test_thermal_harness_matches_literal_between_sorts(oracle_built):
     assert np.linalg.norm(port - har) <= 1e-12 * dT
     garbled = range(0, 9)
     assert np.linalg.norm(temp_after("ref", 0, garbled) - temp_after("ref", 1, garbled)) > 1e-3 * dT
+
+
+@pytest.mark.parametrize("model", [1, 2])
+def test_elastic_and_newtonian_first_step_known_answer(oracle_built, model):
+    """Under an affine velocity field the first step's strain rate is sym(A) at interior
+    particles, so their stress and strain follow the closed forms of the elastic and Newtonian
+    laws with the reference's literal constants (0.3333, 0.33333 for 1/3)."""
+    from oracle.oracle import Oracle
+    sc, inner = affine_block(model)
+    o = Oracle(sc, "port")
+    o.run(1)
+    want_s, want_e = affine_block_stress(model, sc.materials[0], o.dt)
+    s, e = o.pfield("stress")[inner], o.pfield("strain")[inner]
+    assert inner.sum() == 216
+    assert np.abs(s - want_s).max() <= 1e-12 * np.abs(want_s).max()
+    assert np.abs(e - want_e).max() <= 1e-12 * np.abs(want_e).max()

@@ -38,6 +38,7 @@ def affine_block(model):
     from graphyt_gb300 import scenes
     sc = scenes.tiny_block(model=model, n_side=16, L=(2.5, 2.5, 2.5), gravity=(0.0, 0.0, 0.0))
     sc.materials[0]["viscosity"] = 2e5
+    sc.materials[0]["yieldStress"] = 300.0
     sc.vel = (sc.pos - sc.pos.mean(axis=0)) @ AFFINE_A.T + np.array([0.05, -0.02, 0.01])
     lo, hi, d = sc.pos.min(axis=0), sc.pos.max(axis=0), 2.5 * sc.cellsize - 1e-9
     inner = np.all((sc.pos > lo + d) & (sc.pos < hi - d), axis=1)
@@ -47,7 +48,9 @@ def affine_block(model):
 def affine_block_stress(model, mat, dt):
     """Stress after one step from zero stress and zero strain under the strain rate sym(A):
     elastic, ConstitutiveModels.cpp:12-28 (1/3 written 0.3333); Newtonian, :41-62 (1/3 written
-    0.33333, pressure K tr(strain), viscous terms multiplied by dt)."""
+    0.33333, pressure K tr(strain), viscous terms multiplied by dt); perfect plasticity,
+    :139-222 (1/3 written 0.33; von Mises trial stress, radial return of the increment
+    dL = (q - Y) / 3G along the deviatoric flow direction)."""
     E = 0.5 * (AFFINE_A + AFFINE_A.T)
     er = np.array([E[0, 0], E[1, 1], E[2, 2], E[0, 1], E[1, 2], E[0, 2]])
     K, G, mu = mat["bulkMod"], mat["shearMod"], mat["viscosity"]
@@ -56,6 +59,20 @@ def affine_block_stress(model, mat, dt):
         vol = 0.3333 * er[:3].sum()
         out[:3] = (2.0 * G * (er[:3] - vol) + 3.0 * K * vol) * dt
         out[3:] = 2.0 * G * er[3:] * dt
+    elif model == 3:
+        vol = 0.3300 * er[:3].sum()
+        tr = np.empty(6)
+        tr[:3] = (2.0 * G * (er[:3] - vol) + 3.0 * K * vol) * dt
+        tr[3:] = 2.0 * G * er[3:] * dt
+        q = np.sqrt(0.5 * ((tr[0] - tr[1]) ** 2 + (tr[1] - tr[2]) ** 2 + (tr[2] - tr[0]) ** 2)
+                    + tr[3] ** 2 + tr[4] ** 2 + tr[5] ** 2)
+        assert q > mat["yieldStress"]  # the case exercises the return
+        dL = (q - mat["yieldStress"]) / (3.0 * G)
+        pl = dL * (0.5 / q) * np.array([2 * tr[0] - tr[1] - tr[2], 2 * tr[1] - tr[2] - tr[0],
+                                        2 * tr[2] - tr[0] - tr[1], 6 * tr[3], 6 * tr[4], 6 * tr[5]])
+        ee = er - pl / dt
+        out[:3] = (2.0 * G * (ee[:3] - vol) + 3.0 * K * vol) * dt
+        out[3:] = 2.0 * G * ee[3:] * dt
     else:
         vol = 0.33333 * er[:3].sum()
         P = K * er[:3].sum() * dt

@@ -204,11 +204,12 @@ def test_thermal_harness_matches_literal_between_sorts(oracle_built):
     assert np.linalg.norm(temp_after("ref", 0, garbled) - temp_after("ref", 1, garbled)) > 1e-3 * dT
 
 
-@pytest.mark.parametrize("model", [1, 2])
-def test_elastic_and_newtonian_first_step_known_answer(oracle_built, model):
+@pytest.mark.parametrize("model", [1, 2, 3])
+def test_constitutive_first_step_known_answer(oracle_built, model):
     """Under an affine velocity field the first step's strain rate is sym(A) at interior
-    particles, so their stress and strain follow the closed forms of the elastic and Newtonian
-    laws with the reference's literal constants (0.3333, 0.33333 for 1/3)."""
+    particles, so their stress and strain follow the closed forms of the elastic, Newtonian
+    and perfectly plastic laws with the reference's literal constants (0.3333, 0.33333, 0.33
+    for 1/3)."""
     from oracle.oracle import Oracle
     sc, inner = affine_block(model)
     o = Oracle(sc, "port")

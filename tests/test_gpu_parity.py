@@ -12,7 +12,7 @@ import pytest
 
 from graphyt_gb300 import scenes
 from tests.golden import make_golden
-from tests.helpers import rel_l2, run_gpu, run_oracle
+from tests.helpers import affine_block, affine_block_stress, rel_l2, run_gpu, run_oracle
 
 pytestmark = pytest.mark.gpu
 
@@ -293,3 +293,17 @@ def test_damage_block_100_steps(gpu_lib, oracle_built):
     for f in ("vel", "stress", "damage", "eqps"):
         err = rel_l2(gpu._get_particles(f), ref.pfield(f))
         assert err <= MANY_STEP_TOL, (f, err)
+
+
+@pytest.mark.parametrize("model", [1, 2, 3])
+def test_constitutive_first_step_known_answer(gpu_lib, model):
+    """The closed-form first-step stress of the elastic, Newtonian and perfectly plastic laws
+    under an affine velocity field (interior particles, strain rate sym(A)), FP32 within 1e-5
+    of the maximum stress; the reference's 0.3333 in place of 1/3 moves the elastic answer by
+    5e-5."""
+    sc, inner = affine_block(model)
+    gpu = run_gpu(sc, 1)
+    want_s, want_e = affine_block_stress(model, sc.materials[0], gpu.dt)
+    s, e = gpu._get_particles("stress")[inner], gpu._get_particles("strain")[inner]
+    assert np.abs(s - want_s).max() <= ONE_STEP_TOL * np.abs(want_s).max()
+    assert np.abs(e - want_e).max() <= ONE_STEP_TOL * np.abs(want_e).max()

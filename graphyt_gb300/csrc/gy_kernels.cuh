@@ -59,7 +59,7 @@ constexpr int STATS_SLOTS = 16;
 // launch with programmatic stream serialization (the kernel starts with pdl_prologue), so the
 // launch of a kernel overlaps the tail of the one before it in the stream or graph
 template <typename... P, typename... A>
-inline void launch_pdl(void (*kernel)(P...), dim3 grid, dim3 block, cudaStream_t s, A &&... args)
+inline cudaError_t launch_pdl(void (*kernel)(P...), dim3 grid, dim3 block, cudaStream_t s, A &&... args)
 {
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -71,7 +71,13 @@ inline void launch_pdl(void (*kernel)(P...), dim3 grid, dim3 block, cudaStream_t
     c.stream = s;
     c.attrs = at;
     c.numAttrs = 1;
-    cudaLaunchKernelEx(&c, kernel, std::forward<A>(args)...);
+    return cudaLaunchKernelEx(&c, kernel, std::forward<A>(args)...);
+}
+
+// keeps the first failure of a sequence of launches (err may be null)
+inline void keep_first(cudaError_t *err, cudaError_t e)
+{
+    if (err && e != cudaSuccess && *err == cudaSuccess) *err = e;
 }
 
 // process-wide count of kernel launches (for the benchmark's launch accounting)
@@ -134,11 +140,30 @@ size_t resort_scratch_ints(long long cap);
 void resort_bind(ResortScratch &rs, int *mem, long long cap);
 void resort_keys(const int *key, const int *prev_skey, int *skey_out, int *perm_out, long long n, int key_bits,
                  ResortScratch &rs, cudaStream_t s);
-const int *sort_pairs(const int *keys_in, int *perm_out, long long n, int key_bits, SortScratch &ws, cudaStream_t s);
+// err (may be null) receives the first launch failure of the sort's kernels
+const int *sort_pairs(const int *keys_in, int *perm_out, long long n, int key_bits, SortScratch &ws, cudaStream_t s,
+                      cudaError_t *err = nullptr);
 // nseg must be zero on entry; clear0..2 (may be null): counters the kernel zeroes on the way
 void launch_block_heads(const int *skey, long long n, int *seg_start, int *nseg, cudaStream_t s,
                         int *clear0 = nullptr, int *clear1 = nullptr, int *clear2 = nullptr);
-void exclusive_scan_int(const int *in, int *out, long long n, int *tmp, cudaStream_t s);
-size_t scan_tmp_ints(long long n);
+void exclusive_scan_int(const int *in, int *out, long long n, int *tmp, cudaStream_t s, cudaError_t *err = nullptr);
+
+// exclusive scan of ints: tiles of SCAN_TILE, scanned recursively over the tile sums
+constexpr int SCAN_THREADS = 512;
+constexpr int SCAN_ITEMS = 4;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+// ints of scratch exclusive_scan_int needs for n elements (constant-evaluable, so fixed
+// scratch sizes can be checked at compile time)
+constexpr size_t scan_tmp_ints(long long n)
+{
+    size_t total = 0;
+    long long m = n;
+    while (m > SCAN_TILE) {
+        m = (m + SCAN_TILE - 1) / SCAN_TILE;
+        total += (size_t)m * 2 + 32;
+    }
+    return total + 64;
+}
 
 }  // namespace gy

@@ -89,9 +89,6 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_scatter(const int *keys_
 }
 
 // ---- exclusive scan of int arrays (three-phase, recursive over block sums) ----
-constexpr int SCAN_THREADS = 512;
-constexpr int SCAN_ITEMS = 4;
-constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_tile(const int *in, int *out, long long n, int *block_sums)
 {
@@ -162,36 +159,25 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_add_self(int *out, long l
     }
 }
 
-size_t scan_tmp_ints(long long n)
-{
-    size_t total = 0;
-    long long m = n;
-    while (m > SCAN_TILE) {
-        m = (m + SCAN_TILE - 1) / SCAN_TILE;
-        total += (size_t)m * 2 + 32;
-    }
-    return total + 64;
-}
-
-void exclusive_scan_int(const int *in, int *out, long long n, int *tmp, cudaStream_t s)
+void exclusive_scan_int(const int *in, int *out, long long n, int *tmp, cudaStream_t s, cudaError_t *err)
 {
     if (n <= 0) return;
     const long long nb = (n + SCAN_TILE - 1) / SCAN_TILE;
     if (nb == 1) {
-        launch_pdl(k_scan_tile, 1, SCAN_THREADS, s, in, out, n, nullptr);
+        keep_first(err, launch_pdl(k_scan_tile, 1, SCAN_THREADS, s, in, out, n, nullptr));
         note_launch(1);
         return;
     }
     int *sums = tmp, *sums_scan = tmp + nb + 16;
-    launch_pdl(k_scan_tile, (unsigned)nb, SCAN_THREADS, s, in, out, n, sums);
+    keep_first(err, launch_pdl(k_scan_tile, (unsigned)nb, SCAN_THREADS, s, in, out, n, sums));
     note_launch(1);
     if (nb <= SCAN_TILE) {
-        launch_pdl(k_scan_add_self, (unsigned)nb, SCAN_THREADS, s, out, n, sums);
+        keep_first(err, launch_pdl(k_scan_add_self, (unsigned)nb, SCAN_THREADS, s, out, n, sums));
         note_launch(1);
         return;
     }
-    exclusive_scan_int(sums, sums_scan, nb, tmp + 2 * nb + 32, s);
-    launch_pdl(k_scan_add, (unsigned)nb, SCAN_THREADS, s, out, n, sums_scan);
+    exclusive_scan_int(sums, sums_scan, nb, tmp + 2 * nb + 32, s, err);
+    keep_first(err, launch_pdl(k_scan_add, (unsigned)nb, SCAN_THREADS, s, out, n, sums_scan));
     note_launch(1);
 }
 
@@ -204,7 +190,8 @@ size_t sort_scratch_bytes(long long n)
 
 // Sorts keys_in[0..n) (non-negative, < 2^key_bits) stably; perm_out[i] is the input index
 // of the i-th element in sorted order.  Returns the device array holding the sorted keys.
-const int *sort_pairs(const int *keys_in, int *perm_out, long long n, int key_bits, SortScratch &ws, cudaStream_t s)
+const int *sort_pairs(const int *keys_in, int *perm_out, long long n, int key_bits, SortScratch &ws, cudaStream_t s,
+                      cudaError_t *err)
 {
     if (n <= 0) return keys_in;
     const int nblocks = (int)((n + SORT_TILE - 1) / SORT_TILE);
@@ -217,11 +204,12 @@ const int *sort_pairs(const int *keys_in, int *perm_out, long long n, int key_bi
         const int shift = 8 * p;
         int *kout = ws.keys[cur];
         int *vout = (p == passes - 1) ? perm_out : ws.vals[cur];
-        launch_pdl(k_radix_hist, nblocks, SORT_THREADS, s, kin, n, shift, ws.hist, nblocks);
+        keep_first(err, launch_pdl(k_radix_hist, nblocks, SORT_THREADS, s, kin, n, shift, ws.hist, nblocks));
         note_launch(1);
-        exclusive_scan_int(ws.hist, ws.hist + (long long)RADIX * nblocks, (long long)RADIX * nblocks, ws.scan_tmp, s);
-        launch_pdl(k_radix_scatter, nblocks, SORT_THREADS, s, kin, vin, kout, vout, n, shift,
-                                                         ws.hist + (long long)RADIX * nblocks, nblocks);
+        exclusive_scan_int(ws.hist, ws.hist + (long long)RADIX * nblocks, (long long)RADIX * nblocks, ws.scan_tmp, s,
+                           err);
+        keep_first(err, launch_pdl(k_radix_scatter, nblocks, SORT_THREADS, s, kin, vin, kout, vout, n, shift,
+                                   ws.hist + (long long)RADIX * nblocks, nblocks));
         note_launch(1);
         kin = kout;
         vin = vout;
@@ -330,15 +318,19 @@ void launch_block_heads(const int *skey, long long n, int *seg_start, int *nseg,
 // ---- allocation-free sort (gy_sort_keys_static) ----
 // The scratch of the radix sort -- two key and two index ping-pong buffers, the per-pass
 // (digit, block) histograms and the scan workspace -- for up to GY_SORT_STATIC_MAX keys, in
-// one file-scope device array.  Every GPU that loads this library holds it (about 4.3 MB)
-// until the process exits.
+// one file-scope device array.  Every GPU that loads this library holds it (1,118,208 ints:
+// 4.47 MB, 4.27 MiB) until the process exits.
 constexpr long long kStaticMax = GY_SORT_STATIC_MAX;
 constexpr long long kStaticBlocks = (kStaticMax + SORT_TILE - 1) / SORT_TILE;
 constexpr long long kStaticScanInts = 4096;
 constexpr long long kStaticInts = 4 * kStaticMax + 2 * RADIX * kStaticBlocks + kStaticScanInts;
+static_assert(scan_tmp_ints(RADIX * kStaticBlocks) <= (size_t)kStaticScanInts,
+              "the scan workspace of the fixed scratch is too small for GY_SORT_STATIC_MAX keys");
 static __device__ __align__(256) int g_sort_static[kStaticInts];
 
 // Device address of g_sort_static per device ordinal, looked up once with that device current.
+// The address belongs to the device's primary context: a cudaDeviceReset by the caller
+// replaces that context and leaves the cached address stale.
 static std::mutex g_static_mu;
 static int *g_static_addr[256] = {};
 
@@ -365,7 +357,6 @@ extern "C" gy_status gy_sort_keys_static(const int *d_keys, int64_t n, int key_b
     if (key_bits < 1 || key_bits > 31) return GY_ERR_ARG;
     if (n == 0) return GY_OK;
     if (!d_keys || !d_perm_out) return GY_ERR_ARG;
-    if (scan_tmp_ints(RADIX * kStaticBlocks) > (size_t)kStaticScanInts) return GY_ERR_UNSUPPORTED;
     int *base = nullptr;
     gy_status st = static_scratch(&base);
     if (st != GY_OK) return st;
@@ -382,6 +373,9 @@ extern "C" gy_status gy_sort_keys_static(const int *d_keys, int64_t n, int key_b
     ws.cap = kStaticMax;
     ws.nblocks_cap = (int)kStaticBlocks;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    (void)sort_pairs(d_keys, d_perm_out, n, key_bits, ws, s);
-    return cudaGetLastError() == cudaSuccess ? GY_OK : GY_ERR_CUDA;
+    // the status is this call's own launches' (errors left by earlier work of the caller
+    // stay where they are); faults while the kernels run surface at the caller's next sync
+    cudaError_t err = cudaSuccess;
+    (void)sort_pairs(d_keys, d_perm_out, n, key_bits, ws, s, &err);
+    return err == cudaSuccess ? GY_OK : GY_ERR_CUDA;
 }

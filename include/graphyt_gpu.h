@@ -229,9 +229,12 @@ gy_status gy_state_load(gy_solver *h, const void *buf, int64_t bytes);
  *   d_perm_out  n device ints: index of the i-th key in ascending order, ties in input order
  *   stream      a cudaStream_t (NULL = legacy default stream); the call only enqueues work
  * Limit: n <= GY_SORT_STATIC_MAX; larger n returns GY_ERR_ARG before any GPU work.  The
- * scratch (about 4.3 MB) is held on every GPU that loads the library until the process
+ * scratch (4.47 MB, 4.27 MiB) is held on every GPU that loads the library until the process
  * exits.  The first call on a device looks the scratch's device address up once, on the
- * calling thread's current device; make that first call before any stream capture.  All
+ * calling thread's current device; make that first call before any stream capture.  The
+ * address is kept for the process: a cudaDeviceReset replaces the device's primary context
+ * and leaves it stale, so do not reset a device this entry point has run on.  The status
+ * reports this call's own launches; an error left by earlier work stays pending.  All
  * calls share the one scratch array: calls whose work overlaps on the GPU (two streams, or
  * two host threads) race and corrupt each other's results; order them on one stream. */
 #define GY_SORT_STATIC_MAX 262144

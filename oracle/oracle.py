@@ -19,6 +19,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "_build", "liboracle.so")
+# the reference source tree, where one exists (not on machines that only run the GPU tests)
+REFERENCE_DIR = os.environ.get("GRAPHYT_REFERENCE", "/root/reference")
 REF_LIB = os.path.join(HERE, "_ref", "libgyref.so")
 
 P_FIELDS = dict(pos=0, pos0=1, disp=2, vel=3, gvel=4, acc=5, strainrate=6, stress=7, strain=8,
@@ -52,7 +54,7 @@ def build(reference: Optional[str] = None, quiet: bool = True) -> None:
     """Compile the restatement, and the reference library when the reference tree exists."""
     out = subprocess.DEVNULL if quiet else None
     subprocess.run(["make", "-C", HERE, "all"], check=True, stdout=out)
-    ref = reference or "/root/reference"
+    ref = reference or REFERENCE_DIR
     if os.path.isdir(ref):
         subprocess.run(["make", "-C", HERE, "ref", f"REFERENCE={ref}"], check=True, stdout=out)
 

@@ -1,4 +1,6 @@
 """Shared helpers for the parity tests."""
+import os
+
 import numpy as np
 
 
@@ -79,3 +81,52 @@ def affine_block_stress(model, mat, dt):
         out[:3] = P + mu * (2.0 - 2.0 / 3.0) * (er[:3] - vol) * dt
         out[3:] = 2.0 * mu * er[3:] * dt
     return out, er * dt
+
+
+def perturbed(scene, eps, seed):
+    """A copy of the scene whose initial positions are scaled by (1 + eps * N(0, 1)), seeded."""
+    import copy
+    sp = copy.deepcopy(scene)
+    rng = np.random.default_rng(seed)
+    sp.pos = scene.pos * (1.0 + eps * rng.standard_normal(scene.pos.shape))
+    return sp
+
+
+def _ensemble_member(args):
+    """One FP64 run (in a worker process): the fields by particle id at each horizon."""
+    scene, horizons, fields, threads = args
+    import os
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    from oracle.oracle import Oracle
+    o = Oracle(scene, "port", mode=1)
+    out = {}
+    for k in range(1, max(horizons) + 1):
+        o.step()
+        if k in horizons:
+            out[k] = {f: o.pfield(f) for f in fields}
+    return out
+
+
+def oracle_ensemble(scene, horizons, fields, members=8, eps=1e-7):
+    """The FP64 restatement run from the scene and from `members` copies with initial positions
+    perturbed by a relative eps (seeds 100, 101, ...), the runs spread over the host's cores in
+    spawned worker processes.  Returns {horizon: (base fields, spread)} where spread[f] is the
+    largest relative L2 distance between two perturbed runs: how far apart rounding-sized input
+    changes carry the reference itself by that step."""
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+    horizons = sorted(set(int(h) for h in horizons))
+    scenes_ = [scene] + [perturbed(scene, eps, 100 + s) for s in range(members)]
+    cores = os.cpu_count() or 1
+    threads = max(1, cores // len(scenes_))
+    with ProcessPoolExecutor(max_workers=min(len(scenes_), cores), mp_context=mp.get_context("spawn")) as ex:
+        runs = list(ex.map(_ensemble_member, [(s, horizons, fields, threads) for s in scenes_]))
+    out = {}
+    for h in horizons:
+        base = runs[0][h]
+        spread = {}
+        for f in fields:
+            mem = [r[h][f] for r in runs[1:]]
+            spread[f] = max(rel_l2(a, b) for i, a in enumerate(mem) for b in mem[i + 1:])
+        out[h] = (base, spread)
+    return out

@@ -12,7 +12,7 @@ import pytest
 
 from graphyt_gb300 import scenes
 from tests.golden import make_golden
-from tests.helpers import affine_block, affine_block_stress, rel_l2, run_gpu, run_oracle
+from tests.helpers import affine_block, affine_block_stress, oracle_ensemble, rel_l2, run_gpu, run_oracle
 
 pytestmark = pytest.mark.gpu
 
@@ -113,6 +113,7 @@ ONE_STEP_CASES = {
     "cube_nodal_fixed": lambda: scenes.elastic_cube("fixed"),
     "dam_break_coarse": lambda: scenes.dam_break(scale=0.125),
     "damage_block": lambda: scenes.damage_block(),
+    "damage_block_12": lambda: scenes.damage_block(n_side=12),
     "two_blocks": lambda: scenes.two_blocks(),
     "two_blocks_rigid": lambda: scenes.two_blocks(rigid_second=True),
     "brazilian_coarse": lambda: scenes.brazilian_disc(scale=0.1),
@@ -263,36 +264,83 @@ def test_dam_break_coarse_1000_steps(gpu_lib, oracle_built):
         assert err <= MANY_STEP_TOL, (f, err)
 
 
-def test_brazilian_disc_coarse_200_steps(gpu_lib, oracle_built):
+def _gpu_at_horizons(scene, horizons, fields):
+    """GPU fields by particle id after each horizon of one run."""
+    from graphyt_gb300 import graphyt
+    s = graphyt.from_scene(scene)
+    dt = s.dt
+    out = {}
+    for k in range(max(horizons)):
+        s.iterate_GPU(k * dt, k)
+        if k + 1 in horizons:
+            s.Synchronise()
+            out[k + 1] = {f: s._get_particles(f) for f in fields}
+    s.close()
+    return out
+
+
+def _check_against_ensemble(scene, horizons, fields, label):
+    """At each horizon the GPU run lies within max(1e-3, 2 x the FP64 ensemble's spread) of
+    the unperturbed FP64 run, per field.  Where the reference is well conditioned (its spread
+    far below 1e-3) this is the fixed 1e-3 bound; where rounding-sized input changes carry the
+    reference itself apart, an FP32 run can be asked to stay only as close as two FP64 runs
+    stay to each other."""
+    ens = oracle_ensemble(scene, horizons, fields)
+    gpu = _gpu_at_horizons(scene, horizons, fields)
+    for h in horizons:
+        base, spread = ens[h]
+        for f in fields:
+            if np.linalg.norm(base[f]) == 0:
+                continue
+            err = rel_l2(gpu[h][f], base[f])
+            tol = max(MANY_STEP_TOL, 2.0 * spread[f])
+            assert err <= tol, (label, h, f, err, spread[f])
+    return ens
+
+
+def test_brazilian_disc_coarse_against_fp64_ensemble(gpu_lib, oracle_built):
     """The Brazilian disc at a tenth of the resolution (11,392 particles, disc and two rigid
-    platens) over 200 steps, through platen contact into Drucker-Prager yielding: velocity,
-    stress and equivalent plastic strain within 1e-3 of the FP64 restatement.  Over this
-    horizon a 1e-7 relative change of the FP64 initial positions moves velocity and stress by
-    3e-6 and the plastic strain by 2e-5; past the onset of yielding the reference itself
-    diverges (6e-3 at 400 steps, 0.35 in velocity at 1000), so no longer run can be held to a
-    fixed bound."""
+    platens, Drucker-Prager + Grady-Kipp) at 200, 400 and 1000 steps against eight FP64 runs
+    whose initial positions differ by 1e-7 relative.  To 200 steps the reference is well
+    conditioned (ensemble spread ~1e-5) and the GPU is held to 1e-3; past the onset of
+    yielding the reference's own runs part (spread ~7e-3 at 400 steps, 0.15 in stress and
+    0.4 in velocity at 1000), and the GPU is held to twice that spread."""
     sc = scenes.brazilian_disc(scale=0.1)
-    gpu = run_gpu(sc, 200)
-    ref = run_oracle(sc, 200)
-    assert np.linalg.norm(ref.pfield("eqps")) > 0  # the return mapping acted
-    for f in ("vel", "stress", "eqps"):
-        err = rel_l2(gpu._get_particles(f), ref.pfield(f))
-        assert err <= MANY_STEP_TOL, (f, err)
+    ens = _check_against_ensemble(sc, (200, 400, 1000), ("vel", "stress", "eqps"), "disc")
+    assert np.linalg.norm(ens[200][0]["eqps"]) > 0  # the return mapping acted
+    assert ens[200][1]["stress"] < 1e-4 and ens[1000][1]["stress"] > 1e-2  # the conditioning claim
 
 
-def test_damage_block_100_steps(gpu_lib, oracle_built):
-    """Drucker-Prager + Grady-Kipp block of 1,728 particles over 100 steps, by which time
-    nearly every particle has grown damage: velocity, stress, damage and equivalent plastic
-    strain within 1e-3 of the FP64 restatement.  Over this horizon a 1e-7 relative change of
-    the FP64 initial positions moves the stress by 1.3e-5 and the damage by 7e-7; by 200 steps
-    the reference itself diverges (0.28 in stress)."""
+def test_damage_block_against_fp64_ensemble(gpu_lib, oracle_built):
+    """A Drucker-Prager + Grady-Kipp block of 1,728 particles at 20, 100 and 200 steps against
+    eight FP64 runs whose initial positions differ by 1e-7 relative.  The reference degrades
+    the tensile principal stresses by (1 - D) only on steps in which damage grows
+    (DamageModels.cpp:104-113), so a particle whose strain sits at its activation threshold
+    takes or skips a tenfold stress drop on rounding alone: from about step 50 the FP64 runs
+    themselves fall into distinct branches 5e-2 apart in stress."""
     sc = scenes.damage_block(n_side=12)
-    gpu = run_gpu(sc, 100)
-    ref = run_oracle(sc, 100)
-    assert (ref.pfield("damage") > 0).mean() > 0.9
-    for f in ("vel", "stress", "damage", "eqps"):
-        err = rel_l2(gpu._get_particles(f), ref.pfield(f))
-        assert err <= MANY_STEP_TOL, (f, err)
+    ens = _check_against_ensemble(sc, (20, 100, 200), ("vel", "stress", "damage", "eqps"), "damage block")
+    assert (ens[100][0]["damage"] > 0).mean() > 0.9
+    assert ens[20][1]["stress"] < 1e-4
+
+
+@pytest.mark.parametrize("name,steps", [("damage_block_12", 20), ("dam_break_coarse", 100), ("two_blocks", 40),
+                                        ("brazilian_coarse", 100)])
+def test_repeat_runs_agree(gpu_lib, name, steps):
+    """Determinism: the same scene stepped twice in one process.  The particle order (integer
+    work: keys, sort, slots) is identical; the float state differs only by the order in which
+    P2G's shared-memory and global atomics add (FP32 rounding), within 1e-6."""
+    sc = ONE_STEP_CASES[name]()
+    a = run_gpu(sc, steps)
+    b = run_gpu(sc, steps)
+    assert np.array_equal(a._get_particles_int("device_slot"), b._get_particles_int("device_slot"))
+    assert np.array_equal(a._get_particles_int("cellid"), b._get_particles_int("cellid"))
+    for f in ("pos", "vel", "stress", "density", "damage", "eqps"):
+        x, y = a._get_particles(f), b._get_particles(f)
+        if np.linalg.norm(y) == 0:
+            assert np.array_equal(x, y), f
+        else:
+            assert rel_l2(x, y) <= 1e-6, (name, f, rel_l2(x, y))
 
 
 @pytest.mark.parametrize("model", [1, 2, 3])

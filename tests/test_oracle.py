@@ -11,6 +11,7 @@ import numpy as np
 import pytest
 
 from graphyt_gb300 import scenes
+from oracle import oracle
 from tests.golden import make_golden
 from tests.helpers import affine_block, affine_block_stress, rel_l2
 
@@ -32,7 +33,7 @@ def test_port_matches_reference_goldens(oracle_built, name):
 
 
 @pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(GOLDEN), "..", "oracle", "_ref", "libgyref.so"))
-                    and not os.path.isdir("/root/reference"), reason="reference tree not available")
+                    and not os.path.isdir(oracle.REFERENCE_DIR), reason="reference tree not available")
 def test_harness_mode_matches_literal_iterate_cpu(oracle_built):
     """The harness sequence (stable (cell, id) sort) equals Solver::iterate_CPU up to the
     summation order std::sort leaves inside a cell."""
@@ -176,7 +177,7 @@ def test_scene_counts():
 
 
 @pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(GOLDEN), "..", "oracle", "_ref", "libgyref.so"))
-                    and not os.path.isdir("/root/reference"), reason="reference tree not available")
+                    and not os.path.isdir(oracle.REFERENCE_DIR), reason="reference tree not available")
 def test_thermal_harness_matches_literal_between_sorts(oracle_built):
     """Heat conduction: the harness sequence and the restatement equal Solver::iterate_CPU
     while no sort has moved a temperature gradient (steps 1-9: the step-1 sort sees the

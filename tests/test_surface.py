@@ -11,10 +11,11 @@ import pytest
 
 from graphyt_gb300 import _lib as L
 from graphyt_gb300 import graphyt
+from oracle import oracle
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER_DIR = os.path.join(ROOT, "include")
-REF_BC_HEADER = "/root/reference/BoundaryConditions.hpp"
+REF_BC_HEADER = os.path.join(oracle.REFERENCE_DIR, "BoundaryConditions.hpp")
 
 _STRUCTS = {
     "gy_grid_desc": L.GridDesc, "gy_material": L.Material, "gy_params": L.Params,

@@ -31,10 +31,11 @@ def test_static_sort_matches_allocating_sort_twice(gpu_lib):
         pytest.skip("no CUDA device")
     from graphyt_gb300 import _lib
     rng = np.random.default_rng(11)
-    # two calls in a row on different inputs: the shared scratch keeps the first call's
-    # contents, which must not leak into the second result
-    cases = [(rng.integers(0, 1 << 20, 200_003).astype(np.int32), 20),
-             (np.repeat(rng.integers(0, 5000, 30_000), 8).astype(np.int32), 13)]
+    # two calls in a row on different inputs, the larger first: the fullest use of the fixed
+    # scratch (GY_SORT_STATIC_MAX keys of 31 bits, four radix passes), then a small input
+    # with few key bits (two passes), which must not see the first call's leftovers
+    cases = [(rng.integers(0, 1 << 31, _lib.GY_SORT_STATIC_MAX, dtype=np.int64).astype(np.int32), 31),
+             (np.repeat(rng.integers(0, 5000, 3_001), 8).astype(np.int32), 13)]
     for keys, bits in cases:
         got = _static_sort(gpu_lib, torch, keys, bits)
         want = _lib.sort_keys(keys)  # the allocating entry point

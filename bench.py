@@ -8,6 +8,12 @@ A step is one full explicit step (sort, P2G, fold + nodal solve + BCs, G2P + upd
 constitutive) over all particles.  State stays resident in HBM; the particle and grid state
 (1.1 GB + 0.5 GB) is far larger than L2, so no explicit L2 flush is needed between steps.
 
+The timed window lies in the developed flow: the run is first advanced (untimed) to the
+middle of the configuration's run -- step 1000 of the dam break's 2000, where the column is
+collapsing and particles change cell every step -- and the K steps after the W warm-up
+steps from there are timed.  The same K steps taken from rest are reported beside them
+(`rest_state`), with the share of particles that change cell per step in both windows.
+
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
 With N > 1 (torchrun) every rank advances an independent replica: the step has no
@@ -176,29 +182,44 @@ WORKLOADS = {
     "brazilian_disc": "brazilian_disc_dp_gk_rigid_platens",
     "impact_batch": "impact_batch_sphere_on_dp_gk_slab",
 }
+# steps of each configuration's run; the timed window starts half-way through it
+RUN_STEPS = {"dam_break": 2000, "brazilian_disc": 5000, "impact_batch": 500}
+
+# the CPU legs step the full workload, timing at most this many steps after one warm-up step
+CPU_MAX_TIMED_STEPS = 3
 
 
-def cpu_sample_scene(workload: str = "dam_break"):
-    """Bounded CPU sample of the same workload at the same resolution.  Dam break: a 0.14 m
-    wide y-slab (200 x 20 x 153 = 612,000 particles, 1.2 M nodes).  Brazilian disc: the disc
-    at a quarter of the resolution (about 160 k particles).  Impact batch: a batch of 16
-    instances drawn like the full one (about 0.8 M particles)."""
+def cpu_scene(workload: str = "dam_break", args=None):
+    """The CPU legs' workload: the GPU run's own scene (same particles, grid and materials),
+    bounded by the number of steps timed, not by a smaller sample.  Returns the scene and a
+    description."""
     from graphyt_gb300 import scenes
     if workload == "brazilian_disc":
-        return scenes.brazilian_disc(scale=0.25), "Brazilian disc at cellsize 2e-3"
+        return scenes.brazilian_disc(scale=args.scale if args else 1.0), "the full Brazilian disc"
     if workload == "impact_batch":
-        return scenes.impact_batch(n_inst=16, seed=0), "16-instance impact batch, cellsize 0.01"
-    return scenes.dam_break(scale=1.0, width=0.14), "dam break y-slab 4 x 0.14 x 2 m, cellsize 0.01"
+        return (scenes.impact_batch(n_inst=args.instances if args else 256, seed=0),
+                "the full impact batch")
+    scale = args.scale if args else 1.0
+    return (scenes.dam_break(scale=scale, height=args.column_height if args else 0.765),
+            "the full dam break" if scale == 1.0 else f"the dam break at scale {scale}")
 
 
-def run_cpu(nsteps: int, warmup: int, prefer_reference: bool = True, workload: str = "dam_break"):
+def run_cpu(nsteps: int, warmup: int, prefer_reference: bool = True, workload: str = "dam_break", args=None,
+            scene=None):
     """Time the reference's CPU step (oracle/_ref when built, else the FP64 restatement) on
-    the bounded sample.  Returns (particle-steps/s, kind, threads, sample description)."""
+    the same workload as the GPU run, from rest, over at most CPU_MAX_TIMED_STEPS steps after
+    one warm-up step (a CPU step of 12 M particles takes seconds).  Returns (particle-steps/s,
+    kind, threads, sample description)."""
     from oracle import oracle as O
     kind = "ref" if (prefer_reference and O.available("ref")) else "port"
     if not O.available(kind):
         O.build()
-    sc, what = cpu_sample_scene(workload)
+    if scene is None:
+        sc, what = cpu_scene(workload, args)
+    else:
+        sc, what = scene, f"the GPU run's {workload} scene"
+    nsteps = max(1, min(nsteps, CPU_MAX_TIMED_STEPS))
+    warmup = max(1, min(warmup, 1))
     o = O.Oracle(sc, kind, mode=1)
     o.run(warmup)
     t0 = time.perf_counter()
@@ -206,19 +227,20 @@ def run_cpu(nsteps: int, warmup: int, prefer_reference: bool = True, workload: s
     dt = time.perf_counter() - t0
     threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     o.close()
-    sample = f"{what}, {sc.n} particles, {sc.num_nodes()} nodes, {nsteps} timed steps after {warmup}"
+    sample = (f"{what}: {sc.n} particles, {sc.num_nodes()} nodes, {nsteps} timed steps after {warmup} "
+              f"from rest")
     return sc.n * nsteps / dt, ("reference" if kind == "ref" else "port"), threads, sample
 
 
 def bench_reference(args, rank):
     if rank != 0:
         return
-    value, kind, threads, sample = run_cpu(args.steps, args.warmup, workload=args.workload)
+    value, kind, threads, sample = run_cpu(args.steps, args.warmup, workload=args.workload, args=args)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOADS[args.workload], "sample": sample},
+        "config": {"workload": WORKLOADS[args.workload], "sample": sample, "same_config": True},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -244,7 +266,11 @@ def main():
     ap.add_argument("--column-height", type=float, default=0.765,
                     help="dam break water column height in m (1.5 gives the configuration's 24 M particles)")
     ap.add_argument("--full-sort", action="store_true", help="full radix sort every step (no incremental re-sort)")
+    ap.add_argument("--preroll", type=int, default=-1,
+                    help="untimed steps before the warm-up (default: half the configuration's run)")
     args = ap.parse_args()
+    if args.preroll < 0:
+        args.preroll = RUN_STEPS[args.workload] // 2
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_env()
     if args.impl == "reference":
@@ -274,38 +300,71 @@ def main():
     solver = graphyt.from_scene(sc, device=local, options=dict(sort_every=args.sort_every, full_sort=int(args.full_sort)))
     lib, h = solver.lib, solver.h
     dt = solver.dt
-    for k in range(args.warmup):
-        solver.iterate_GPU(k * dt, k)
-    solver.Synchronise()
-    dist.barrier()
+    import numpy as np
+    step = 0
 
-    # the timed region: K steps as the library runs them (graph replay), CUDA events on the
-    # handle's stream around them
+    def advance(k):
+        """k untimed steps."""
+        nonlocal step
+        for _ in range(k):
+            solver.iterate_GPU(step * dt, step)
+            step += 1
+        solver.Synchronise()
+
+    def timed(k):
+        """Device time of k steps as the library runs them (graph replay), CUDA events on the
+        handle's stream around them."""
+        nonlocal step
+        ms = C.c_float()
+        L.check(lib.gy_time_steps(h, step * dt, step, k, C.byref(ms)), h, "timed steps")
+        step += k
+        return ms.value
+
+    def phases(k):
+        """Per-phase ms per step over k kernel-by-kernel steps (events between the phases)."""
+        nonlocal step
+        L.check(lib.gy_set_phase_timing(h, 1), h)
+        L.check(lib.gy_steps(h, step * dt, step, k, 0), h, "phase-timed steps")
+        step += k
+        solver.Synchronise()
+        ph = (C.c_float * 5)()
+        nph = C.c_int64()
+        L.check(lib.gy_get_phase_times(h, ph, C.byref(nph)), h)
+        L.check(lib.gy_set_phase_timing(h, 0), h)
+        return [ph[q] / max(nph.value, 1) for q in range(4)]
+
+    def mover_fraction():
+        """Share of the particles whose cell changes in one step."""
+        c0 = solver._get_particles_int("cellid")
+        advance(1)
+        return float(np.mean(c0 != solver._get_particles_int("cellid")))
+
+    advance(args.warmup)
+    names = ["sort", "p2g", "grid", "g2p_update"]
+    # the same window from rest: few particles change cell, so the re-sort is cheapest here
+    rest_ms = timed(args.steps)
+    rest_phase = phases(args.steps)
+    rest_movers = mover_fraction()
+    # the developed flow: advance to the middle of the configuration's run, warm up, time
+    advance(max(0, args.preroll - step))
+    advance(args.warmup)
+    dist.barrier()
     sampler = ClockSampler(local)
     if rank == 0:
         sampler.start()
     launches0 = lib.gy_kernel_launches()
-    ms = C.c_float()
-    step0 = args.warmup
-    L.check(lib.gy_time_steps(h, step0 * dt, step0, args.steps, C.byref(ms)), h, "timed steps")
+    step_timed0 = step
+    ms_timed = timed(args.steps)
     launches = lib.gy_kernel_launches() - launches0
     clocks = sampler.stop() if rank == 0 else None
     solver.Synchronise()
-    ms_max = dist.max(ms.value)
+    ms_max = dist.max(ms_timed)
     ms_per_step = ms_max / args.steps
     sharded = args.workload == "impact_batch" and world > 1
     n_job = dist.sum(float(n)) if sharded else float(n) * world  # particles the job steps
     value = n_job * args.steps / (ms_max / 1e3)
-
-    # phase breakdown, separately: events between the phases need kernel-by-kernel launches
-    L.check(lib.gy_set_phase_timing(h, 1), h)
-    step0 += args.steps
-    L.check(lib.gy_steps(h, step0 * dt, step0, args.steps, 0), h, "phase-timed steps")
-    solver.Synchronise()
-    phase = (C.c_float * 5)()
-    nph = C.c_int64()
-    L.check(lib.gy_get_phase_times(h, phase, C.byref(nph)), h)
-    L.check(lib.gy_set_phase_timing(h, 0), h)
+    per_step = phases(args.steps)
+    movers = mover_fraction()
 
     st = solver.stats()
     n_active = int(st["active_nodes"])
@@ -316,16 +375,14 @@ def main():
     prm = solver.params
     dist.barrier()
     t0 = time.perf_counter()
-    s0 = step0 + args.steps
     for k in range(args.steps):
-        solver.iterate_GPU((s0 + k) * dt, s0 + k, prm)
+        solver.iterate_GPU(step * dt, step, prm)
+        step += 1
         solver.stats()
     e2e_s = dist.max(time.perf_counter() - t0)
     e2e_value = n_job * args.steps / e2e_s
 
     # roofline of the dominant kernel
-    names = ["sort", "p2g", "grid", "g2p_update"]
-    per_step = [phase[k] / max(nph.value, 1) for k in range(4)]
     multi = args.workload != "dam_break"
     algo = {
         "sort": 0.0,
@@ -347,7 +404,7 @@ def main():
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        v, kind, threads, sample = run_cpu(2, 1, workload=args.workload)
+        v, kind, threads, sample = run_cpu(2, 1, workload=args.workload, args=args, scene=sc)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample}
 
     if rank == 0:
@@ -369,7 +426,12 @@ def main():
                                                  "2 bodies"}[args.workload],
                        "sort_every": args.sort_every, "sort": "full" if args.full_sort else "incremental", "l2": "state larger than L2 (no flush needed)",
                        "parallelism": ("instances sharded" if sharded else "replicas") if world > 1 else "single"},
+            "window": {"first_timed_step": step_timed0, "of_run_steps": RUN_STEPS[args.workload],
+                       "movers_per_step": movers},
             "phase_ms_per_step": dict(zip(names, per_step)),
+            "rest_state": {"first_timed_step": args.warmup, "ms_per_step": rest_ms / args.steps,
+                           "value": n_job * args.steps / (dist.max(rest_ms) / 1e3),
+                           "phase_ms_per_step": dict(zip(names, rest_phase)), "movers_per_step": rest_movers},
             "roofline": roofline,
             "step_roofline": {"achieved": whole, "peak": peak, "unit": "GB/s", "frac": whole / peak,
                               "bytes_per_step": step_bytes},

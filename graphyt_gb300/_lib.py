@@ -71,6 +71,7 @@ SIGNATURES = {
     "gy_set_particle_vel": (C.c_int, [_vp, C.c_int64, _i64p, _dp]),
     "gy_set_particle_stress": (C.c_int, [_vp, C.c_int64, _i64p, _dp]),
     "gy_set_particle_damage": (C.c_int, [_vp, C.c_int64, _i64p, _dp]),
+    "gy_set_particle_flaw": (C.c_int, [_vp, C.c_int64, _i64p, _dp]),
     "gy_set_particle_temp": (C.c_int, [_vp, C.c_int64, _i64p, _dp]),
     "gy_hold_particles": (C.c_int, [_vp, C.c_int64, _i64p]),
     "gy_set_particle_bc": (C.c_int, [_vp, C.c_int64, _i64p, _ip, _dp]),

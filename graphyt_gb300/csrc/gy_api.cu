@@ -50,6 +50,7 @@ struct gy_solver {
 
     // host staging, insertion order (MaterialPoints)
     std::vector<double> pos, vel, stress, dmg, temp;
+    std::vector<double> flaw;        // Grady-Kipp activation strain scale (1: the reference's e_min)
     std::vector<int> mat, obj, pbc_type;
     std::vector<double> pbc_val;
     std::vector<unsigned char> hold;
@@ -96,6 +97,7 @@ struct gy_solver {
     long long ring_pos = 0;
     std::vector<StepGraph> graphs;          // captured steps, one per StepVariant
     float4 *d_pbc_val = nullptr;
+    float *d_flaw = nullptr;                // flaw scale by insertion index, or null (every scale 1)
     int *d_refkey0 = nullptr;
     DevMaterial *d_mats = nullptr;
     int *d_status = nullptr;
@@ -176,7 +178,7 @@ void free_device(gy_solver *h)
     }
     void *ptrs[] = {h->slab[0], h->slab[1], h->d_perm, h->d_seg, h->d_nseg, h->sort_mem, h->resort_mem, h->d_pbc_val,
                     h->d_refkey0, h->d_mats, h->d_status, h->d_stats, h->node_mem, h->d_cell_min,
-                    h->d_nidx[0], h->d_nidx[1], h->d_nidx[2], h->d_sc, h->d_therm, h->d_tnode, h->d_tset};
+                    h->d_nidx[0], h->d_nidx[1], h->d_nidx[2], h->d_sc, h->d_therm, h->d_tnode, h->d_tset, h->d_flaw};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     h->d_sc = nullptr;
@@ -191,6 +193,7 @@ void free_device(gy_solver *h)
     h->resort_mem = nullptr;
     h->skey_buf[0] = h->skey_buf[1] = nullptr;
     h->d_pbc_val = nullptr;
+    h->d_flaw = nullptr;
     h->d_refkey0 = nullptr;
     h->d_mats = nullptr;
     h->d_status = nullptr;
@@ -326,6 +329,7 @@ gy_status gy_add_particles(gy_solver *h, int64_t n, const double *pos3, const in
         }
         for (int k = 0; k < 6; k++) h->stress.push_back(0.0);
         h->dmg.push_back(0.0);
+        h->flaw.push_back(1.0);
         h->temp.push_back(0.0);
         h->mat.push_back(mat ? mat[i] : 0);
         h->obj.push_back(obj ? obj[i] : 0);
@@ -368,6 +372,18 @@ gy_status gy_set_particle_damage(gy_solver *h, int64_t count, const int64_t *idx
     for (int64_t q = 0; q < count; q++) {
         if (!valid_index(h, idx[q])) return fail(h, GY_ERR_ARG, "particle index out of range");
         h->dmg[idx[q]] = d[q];
+    }
+    return GY_OK;
+}
+
+gy_status gy_set_particle_flaw(gy_solver *h, int64_t count, const int64_t *idx, const double *w)
+{
+    PRE_INIT(h);
+    if (count < 0 || (count > 0 && (!idx || !w))) return GY_ERR_ARG;
+    for (int64_t q = 0; q < count; q++) {
+        if (!valid_index(h, idx[q])) return fail(h, GY_ERR_ARG, "particle index out of range");
+        if (!(w[q] > 0.0) || !std::isfinite(w[q])) return fail(h, GY_ERR_ARG, "flaw scale must be positive and finite");
+        h->flaw[idx[q]] = w[q];
     }
     return GY_OK;
 }
@@ -712,6 +728,13 @@ gy_status gy_initialize(gy_solver *h, const gy_material *mats, int nmat, const g
     gy_status st;
     if ((st = dalloc(h, &h->d_pbc_val, h->cap))) return st;
     CK(h, cudaMemcpyAsync(h->d_pbc_val, pbcv.data(), h->cap * sizeof(float4), cudaMemcpyHostToDevice, h->stream));
+    if (std::any_of(h->flaw.begin(), h->flaw.end(), [](double w) { return w != 1.0; })) {
+        std::vector<float> fw((size_t)h->cap, 1.0f);
+        for (long long i = 0; i < h->n; i++) fw[i] = (float)h->flaw[i];
+        if ((st = dalloc(h, &h->d_flaw, h->cap))) return st;
+        CK(h, cudaMemcpyAsync(h->d_flaw, fw.data(), h->cap * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));  // fw dies on return
+    }
     if (h->multi) {
         if ((st = dalloc(h, &h->d_refkey0, h->cap))) return st;
         CK(h, cudaMemcpyAsync(h->d_refkey0, refkey0.data(), h->cap * sizeof(int), cudaMemcpyHostToDevice, h->stream));
@@ -861,6 +884,7 @@ static StepArgs make_args(gy_solver *h)
     a.multi_body = h->multi ? 1 : 0;
     a.mats = h->d_mats;
     a.pbc_val = h->d_pbc_val;
+    a.flaw = h->d_flaw;
     a.status = h->d_status;
     a.stats = h->d_stats;
     return a;

@@ -1268,7 +1268,7 @@ __device__ __forceinline__ void update_after_g2p(PState &st, const int c0[3], fl
     if (!(st.info & INFO_RIGID)) {
         const DevMaterial &M = a.mats[info_mat(st.info)];
         if (HAS_DP) {
-            constitutive_update(c, M, dt, g.is3d);
+            constitutive_update(c, M, dt, g.is3d, a.flaw, st.pid);
         } else {
             if (M.model == 1) cm_elastic(c, M, dt);
             else if (M.model == 2) cm_newtonian(c, M.K, M.viscosity, dt, g.is3d, false);

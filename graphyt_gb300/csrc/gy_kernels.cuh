@@ -48,6 +48,7 @@ struct StepArgs {
     int multi_body;          // host-side launch choice, fixed per handle
     const DevMaterial *mats;
     const float4 *pbc_val;   // particle BC values by pid
+    const float *flaw;       // Grady-Kipp activation strain scale by pid, or null (every scale 1)
     int *status;
     double *stats;           // STATS_SLOTS x 8 conservation partials written by G2P, or null
 };

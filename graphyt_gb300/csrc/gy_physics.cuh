@@ -238,10 +238,20 @@ __device__ __forceinline__ void sym_eigen3(float A[3][3], float V[3][3])
     }
 }
 
+// Activation strain of the particle's weakest flaw, e_min = w (V k)^(-1/m) (DamageModels.cpp:
+// 102-103 with w = 1), evaluated as exp(-(ln V + ln k)/m) so V*k never overflows.  w is the
+// particle's flaw scale (a per-particle Weibull draw) where the handle has a flaw table.
+__device__ __forceinline__ float gk_emin(const Constit &c, const DevMaterial &M, const float *flaw, int pid)
+{
+    const float vol = c.mass / c.rho;
+    const float emin = expf(-(logf(vol) + M.gk_logk) / M.gk_m);
+    return flaw ? emin * __ldg(flaw + pid) : emin;
+}
+
 // Grady-Kipp damage, 3D branch of DamageModels.cpp:71-150.  The stress is rebuilt from the
 // principal values only when damage grew: without growth V diag(s) V^T is the stress
 // itself, which the reference recomputes with rounding only.
-__device__ __forceinline__ void dm_grady_kipp3(Constit &c, const DevMaterial &M, float dt)
+__device__ __forceinline__ void dm_grady_kipp3(Constit &c, const DevMaterial &M, float dt, const float *flaw, int pid)
 {
     const float chk = fabsf(c.s[0] + c.s[1] + c.s[2] + c.s[3] + c.s[4] + c.s[5]);
     if (!(chk > 1e-3f)) return;
@@ -253,10 +263,7 @@ __device__ __forceinline__ void dm_grady_kipp3(Constit &c, const DevMaterial &M,
     c.smax = smx;
     if (!(smx > 1e-3f)) return;
     const float eff = smx / (M.K + 4.0f * M.G / 3.0f);
-    const float vol = c.mass / c.rho;
-    // e_min = (V k)^(-1/m), evaluated as exp(-(ln V + ln k)/m) so V*k never overflows
-    const float emin = expf(-(logf(vol) + M.gk_logk) / M.gk_m);
-    if (!(eff > emin)) return;
+    if (!(eff > gk_emin(c, M, flaw, pid))) return;
     const float rate = M.gk_rate_coef * powf(eff, M.gk_m / 3.0f);
     const float root = cbrtf(c.dmg) + dt * rate;
     float D = root * root * root;
@@ -275,7 +282,7 @@ __device__ __forceinline__ void dm_grady_kipp3(Constit &c, const DevMaterial &M,
 }
 
 // Grady-Kipp, 2D branch of DamageModels.cpp:11-70 (principal axes in closed form).
-__device__ __forceinline__ void dm_grady_kipp2(Constit &c, const DevMaterial &M, float dt)
+__device__ __forceinline__ void dm_grady_kipp2(Constit &c, const DevMaterial &M, float dt, const float *flaw, int pid)
 {
     float sxx = c.s[0], syy = c.s[1], sxy = c.s[3], szz = c.s[2];
     float th;
@@ -289,9 +296,7 @@ __device__ __forceinline__ void dm_grady_kipp2(Constit &c, const DevMaterial &M,
     bool rebuilt = false;
     if (smx > 1e-3f) {
         const float eff = smx / (M.K + 4.0f * M.G / 3.0f);
-        const float vol = c.mass / c.rho;
-        const float emin = expf(-(logf(vol) + M.gk_logk) / M.gk_m);
-        if (eff > emin) {
+        if (eff > gk_emin(c, M, flaw, pid)) {
             const float rate = M.gk_rate_coef * powf(eff, M.gk_m / 3.0f);
             const float root = cbrtf(c.dmg) + dt * rate;
             float D = root * root * root;
@@ -316,8 +321,10 @@ __device__ __forceinline__ void dm_grady_kipp2(Constit &c, const DevMaterial &M,
     c.s[0] = sxx; c.s[1] = syy; c.s[2] = szz; c.s[3] = sxy;
 }
 
-// constitutiveModel dispatch (TimeIntegration.cpp:120-143) and applyDamage (:165-173)
-__device__ __forceinline__ void constitutive_update(Constit &c, const DevMaterial &M, float dt, int is3d)
+// constitutiveModel dispatch (TimeIntegration.cpp:120-143) and applyDamage (:165-173); flaw
+// (may be null) is the per-particle flaw scale table, pid the particle's insertion index
+__device__ __forceinline__ void constitutive_update(Constit &c, const DevMaterial &M, float dt, int is3d,
+                                                    const float *flaw, int pid)
 {
     switch (M.model) {
     case 1: cm_elastic(c, M, dt); break;
@@ -328,8 +335,8 @@ __device__ __forceinline__ void constitutive_update(Constit &c, const DevMateria
     default: break;
     }
     if (M.damage && M.damage_model == 1) {
-        if (is3d) dm_grady_kipp3(c, M, dt);
-        else dm_grady_kipp2(c, M, dt);
+        if (is3d) dm_grady_kipp3(c, M, dt, flaw, pid);
+        else dm_grady_kipp2(c, M, dt, flaw, pid);
     }
 }
 

@@ -135,6 +135,7 @@ class MaterialPoints:
         self._vel = {}
         self._stress = {}
         self._damage = {}
+        self._flaw = None
         self._temp = {}
         self._hold = set()
         self._bc = {}
@@ -197,6 +198,13 @@ class MaterialPoints:
 
     def setDamage(self, p, D):
         self._damage[int(p)] = float(D)
+
+    def setFlawScales(self, w):
+        """Per-particle scale of the Grady-Kipp activation strain, e_min = w (V k)^(-1/m), one
+        value per particle in insertion order (1 everywhere is the reference's deterministic
+        e_min, DamageModels.cpp:102-103; scenes.weibull_flaws draws Weibull scales).  No
+        reference counterpart."""
+        self._flaw = np.ascontiguousarray(w, np.float64).reshape(-1)
 
     def setTemp(self, p, T):
         """MaterialPoints::setTemp (MaterialPoints.cpp:319-322); also between steps."""
@@ -504,6 +512,12 @@ class Solver:
             idx = np.fromiter(mp._damage.keys(), np.int64)
             d = np.ascontiguousarray(np.array(list(mp._damage.values()), np.float64))
             L.check(lib.gy_set_particle_damage(h, len(idx), L.i64ptr(idx), L.dptr(d)), h, "setDamage")
+        if mp._flaw is not None:
+            w = mp._flaw
+            if len(w) != mp._n:
+                raise ValueError("setFlawScales: one scale per particle")
+            idx = np.arange(len(w), dtype=np.int64)
+            L.check(lib.gy_set_particle_flaw(h, len(idx), L.i64ptr(idx), L.dptr(w)), h, "setFlawScales")
         if mp._temp:
             idx = np.fromiter(mp._temp.keys(), np.int64)
             t = np.ascontiguousarray(np.fromiter(mp._temp.values(), np.float64))
@@ -691,6 +705,9 @@ def from_scene(scene, device: int = -1, options: Optional[dict] = None) -> Solve
     temp = getattr(scene, "temp", None)
     if temp is not None:
         mp._temp = {int(p): float(temp[p]) for p in np.nonzero(temp)[0]}
+    flaw = getattr(scene, "flaw", None)
+    if flaw is not None and np.any(flaw != 1.0):
+        mp.setFlawScales(flaw)
     nzb = np.nonzero(scene.pbc_type)[0]
     mp._bc = {int(p): (int(scene.pbc_type[p]), list(scene.pbc_val[p])) for p in nzb}
     nodes._bc_type = scene.node_bc_type.astype(np.int32).copy()

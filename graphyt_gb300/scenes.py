@@ -66,6 +66,7 @@ class Scene:
     node_bc_type: Optional[np.ndarray] = None  # (Nn,)
     node_bc_val: Optional[np.ndarray] = None   # (Nn, 4)
     temp: Optional[np.ndarray] = None          # (N,) temperature (MaterialPoints::setTemp)
+    flaw: Optional[np.ndarray] = None          # (N,) Grady-Kipp activation strain scale (1: reference)
     inst: Optional[np.ndarray] = None          # (N,) instance index, for a batch of instances
     instances: Optional[List["Instance"]] = None
 
@@ -138,7 +139,7 @@ def _finish(scene: Scene, seed: int) -> Scene:
         scene.node_bc_val = np.zeros((nn, 4))
     if seed is not None:
         perm = np.random.default_rng(seed).permutation(n)
-        for f in ("pos", "mat", "obj", "vel", "stress", "pbc_type", "pbc_val", "hold", "temp", "inst"):
+        for f in ("pos", "mat", "obj", "vel", "stress", "pbc_type", "pbc_val", "hold", "temp", "inst", "flaw"):
             if getattr(scene, f) is not None:
                 setattr(scene, f, np.ascontiguousarray(getattr(scene, f)[perm]))
     scene.pos = np.ascontiguousarray(scene.pos, np.float64)
@@ -146,6 +147,27 @@ def _finish(scene: Scene, seed: int) -> Scene:
     scene.obj = np.ascontiguousarray(scene.obj, np.int32)
     scene.pbc_type = np.ascontiguousarray(scene.pbc_type, np.int32)
     scene.node_bc_type = np.ascontiguousarray(scene.node_bc_type, np.int32)
+    return scene
+
+
+def weibull_flaws(scene: Scene, seed: int = 0) -> Scene:
+    """Per-particle flaw activation strains drawn from the Weibull law, seeded.
+
+    Grady-Kipp flaws are a Poisson population whose number per unit volume with activation
+    strain below e is k e^m, so the weakest flaw of a particle of volume V activates at the
+    strain e with P(e_w > e) = exp(-V k e^m): e_w = (V k)^(-1/m) (-ln U)^(1/m) for uniform U.
+    The reference uses the deterministic (V k)^(-1/m) (DamageModels.cpp:102-103), the case
+    -ln U = 1.  The draw is stored as the scale w = (-ln U)^(1/m), applied to the e_min the
+    step computes from the particle's current volume.  Particles of materials without
+    Grady-Kipp damage keep w = 1."""
+    rng = np.random.default_rng(seed)
+    u = 1.0 - rng.random(scene.n)  # in (0, 1]
+    m = np.array([float(mt["damageM"]) if mt["isDamage"] and mt["damageModel"] == 1 else 0.0
+                  for mt in scene.materials])[scene.mat]
+    w = np.ones(scene.n)
+    on = m > 0
+    w[on] = (-np.log(u[on])) ** (1.0 / m[on])
+    scene.flaw = w
     return scene
 
 
@@ -235,15 +257,17 @@ def dam_break(scale: float = 1.0, height: float = 0.765, seed: int = 0, walls: b
     return _finish(sc, seed)
 
 
-def brazilian_disc(scale: float = 1.0, seed: int = 0, platen_speed: float = 0.5, shift: bool = True) -> Scene:
+def brazilian_disc(scale: float = 1.0, seed: int = 0, platen_speed: float = 0.5, shift: bool = True,
+                   weibull_seed: Optional[int] = None) -> Scene:
     """3D Brazilian disc: a Drucker-Prager + Grady-Kipp cylinder (radius 0.05 m, thickness
     0.02 m, axis along z) squeezed along y by two rigid platens at +/-platen_speed.
     cellsize 5e-4/scale, psep half of it.  DP: K 3e10, G 2e10, rho 2600, cohesion 1e7,
     friction 30 deg, dilatancy 0, critical strain 0.01.  GK: m 9, k 5e32, Cg = 0.4 x the
     P-wave speed (1867.40 m/s).  objectIDs: disc 1, top platen 2, bottom platen 3 (the
-    layout of Examples/brazillian3D.py:31-108).  At scale 1 this is about 10 M particles;
-    the reference's Grady-Kipp has no per-particle Weibull flaws (DamageModels.cpp:102-103),
-    so the flaw threshold is the deterministic e_min = (V k)^(-1/m).
+    layout of Examples/brazillian3D.py:31-108).  At scale 1 this is about 10 M particles.
+    The reference's Grady-Kipp flaw threshold is the deterministic e_min = (V k)^(-1/m)
+    (DamageModels.cpp:102-103); weibull_seed draws per-particle Weibull activation strains
+    instead (weibull_flaws).
 
     shift moves the whole lattice by (0.0931, 0.0517, 0.0713) psep.  Unshifted, particles sit
     exactly on the reference's quarter-cell binning boundaries (TimeIntegration.cpp:111-113),
@@ -282,7 +306,8 @@ def brazilian_disc(scale: float = 1.0, seed: int = 0, platen_speed: float = 0.5,
     vel[obj == 2, 1] = -platen_speed
     vel[obj == 3, 1] = platen_speed
     sc.vel = vel
-    return _finish(sc, seed)
+    sc = _finish(sc, seed)
+    return sc if weibull_seed is None else weibull_flaws(sc, weibull_seed)
 
 
 def tiny_block(seed: int = 0, model: int = 1, n_side: int = 4, cellsize: float = 0.125,
@@ -306,7 +331,7 @@ def tiny_block(seed: int = 0, model: int = 1, n_side: int = 4, cellsize: float =
     return _finish(sc, seed)
 
 
-def damage_block(seed: int = 0, n_side: int = 8) -> Scene:
+def damage_block(seed: int = 0, n_side: int = 8, weibull_seed: Optional[int] = None) -> Scene:
     """A Drucker-Prager + Grady-Kipp block on a 12^3-cell grid, stretched along x and
     squeezed along z by its initial velocity field so that both the damage growth (tension)
     and the plastic return (compression) act within a few tens of steps."""
@@ -327,7 +352,8 @@ def damage_block(seed: int = 0, n_side: int = 8) -> Scene:
     v[:, 2] = -2.0 * (pos[:, 2] - c[2])
     v += 0.02 * np.random.default_rng(seed + 5).standard_normal((n, 3))
     sc.vel = v
-    return _finish(sc, seed)
+    sc = _finish(sc, seed)
+    return sc if weibull_seed is None else weibull_flaws(sc, weibull_seed)
 
 
 def two_blocks(seed: int = 0, speed: float = 1.5, rigid_second: bool = False) -> Scene:

@@ -147,6 +147,14 @@ gy_status gy_set_particle_damage(gy_solver *h, int64_t count, const int64_t *idx
 gy_status gy_hold_particles(gy_solver *h, int64_t count, const int64_t *idx);
 gy_status gy_set_particle_bc(gy_solver *h, int64_t count, const int64_t *idx, const int *type, const double *val4);
 
+/* Per-particle scale w > 0 of the Grady-Kipp activation strain, e_min = w (V k)^(-1/m), for
+ * many particles (before gy_initialize).  The reference computes the deterministic
+ * e_min = (V k)^(-1/m) (DamageModels.cpp:102-103), which is w = 1, every particle's default;
+ * a per-particle Weibull draw w = (-ln U)^(1/m) gives each particle the activation strain of
+ * the weakest flaw of a Poisson flaw population k e^m in its volume.  No reference
+ * counterpart (the reference has no per-particle flaw field). */
+gy_status gy_set_particle_flaw(gy_solver *h, int64_t count, const int64_t *idx, const double *w);
+
 /* MaterialPoints::setTemp (MaterialPoints.cpp:319-322) for many particles.  Unlike the other
  * setters it also works between steps (the reference's scripts reset temperatures every step,
  * Examples/thermalTest.py:110-117).  The heat conduction terms of the step run once any

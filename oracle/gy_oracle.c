@@ -68,6 +68,7 @@ struct gyo {
     double psep, t;
     double *x, *x0, *u, *v, *gv, *a, *er, *dr, *s, *e, *ep, *eqp, *D, *smax, *m, *rho, *V, *nrm;
     double *T, *gT, *Tr; /* temperature, its gradient, its rate (MaterialPoints.hpp:103-105) */
+    double *flaw;        /* scale of the Grady-Kipp activation strain (1: the reference's e_min) */
     int *cell, *mat, *obj, *bct, *pid;
     double *bcv;
     unsigned char *hold;
@@ -158,7 +159,7 @@ static void free_particles(gyo *o)
 {
     double **d[] = {&o->x, &o->x0, &o->u, &o->v, &o->gv, &o->a, &o->er, &o->dr, &o->s, &o->e,
                     &o->ep, &o->eqp, &o->D, &o->smax, &o->m, &o->rho, &o->V, &o->nrm, &o->bcv,
-                    &o->T, &o->gT, &o->Tr};
+                    &o->T, &o->gT, &o->Tr, &o->flaw};
     for (size_t i = 0; i < sizeof(d) / sizeof(d[0]); i++) { free(*d[i]); *d[i] = NULL; }
     int **ii[] = {&o->cell, &o->mat, &o->obj, &o->bct, &o->pid};
     for (size_t i = 0; i < sizeof(ii) / sizeof(ii[0]); i++) { free(*ii[i]); *ii[i] = NULL; }
@@ -190,7 +191,7 @@ int gyo_add_particles(gyo *o, int n, const double *pos, const int *mat, const in
         GROW(o->s, double, 6); GROW(o->e, double, 6); GROW(o->ep, double, 6); GROW(o->eqp, double, 1);
         GROW(o->D, double, 1); GROW(o->smax, double, 1); GROW(o->m, double, 1); GROW(o->rho, double, 1);
         GROW(o->V, double, 1); GROW(o->nrm, double, 3); GROW(o->bcv, double, 4);
-        GROW(o->T, double, 1); GROW(o->gT, double, 3); GROW(o->Tr, double, 1);
+        GROW(o->T, double, 1); GROW(o->gT, double, 3); GROW(o->Tr, double, 1); GROW(o->flaw, double, 1);
         GROW(o->cell, int, 1); GROW(o->mat, int, 1); GROW(o->obj, int, 1); GROW(o->bct, int, 1);
         GROW(o->pid, int, 1);
         o->hold = (unsigned char *)realloc(o->hold, (size_t)cap);
@@ -206,6 +207,7 @@ int gyo_add_particles(gyo *o, int n, const double *pos, const int *mat, const in
             o->gT[3 * p + k] = 0.0;
         }
         o->T[p] = o->Tr[p] = 0.0;
+        o->flaw[p] = 1.0;
         for (int k = 0; k < 6; k++) o->er[6 * p + k] = o->s[6 * p + k] = o->e[6 * p + k] = o->ep[6 * p + k] = 0.0;
         for (int k = 0; k < 4; k++) o->bcv[4 * p + k] = 0.0;
         o->dr[p] = o->eqp[p] = o->D[p] = o->smax[p] = o->m[p] = o->rho[p] = o->V[p] = 0.0;
@@ -245,6 +247,18 @@ void gyo_set_particle_temps(gyo *o, int count, const int *ids, const double *T)
     for (int q = 0; q < o->N; q++) at[o->pid[q]] = q;
     for (int q = 0; q < count; q++)
         if (ids[q] >= 0 && ids[q] < o->N) o->T[at[ids[q]]] = T[q];
+    free(at);
+}
+/* Per-particle scale of the Grady-Kipp activation strain, by particle id: e_min = w (V k)^(-1/m).
+ * The reference's deterministic e_min (DamageModels.cpp:102-103) is w = 1, the default; a
+ * Weibull draw w = (-ln U)^(1/m) gives the weakest flaw of a Poisson flaw population of
+ * density k e^m in the particle's volume. */
+void gyo_set_particle_flaws(gyo *o, int count, const int *ids, const double *w)
+{
+    int *at = ialloc((size_t)o->N);
+    for (int q = 0; q < o->N; q++) at[o->pid[q]] = q;
+    for (int q = 0; q < count; q++)
+        if (ids[q] >= 0 && ids[q] < o->N) o->flaw[at[ids[q]]] = w[q];
     free(at);
 }
 void gyo_set_node_bc(gyo *o, int n, int type, const double *val, int nval)
@@ -332,6 +346,7 @@ static void sort_particles(gyo *o)
     PERM(o->rho, double, 1); PERM(o->obj, int, 1); PERM(o->V, double, 1); PERM(o->nrm, double, 3);
     PERM(o->bcv, double, 4); PERM(o->mat, int, 1); PERM(o->cell, int, 1); PERM(o->hold, unsigned char, 1);
     PERM(o->bct, int, 1); PERM(o->pid, int, 1); PERM(o->T, double, 1); PERM(o->gT, double, 3);
+    PERM(o->flaw, double, 1);
     o->cap = N;
     free(order);
     /* cell start table: exclusive scan with cells[0] = 0 (Extrapolation.cpp:494-501) */
@@ -978,7 +993,7 @@ static void grady_kipp(gyo *o, int mp, const gyo_material *M, double dt)
         if (smx > 1e-3) {
             double eff = smx / (K + (4.0 * G / 3.0));
             double vol = o->m[mp] / o->rho[mp];
-            double emin = pow(vol * k, -1.0 / mm);
+            double emin = o->flaw[mp] * pow(vol * k, -1.0 / mm);
             if (eff > emin) {
                 double rate = ((mm + 3.0) / 3.0) * pow(alpha, 1.0 / 3.0) * pow(eff, mm / 3.0);
                 o->D[mp] = pow(pow(o->D[mp], 1.0 / 3.0) + (dt * rate), 3.0);
@@ -1016,7 +1031,7 @@ static void grady_kipp(gyo *o, int mp, const gyo_material *M, double dt)
     if (smx > 1e-3) {
         double eff = smx / (K + 4.0 * G / 3.0);
         double vol = o->m[mp] / o->rho[mp];
-        double emin = pow(vol * k, -1.0 / mm);
+        double emin = o->flaw[mp] * pow(vol * k, -1.0 / mm);
         if (eff > emin) {
             double rate = ((mm + 3.0) / 3.0) * pow(alpha, 1.0 / 3.0) * pow(eff, mm / 3.0);
             o->D[mp] = pow(pow(o->D[mp], 1.0 / 3.0) + (dt * rate), 3.0);

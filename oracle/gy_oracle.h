@@ -54,6 +54,9 @@ void gyo_set_node_bc(gyo *o, int n, int type, const double *val, int nval);
 /* MaterialPoints::setTemp (MaterialPoints.cpp:319-322) for `count` particles given by their
  * original index; valid before and between steps. */
 void gyo_set_particle_temps(gyo *o, int count, const int *ids, const double *T);
+/* Per-particle scale w of the Grady-Kipp activation strain, e_min = w (V k)^(-1/m), by particle
+ * id (default 1, the reference's DamageModels.cpp:102-103).  No reference counterpart. */
+void gyo_set_particle_flaws(gyo *o, int count, const int *ids, const double *w);
 
 /* Solver(nds, mpts, params, materials): dt from CFL and initialize() (Solver.cpp:7-69). */
 int gyo_init_solver(gyo *o, const gyo_params *prm, int nmat, const gyo_material *mats);

@@ -106,6 +106,8 @@ def _lib(kind: str):
     step.restype = C.c_int
     step.argtypes = [vp, C.c_double, C.c_int] + ([] if kind == "port" else [C.c_int])
     if kind == "port":
+        lib.gyo_set_particle_flaws.restype = None
+        lib.gyo_set_particle_flaws.argtypes = [vp, C.c_int, ip, dp]
         lib.gyo_gimp_shape.restype = C.c_double
         lib.gyo_gimp_shape.argtypes = [C.c_double] * 3
         lib.gyo_gimp_grad.restype = C.c_double
@@ -181,6 +183,13 @@ class Oracle:
         temp = getattr(scene, "temp", None)
         if temp is not None and np.any(temp != 0.0):
             self.set_temps(np.nonzero(temp)[0], temp[temp != 0.0])
+        flaw = getattr(scene, "flaw", None)
+        if flaw is not None and np.any(flaw != 1.0):
+            if kind != "port":
+                raise ValueError("the reference has no per-particle flaw strains (only the restatement)")
+            ids = np.nonzero(flaw != 1.0)[0].astype(np.int32)
+            w = np.ascontiguousarray(flaw[ids], np.float64)
+            self.lib.gyo_set_particle_flaws(self.h, int(ids.size), _ip(ids), _dp(w))
         for n in np.nonzero(scene.node_bc_type)[0]:
             v = np.ascontiguousarray(scene.node_bc_val[n], np.float64)
             self._call("set_node_bc", self.h, int(n), int(scene.node_bc_type[n]), _dp(v), 4)

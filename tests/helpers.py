@@ -111,8 +111,8 @@ def oracle_ensemble(scene, horizons, fields, members=8, eps=1e-7):
     """The FP64 restatement run from the scene and from `members` copies with initial positions
     perturbed by a relative eps (seeds 100, 101, ...), the runs spread over the host's cores in
     spawned worker processes.  Returns {horizon: (base fields, spread)} where spread[f] is the
-    largest relative L2 distance between two perturbed runs: how far apart rounding-sized input
-    changes carry the reference itself by that step."""
+    largest relative L2 distance between two of the runs (perturbed or not): how far apart
+    rounding-sized input changes carry the reference itself by that step."""
     import multiprocessing as mp
     from concurrent.futures import ProcessPoolExecutor
     horizons = sorted(set(int(h) for h in horizons))
@@ -127,6 +127,7 @@ def oracle_ensemble(scene, horizons, fields, members=8, eps=1e-7):
         spread = {}
         for f in fields:
             mem = [r[h][f] for r in runs[1:]]
-            spread[f] = max(rel_l2(a, b) for i, a in enumerate(mem) for b in mem[i + 1:])
+            pair = max(rel_l2(a, b) for i, a in enumerate(mem) for b in mem[i + 1:])
+            spread[f] = max(pair, max(rel_l2(m, base[f]) for m in mem))
         out[h] = (base, spread)
     return out

@@ -195,3 +195,34 @@ def test_no_particles(gpu_lib):
     st = s.stats()
     assert st["mass"] == 0.0 and st["kinetic"] == 0.0 and st["steps"] == 5
     assert s._get_particles("vel").shape[0] == 0
+
+
+def test_weibull_flaws_match_oracle(gpu_lib, oracle_built):
+    """Per-particle Weibull activation strains (scene weibull_flaws, seed 0) on the damage
+    block: the GPU's damage gate uses the particle's own scale -- the state after two steps
+    within 1e-5 of the FP64 restatement with the same scales, after 20 steps within the FP64
+    ensemble's reach (the damage gate makes this scene ill-conditioned past a few steps)."""
+    from tests.helpers import oracle_ensemble
+    sc = scenes.damage_block(n_side=12, weibull_seed=0)
+    assert np.any(sc.flaw != 1.0)
+    gpu = run_gpu(sc, 2)
+    ref = run_oracle(sc, 2)
+    for f in ("vel", "stress", "damage"):
+        assert rel_l2(gpu._get_particles(f), ref.pfield(f)) <= 1e-5, f
+    ens = oracle_ensemble(sc, (20,), ("vel", "stress", "damage"), eps=1e-6)
+    base, spread = ens[20]
+    gpu = run_gpu(sc, 20)
+    for f in ("vel", "stress", "damage"):
+        assert rel_l2(gpu._get_particles(f), base[f]) <= max(1e-3, 2.0 * spread[f]), f
+
+
+def test_flaw_scale_one_equals_plain_run(gpu_lib):
+    """A flaw table of ones is the reference's deterministic e_min: the run equals the run
+    without a table to FP32 summation order."""
+    sc = scenes.damage_block(n_side=12)
+    plain = run_gpu(sc, 20)
+    sc.flaw = np.ones(sc.n)
+    sc.flaw[0] = 1.0 + 2.0 ** -40  # a table is built (one scale differs from 1 below FP32 resolution)
+    ones = run_gpu(sc, 20)
+    for f in ("vel", "stress", "damage"):
+        assert rel_l2(ones._get_particles(f), plain._get_particles(f)) <= 2e-6, f

@@ -220,3 +220,50 @@ def test_constitutive_first_step_known_answer(oracle_built, model):
     assert inner.sum() == 216
     assert np.abs(s - want_s).max() <= 1e-12 * np.abs(want_s).max()
     assert np.abs(e - want_e).max() <= 1e-12 * np.abs(want_e).max()
+
+
+def test_flaw_scale_one_is_the_reference(oracle_built):
+    """A flaw table of ones (every particle's activation strain the deterministic
+    (V k)^(-1/m), DamageModels.cpp:102-103) reproduces the reference's golden damage block."""
+    import ctypes as C
+    from oracle.oracle import Oracle
+    gold = np.load(os.path.join(GOLDEN, "damage_block.npz"))
+    make, steps, _ = make_golden.CASES["damage_block"]
+    sc = make()
+    o = Oracle(sc, "port", mode=1)
+    ids = np.arange(sc.n, dtype=np.int32)
+    ones = np.ones(sc.n)
+    o.lib.gyo_set_particle_flaws(o.h, sc.n, ids.ctypes.data_as(C.POINTER(C.c_int)),
+                                 ones.ctypes.data_as(C.POINTER(C.c_double)))
+    o.run(int(gold["steps"]))
+    for f in ("stress", "damage", "vel", "eqps"):
+        assert rel_l2(o.pfield(f)[gold["ids"]], gold[f]) <= 1e-12, f
+
+
+def test_weibull_flaw_draw():
+    """weibull_flaws: w = (-ln U)^(1/m) for the Grady-Kipp material, 1 elsewhere; w^m is then
+    exponentially distributed with mean 1 (the reference's e_min is its w = 1 case)."""
+    sc = scenes.brazilian_disc(scale=0.1, weibull_seed=0)
+    m = sc.materials[0]["damageM"]
+    rock = sc.mat == 0
+    assert np.all(sc.flaw[~rock] == 1.0)
+    x = sc.flaw[rock] ** m
+    assert abs(x.mean() - 1.0) < 0.05 and abs(np.median(x) - np.log(2.0)) < 0.05
+    again = scenes.brazilian_disc(scale=0.1, weibull_seed=0)
+    assert np.array_equal(sc.flaw, again.flaw)
+
+
+def test_weibull_flaws_change_damage(oracle_built):
+    """With Weibull scales (m = 9: w spread over about 0.8-1.15) the damage field departs from
+    the deterministic threshold's, and the particles whose damage has grown are those with
+    the smaller scales."""
+    from tests.helpers import run_oracle
+    plain = run_oracle(scenes.damage_block(n_side=8), 10)
+    wb_scene = scenes.damage_block(n_side=8, weibull_seed=0)
+    wb = run_oracle(wb_scene, 10)
+    d0, d1 = plain.pfield("damage"), wb.pfield("damage")
+    assert rel_l2(d1, d0) > 1e-3
+    assert (d1 > 0).sum() != (d0 > 0).sum()
+    grown = d1 > 0
+    assert grown.any() and (~grown).any()
+    assert np.median(wb_scene.flaw[grown]) < np.median(wb_scene.flaw[~grown])

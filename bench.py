@@ -266,6 +266,8 @@ def main():
     ap.add_argument("--column-height", type=float, default=0.765,
                     help="dam break water column height in m (1.5 gives the configuration's 24 M particles)")
     ap.add_argument("--full-sort", action="store_true", help="full radix sort every step (no incremental re-sort)")
+    ap.add_argument("--p2g-lanes", type=int, default=3, choices=[3, 9],
+                    help="single-body P2G lanes per run of equal cell: 3 z-plane lanes or 9 x-column lanes")
     ap.add_argument("--preroll", type=int, default=-1,
                     help="untimed steps before the warm-up (default: half the configuration's run)")
     args = ap.parse_args()
@@ -297,7 +299,8 @@ def main():
         x = sc.pos[:, 0]
         sc.temp = args.temperature * (1.0 + (x - x.min()) / max(x.max() - x.min(), 1e-30))
     n = sc.n
-    solver = graphyt.from_scene(sc, device=local, options=dict(sort_every=args.sort_every, full_sort=int(args.full_sort)))
+    solver = graphyt.from_scene(sc, device=local, options=dict(sort_every=args.sort_every, full_sort=int(args.full_sort),
+                                                               p2g_lanes=args.p2g_lanes))
     lib, h = solver.lib, solver.h
     dt = solver.dt
     import numpy as np
@@ -424,7 +427,7 @@ def main():
                        "model": {"dam_break": "newtonian", "brazilian_disc": "drucker_prager+grady_kipp, 3 bodies",
                                  "impact_batch": "drucker_prager+grady_kipp slab + elastic sphere per instance, "
                                                  "2 bodies"}[args.workload],
-                       "sort_every": args.sort_every, "sort": "full" if args.full_sort else "incremental", "l2": "state larger than L2 (no flush needed)",
+                       "sort_every": args.sort_every, "p2g_lanes": args.p2g_lanes, "sort": "full" if args.full_sort else "incremental", "l2": "state larger than L2 (no flush needed)",
                        "parallelism": ("instances sharded" if sharded else "replicas") if world > 1 else "single"},
             "window": {"first_timed_step": step_timed0, "of_run_steps": RUN_STEPS[args.workload],
                        "movers_per_step": movers},

@@ -50,7 +50,8 @@ class Params(C.Structure):
 
 class Options(C.Structure):
     _fields_ = [("sort_every", C.c_int), ("full_sort", C.c_int), ("use_graph", C.c_int),
-                ("track_normals", C.c_int), ("check_finite", C.c_int), ("keep_node_fields", C.c_int)]
+                ("track_normals", C.c_int), ("check_finite", C.c_int), ("keep_node_fields", C.c_int),
+                ("p2g_lanes", C.c_int)]
 
 
 class Stats(C.Structure):
@@ -72,6 +73,9 @@ SIGNATURES = {
     "gy_set_particle_stress": (C.c_int, [_vp, C.c_int64, _i64p, _dp]),
     "gy_set_particle_damage": (C.c_int, [_vp, C.c_int64, _i64p, _dp]),
     "gy_set_particle_flaw": (C.c_int, [_vp, C.c_int64, _i64p, _dp]),
+    "gy_tc_gemm_bf16": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int, C.c_int, _vp, _vp]),
+    "gy_mlp_param_count": (C.c_int64, []),
+    "gy_mlp_forward": (C.c_int, [_vp, _vp, C.c_int64, _vp, _vp, _vp]),
     "gy_set_particle_temp": (C.c_int, [_vp, C.c_int64, _i64p, _dp]),
     "gy_hold_particles": (C.c_int, [_vp, C.c_int64, _i64p]),
     "gy_set_particle_bc": (C.c_int, [_vp, C.c_int64, _i64p, _ip, _dp]),

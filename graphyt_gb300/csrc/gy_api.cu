@@ -65,7 +65,7 @@ struct gy_solver {
     gy_params prm{};
     double dt = 0.0;
     bool initialized = false;
-    gy_options opt{1, 0, 1, 0, 0, 0};
+    gy_options opt{1, 0, 1, 0, 0, 0, 3};
     std::vector<int> slot_obj;       // dense object slot -> objectID
     bool multi = false, has_dp = false;
     int nbody = 1;
@@ -845,6 +845,7 @@ gy_status gy_set_options(gy_solver *h, const gy_options *opt)
     if (!h || !opt) return GY_ERR_ARG;
     if (opt->sort_every < 1) return fail(h, GY_ERR_ARG, "sort_every must be >= 1");
     if (opt->use_graph != 0 && opt->use_graph != 1) return fail(h, GY_ERR_ARG, "use_graph must be 0 or 1");
+    if (opt->p2g_lanes != 3 && opt->p2g_lanes != 9) return fail(h, GY_ERR_ARG, "p2g_lanes must be 3 or 9");
     if (h->initialized && (opt->track_normals != h->opt.track_normals || opt->keep_node_fields != h->opt.keep_node_fields))
         return fail(h, GY_ERR_STATE, "track_normals / keep_node_fields must be set before gy_initialize");
     h->opt = *opt;
@@ -931,7 +932,7 @@ static void issue_step(gy_solver *h, const StepVariant &v, cudaEvent_t *tev)
     // heat conduction: fused into the single-body P2G, a separate pass for body slots
     const bool fused_thermal = h->thermal && !h->multi;
     launch_p2g(src, perm, skey, h->n, h->d_seg, nseg, h->persist_grid, h->nb, a, s,
-               fused_thermal ? h->d_therm : nullptr, fused_thermal ? h->d_tnode : nullptr);
+               fused_thermal ? h->d_therm : nullptr, fused_thermal ? h->d_tnode : nullptr, h->opt.p2g_lanes);
     if (h->thermal && h->multi)
         launch_thermal_p2g(src, h->d_therm, perm, skey, h->n, h->d_seg, nseg, h->d_tnode, a, s);
     if (tev) cudaEventRecord(tev[2], s);

@@ -445,6 +445,213 @@ __global__ void __launch_bounds__(PC_THREADS, GY_PC_MINB) k_p2g_cols(PView P, co
     }
 }
 
+// Single-body P2G with z-plane lanes.  The segments, chunks and runs of equal cell are
+// those of k_p2g_cols; the work of a run is split over three lanes instead of nine: lane kk
+// of a run's group owns the 3x3 stencil nodes (i, j, kk) of its plane and sums the run's
+// particles into 63 registers (m, p, f of nine nodes, packed along the fields), then adds them
+// into the node tile once per run.  Ten groups share a warp (lanes 0-29), one particle per
+// group and step, so a particle's staged weights and payload reach three lanes rather than
+// nine -- the shared-memory loads per particle, which bound the column kernel, drop about
+// threefold -- at the cost of recomputing the y/z factors per lane.  Staged per particle
+// (rows swizzled q + q/8 so the ten groups' rows spread over the banks):
+//   A = (Sx0, Sx1, Sx2, Gx0)  B = (Gx1, Gx2, Sy0, Sy1)  C = (Sy2, Gy0, Gy1, Gy2)
+//   D = (m, m vx, m vy, m vz) E = (s0, s3, s5, s4)      F = (s3, s1, s2, -)
+//   Z[kk] = (Sz_kk, Gz_kk),   s = V sigma / h in the order xx yy zz xy yz xz,
+// laid out so that every packed FP32x2 operand is a stored pair.
+constexpr int PP_THREADS = 128;
+constexpr int PP_GPW = 10;                              // lane groups per warp
+constexpr int PP_GROUPS = PP_GPW * (PP_THREADS / 32);   // 40
+constexpr int PP_CH = 2 * PP_THREADS;                   // particles per chunk (a pair per thread)
+constexpr int PP_ROWS = PP_CH + PP_CH / 8;
+__device__ __forceinline__ int pp_row(int q) { return q + (q >> 3); }
+static_assert(PP_CH == PC_CH, "the chunk bounds helper assumes two particles per thread");
+
+__device__ __forceinline__ float2 dup2(float x) { return make_float2(x, x); }
+
+__global__ void __launch_bounds__(PP_THREADS, 4) k_p2g_planes(PView P, const int *perm, const int *skey, long long n,
+                                                              const int *seg_start, const int *nseg_ptr, int sorted,
+                                                              NodeBufs nb, GridGeom g)
+{
+    __shared__ float tile[P2G_FIELDS * PT_NODES];
+    __shared__ float4 SA[PP_ROWS], SB[PP_ROWS], SC[PP_ROWS], SD[PP_ROWS], SE[PP_ROWS], SF[PP_ROWS];
+    __shared__ float2 SZ[3][PP_ROWS];
+    __shared__ int run_start[PP_CH + 1];
+    __shared__ int run_cell[PP_CH];
+    __shared__ int wcount[PP_THREADS / 32];
+    __shared__ long long s_end;
+    const int nseg = *nseg_ptr;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    const int grp = lane / 3, kk = lane - 3 * grp;      // lanes 30, 31: group 10, no run
+    const float2 z2 = make_float2(0.f, 0.f);
+    for (int sgi = blockIdx.x; sgi < nseg; sgi += gridDim.x) {
+        const long long start = seg_start[sgi];
+        const int blk = seg_block(skey, start);
+        int bx, by, bz;
+        decode_block(blk, g, bx, by, bz);
+        const int tox = bx * CB, toy = by * CB, toz = g.is3d ? bz * CB : 0;
+        for (int t = tid; t < P2G_FIELDS * PT_NODES; t += PP_THREADS) tile[t] = 0.f;
+        for (long long base = start;; base += PP_CH) {
+            const long long ia = base + 2 * tid, ib = ia + 1;
+            int cnt, ka = -1, kb = -1, kp = -1;
+            long long ja = 0, jb = 0;
+            if (sorted) {
+                ka = ia < n ? skey[ia] : -1;
+                kb = ib < n ? skey[ib] : -1;
+                kp = (ia < n && tid > 0) ? skey[ia - 1] : -1;
+                ja = ia < n ? perm[ia] : 0;
+                jb = ib < n ? perm[ib] : 0;
+                cnt = __syncthreads_count(ia < n && (ka >> CB_SHIFT) == blk);
+                cnt += __syncthreads_count(ib < n && (kb >> CB_SHIFT) == blk);
+            } else {
+                cnt = (int)min((long long)PP_CH, segment_chunk_end2(skey, n, blk, base, &s_end) - base);
+                if (2 * tid < cnt) {
+                    ka = skey[ia];
+                    kp = tid > 0 ? skey[ia - 1] : -1;
+                }
+                if (2 * tid + 1 < cnt) kb = skey[ib];
+                ja = ia;
+                jb = ib;
+            }
+            if (cnt <= 0) break;
+            // ---- stage particles 2 tid and 2 tid + 1 of the chunk ----
+#pragma unroll
+            for (int h2 = 0; h2 < 2; h2++) {
+                const int q = 2 * tid + h2;
+                if (q >= cnt) break;
+                const long long j = h2 ? jb : ja;
+                const int row = pp_row(q);
+                float Sx[3], Gx[3], Sy[3], Gy[3], Sz[3], Gz[3];
+                gimp_axis(P.f(PF_OX, j), g, Sx, Gx);
+                gimp_axis(P.f(PF_OY, j), g, Sy, Gy);
+                if (g.is3d) {
+                    gimp_axis(P.f(PF_OZ, j), g, Sz, Gz);
+                } else {
+                    Sz[0] = 1.f; Sz[1] = 0.f; Sz[2] = 0.f; Gz[0] = 0.f; Gz[1] = 0.f; Gz[2] = 0.f;
+                }
+                const float m = P.f(PF_MASS, j);
+                const float sc = (m / P.f(PF_RHO, j)) * g.inv_h;  // V sigma with the gradient's 1/h
+                const float s0 = P.f(PF_S0, j) * sc, s1 = P.f(PF_S1, j) * sc, s2 = P.f(PF_S2, j) * sc;
+                const float s3 = P.f(PF_S3, j) * sc, s4 = P.f(PF_S4, j) * sc, s5 = P.f(PF_S5, j) * sc;
+                SA[row] = make_float4(Sx[0], Sx[1], Sx[2], Gx[0]);
+                SB[row] = make_float4(Gx[1], Gx[2], Sy[0], Sy[1]);
+                SC[row] = make_float4(Sy[2], Gy[0], Gy[1], Gy[2]);
+                SD[row] = make_float4(m, m * P.f(PF_VX, j), m * P.f(PF_VY, j), m * P.f(PF_VZ, j));
+                SE[row] = make_float4(s0, s3, s5, s4);
+                SF[row] = make_float4(s3, s1, s2, 0.f);
+#pragma unroll
+                for (int z = 0; z < 3; z++) SZ[z][row] = make_float2(Sz[z], Gz[z]);
+            }
+            // ---- runs of equal cell, in order: run r is [run_start[r], run_start[r+1]) ----
+            const bool va = 2 * tid < cnt, vb = 2 * tid + 1 < cnt;
+            const int ca = ka & 63, cb = kb & 63;
+            const bool ha = va && (tid == 0 || (kp & 63) != ca);
+            const bool hb = vb && cb != ca;
+            const unsigned ba = __ballot_sync(0xffffffffu, ha), bb = __ballot_sync(0xffffffffu, hb);
+            if (lane == 0) wcount[warp] = __popc(ba) + __popc(bb);
+            __syncthreads();
+            int wbase = 0, R = 0;
+#pragma unroll
+            for (int w2 = 0; w2 < PP_THREADS / 32; w2++) {
+                const int c = wcount[w2];
+                wbase += (w2 < warp) ? c : 0;
+                R += c;
+            }
+            int ri = wbase + __popc(ba & lt) + __popc(bb & lt);
+            if (ha) {
+                run_start[ri] = 2 * tid;
+                run_cell[ri] = ca;
+                ri++;
+            }
+            if (hb) {
+                run_start[ri] = 2 * tid + 1;
+                run_cell[ri] = cb;
+            }
+            if (tid == 0) run_start[R] = cnt;
+            __syncthreads();
+            // ---- ten runs per warp and round, three plane lanes per run ----
+            for (int rb = warp * PP_GPW; rb < R; rb += PP_GROUPS) {
+                const int r = rb + grp;
+                const bool rv = grp < PP_GPW && r < R;
+                const int p0 = rv ? run_start[r] : 0, len = rv ? run_start[r + 1] - p0 : 0;
+                const int maxlen = __reduce_max_sync(0xffffffffu, len);
+                float2 amp[3][3], app[3][3], afxy[3][3];
+                float afz[3][3];
+#pragma unroll
+                for (int i = 0; i < 3; i++)
+#pragma unroll
+                    for (int j = 0; j < 3; j++) {
+                        amp[i][j] = app[i][j] = afxy[i][j] = z2;
+                        afz[i][j] = 0.f;
+                    }
+                for (int k = 0; k < maxlen; k++) {
+                    const int row = pp_row(p0 + min(k, max(len - 1, 0)));
+                    const float4 A = SA[row], B = SB[row], C = SC[row], D = SD[row], E = SE[row], F = SF[row];
+                    float2 Z = SZ[kk][row];
+                    if (k >= len) Z = z2;  // past the run (or no run): the particle adds nothing
+                    const float Sx[3] = {A.x, A.y, A.z}, Gx[3] = {A.w, B.x, B.y};
+                    const float Sy[3] = {B.z, B.w, C.x}, Gy[3] = {C.y, C.z, C.w};
+                    const float2 mvx = make_float2(D.x, D.y), mvyz = make_float2(D.z, D.w);
+                    const float2 s03 = make_float2(E.x, E.y), s54 = make_float2(E.z, E.w);
+                    const float2 s31 = make_float2(F.x, F.y);
+#pragma unroll
+                    for (int j = 0; j < 3; j++) {
+                        const float syz = Sy[j] * Z.x, gyz = Gy[j] * Z.x, syg = Sy[j] * Z.y;
+                        const float2 syz2 = dup2(syz);
+                        const float2 mp = mul2(syz2, mvx);                    // (m, m vx) S_y S_z
+                        const float2 pp = mul2(syz2, mvyz);                   // (m vy, m vz) S_y S_z
+                        const float2 Bxy = mul2(syz2, s03);                   // (s0, s3) S_y S_z
+                        const float Bz = E.z * syz;                           // s5 S_y S_z
+                        const float2 Cxy = fma2(dup2(gyz), s31, mul2(dup2(syg), s54));  // (s3, s1) G_y S_z + (s5, s4) S_y G_z
+                        const float Cz = fmaf(E.w, gyz, F.z * syg);           // s4 G_y S_z + s2 S_y G_z
+#pragma unroll
+                        for (int i = 0; i < 3; i++) {
+                            const float2 sx = dup2(Sx[i]), gx = dup2(Gx[i]);
+                            amp[i][j] = fma2(sx, mp, amp[i][j]);
+                            app[i][j] = fma2(sx, pp, app[i][j]);
+                            afxy[i][j] = fma2(gx, Bxy, fma2(sx, Cxy, afxy[i][j]));
+                            afz[i][j] = fmaf(Gx[i], Bz, fmaf(Sx[i], Cz, afz[i][j]));
+                        }
+                    }
+                }
+                if (!rv) continue;
+                const int cell = run_cell[r];
+                const int li = cell & 3, lj = (cell >> 2) & 3, lk = cell >> 4;
+#pragma unroll
+                for (int j = 0; j < 3; j++)
+#pragma unroll
+                    for (int i = 0; i < 3; i++) {
+                        // a node outside every particle's support has no weight and no gradient
+                        if (amp[i][j].x == 0.f) continue;
+                        const int t = ((lk + kk) * PT + (lj + j)) * PT + li + i;
+                        atomicAdd(&tile[0 * PT_NODES + t], amp[i][j].x);
+                        atomicAdd(&tile[1 * PT_NODES + t], amp[i][j].y);
+                        atomicAdd(&tile[2 * PT_NODES + t], app[i][j].x);
+                        atomicAdd(&tile[3 * PT_NODES + t], app[i][j].y);
+                        atomicAdd(&tile[4 * PT_NODES + t], -afxy[i][j].x);
+                        atomicAdd(&tile[5 * PT_NODES + t], -afxy[i][j].y);
+                        atomicAdd(&tile[6 * PT_NODES + t], -afz[i][j]);
+                    }
+            }
+            if (cnt < PP_CH) break;
+        }
+        __syncthreads();
+        // ---- flush the tile: two vector reductions per touched node ----
+        for (int t = tid; t < PT_NODES; t += PP_THREADS) {
+            const float m = tile[t], px = tile[PT_NODES + t], py = tile[2 * PT_NODES + t], pz = tile[3 * PT_NODES + t];
+            const float fx = tile[4 * PT_NODES + t], fy = tile[5 * PT_NODES + t], fz = tile[6 * PT_NODES + t];
+            if (m == 0.f && px == 0.f && py == 0.f && pz == 0.f && fx == 0.f && fy == 0.f && fz == 0.f) continue;
+            const int ni = tox + t % PT, nj = toy + (t / PT) % PT, nk = toz + t / (PT * PT);
+            if (ni >= g.nx || nj >= g.ny || nk >= g.nz) continue;
+            const int nd = node_index(ni, nj, nk, g);
+            red_add4(&nb.acc0[nd], m, px, py, pz);
+            red_add4(&nb.acc1[nd], fx, fy, fz, 0.f);
+            mark_node(nb, ni, nj, nk, g);
+        }
+        __syncthreads();
+    }
+}
+
 // Multi-body P2G through a shared-memory node tile: segments, staging and runs of equal cell
 // as in the single-body kernel, with a warp taking one run at a time (lane k = stencil node
 // k), one particle per step, and, per node, the centre-of-mass fields plus the two body
@@ -723,7 +930,7 @@ __global__ void __launch_bounds__(P2G_CH) k_p2g_multi_tiled(PView P, const int *
 
 void launch_p2g(const PView &p, const int *perm, const int *skey, long long n, const int *seg_start,
                 const int *nseg, int persist_grid, const NodeBufs &nb, const StepArgs &a, cudaStream_t s,
-                const float4 *therm, float2 *tnode)
+                const float4 *therm, float2 *tnode, int lanes)
 {
     if (n == 0) return;
     if (a.multi_body) {
@@ -748,6 +955,16 @@ void launch_p2g(const PView &p, const int *perm, const int *skey, long long n, c
             }
             k_p2g_cols<true><<<tgrid, PC_THREADS, 0, s>>>(p, perm, skey, n, seg_start, nseg, perm ? 1 : 0, nb, a.g,
                                                            therm, tnode, a.mats);
+        } else if (lanes == 3) {
+            static int pgrid = 0;  // persistent grid of the plane-lane kernel (its own occupancy)
+            if (pgrid == 0) {
+                int dev = 0, sms = 1, b = 0;
+                cudaGetDevice(&dev);
+                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_p2g_planes, PP_THREADS, 0);
+                pgrid = sms * std::max(b, 1);
+            }
+            k_p2g_planes<<<pgrid, PP_THREADS, 0, s>>>(p, perm, skey, n, seg_start, nseg, perm ? 1 : 0, nb, a.g);
         } else {
             k_p2g_cols<false><<<persist_grid, PC_THREADS, 0, s>>>(p, perm, skey, n, seg_start, nseg, perm ? 1 : 0, nb,
                                                                    a.g, nullptr, nullptr, nullptr);

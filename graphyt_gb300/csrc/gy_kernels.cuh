@@ -87,10 +87,11 @@ long long launch_count();
 
 // launchers (gy_kernels.cu)
 // therm / tnode non-null: the single-body kernel also sums the heat conduction node fields
-// (multi-body problems run launch_thermal_p2g instead)
+// (multi-body problems run launch_thermal_p2g instead).  lanes: lanes per run of equal cell in
+// the single-body kernel without heat conduction, 3 (z-plane lanes) or 9 (x-column lanes).
 void launch_p2g(const PView &p, const int *perm, const int *skey, long long n, const int *seg_start,
                 const int *nseg, int persist_grid, const NodeBufs &nb, const StepArgs &a, cudaStream_t s,
-                const float4 *therm = nullptr, float2 *tnode = nullptr);
+                const float4 *therm = nullptr, float2 *tnode = nullptr, int lanes = 3);
 void launch_fold(const NodeBufs &nb, const StepArgs &a, cudaStream_t s);
 void launch_solve(const NodeBufs &nb, const StepArgs &a, bool keep_node_fields, cudaStream_t s);
 // therm / tnode non-null: the single-body kernel also runs the heat conduction G2P and the

@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define GY_ABI_VERSION 3
+#define GY_ABI_VERSION 4
 
 typedef int gy_status;
 enum {
@@ -83,6 +83,9 @@ typedef struct gy_options {
     int track_normals;  /* 1: keep per-particle contact normals (getNormalsArr) */
     int check_finite;   /* 1: flag NaN/Inf in particle state every step */
     int keep_node_fields; /* 1: keep centre-of-mass node velocity/force for node getters */
+    int p2g_lanes;      /* single-body P2G without heat conduction: lanes per run of equal cell,
+                           3 (default: each lane sums a z-plane of nine stencil nodes) or 9 (each
+                           lane a column of three x nodes); same sums, different speed */
 } gy_options;
 
 /* FP64 conservation sums and counters, Solver.cpp:264-289's printout made a struct. */
@@ -261,6 +264,28 @@ gy_status gy_get_phase_times(gy_solver *h, float *ms5, int64_t *steps);
 /* Device time of nsteps consecutive steps (as gy_steps), from CUDA events recorded on the
  * handle's stream before the first and after the last step. */
 gy_status gy_time_steps(gy_solver *h, double t0, int step0, int nsteps, float *ms);
+
+/* Tensor-core GEMM, C[M x N] = A[M x K] * B[N x K]^T: BF16 row-major A and B (K contiguous),
+ * FP32 row-major C, all in device memory; 16 <= N <= 256 and 16 <= K <= 256, both multiples of
+ * 16.  tcgen05 MMAs from shared memory into tensor memory, one 128-row tile per CTA.  No
+ * reference counterpart: the building block of the learned constitutive surrogate's kernels,
+ * exposed so it can be checked on its own.  d_status (may be null) receives bit 4 if a
+ * tensor-core wait gave up.  Only enqueues work on stream. */
+gy_status gy_tc_gemm_bf16(const uint16_t *d_A, const uint16_t *d_B, float *d_C, int M, int N, int K, int *d_status,
+                          void *stream);
+
+/* ---- learned Drucker-Prager surrogate (no reference counterpart) --------------------------
+ * A 16 -> 64 -> 64 -> 7 MLP with SiLU in one packed FP32 parameter vector of
+ * gy_mlp_param_count() floats: W1 [16][64], b1 [64], W2 [64][64], b2 [64], W3 [64][7], b3 [7]
+ * (y = x W + b, weights input-major), then the input mean [16] and std [16] and the output
+ * mean [7] and std [7] (x_n = (x - mean) / std, y = y_n std + mean).  The kernels run it in
+ * BF16 on the tensor cores (tcgen05 MMAs, FP32 accumulation in tensor memory) over tiles of
+ * 128 rows. */
+int64_t gy_mlp_param_count(void);
+
+/* Y [n][7] = MLP(X [n][16]), raw FP32 rows in device memory; only enqueues work on stream.
+ * d_status (may be null) receives bit 4 if a tensor-core wait gave up. */
+gy_status gy_mlp_forward(const float *d_params, const float *d_X, int64_t n, float *d_Y, int *d_status, void *stream);
 
 /* Number of kernels this library has launched in the process so far. */
 int64_t gy_kernel_launches(void);

@@ -30,7 +30,7 @@ def test_python_binding_covers_header(gpu_lib):
 
 
 def test_abi_version(gpu_lib):
-    assert gpu_lib.gy_abi_version() == 3
+    assert gpu_lib.gy_abi_version() == 4
 
 
 def test_create_rejects_inconsistent_grid(gpu_lib):

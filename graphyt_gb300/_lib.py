@@ -76,6 +76,9 @@ SIGNATURES = {
     "gy_tc_gemm_bf16": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int, C.c_int, _vp, _vp]),
     "gy_mlp_param_count": (C.c_int64, []),
     "gy_mlp_forward": (C.c_int, [_vp, _vp, C.c_int64, _vp, _vp, _vp]),
+    "gy_mlp_grad": (C.c_int, [_vp, _vp, _vp, C.c_int64, _vp, _vp, _vp, _vp]),
+    "gy_mlp_train": (C.c_int, [_vp, _vp, _vp, C.c_int64, C.c_int, C.c_int, C.c_float, C.c_uint64, C.c_int,
+                               C.POINTER(C.c_float), _vp, _vp]),
     "gy_set_particle_temp": (C.c_int, [_vp, C.c_int64, _i64p, _dp]),
     "gy_hold_particles": (C.c_int, [_vp, C.c_int64, _i64p]),
     "gy_set_particle_bc": (C.c_int, [_vp, C.c_int64, _i64p, _ip, _dp]),

@@ -1,7 +1,9 @@
 // gy_mlp.cu -- BF16 tensor-core (tcgen05 + TMEM) kernels of the learned Drucker-Prager
 // surrogate, and the plain GEMM they are checked against.
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
+#include <vector>
 
 #include <cuda_bf16.h>
 
@@ -298,6 +300,335 @@ __global__ void __launch_bounds__(128) k_mlp_forward(const float *prm, const flo
     mlp_end(S);
 }
 
+// ---------------------------------------------------------------------------------------
+// Training.  One CTA trains on one 128-sample tile of the batch: forward (three MMAs, the
+// pre-activations kept in TMEM), the MSE gradient, backward through the layers (two MMAs) and
+// the weight gradients (three MMAs with K = 128 samples), added into the global gradient with
+// atomics.  Operands of the weight-gradient MMAs are the transposed activations (K = samples),
+// stored in one region as rows XT (16) | H2T (64) | H1T (64) | DZ1T (64) of 128 samples, so
+// each of them is the first rows of a 128-row window starting at its first row; the rows past
+// the valid ones feed only TMEM lanes that are never read.
+constexpr int MLP_TR = 16 + 64 + 64 + 64;            // rows of the transposed region
+constexpr int TR_XT = 0, TR_H2T = 16, TR_H1T = 80, TR_DZ1T = 144;
+constexpr int MLP_TRAIN_PARAMS = MP_IN_MEAN;          // trainable: weights and biases
+// TMEM columns of the training kernel
+constexpr int TM_Z1 = 0, TM_Z2 = 64, TM_Y = 128, TM_DH = 192, TM_G3 = 256, TM_G2 = 320, TM_G1 = 384;
+constexpr uint32_t MLP_TRAIN_TMEM_COLS = 512;
+
+struct MlpTrainSmem {
+    alignas(1024) unsigned char xn[128 * MLP_IN * 2];    // A of layer 1
+    alignas(1024) unsigned char h[128 * MLP_H * 2];      // A of layer 2 (h1), layer 3 (h2), then dz2
+    alignas(1024) unsigned char dy[128 * MLP_OUTP * 2];  // A of dH2 = dY W3^T
+    alignas(1024) unsigned char tr[MLP_TR * 128 * 2];    // transposed activations, K = 128 samples
+    alignas(1024) unsigned char dyt[MLP_OUTP * 128 * 2]; // B of dW3
+    alignas(1024) unsigned char dz2t[MLP_H * 128 * 2];   // B of dW2
+    alignas(1024) unsigned char w1t[MLP_H * MLP_IN * 2];
+    alignas(1024) unsigned char w2t[MLP_H * MLP_H * 2];
+    alignas(1024) unsigned char w3t[MLP_OUTP * MLP_H * 2];
+    alignas(1024) unsigned char w3[MLP_H * MLP_OUTP * 2]; // B of dH2: B[i][o] = W3[i][o]
+    alignas(1024) unsigned char w2[MLP_H * MLP_H * 2];    // B of dH1: B[i][o] = W2[i][o]
+    float b1[MLP_H], b2[MLP_H], b3[MLP_OUTP];
+    float gb1[MLP_H], gb2[MLP_H], gb3[MLP_OUTP];
+    float in_mean[MLP_IN], in_rstd[MLP_IN], out_mean[MLP_OUT], out_rstd[MLP_OUT];
+    float loss;
+    uint64_t mbar;
+    uint32_t tbase;
+};
+
+__device__ __forceinline__ void put_bf16(unsigned char *tile, int r, int k, int K, float v)
+{
+    *reinterpret_cast<uint16_t *>(tile + tc_off(r, k, K)) = bf16_rn(v);
+}
+
+// d/dz silu(z) = s (1 + z (1 - s)), s = sigmoid(z)
+__device__ __forceinline__ float silu_grad(float z)
+{
+    const float sg = 1.0f / (1.0f + __expf(-z));
+    return sg * (1.0f + z * (1.0f - sg));
+}
+
+// issue `count` MMAs over K (16 columns each) into TMEM column `col`
+__device__ __forceinline__ void mma_k(uint32_t tbase, int col, const unsigned char *A, const unsigned char *B, int N,
+                                      int K)
+{
+    const uint32_t idesc = tc_idesc_bf16(128, N);
+    const uint32_t sbo = (uint32_t)(K / 8) * 128;
+    for (int j = 0; j < K / 16; j++)
+        tc_mma(tbase + (uint32_t)col, tc_sdesc(smem_u32(A) + 256 * j, 128, sbo),
+               tc_sdesc(smem_u32(B) + 256 * j, 128, sbo), idesc, j > 0);
+}
+
+// all threads: wait for the MMAs committed as phase `ph` (CTA-uniform verdict)
+__device__ __forceinline__ bool mma_done(uint64_t *mbar, uint32_t &ph)
+{
+    const bool ok = __syncthreads_and(mbar_wait(mbar, ph & 1)) != 0;
+    ph++;
+    tc_fence_after();
+    return ok;
+}
+
+// shared-memory writes of this phase visible to the tensor core, then a CTA barrier
+__device__ __forceinline__ void smem_to_tc()
+{
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+}
+
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z)
+{
+    // splitmix64 finaliser
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// rows: sampled from [0, n) by a hash of (seed, step, row) when sample != 0, else row r of
+// the batch is data row r (gradient checks)
+__global__ void __launch_bounds__(128) k_mlp_train_tile(const float *prm, const float *X, const float *T, long long n,
+                                                        int sample, unsigned long long seed, const int *step_ctr,
+                                                        float *grad, float *loss_acc, int batch, int *status)
+{
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    MlpTrainSmem &S = *reinterpret_cast<MlpTrainSmem *>(smem_raw);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    if (warp == 0) tmem_alloc(&S.tbase, MLP_TRAIN_TMEM_COLS);
+    if (tid == 0) {
+        mbar_init(&S.mbar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        S.loss = 0.f;
+    }
+    // ---- weights and biases (BF16 operand tiles in both orientations), normalisation ----
+    for (int e = tid; e < MLP_H * MLP_IN; e += 128) {
+        const int i = e / MLP_H, o = e - i * MLP_H;  // W1[i][o]
+        put_bf16(S.w1t, o, i, MLP_IN, prm[MP_W1 + e]);
+    }
+    for (int e = tid; e < MLP_H * MLP_H; e += 128) {
+        const int i = e / MLP_H, o = e - i * MLP_H;  // W2[i][o]
+        const float w = prm[MP_W2 + e];
+        put_bf16(S.w2t, o, i, MLP_H, w);
+        put_bf16(S.w2, i, o, MLP_H, w);
+    }
+    for (int e = tid; e < MLP_H * MLP_OUTP; e += 128) {
+        const int i = e / MLP_OUTP, o = e - i * MLP_OUTP;
+        const float w = o < MLP_OUT ? prm[MP_W3 + i * MLP_OUT + o] : 0.f;
+        put_bf16(S.w3t, o, i, MLP_H, w);
+        put_bf16(S.w3, i, o, MLP_OUTP, w);
+    }
+    for (int e = tid; e < MLP_H; e += 128) {
+        S.b1[e] = prm[MP_B1 + e];
+        S.b2[e] = prm[MP_B2 + e];
+        S.gb1[e] = 0.f;
+        S.gb2[e] = 0.f;
+    }
+    if (tid < MLP_OUTP) {
+        S.b3[tid] = tid < MLP_OUT ? prm[MP_B3 + tid] : 0.f;
+        S.gb3[tid] = 0.f;
+    }
+    if (tid < MLP_IN) {
+        S.in_mean[tid] = prm[MP_IN_MEAN + tid];
+        S.in_rstd[tid] = 1.0f / prm[MP_IN_STD + tid];
+    }
+    if (tid < MLP_OUT) {
+        S.out_mean[tid] = prm[MP_OUT_MEAN + tid];
+        S.out_rstd[tid] = 1.0f / prm[MP_OUT_STD + tid];
+    }
+    __syncthreads();
+    // ---- this thread's sample ----
+    const int s = tid;
+    const long long grow = (long long)blockIdx.x * 128 + s;
+    long long idx = grow;
+    if (sample) idx = (long long)(mix64(seed ^ mix64((unsigned long long)(*step_ctr) * 0x100000001ull + (unsigned long long)grow)) %
+                                  (unsigned long long)n);
+    const bool live = idx < n;
+    float tn[MLP_OUT];
+#pragma unroll
+    for (int k = 0; k < MLP_IN; k++) {
+        const float xv = live ? (X[idx * MLP_IN + k] - S.in_mean[k]) * S.in_rstd[k] : 0.f;
+        put_bf16(S.xn, s, k, MLP_IN, xv);
+        put_bf16(S.tr, TR_XT + k, s, 128, xv);
+    }
+#pragma unroll
+    for (int o = 0; o < MLP_OUT; o++) tn[o] = live ? (T[idx * MLP_OUT + o] - S.out_mean[o]) * S.out_rstd[o] : 0.f;
+    smem_to_tc();
+    const uint32_t tb = S.tbase;
+    uint32_t ph = 0;
+    bool ok = true;
+    // ---- layer 1 ----
+    if (tid == 0) { mma_k(tb, TM_Z1, S.xn, S.w1t, MLP_H, MLP_IN); tc_commit(&S.mbar); }
+    ok = mma_done(&S.mbar, ph) && ok;
+    for (int c = 0; c < MLP_H; c += 16) {
+        float v[16];
+        tmem_ld16(tmem_at(tb, 32 * warp, TM_Z1 + c), v);
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+            const float hv = silu(v[q] + S.b1[c + q]);
+            put_bf16(S.h, s, c + q, MLP_H, hv);
+            put_bf16(S.tr, TR_H1T + c + q, s, 128, hv);
+        }
+    }
+    smem_to_tc();
+    // ---- layer 2 ----
+    if (tid == 0) { mma_k(tb, TM_Z2, S.h, S.w2t, MLP_H, MLP_H); tc_commit(&S.mbar); }
+    ok = mma_done(&S.mbar, ph) && ok;
+    for (int c = 0; c < MLP_H; c += 16) {
+        float v[16];
+        tmem_ld16(tmem_at(tb, 32 * warp, TM_Z2 + c), v);
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+            const float hv = silu(v[q] + S.b2[c + q]);
+            put_bf16(S.h, s, c + q, MLP_H, hv);
+            put_bf16(S.tr, TR_H2T + c + q, s, 128, hv);
+        }
+    }
+    smem_to_tc();
+    // ---- layer 3 and the loss gradient: L = sum (y - t)^2 / (batch * 7) ----
+    if (tid == 0) { mma_k(tb, TM_Y, S.h, S.w3t, MLP_OUTP, MLP_H); tc_commit(&S.mbar); }
+    ok = mma_done(&S.mbar, ph) && ok;
+    {
+        float v[16];
+        tmem_ld16(tmem_at(tb, 32 * warp, TM_Y), v);
+        float l2 = 0.f;
+        const float gs = 2.0f / ((float)batch * (float)MLP_OUT);
+#pragma unroll
+        for (int o = 0; o < MLP_OUTP; o++) {
+            float dyv = 0.f;
+            if (o < MLP_OUT && live) {
+                const float d = v[o] + S.b3[o] - tn[o];
+                l2 += d * d;
+                dyv = gs * d;
+                atomicAdd(&S.gb3[o], dyv);
+            }
+            put_bf16(S.dy, s, o, MLP_OUTP, dyv);
+            put_bf16(S.dyt, o, s, 128, dyv);
+        }
+        for (int off = 16; off > 0; off >>= 1) l2 += __shfl_xor_sync(0xffffffffu, l2, off);
+        if ((tid & 31) == 0) atomicAdd(&S.loss, l2);
+    }
+    smem_to_tc();
+    // ---- dH2 = dY W3^T ----
+    if (tid == 0) { mma_k(tb, TM_DH, S.dy, S.w3, MLP_H, MLP_OUTP); tc_commit(&S.mbar); }
+    ok = mma_done(&S.mbar, ph) && ok;
+    for (int c = 0; c < MLP_H; c += 16) {
+        float dh[16], z[16];
+        tmem_ld16(tmem_at(tb, 32 * warp, TM_DH + c), dh);
+        tmem_ld16(tmem_at(tb, 32 * warp, TM_Z2 + c), z);
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+            const float dz = live ? dh[q] * silu_grad(z[q] + S.b2[c + q]) : 0.f;
+            atomicAdd(&S.gb2[c + q], dz);
+            put_bf16(S.h, s, c + q, MLP_H, dz);       // layer 3 is done with h2
+            put_bf16(S.dz2t, c + q, s, 128, dz);
+        }
+    }
+    smem_to_tc();
+    // ---- dH1 = dZ2 W2^T, dW3 = H2^T dY, dW2 = H1^T dZ2 ----
+    if (tid == 0) {
+        mma_k(tb, TM_DH, S.h, S.w2, MLP_H, MLP_H);
+        mma_k(tb, TM_G3, S.tr + TR_H2T * 256, S.dyt, MLP_OUTP, 128);
+        mma_k(tb, TM_G2, S.tr + TR_H1T * 256, S.dz2t, MLP_H, 128);
+        tc_commit(&S.mbar);
+    }
+    ok = mma_done(&S.mbar, ph) && ok;
+    for (int c = 0; c < MLP_H; c += 16) {
+        float dh[16], z[16];
+        tmem_ld16(tmem_at(tb, 32 * warp, TM_DH + c), dh);
+        tmem_ld16(tmem_at(tb, 32 * warp, TM_Z1 + c), z);
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+            const float dz = live ? dh[q] * silu_grad(z[q] + S.b1[c + q]) : 0.f;
+            atomicAdd(&S.gb1[c + q], dz);
+            put_bf16(S.tr, TR_DZ1T + c + q, s, 128, dz);
+        }
+    }
+    if (warp < 2) {  // TMEM lanes 0-63: rows i of dW3 and dW2
+        const int i = tid;
+        float g3[16];
+        tmem_ld16(tmem_at(tb, 32 * warp, TM_G3), g3);
+#pragma unroll
+        for (int o = 0; o < MLP_OUT; o++) atomicAdd(&grad[MP_W3 + i * MLP_OUT + o], g3[o]);
+        for (int c = 0; c < MLP_H; c += 16) {
+            float g2[16];
+            tmem_ld16(tmem_at(tb, 32 * warp, TM_G2 + c), g2);
+#pragma unroll
+            for (int q = 0; q < 16; q++) atomicAdd(&grad[MP_W2 + i * MLP_H + c + q], g2[q]);
+        }
+    }
+    smem_to_tc();
+    // ---- dW1 = X^T dZ1 ----
+    if (tid == 0) { mma_k(tb, TM_G1, S.tr + TR_XT * 256, S.tr + TR_DZ1T * 256, MLP_H, 128); tc_commit(&S.mbar); }
+    ok = mma_done(&S.mbar, ph) && ok;
+    if (warp == 0) {  // TMEM lanes 0-15: rows k of dW1
+        for (int c = 0; c < MLP_H; c += 16) {
+            float g1[16];
+            tmem_ld16(tmem_at(tb, 0, TM_G1 + c), g1);
+            if (tid < MLP_IN)
+#pragma unroll
+                for (int q = 0; q < 16; q++) atomicAdd(&grad[MP_W1 + tid * MLP_H + c + q], g1[q]);
+        }
+    }
+    __syncthreads();
+    for (int e = tid; e < MLP_H; e += 128) {
+        atomicAdd(&grad[MP_B1 + e], S.gb1[e]);
+        atomicAdd(&grad[MP_B2 + e], S.gb2[e]);
+    }
+    if (tid < MLP_OUT) atomicAdd(&grad[MP_B3 + tid], S.gb3[tid]);
+    if (tid == 0) atomicAdd(loss_acc, S.loss / ((float)batch * (float)MLP_OUT));
+    if (!ok && tid == 0 && status) atomicOr(status, ERR_TC_TIMEOUT);
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tb, MLP_TRAIN_TMEM_COLS);
+}
+
+// Adam on the trainable parameters, one CTA; the step counter advances at the end.  The
+// step's loss moves from the accumulator to loss_last.
+__global__ void __launch_bounds__(1024) k_mlp_adam(float *prm, float *grad, float *m, float *v, int *step_ctr, float lr,
+                                                   float *loss_acc, float *loss_last)
+{
+    const int t = *step_ctr + 1;
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    const float c1 = 1.0f / (1.0f - powf(b1, (float)t)), c2 = 1.0f / (1.0f - powf(b2, (float)t));
+    for (int p = threadIdx.x; p < MLP_TRAIN_PARAMS; p += blockDim.x) {
+        const float g = grad[p];
+        const float mm = b1 * m[p] + (1.0f - b1) * g;
+        const float vv = b2 * v[p] + (1.0f - b2) * g * g;
+        m[p] = mm;
+        v[p] = vv;
+        prm[p] -= lr * (mm * c1) / (sqrtf(vv * c2) + eps);
+        grad[p] = 0.f;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        *loss_last = *loss_acc;
+        *loss_acc = 0.f;
+        *step_ctr = t;
+    }
+}
+
+// per-column sums and sums of squares of a row-major n x w FP32 matrix, into double acc[2w]
+__global__ void k_colstats(const float *A, long long n, int w, double *acc)
+{
+    __shared__ double sm[2 * 32];
+    for (int c = threadIdx.x; c < 2 * w; c += blockDim.x) sm[c] = 0.0;
+    __syncthreads();
+    double ls[32], lq[32];
+    for (int c = 0; c < w; c++) { ls[c] = 0.0; lq[c] = 0.0; }
+    for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long long)gridDim.x * blockDim.x)
+        for (int c = 0; c < w; c++) {
+            const double x = A[r * w + c];
+            ls[c] += x;
+            lq[c] += x * x;
+        }
+    for (int c = 0; c < w; c++) {
+        atomicAdd(&sm[c], ls[c]);
+        atomicAdd(&sm[w + c], lq[c]);
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < 2 * w; c += blockDim.x) atomicAdd(&acc[c], sm[c]);
+}
+
 }  // namespace gy
 
 extern "C" gy_status gy_tc_gemm_bf16(const uint16_t *d_A, const uint16_t *d_B, float *d_C, int M, int N, int K,
@@ -342,4 +673,132 @@ extern "C" gy_status gy_mlp_forward(const float *d_params, const float *d_X, int
     k_mlp_forward<<<grid, 128, smem, static_cast<cudaStream_t>(stream)>>>(d_params, d_X, n, d_Y, d_status);
     note_launch(1);
     return cudaPeekAtLastError() == cudaSuccess ? GY_OK : GY_ERR_CUDA;
+}
+
+namespace {
+
+size_t train_smem() { return sizeof(gy::MlpTrainSmem) + 1024; }
+
+gy_status train_attr()
+{
+    static bool done = false;
+    if (done) return GY_OK;
+    if (cudaFuncSetAttribute(gy::k_mlp_train_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem()) !=
+        cudaSuccess)
+        return GY_ERR_CUDA;
+    done = true;
+    return GY_OK;
+}
+
+}  // namespace
+
+extern "C" gy_status gy_mlp_grad(const float *d_params, const float *d_X, const float *d_T, int64_t n, float *d_grad,
+                                 float *d_loss, int *d_status, void *stream)
+{
+    using namespace gy;
+    if (!d_params || !d_X || !d_T || !d_grad || !d_loss || n <= 0 || n % 128) return GY_ERR_ARG;
+    if (train_attr() != GY_OK) return GY_ERR_CUDA;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // the step counter is read only when sampling; a zero from the status word's neighbour
+    // is not needed: pass the loss word itself as an unused counter
+    k_mlp_train_tile<<<(unsigned)(n / 128), 128, train_smem(), s>>>(d_params, d_X, d_T, n, 0, 0ull,
+                                                                      reinterpret_cast<const int *>(d_loss), d_grad,
+                                                                      d_loss, (int)n, d_status);
+    note_launch(1);
+    return cudaPeekAtLastError() == cudaSuccess ? GY_OK : GY_ERR_CUDA;
+}
+
+extern "C" gy_status gy_mlp_train(float *d_params, const float *d_X, const float *d_T, int64_t n, int steps, int batch,
+                                  float lr, uint64_t seed, int init, float *loss_out, int *d_status, void *stream)
+{
+    using namespace gy;
+    if (!d_params || !d_X || !d_T || n < 1 || steps < 0 || batch < 128 || batch % 128 || !(lr > 0.f))
+        return GY_ERR_ARG;
+    if (train_attr() != GY_OK) return GY_ERR_CUDA;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int np = MP_COUNT;
+    std::vector<float> host(np, 0.0f);
+    if (cudaMemcpyAsync(host.data(), d_params, np * sizeof(float), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return GY_ERR_CUDA;
+    if (init) {
+        // normalisation from the data (per-column mean and standard deviation; constant
+        // columns keep a unit scale), weights uniform in +-sqrt(6 / (fan_in + fan_out)),
+        // biases zero
+        double *acc = nullptr;
+        if (cudaMalloc(&acc, 2 * (MLP_IN + MLP_OUT) * sizeof(double)) != cudaSuccess) return GY_ERR_NOMEM;
+        cudaMemsetAsync(acc, 0, 2 * (MLP_IN + MLP_OUT) * sizeof(double), s);
+        const int g = (int)std::min<long long>((n + 255) / 256, 1024);
+        k_colstats<<<g, 256, 0, s>>>(d_X, n, MLP_IN, acc);
+        k_colstats<<<g, 256, 0, s>>>(d_T, n, MLP_OUT, acc + 2 * MLP_IN);
+        note_launch(2);
+        std::vector<double> a(2 * (MLP_IN + MLP_OUT));
+        const cudaError_t e1 = cudaMemcpyAsync(a.data(), acc, a.size() * sizeof(double), cudaMemcpyDeviceToHost, s);
+        const cudaError_t e2 = cudaStreamSynchronize(s);
+        cudaFree(acc);
+        if (e1 != cudaSuccess || e2 != cudaSuccess) return GY_ERR_CUDA;
+        auto fill = [&](const double *sum, int w, int mean_off, int std_off) {
+            for (int c = 0; c < w; c++) {
+                const double mu = sum[c] / (double)n;
+                const double var = std::max(sum[w + c] / (double)n - mu * mu, 0.0);
+                double sd = std::sqrt(var);
+                if (!(sd > 1e-12 * std::max(1.0, std::fabs(mu)))) sd = 1.0;
+                host[mean_off + c] = (float)mu;
+                host[std_off + c] = (float)sd;
+            }
+        };
+        fill(a.data(), MLP_IN, MP_IN_MEAN, MP_IN_STD);
+        fill(a.data() + 2 * MLP_IN, MLP_OUT, MP_OUT_MEAN, MP_OUT_STD);
+        unsigned long long st = seed * 0x9E3779B97F4A7C15ull + 1ull;
+        auto uni = [&]() {  // uniform in [-1, 1)
+            st = st * 6364136223846793005ull + 1442695040888963407ull;
+            return (double)(st >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
+        };
+        auto init_w = [&](int off, int fin, int fout) {
+            const double b = std::sqrt(6.0 / (fin + fout));
+            for (int k = 0; k < fin * fout; k++) host[off + k] = (float)(b * uni());
+        };
+        init_w(MP_W1, MLP_IN, MLP_H);
+        init_w(MP_W2, MLP_H, MLP_H);
+        init_w(MP_W3, MLP_H, MLP_OUT);
+        for (int k = 0; k < MLP_H; k++) host[MP_B1 + k] = host[MP_B2 + k] = 0.f;
+        for (int k = 0; k < MLP_OUT; k++) host[MP_B3 + k] = 0.f;
+        if (cudaMemcpyAsync(d_params, host.data(), np * sizeof(float), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return GY_ERR_CUDA;
+    }
+    if (steps == 0) return GY_OK;
+    // optimizer state: gradient, two moments, step counter, loss words
+    float *buf = nullptr;
+    const size_t nf = 3 * (size_t)np + 8;
+    if (cudaMalloc(&buf, nf * sizeof(float)) != cudaSuccess) return GY_ERR_NOMEM;
+    cudaMemsetAsync(buf, 0, nf * sizeof(float), s);
+    float *grad = buf, *m1 = buf + np, *m2 = buf + 2 * np;
+    int *ctr = reinterpret_cast<int *>(buf + 3 * np);
+    float *loss_acc = buf + 3 * np + 1, *loss_last = buf + 3 * np + 2;
+    // one step captured as a graph and replayed
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    gy_status rc = GY_OK;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) rc = GY_ERR_CUDA;
+    if (rc == GY_OK) {
+        k_mlp_train_tile<<<(unsigned)(batch / 128), 128, train_smem(), s>>>(d_params, d_X, d_T, n, 1, seed, ctr, grad,
+                                                                              loss_acc, batch, d_status);
+        k_mlp_adam<<<1, 1024, 0, s>>>(d_params, grad, m1, m2, ctr, lr, loss_acc, loss_last);
+        if (cudaStreamEndCapture(s, &graph) != cudaSuccess) rc = GY_ERR_CUDA;
+    }
+    if (rc == GY_OK && cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) rc = GY_ERR_CUDA;
+    for (int k = 0; k < steps && rc == GY_OK; k++) {
+        if (cudaGraphLaunch(exec, s) != cudaSuccess) rc = GY_ERR_CUDA;
+        note_launch(2);
+    }
+    float lh = 0.f;
+    if (rc == GY_OK && (cudaMemcpyAsync(&lh, loss_last, sizeof(float), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                        cudaStreamSynchronize(s) != cudaSuccess))
+        rc = GY_ERR_CUDA;
+    if (loss_out) *loss_out = lh;
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    cudaFree(buf);
+    return rc;
 }

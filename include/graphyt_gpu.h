@@ -287,6 +287,22 @@ int64_t gy_mlp_param_count(void);
  * d_status (may be null) receives bit 4 if a tensor-core wait gave up. */
 gy_status gy_mlp_forward(const float *d_params, const float *d_X, int64_t n, float *d_Y, int *d_status, void *stream);
 
+/* Gradient of the mean squared error over rows [0, n) (n a multiple of 128), normalised
+ * targets: d_grad [gy_mlp_param_count()] and d_loss [1] receive += (zero them first).  The
+ * training kernel's own pass (BF16 tensor-core forward, backward and weight gradients), for
+ * checking it. */
+gy_status gy_mlp_grad(const float *d_params, const float *d_X, const float *d_T, int64_t n, float *d_grad,
+                      float *d_loss, int *d_status, void *stream);
+
+/* Train the MLP in place: steps Adam steps (lr, betas 0.9 / 0.999) on batches of `batch` rows
+ * (a multiple of 128) drawn with replacement from X [n][16] -> T [n][7] by a hash of (seed,
+ * step, row); the loss is the mean squared error of the normalised outputs.  init != 0 first
+ * sets the normalisation from the data and draws the weights (seeded).  Each step is one
+ * tensor-core kernel over the batch plus one Adam kernel, replayed from a CUDA graph; the call
+ * allocates its optimizer state and returns after the last step with its loss in *loss_out. */
+gy_status gy_mlp_train(float *d_params, const float *d_X, const float *d_T, int64_t n, int steps, int batch, float lr,
+                       uint64_t seed, int init, float *loss_out, int *d_status, void *stream);
+
 /* Number of kernels this library has launched in the process so far. */
 int64_t gy_kernel_launches(void);
 

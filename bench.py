@@ -59,8 +59,9 @@ MB_STEP_BYTES_PER_NODE = 312
 # the four status words
 STATS_D2H_BYTES = 16 * 8 * 8 + 4 * 4
 # the step's device scalars (dt, dt at the nodes, gravity x3, damping, friction, BC time, grid-BC
-# switch, body count, initial volume: 11 four-byte words), copied host-to-device every step
-STEP_SCALARS_H2D_BYTES = 11 * 4
+# switch, body count, initial volume, step index: 12 four-byte words), copied host-to-device
+# every step
+STEP_SCALARS_H2D_BYTES = 12 * 4
 
 
 def dist_env():

@@ -77,6 +77,14 @@ SIGNATURES = {
     "gy_mlp_param_count": (C.c_int64, []),
     "gy_mlp_forward": (C.c_int, [_vp, _vp, C.c_int64, _vp, _vp, _vp]),
     "gy_mlp_grad": (C.c_int, [_vp, _vp, _vp, C.c_int64, _vp, _vp, _vp, _vp]),
+    "gy_dp_log_begin": (C.c_int, [_vp, C.c_int64, C.c_int]),
+    "gy_dp_log_end": (C.c_int, [_vp]),
+    "gy_dp_log_count": (C.c_int, [_vp, _i64p]),
+    "gy_dp_log_read": (C.c_int, [_vp, _vp, _vp, C.c_int64]),
+    "gy_dp_surrogate_train": (C.c_int, [_vp, C.c_int, C.c_int, C.c_float, C.c_uint64, C.POINTER(C.c_float)]),
+    "gy_set_dp_surrogate": (C.c_int, [_vp, _vp, C.c_int, C.c_float]),
+    "gy_get_dp_surrogate": (C.c_int, [_vp, _vp]),
+    "gy_dp_surrogate_counts": (C.c_int, [_vp, _i64p, _i64p]),
     "gy_mlp_train": (C.c_int, [_vp, _vp, _vp, C.c_int64, C.c_int, C.c_int, C.c_float, C.c_uint64, C.c_int,
                                C.POINTER(C.c_float), _vp, _vp]),
     "gy_set_particle_temp": (C.c_int, [_vp, C.c_int64, _i64p, _dp]),

@@ -98,6 +98,18 @@ struct gy_solver {
     std::vector<StepGraph> graphs;          // captured steps, one per StepVariant
     float4 *d_pbc_val = nullptr;
     float *d_flaw = nullptr;                // flaw scale by insertion index, or null (every scale 1)
+    // learned Drucker-Prager surrogate: training-pair log, deferred particles, parameters
+    float *d_dplog = nullptr;               // [cap][16] inputs then [cap][7] targets
+    unsigned int *d_dplog_n = nullptr;
+    unsigned int dplog_cap = 0;
+    int dplog_every = 1;
+    bool dplog_on = false;
+    float4 *d_pend = nullptr;               // [n][2] deferred particles
+    unsigned int *d_pend_n = nullptr;
+    float *d_surr = nullptr;                // gy_mlp_param_count() floats
+    unsigned long long *d_surr_counts = nullptr;  // kept predictions, fallbacks
+    float surr_tol = 1e-4f;
+    bool surr_on = false;
     int *d_refkey0 = nullptr;
     DevMaterial *d_mats = nullptr;
     int *d_status = nullptr;
@@ -178,7 +190,8 @@ void free_device(gy_solver *h)
     }
     void *ptrs[] = {h->slab[0], h->slab[1], h->d_perm, h->d_seg, h->d_nseg, h->sort_mem, h->resort_mem, h->d_pbc_val,
                     h->d_refkey0, h->d_mats, h->d_status, h->d_stats, h->node_mem, h->d_cell_min,
-                    h->d_nidx[0], h->d_nidx[1], h->d_nidx[2], h->d_sc, h->d_therm, h->d_tnode, h->d_tset, h->d_flaw};
+                    h->d_nidx[0], h->d_nidx[1], h->d_nidx[2], h->d_sc, h->d_therm, h->d_tnode, h->d_tset, h->d_flaw,
+                    h->d_dplog, h->d_dplog_n, h->d_pend, h->d_pend_n, h->d_surr, h->d_surr_counts};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     h->d_sc = nullptr;
@@ -194,6 +207,15 @@ void free_device(gy_solver *h)
     h->skey_buf[0] = h->skey_buf[1] = nullptr;
     h->d_pbc_val = nullptr;
     h->d_flaw = nullptr;
+    h->d_dplog = nullptr;
+    h->d_dplog_n = nullptr;
+    h->dplog_cap = 0;
+    h->dplog_on = false;
+    h->d_pend = nullptr;
+    h->d_pend_n = nullptr;
+    h->d_surr = nullptr;
+    h->d_surr_counts = nullptr;
+    h->surr_on = false;
     h->d_refkey0 = nullptr;
     h->d_mats = nullptr;
     h->d_status = nullptr;
@@ -517,6 +539,7 @@ static DevMaterial to_dev(const gy_material &m)
     d.turb_stress = (float)m.turbStress;
     d.k_th = (float)m.thermalConductivity;
     d.c_th = (float)m.specificHeatCapacity;
+    d.phi_deg = (float)m.phi;
     d.model = m.model;
     d.rigid = m.isRigid ? 1 : 0;
     d.damage = m.isDamage ? 1 : 0;
@@ -874,6 +897,7 @@ static StepScalars make_scalars(const gy_solver *h, int step)
     sc.fixed_grid_bcs = h->prm.fixed_grid_bcs;
     sc.multi_body = h->multi ? 1 : 0;
     sc.init_volume = (float)(h->g.is3d ? h->psep * h->psep * h->psep : h->psep * h->psep);
+    sc.step = step;
     return sc;
 }
 
@@ -886,6 +910,18 @@ static StepArgs make_args(gy_solver *h)
     a.mats = h->d_mats;
     a.pbc_val = h->d_pbc_val;
     a.flaw = h->d_flaw;
+    if (h->dplog_on) {
+        a.dp.log_x = h->d_dplog;
+        a.dp.log_y = h->d_dplog + (size_t)h->dplog_cap * 16;
+        a.dp.log_n = h->d_dplog_n;
+        a.dp.log_cap = h->dplog_cap;
+        a.dp.log_every = h->dplog_every;
+    }
+    if (h->surr_on) {
+        a.dp.pend = h->d_pend;
+        a.dp.pend_n = h->d_pend_n;
+        a.dp.pend_cap = (unsigned int)h->n;
+    }
     a.status = h->d_status;
     a.stats = h->d_stats;
     return a;
@@ -942,9 +978,13 @@ static void issue_step(gy_solver *h, const StepVariant &v, cudaEvent_t *tev)
     if (tev) cudaEventRecord(tev[3], s);
     // (d) G2P + particle BCs + update + constitutive + damage, written in sorted order, with
     // the conservation sums of the updated state (their partials zeroed by the compaction)
+    if (h->surr_on) cudaMemsetAsync(h->d_pend_n, 0, sizeof(unsigned int), s);
     launch_g2p_update(src, dst, perm, skey, h->n, h->d_seg, nseg, h->g2p_grid, h->nb, a,
                       h->opt.track_normals != 0, h->opt.check_finite != 0, h->has_dp, s,
                       fused_thermal ? h->d_therm : nullptr, fused_thermal ? h->d_tnode : nullptr);
+    if (h->surr_on)
+        launch_dp_surrogate(dst, h->d_pend, h->d_pend_n, (unsigned int)h->n, h->d_mats, h->d_surr, h->d_sc, h->d_flaw,
+                            h->surr_tol, h->d_surr_counts, h->d_status, s);
     if (h->thermal && h->multi)
         launch_thermal_g2p(src, h->d_therm, perm, skey, h->n, h->d_seg, nseg, h->d_tnode, h->nb, a, s);
     else if (h->thermal)
@@ -1526,3 +1566,149 @@ gy_status gy_resort_keys(const int *keys, const int *prev_sorted, int64_t n, int
 }
 
 }  // extern "C"
+
+// ---- learned Drucker-Prager surrogate ----------------------------------------------------
+
+extern "C" int64_t gy_mlp_param_count(void);
+extern "C" gy_status gy_mlp_train(float *d_params, const float *d_X, const float *d_T, int64_t n, int steps, int batch,
+                                  float lr, uint64_t seed, int init, float *loss_out, int *d_status, void *stream);
+
+gy_status gy_dp_log_begin(gy_solver *h, int64_t cap, int every)
+{
+    if (!h || cap < 1 || cap > 0x7fffffff || every < 1) return GY_ERR_ARG;
+    if (!h->initialized) return fail(h, GY_ERR_STATE, "gy_dp_log_begin needs an initialized solver");
+    cudaSetDevice(h->device);
+    CK(h, cudaStreamSynchronize(h->stream));
+    if (h->d_dplog && h->dplog_cap != (unsigned int)cap) {
+        cudaFree(h->d_dplog);
+        h->d_dplog = nullptr;
+    }
+    gy_status st;
+    if (!h->d_dplog && (st = dalloc(h, &h->d_dplog, (size_t)cap * (16 + 7)))) return st;
+    if (!h->d_dplog_n && (st = dalloc(h, &h->d_dplog_n, 1))) return st;
+    CK(h, cudaMemsetAsync(h->d_dplog_n, 0, sizeof(unsigned int), h->stream));
+    h->dplog_cap = (unsigned int)cap;
+    h->dplog_every = every;
+    h->dplog_on = true;
+    drop_graphs(h);
+    return GY_OK;
+}
+
+gy_status gy_dp_log_end(gy_solver *h)
+{
+    if (!h) return GY_ERR_ARG;
+    if (h->dplog_on) {
+        h->dplog_on = false;
+        drop_graphs(h);
+    }
+    return GY_OK;
+}
+
+static gy_status dplog_count(gy_solver *h, unsigned int *out)
+{
+    unsigned int c = 0;
+    if (h->d_dplog_n) {
+        CK(h, cudaMemcpyAsync(&c, h->d_dplog_n, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
+    }
+    *out = std::min(c, h->dplog_cap);
+    return GY_OK;
+}
+
+gy_status gy_dp_log_count(gy_solver *h, int64_t *count)
+{
+    if (!h || !count) return GY_ERR_ARG;
+    unsigned int c = 0;
+    gy_status st = dplog_count(h, &c);
+    *count = c;
+    return st;
+}
+
+gy_status gy_dp_log_read(gy_solver *h, float *x16, float *y7, int64_t max_records)
+{
+    if (!h || !x16 || !y7 || max_records < 0) return GY_ERR_ARG;
+    unsigned int c = 0;
+    gy_status st = dplog_count(h, &c);
+    if (st) return st;
+    const size_t m = (size_t)std::min<int64_t>(c, max_records);
+    if (m == 0) return GY_OK;
+    CK(h, cudaMemcpyAsync(x16, h->d_dplog, m * 16 * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaMemcpyAsync(y7, h->d_dplog + (size_t)h->dplog_cap * 16, m * 7 * sizeof(float), cudaMemcpyDeviceToHost,
+                          h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return GY_OK;
+}
+
+static gy_status surr_alloc(gy_solver *h)
+{
+    gy_status st;
+    if (!h->d_surr && (st = dalloc(h, &h->d_surr, (size_t)gy_mlp_param_count()))) return st;
+    if (!h->d_surr_counts) {
+        if ((st = dalloc(h, &h->d_surr_counts, 2))) return st;
+        CK(h, cudaMemsetAsync(h->d_surr_counts, 0, 2 * sizeof(unsigned long long), h->stream));
+    }
+    return GY_OK;
+}
+
+gy_status gy_dp_surrogate_train(gy_solver *h, int steps, int batch, float lr, uint64_t seed, float *loss_out)
+{
+    if (!h || steps < 0 || batch < 128 || batch % 128 || !(lr > 0.f)) return GY_ERR_ARG;
+    cudaSetDevice(h->device);
+    unsigned int c = 0;
+    gy_status st = dplog_count(h, &c);
+    if (st) return st;
+    if (c == 0) return fail(h, GY_ERR_STATE, "no logged Drucker-Prager returns to train on (gy_dp_log_begin)");
+    if ((st = surr_alloc(h))) return st;
+    const float *X = h->d_dplog, *T = h->d_dplog + (size_t)h->dplog_cap * 16;
+    st = gy_mlp_train(h->d_surr, X, T, c, steps, batch, lr, seed, 1, loss_out, h->d_status, h->stream);
+    if (st) return fail(h, st, "surrogate training failed");
+    return GY_OK;
+}
+
+gy_status gy_set_dp_surrogate(gy_solver *h, const float *params, int on, float tol)
+{
+    if (!h || !(tol > 0.f)) return GY_ERR_ARG;
+    if (!h->initialized) return fail(h, GY_ERR_STATE, "gy_set_dp_surrogate needs an initialized solver");
+    cudaSetDevice(h->device);
+    gy_status st;
+    if ((st = surr_alloc(h))) return st;
+    if (params) {
+        CK(h, cudaMemcpyAsync(h->d_surr, params, (size_t)gy_mlp_param_count() * sizeof(float), cudaMemcpyHostToDevice,
+                              h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
+    }
+    if (on && !h->d_pend) {
+        if ((st = dalloc(h, &h->d_pend, (size_t)h->cap * 2))) return st;
+        if ((st = dalloc(h, &h->d_pend_n, 1))) return st;
+        CK(h, cudaMemsetAsync(h->d_pend_n, 0, sizeof(unsigned int), h->stream));
+    }
+    h->surr_tol = tol;
+    if ((on != 0) != h->surr_on) {
+        h->surr_on = on != 0;
+        drop_graphs(h);
+    }
+    return GY_OK;
+}
+
+gy_status gy_get_dp_surrogate(gy_solver *h, float *params)
+{
+    if (!h || !params) return GY_ERR_ARG;
+    if (!h->d_surr) return fail(h, GY_ERR_STATE, "no surrogate parameters");
+    CK(h, cudaMemcpyAsync(params, h->d_surr, (size_t)gy_mlp_param_count() * sizeof(float), cudaMemcpyDeviceToHost,
+                          h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return GY_OK;
+}
+
+gy_status gy_dp_surrogate_counts(gy_solver *h, int64_t *kept, int64_t *fallback)
+{
+    if (!h || !kept || !fallback) return GY_ERR_ARG;
+    unsigned long long c[2] = {0, 0};
+    if (h->d_surr_counts) {
+        CK(h, cudaMemcpyAsync(c, h->d_surr_counts, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
+    }
+    *kept = (int64_t)c[0];
+    *fallback = (int64_t)c[1];
+    return GY_OK;
+}

@@ -59,6 +59,7 @@ struct DevMaterial {
     float gk_logk;              // log(k) for e_min = (V k)^(-1/m)
     float turb_stress;
     float k_th, c_th;           // thermal conductivity, specific heat capacity
+    float phi_deg;              // friction angle in degrees (an input of the learned surrogate)
     int model, rigid, damage, damage_model;
 };
 constexpr int MAX_MATERIALS = 4096;  // a batch of independent instances carries one per instance
@@ -95,6 +96,7 @@ struct StepScalars {
     int fixed_grid_bcs;
     int multi_body;
     float init_volume;        // psep^3 (psep^2 in 2D): volume before the first update
+    int step;                 // the step index (sampling of logged Drucker-Prager returns)
 };
 
 // ---------------------------------------------------------------------------------------

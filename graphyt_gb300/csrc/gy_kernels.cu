@@ -85,6 +85,27 @@ __device__ __forceinline__ void store_state(const PView &P, long long i, const P
 }
 
 
+// L2 prefetch of the segment a CTA takes next: the window of PF_WINDOW source slots that
+// starts at the slot of the segment's first particle (the slab is in the order of the last
+// sort, so a segment's particles sit close together there), for the fields [f0, f1), one
+// bulk prefetch per field issued by thread 0.  A hint only: the window stays inside the
+// slab, and a short segment costs some L2 space, not results.
+constexpr long long PF_WINDOW = 512;
+__device__ __forceinline__ void prefetch_next_segment(const PView &P, const int *perm, const int *seg_start, int nseg,
+                                                      int next, int f0, int f1)
+{
+    if (threadIdx.x != 0 || next >= nseg) return;
+    const long long s = seg_start[next];
+    long long j0 = perm ? (long long)perm[s] : s;
+    j0 &= ~3ll;  // 16-byte aligned
+    long long len = min(PF_WINDOW, P.cap - j0);
+    len &= ~3ll;
+    if (len <= 0) return;
+    for (int f = f0; f < f1; f++)
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(&P.f(f, j0)), "r"((unsigned)(len * 4))
+                     : "memory");
+}
+
 // ---------------------------------------------------------------------------------------
 // Single-body P2G through a shared-memory node tile.  Gravity is added per node in the
 // solve as m_node * g, which equals sum_p w m_p g (Extrapolation.cpp:226-278).
@@ -247,6 +268,8 @@ __global__ void __launch_bounds__(PC_THREADS, GY_PC_MINB) k_p2g_cols(PView P, co
     const bool scatter_lane = lane < 27;
     const float2 z2 = make_float2(0.f, 0.f);
     for (int sgi = blockIdx.x; sgi < nseg; sgi += gridDim.x) {
+        prefetch_next_segment(P, perm, seg_start, nseg, sgi + gridDim.x, PF_OX, PF_S5 + 1);
+        prefetch_next_segment(P, perm, seg_start, nseg, sgi + gridDim.x, PF_RHO, PF_MASS + 1);
         const long long start = seg_start[sgi];
         const int blk = seg_block(skey, start);
         int bx, by, bz;
@@ -485,6 +508,8 @@ __global__ void __launch_bounds__(PP_THREADS, 4) k_p2g_planes(PView P, const int
     const int grp = lane / 3, kk = lane - 3 * grp;      // lanes 30, 31: group 10, no run
     const float2 z2 = make_float2(0.f, 0.f);
     for (int sgi = blockIdx.x; sgi < nseg; sgi += gridDim.x) {
+        prefetch_next_segment(P, perm, seg_start, nseg, sgi + gridDim.x, PF_OX, PF_S5 + 1);
+        prefetch_next_segment(P, perm, seg_start, nseg, sgi + gridDim.x, PF_RHO, PF_MASS + 1);
         const long long start = seg_start[sgi];
         const int blk = seg_block(skey, start);
         int bx, by, bz;
@@ -1433,12 +1458,61 @@ __device__ __forceinline__ void renorm(float &o, int &c, float lp)
     }
 }
 
+// The Drucker-Prager + damage update of one particle with the learned surrogate's hooks
+// (DpHooks): a yielding particle without a BC is deferred to the surrogate pass when that is
+// on (its stress, plastic strain and damage left as they were; returns true), else the exact
+// return mapping runs and, when logging, the yielding particles of the sample record their
+// training pair; the damage update follows.
+__device__ __forceinline__ bool dp_hooked(Constit &c, const DevMaterial &M, float dt, int is3d, const StepArgs &a,
+                                       int pid, int step, long long slot, int bct)
+{
+    float t[6];
+    const bool yields = is3d && dp_trial_yields(c, M, dt, t);
+    if (yields && a.dp.pend && bct == 0) {
+        const unsigned int e = atomicAdd(a.dp.pend_n, 1u);
+        if (e < a.dp.pend_cap) {
+            a.dp.pend[2 * e] = make_float4(__int_as_float((int)slot), c.r[0] * dt, c.r[1] * dt, c.r[2] * dt);
+            a.dp.pend[2 * e + 1] = make_float4(c.r[3] * dt, c.r[4] * dt, c.r[5] * dt, 0.f);
+            return true;
+        }
+    }
+    float s0[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) s0[k] = c.s[k];
+    const float eq0 = c.eqps, d0 = c.dmg;
+    cm_drucker_prager(c, M, dt);
+    if (yields && a.dp.log_x && ((unsigned)(pid + step) % (unsigned)a.dp.log_every) == 0u) {
+        const unsigned int e = atomicAdd(a.dp.log_n, 1u);
+        if (e < a.dp.log_cap) {
+            float *x = a.dp.log_x + (size_t)e * 16;
+            float *y = a.dp.log_y + (size_t)e * 7;
+#pragma unroll
+            for (int k = 0; k < 6; k++) {
+                x[k] = c.r[k] * dt;
+                x[6 + k] = s0[k];
+                y[k] = c.s[k] - t[k];
+            }
+            x[12] = eq0;
+            x[13] = d0;
+            x[14] = M.cohesion;
+            x[15] = M.phi_deg;
+            y[6] = c.eqps - eq0;
+        }
+    }
+    if (M.damage && M.damage_model == 1) {
+        if (is3d) dm_grady_kipp3(c, M, dt, a.flaw, pid);
+        else dm_grady_kipp2(c, M, dt, a.flaw, pid);
+    }
+    return false;
+}
+
 // Everything after the G2P sums, for one particle: particle BCs, update, constitutive model,
 // damage, periodic wrap and the new cell key (TimeIntegration.cpp:11-296).  c0 is the cell of
-// the particle's first stencil node before the update.
+// the particle's first stencil node before the update; slot is where G2P writes the particle.
 template <bool HAS_DP>
 __device__ __forceinline__ void update_after_g2p(PState &st, const int c0[3], float acc[3], float vg[3],
-                                                 const float L[3][3], const StepArgs &a, bool check_finite)
+                                                 const float L[3][3], const StepArgs &a, bool check_finite,
+                                                 long long slot)
 {
     const GridGeom &g = a.g;
     const StepScalars sc = *a.sc;
@@ -1485,7 +1559,10 @@ __device__ __forceinline__ void update_after_g2p(PState &st, const int c0[3], fl
     if (!(st.info & INFO_RIGID)) {
         const DevMaterial &M = a.mats[info_mat(st.info)];
         if (HAS_DP) {
-            constitutive_update(c, M, dt, g.is3d, a.flaw, st.pid);
+            if (M.model == 4 && (a.dp.pend || a.dp.log_x))
+                dp_hooked(c, M, dt, g.is3d, a, st.pid, sc.step, slot, bct);
+            else
+                constitutive_update(c, M, dt, g.is3d, a.flaw, st.pid);
         } else {
             if (M.model == 1) cm_elastic(c, M, dt);
             else if (M.model == 2) cm_newtonian(c, M.K, M.viscosity, dt, g.is3d, false);
@@ -1641,6 +1718,7 @@ __global__ void __launch_bounds__(GY_G2P_THREADS, THERMAL ? GY_G2P_MINB_TH : GY_
 #pragma unroll
     for (int k = 0; k < NSTAT; k++) s_st[k][tid] = 0.f;  // each thread's own column
     for (int sgi = blockIdx.x; sgi < nseg; sgi += gridDim.x) {
+        prefetch_next_segment(src, perm, seg_start, nseg, sgi + gridDim.x, PF_OX, (HAS_DP ? PF_SMAX : PF_PID) + 1);
         const long long start = seg_start[sgi];
         const int blk = seg_block(skey, start);
         int bx, by, bz;
@@ -1809,7 +1887,7 @@ __global__ void __launch_bounds__(GY_G2P_THREADS, THERMAL ? GY_G2P_MINB_TH : GY_
                 int c0[3];
                 decode_key(st.key, g, c0[0], c0[1], c0[2]);
                 if (!g.is3d) c0[2] = 0;
-                update_after_g2p<HAS_DP>(st, c0, acc, vg, L, a, check_finite != 0);
+                update_after_g2p<HAS_DP>(st, c0, acc, vg, L, a, check_finite != 0, i);
                 store_state<HAS_DP>(dst, i, st);
                 if (THERMAL) therm[st.pid] = make_float4(th.x + trate * a.sc->dt, gtx, gty, gtz);
                 if (a.stats) particle_stats(s_st, st);
@@ -1845,6 +1923,7 @@ __global__ void __launch_bounds__(GY_G2PM_THREADS, GY_G2PM_MINB) k_g2p_multi_til
 #pragma unroll
     for (int k = 0; k < NSTAT; k++) s_st[k][tid] = 0.f;  // each thread's own column
     for (int sgi = blockIdx.x; sgi < nseg; sgi += gridDim.x) {
+        prefetch_next_segment(src, perm, seg_start, nseg, sgi + gridDim.x, PF_OX, (HAS_DP ? PF_SMAX : PF_PID) + 1);
         const long long start = seg_start[sgi];
         const int blk = seg_block(skey, start);
         int bx, by, bz;
@@ -1975,7 +2054,7 @@ __global__ void __launch_bounds__(GY_G2PM_THREADS, GY_G2PM_MINB) k_g2p_multi_til
                 int c0[3];
                 decode_key(st.key, g, c0[0], c0[1], c0[2]);
                 if (!g.is3d) c0[2] = 0;
-                update_after_g2p<HAS_DP>(st, c0, acc, vg, L, a, check_finite != 0);
+                update_after_g2p<HAS_DP>(st, c0, acc, vg, L, a, check_finite != 0, i);
                 store_state<HAS_DP>(dst, i, st);
                 if (NRM) {
                     dst.f(PF_NX, i) = nrm[0];

@@ -42,6 +42,23 @@ struct NodeBufs {
     int *active_count;            // nodes with mass (stats)
 };
 
+// Hooks of the learned Drucker-Prager surrogate into the step (every pointer null when off).
+// Logging: the exact return mapping records, for particles that yield and whose
+// (insertion index + step) is a multiple of log_every, the MLP input (strain increment,
+// previous stress, plastic strain, damage, cohesion, friction angle) and target (stress
+// minus the elastic trial stress, plastic strain increment).  Deferral: a yielding particle
+// without a BC goes to the pending list (slot and strain increment) with its stress left at
+// the previous value; the surrogate pass finishes its return mapping and damage.
+struct DpHooks {
+    float *log_x, *log_y;         // [log_cap][16], [log_cap][7]
+    unsigned int *log_n;          // records claimed (those past log_cap are dropped)
+    unsigned int log_cap;
+    int log_every;
+    float4 *pend;                 // [pend_cap][2]: (slot bits, de0, de1, de2), (de3, de4, de5, -)
+    unsigned int *pend_n;
+    unsigned int pend_cap;
+};
+
 struct StepArgs {
     GridGeom g;
     const StepScalars *sc;   // per-step scalars in device memory (one small copy per step)
@@ -51,6 +68,7 @@ struct StepArgs {
     const float *flaw;       // Grady-Kipp activation strain scale by pid, or null (every scale 1)
     int *status;
     double *stats;           // STATS_SLOTS x 8 conservation partials written by G2P, or null
+    DpHooks dp;              // learned-surrogate logging / deferral (zero when off)
 };
 
 // partials of the conservation sums (mass, momentum, kinetic and strain energy); the host
@@ -102,6 +120,10 @@ void launch_g2p_update(const PView &src, const PView &dst, const int *perm, cons
                        const float2 *tnode = nullptr);
 int g2p_blocks_per_sm(bool has_dp);
 int p2g_blocks_per_sm();
+// the learned surrogate's pass over the particles G2P deferred (gy_mlp.cu)
+void launch_dp_surrogate(const PView &P, const float4 *pend, const unsigned int *pend_n, unsigned int cap,
+                         const DevMaterial *mats, const float *prm, const StepScalars *scp, const float *flaw, float tol,
+                         unsigned long long *counts, int *status, cudaStream_t s);
 void launch_body_tables(const PView &p, long long n, const StepArgs &a, int *cell_min, int nbody,
                         const int *refkeys, cudaStream_t s);
 void launch_body_assign(const NodeBufs &nb, const StepArgs &a, const int *cell_min, int nbody,

@@ -9,6 +9,7 @@
 
 #include "../../include/graphyt_gpu.h"
 #include "gy_kernels.cuh"
+#include "gy_physics.cuh"
 #include "gy_tc.cuh"
 
 namespace gy {
@@ -629,6 +630,146 @@ __global__ void k_colstats(const float *A, long long n, int w, double *acc)
     for (int c = threadIdx.x; c < 2 * w; c += blockDim.x) atomicAdd(&acc[c], sm[c]);
 }
 
+// ---------------------------------------------------------------------------------------
+// The surrogate pass of a step: the particles G2P deferred (yielding Drucker-Prager particles,
+// their stress still the previous step's) in tiles of 128.  Per particle the MLP predicts the
+// return from the elastic trial stress -- stress = trial + predicted correction, plastic
+// strain + predicted increment -- and the prediction is kept when the yield function there is
+// within tol x cohesion of zero (the exact mapping lands on zero) and the increment is not
+// negative; the plastic strain tensor then follows the flow direction of the trial deviator
+// with the multiplier the increment implies (ConstitutiveModels.cpp:402-416).  Otherwise
+// the exact return mapping runs.  The Grady-Kipp update follows in both cases.
+__global__ void __launch_bounds__(128) k_dp_surrogate(PView P, const float4 *pend, const unsigned int *pend_n,
+                                                      unsigned int cap, const DevMaterial *mats, const float *prm,
+                                                      const StepScalars *scp, const float *flaw, float tol,
+                                                      unsigned long long *counts, int *status)
+{
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    MlpSmem &S = *reinterpret_cast<MlpSmem *>(smem_raw);
+    mlp_begin(S, prm);
+    const unsigned int cnt = min(*pend_n, cap);
+    const float dt = scp->dt;
+    uint32_t phase = 0;
+    bool ok = true;
+    unsigned int acc = 0, fb = 0;
+    const unsigned int tiles = (cnt + 127u) / 128u;
+    for (unsigned int tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+        const unsigned int e = tile * 128u + threadIdx.x;
+        const bool live = e < cnt;
+        Constit c;
+        long long slot = 0;
+        float de[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        int mat = 0, pid = 0;
+        if (live) {
+            const float4 q0 = pend[2 * e], q1 = pend[2 * e + 1];
+            slot = (long long)__float_as_int(q0.x);
+            de[0] = q0.y; de[1] = q0.z; de[2] = q0.w; de[3] = q1.x; de[4] = q1.y; de[5] = q1.z;
+#pragma unroll
+            for (int k = 0; k < 6; k++) {
+                c.s[k] = P.f(PF_S0 + k, slot);
+                c.ep[k] = P.f(PF_EP0 + k, slot);
+                c.r[k] = de[k] / dt;
+                c.e[k] = 0.f;
+            }
+            c.eqps = P.f(PF_EQPS, slot);
+            c.dmg = P.f(PF_DMG, slot);
+            c.smax = P.f(PF_SMAX, slot);
+            c.mass = P.f(PF_MASS, slot);
+            c.rho = P.f(PF_RHO, slot);
+            mat = info_mat((uint32_t)P.ii(PF_INFO, slot));
+            pid = P.ii(PF_PID, slot);
+        }
+        const DevMaterial &M = mats[mat];
+        float x[MLP_IN];
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            x[k] = de[k];
+            x[6 + k] = live ? c.s[k] : 0.f;
+        }
+        x[12] = live ? c.eqps : 0.f;
+        x[13] = live ? c.dmg : 0.f;
+        x[14] = M.cohesion;
+        x[15] = M.phi_deg;
+        if (!live) {
+#pragma unroll
+            for (int k = 0; k < MLP_IN; k++) x[k] = S.in_mean[k];
+        }
+        mlp_put_input(S, threadIdx.x, x);
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        float y[MLP_OUT];
+        ok = mlp_forward_tile(S, phase, y);
+        if (live) {
+            float t[6];
+            dp_trial_yields(c, M, dt, t);
+            float sp[6];
+#pragma unroll
+            for (int k = 0; k < 6; k++) sp[k] = t[k] + y[k];
+            const float deq = y[6];
+            const float res = dp_residual(sp, c.eqps + deq, M);
+            if (ok && deq >= 0.f && fabsf(res) <= tol * M.cohesion) {
+                const float I1 = (1.0f / 3.0f) * (t[0] + t[1] + t[2]);
+                const float sd[6] = {t[0] - I1, t[1] - I1, t[2] - I1, t[3], t[4], t[5]};
+                const float J2 = 0.5f * (sd[0] * sd[0] + sd[1] * sd[1] + sd[2] * sd[2] + 2.0f * sd[3] * sd[3] +
+                                         2.0f * sd[4] * sd[4] + 2.0f * sd[5] * sd[5]);
+                const float dL = deq / M.xi, hj = J2 > 0.f ? 0.5f / J2 : 0.f;
+#pragma unroll
+                for (int k = 0; k < 6; k++) {
+                    c.s[k] = sp[k];
+                    c.ep[k] += dL * (hj * sd[k] + (k < 3 ? M.eta_bar / 3.0f : 0.f));
+                }
+                c.eqps += deq;
+                acc++;
+            } else {
+                cm_drucker_prager(c, M, dt);
+                fb++;
+            }
+            if (M.damage && M.damage_model == 1) dm_grady_kipp3(c, M, dt, flaw, pid);
+#pragma unroll
+            for (int k = 0; k < 6; k++) {
+                P.f(PF_S0 + k, slot) = c.s[k];
+                P.f(PF_EP0 + k, slot) = c.ep[k];
+            }
+            P.f(PF_EQPS, slot) = c.eqps;
+            P.f(PF_DMG, slot) = c.dmg;
+            P.f(PF_SMAX, slot) = c.smax;
+        }
+    }
+    // counts of kept predictions and of fallbacks to the exact mapping
+    for (int off = 16; off > 0; off >>= 1) {
+        acc += __shfl_xor_sync(0xffffffffu, acc, off);
+        fb += __shfl_xor_sync(0xffffffffu, fb, off);
+    }
+    if ((threadIdx.x & 31) == 0 && counts) {
+        atomicAdd(&counts[0], (unsigned long long)acc);
+        atomicAdd(&counts[1], (unsigned long long)fb);
+    }
+    if (!ok && threadIdx.x == 0 && status) atomicOr(status, ERR_TC_TIMEOUT);
+    mlp_end(S);
+}
+
+void launch_dp_surrogate(const PView &P, const float4 *pend, const unsigned int *pend_n, unsigned int cap,
+                         const DevMaterial *mats, const float *prm, const StepScalars *scp, const float *flaw, float tol,
+                         unsigned long long *counts, int *status, cudaStream_t s)
+{
+    const size_t smem = sizeof(MlpSmem) + 1024;
+    static int grid = 0;
+    if (grid == 0) {
+        cudaFuncSetAttribute(k_dp_surrogate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        int dev = 0, sms = 1, b = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_dp_surrogate, 128, smem);
+        // every resident CTA holds MLP_TMEM_COLS of the 512 tensor-memory columns
+        b = std::max(1, std::min(b, (int)(512 / MLP_TMEM_COLS)));
+        grid = sms * b;
+    }
+    k_dp_surrogate<<<grid, 128, smem, s>>>(P, pend, pend_n, cap, mats, prm, scp, flaw, tol, counts, status);
+    note_launch(1);
+}
+
 }  // namespace gy
 
 extern "C" gy_status gy_tc_gemm_bf16(const uint16_t *d_A, const uint16_t *d_B, float *d_C, int M, int N, int K,
@@ -768,37 +909,50 @@ extern "C" gy_status gy_mlp_train(float *d_params, const float *d_X, const float
             return GY_ERR_CUDA;
     }
     if (steps == 0) return GY_OK;
+    // the steps run on a private stream (a graph cannot be captured on the legacy default
+    // stream), ordered after the caller's work and waited for before returning
+    cudaStream_t ts = nullptr;
+    cudaEvent_t ev = nullptr;
+    if (cudaStreamCreateWithFlags(&ts, cudaStreamNonBlocking) != cudaSuccess) return GY_ERR_CUDA;
+    if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
+        cudaStreamDestroy(ts);
+        return GY_ERR_CUDA;
+    }
+    gy_status rc = GY_OK;
+    if (cudaEventRecord(ev, s) != cudaSuccess || cudaStreamWaitEvent(ts, ev, 0) != cudaSuccess) rc = GY_ERR_CUDA;
     // optimizer state: gradient, two moments, step counter, loss words
     float *buf = nullptr;
     const size_t nf = 3 * (size_t)np + 8;
-    if (cudaMalloc(&buf, nf * sizeof(float)) != cudaSuccess) return GY_ERR_NOMEM;
-    cudaMemsetAsync(buf, 0, nf * sizeof(float), s);
+    if (rc == GY_OK && cudaMalloc(&buf, nf * sizeof(float)) != cudaSuccess) rc = GY_ERR_NOMEM;
+    if (rc == GY_OK && cudaMemsetAsync(buf, 0, nf * sizeof(float), ts) != cudaSuccess) rc = GY_ERR_CUDA;
     float *grad = buf, *m1 = buf + np, *m2 = buf + 2 * np;
     int *ctr = reinterpret_cast<int *>(buf + 3 * np);
     float *loss_acc = buf + 3 * np + 1, *loss_last = buf + 3 * np + 2;
     // one step captured as a graph and replayed
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    gy_status rc = GY_OK;
-    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) rc = GY_ERR_CUDA;
+    if (rc == GY_OK && cudaStreamBeginCapture(ts, cudaStreamCaptureModeThreadLocal) != cudaSuccess) rc = GY_ERR_CUDA;
     if (rc == GY_OK) {
-        k_mlp_train_tile<<<(unsigned)(batch / 128), 128, train_smem(), s>>>(d_params, d_X, d_T, n, 1, seed, ctr, grad,
-                                                                              loss_acc, batch, d_status);
-        k_mlp_adam<<<1, 1024, 0, s>>>(d_params, grad, m1, m2, ctr, lr, loss_acc, loss_last);
-        if (cudaStreamEndCapture(s, &graph) != cudaSuccess) rc = GY_ERR_CUDA;
+        k_mlp_train_tile<<<(unsigned)(batch / 128), 128, train_smem(), ts>>>(d_params, d_X, d_T, n, 1, seed, ctr, grad,
+                                                                               loss_acc, batch, d_status);
+        k_mlp_adam<<<1, 1024, 0, ts>>>(d_params, grad, m1, m2, ctr, lr, loss_acc, loss_last);
+        if (cudaStreamEndCapture(ts, &graph) != cudaSuccess) rc = GY_ERR_CUDA;
     }
     if (rc == GY_OK && cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) rc = GY_ERR_CUDA;
     for (int k = 0; k < steps && rc == GY_OK; k++) {
-        if (cudaGraphLaunch(exec, s) != cudaSuccess) rc = GY_ERR_CUDA;
+        if (cudaGraphLaunch(exec, ts) != cudaSuccess) rc = GY_ERR_CUDA;
         note_launch(2);
     }
     float lh = 0.f;
-    if (rc == GY_OK && (cudaMemcpyAsync(&lh, loss_last, sizeof(float), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-                        cudaStreamSynchronize(s) != cudaSuccess))
+    if (rc == GY_OK && (cudaMemcpyAsync(&lh, loss_last, sizeof(float), cudaMemcpyDeviceToHost, ts) != cudaSuccess ||
+                        cudaStreamSynchronize(ts) != cudaSuccess))
         rc = GY_ERR_CUDA;
+    if (rc != GY_OK) cudaStreamSynchronize(ts);
     if (loss_out) *loss_out = lh;
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
-    cudaFree(buf);
+    if (buf) cudaFree(buf);
+    cudaEventDestroy(ev);
+    cudaStreamDestroy(ts);
     return rc;
 }

@@ -193,6 +193,40 @@ __device__ __forceinline__ void cm_drucker_prager(Constit &c, const DevMaterial 
     }
 }
 
+// The elastic trial stress of the Drucker-Prager update (ConstitutiveModels.cpp:254-300) and
+// its yield test (:300-307: with damage on, only compressive states yield); t receives the
+// trial stress.
+__device__ __forceinline__ bool dp_trial_yields(const Constit &c, const DevMaterial &M, float dt, float t[6])
+{
+    const float G = M.G, K = M.K;
+    const float vol = 0.3333f * (c.r[0] + c.r[1] + c.r[2]);
+    t[0] = c.s[0] + (2.0f * G * (c.r[0] - vol) + 3.0f * K * vol) * dt;
+    t[1] = c.s[1] + (2.0f * G * (c.r[1] - vol) + 3.0f * K * vol) * dt;
+    t[2] = c.s[2] + (2.0f * G * (c.r[2] - vol) + 3.0f * K * vol) * dt;
+    t[3] = c.s[3] + (2.0f * G * c.r[3]) * dt;
+    t[4] = c.s[4] + (2.0f * G * c.r[4]) * dt;
+    t[5] = c.s[5] + (2.0f * G * c.r[5]) * dt;
+    const float I1 = (1.0f / 3.0f) * (t[0] + t[1] + t[2]);
+    const float sxx = t[0] - I1, syy = t[1] - I1, szz = t[2] - I1;
+    const float J2 = 0.5f * (sxx * sxx + syy * syy + szz * szz + 2.0f * t[3] * t[3] + 2.0f * t[4] * t[4] +
+                             2.0f * t[5] * t[5]);
+    const float F = sqrtf(J2) + M.eta * I1 - M.xi * M.cohesion;
+    return M.damage ? (F > 0.0f && I1 < 0.0f) : (F > 0.0f);
+}
+
+// Residual of the Drucker-Prager yield function at a stress and accumulated plastic strain,
+// with the softened cohesion max(c - eqps c / eps_cr, c / 10) (ConstitutiveModels.cpp:321-344):
+// the exact return mapping lands on F = 0.
+__device__ __forceinline__ float dp_residual(const float s[6], float eqps, const DevMaterial &M)
+{
+    const float I1 = (1.0f / 3.0f) * (s[0] + s[1] + s[2]);
+    const float sxx = s[0] - I1, syy = s[1] - I1, szz = s[2] - I1;
+    const float J2 = 0.5f * (sxx * sxx + syy * syy + szz * szz + 2.0f * s[3] * s[3] + 2.0f * s[4] * s[4] +
+                             2.0f * s[5] * s[5]);
+    const float cv = fmaxf(M.cohesion - eqps * (M.cohesion / M.crit_strain), M.cohesion / 10.0f);
+    return sqrtf(J2) + M.eta * I1 - M.xi * cv;
+}
+
 // Symmetric 3x3 eigen-decomposition by cyclic Jacobi rotations (FP32).  A is overwritten;
 // on return A[i][i] hold the eigenvalues and V's columns the eigenvectors.  The reference
 // uses JAMA's tred2+tql2 (eig3.cpp:258-267); the damaged stress V diag(s') V^T depends

@@ -597,31 +597,94 @@ class Solver:
         L.check(self.lib.gy_set_options(self.h, C.byref(o)), self.h, "options")
 
     def autotune(self, step0: int = 0, steps: int = 6,
-                 candidates=((1, 0), (2, 0), (4, 0), (1, 1))) -> dict:
-        """Choose the fastest (sort_every, full_sort) pair for this problem and keep it.
+                 candidates=((1, 0), (2, 0), (4, 0), (1, 1)), lanes=(3, 9)) -> dict:
+        """Choose the fastest step configuration for this problem and keep it.
 
-        Each candidate runs a few untimed steps (its CUDA graphs are captured there), then
-        ``steps`` steps timed with CUDA events.  These are real steps of the run, from step
-        ``step0`` on, since the knobs change speed and never results beyond summation order;
-        the returned ``next_step`` is where the caller continues.  The cell block (4^3 cells
-        and its 6^3-node shared-memory tile) and the work of a lane group (one run of equal
-        cell) are fixed by the kernels, so the sort cadence and the sort kind are what is
-        left to tune."""
+        Two stages: the sort cadence and kind (``candidates``: (sort_every, full_sort) pairs),
+        then, with those fixed, the single-body P2G's lane mapping (``lanes``: 3 z-plane lanes
+        per run of equal cell, ten runs per warp, or 9 x-column lanes, three runs per warp --
+        how many particles a warp sums at once).  Each candidate runs a few untimed steps (its
+        CUDA graphs are captured there), then ``steps`` steps timed with CUDA events.  These
+        are real steps of the run, from step ``step0`` on, since the knobs change speed and
+        never results beyond summation order; the returned ``next_step`` is where the caller
+        continues.  The cell block (4^3 cells and its 6^3-node shared-memory tile) is fixed by
+        the kernels' key encoding."""
         ms = C.c_float()
         dt = self.dt
         step = int(step0)
-        times = {}
-        for sort_every, full_sort in candidates:
-            self.set_options(sort_every=int(sort_every), full_sort=int(full_sort))
-            warm = max(2, 2 * int(sort_every))
+
+        def timed(**opts):
+            nonlocal step
+            self.set_options(**opts)
+            warm = max(2, 2 * int(opts.get("sort_every", 1)))
             L.check(self.lib.gy_steps(self.h, step * dt, step, warm, 1), self.h, "autotune")
             step += warm
             L.check(self.lib.gy_time_steps(self.h, step * dt, step, int(steps), C.byref(ms)), self.h, "autotune")
             step += int(steps)
-            times[(int(sort_every), int(full_sort))] = ms.value / max(int(steps), 1)
+            return ms.value / max(int(steps), 1)
+
+        times = {}
+        for sort_every, full_sort in candidates:
+            times[(int(sort_every), int(full_sort))] = timed(sort_every=int(sort_every), full_sort=int(full_sort))
         best = min(times, key=times.get)
-        self.set_options(sort_every=best[0], full_sort=best[1])
-        return dict(sort_every=best[0], full_sort=best[1], ms_per_step=times, next_step=step)
+        lane_times = {}
+        for ln in lanes:
+            lane_times[int(ln)] = timed(sort_every=best[0], full_sort=best[1], p2g_lanes=int(ln))
+        best_lanes = min(lane_times, key=lane_times.get)
+        self.set_options(sort_every=best[0], full_sort=best[1], p2g_lanes=best_lanes)
+        return dict(sort_every=best[0], full_sort=best[1], p2g_lanes=best_lanes, ms_per_step=times,
+                    lanes_ms_per_step=lane_times, next_step=step)
+
+    # ---- learned Drucker-Prager surrogate (no reference counterpart) ------------------------
+    def dp_log_begin(self, cap: int, every: int = 1):
+        """Record (strain increment, state) -> (return correction, plastic strain increment)
+        pairs of yielding Drucker-Prager particles from the exact return mapping of the coming
+        steps, up to cap records, one particle in `every`."""
+        L.check(self.lib.gy_dp_log_begin(self.h, int(cap), int(every)), self.h, "dp_log_begin")
+
+    def dp_log_end(self):
+        L.check(self.lib.gy_dp_log_end(self.h), self.h, "dp_log_end")
+
+    def dp_log_count(self) -> int:
+        c = C.c_int64()
+        L.check(self.lib.gy_dp_log_count(self.h, C.byref(c)), self.h, "dp_log_count")
+        return int(c.value)
+
+    def dp_log_read(self):
+        """The logged records as (inputs [m][16], targets [m][7]) float32 arrays."""
+        m = self.dp_log_count()
+        x = np.empty((m, 16), np.float32)
+        y = np.empty((m, 7), np.float32)
+        if m:
+            L.check(self.lib.gy_dp_log_read(self.h, x.ctypes.data_as(C.c_void_p), y.ctypes.data_as(C.c_void_p), m),
+                    self.h, "dp_log_read")
+        return x, y
+
+    def train_surrogate(self, steps: int = 20000, batch: int = 4096, lr: float = 1e-3, seed: int = 0) -> float:
+        """Train the surrogate MLP on the logged records on the GPU; returns the final loss."""
+        loss = C.c_float()
+        L.check(self.lib.gy_dp_surrogate_train(self.h, int(steps), int(batch), C.c_float(lr), int(seed),
+                                               C.byref(loss)), self.h, "train_surrogate")
+        return float(loss.value)
+
+    def set_surrogate(self, on: bool = True, params=None, tol: float = 1e-4):
+        """Switch the surrogate return mapping on or off; params (gy_mlp_param_count floats)
+        replace the trained parameters when given."""
+        p = None
+        if params is not None:
+            params = np.ascontiguousarray(params, np.float32)
+            p = params.ctypes.data_as(C.c_void_p)
+        L.check(self.lib.gy_set_dp_surrogate(self.h, p, 1 if on else 0, C.c_float(tol)), self.h, "set_surrogate")
+
+    def surrogate_params(self) -> np.ndarray:
+        out = np.empty(int(self.lib.gy_mlp_param_count()), np.float32)
+        L.check(self.lib.gy_get_dp_surrogate(self.h, out.ctypes.data_as(C.c_void_p)), self.h, "surrogate_params")
+        return out
+
+    def surrogate_counts(self) -> dict:
+        k, f = C.c_int64(), C.c_int64()
+        L.check(self.lib.gy_dp_surrogate_counts(self.h, C.byref(k), C.byref(f)), self.h, "surrogate_counts")
+        return dict(kept=int(k.value), fallback=int(f.value))
 
     def _set_temps(self, idx, T):
         idx = np.ascontiguousarray(idx, np.int64)

@@ -303,6 +303,26 @@ gy_status gy_mlp_grad(const float *d_params, const float *d_X, const float *d_T,
 gy_status gy_mlp_train(float *d_params, const float *d_X, const float *d_T, int64_t n, int steps, int batch, float lr,
                        uint64_t seed, int init, float *loss_out, int *d_status, void *stream);
 
+/* The surrogate in the step (Drucker-Prager materials, 3D).  Logging: while on, the exact
+ * return mapping records, for yielding particles whose (insertion index + step) is a multiple
+ * of `every`, the MLP input (strain increment 6, previous stress 6, accumulated plastic
+ * strain, damage, cohesion, friction angle in degrees) and target (stress minus the elastic
+ * trial stress 6, plastic strain increment), up to cap records (later ones are dropped).
+ * gy_dp_surrogate_train trains the handle's surrogate on the logged records (normalisation and
+ * weights from scratch).  With the surrogate on, a yielding particle without a BC takes the
+ * MLP's return (stress = trial + predicted correction) when the yield function there is
+ * within tol x cohesion of zero and the predicted increment is not negative, else the exact
+ * return mapping (ConstitutiveModels.cpp:238-429); damage stays exact.  counts: predictions
+ * kept and fallbacks since the surrogate parameters were first set. */
+gy_status gy_dp_log_begin(gy_solver *h, int64_t cap, int every);
+gy_status gy_dp_log_end(gy_solver *h);
+gy_status gy_dp_log_count(gy_solver *h, int64_t *count);
+gy_status gy_dp_log_read(gy_solver *h, float *x16, float *y7, int64_t max_records);
+gy_status gy_dp_surrogate_train(gy_solver *h, int steps, int batch, float lr, uint64_t seed, float *loss_out);
+gy_status gy_set_dp_surrogate(gy_solver *h, const float *params, int on, float tol);
+gy_status gy_get_dp_surrogate(gy_solver *h, float *params);
+gy_status gy_dp_surrogate_counts(gy_solver *h, int64_t *kept, int64_t *fallback);
+
 /* Number of kernels this library has launched in the process so far. */
 int64_t gy_kernel_launches(void);
 

@@ -248,6 +248,61 @@ def bench_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
+def bench_surrogate(solver, args, step, n_job, names):
+    """The learned surrogate against the plain return mapping from the same state: train on the
+    logged returns (timed on the host clock), then time K steps of each arm (CUDA events, graph
+    replay) after W warm-up steps, both from the state at `step`, and compare the stress,
+    velocity and plastic strain they reach."""
+    import numpy as np
+    from graphyt_gb300 import _lib as L
+    lib, h = solver.lib, solver.h
+    dt = solver.dt
+    logged = solver.dp_log_count()
+    solver.dp_log_end()
+    t0 = time.perf_counter()
+    loss = solver.train_surrogate(steps=args.surrogate_train_steps, batch=4096, lr=1e-3, seed=0)
+    solver.Synchronise()
+    train_s = time.perf_counter() - t0
+    fd, path = tempfile.mkstemp(suffix=".gystate")
+    os.close(fd)
+    solver.save(path)
+
+    def arm():
+        k = step
+        for _ in range(args.warmup):
+            solver.iterate_GPU(k * dt, k)
+            k += 1
+        solver.Synchronise()
+        ms = C.c_float()
+        L.check(lib.gy_time_steps(h, k * dt, k, args.steps, C.byref(ms)), h, "timed steps")
+        solver.Synchronise()
+        return ms.value / args.steps, {f: solver._get_particles(f) for f in ("stress", "vel", "eqps")}
+
+    ms_plain, plain = arm()
+    solver.load(path)
+    solver.set_surrogate(True, tol=1e-4)
+    c0 = solver.surrogate_counts()
+    ms_surr, surr = arm()
+    c1 = solver.surrogate_counts()
+    solver.set_surrogate(False)
+    solver.load(path)
+    os.unlink(path)
+
+    def rel(a, b):
+        d = np.linalg.norm(b)
+        return float(np.linalg.norm(a - b) / d) if d > 0 else float(np.linalg.norm(a))
+
+    kept, fb = c1["kept"] - c0["kept"], c1["fallback"] - c0["fallback"]
+    return {"metric": "particle-steps/s, plain return mapping vs learned surrogate, same state and steps",
+            "plain_ms_per_step": ms_plain, "plain_value": n_job / (ms_plain / 1e3),
+            "surrogate_ms_per_step": ms_surr, "surrogate_value": n_job / (ms_surr / 1e3),
+            "rel_l2_vs_plain": {f: rel(surr[f], plain[f]) for f in plain},
+            "deferred_per_step": (kept + fb) / max(args.warmup + args.steps, 1),
+            "kept_fraction": kept / max(kept + fb, 1), "tol_x_cohesion": 1e-4,
+            "logged_returns": logged, "train_steps": args.surrogate_train_steps, "train_batch": 4096,
+            "train_s": train_s, "train_loss": loss, "first_step": step}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -269,6 +324,10 @@ def main():
     ap.add_argument("--full-sort", action="store_true", help="full radix sort every step (no incremental re-sort)")
     ap.add_argument("--p2g-lanes", type=int, default=3, choices=[3, 9],
                     help="single-body P2G lanes per run of equal cell: 3 z-plane lanes or 9 x-column lanes")
+    ap.add_argument("--surrogate", action="store_true",
+                    help="brazilian_disc: also train the learned Drucker-Prager surrogate on the returns the plain "
+                         "solver logs up to the timed window, and time the surrogate step beside the plain one")
+    ap.add_argument("--surrogate-train-steps", type=int, default=20000)
     ap.add_argument("--preroll", type=int, default=-1,
                     help="untimed steps before the warm-up (default: half the configuration's run)")
     args = ap.parse_args()
@@ -343,6 +402,9 @@ def main():
         advance(1)
         return float(np.mean(c0 != solver._get_particles_int("cellid")))
 
+    if args.surrogate:
+        # the plain solver logs its Drucker-Prager returns up to the timed window
+        solver.dp_log_begin(cap=50_000_000, every=1)
     advance(args.warmup)
     names = ["sort", "p2g", "grid", "g2p_update"]
     # the same window from rest: few particles change cell, so the re-sort is cheapest here
@@ -351,6 +413,9 @@ def main():
     rest_movers = mover_fraction()
     # the developed flow: advance to the middle of the configuration's run, warm up, time
     advance(max(0, args.preroll - step))
+    surrogate = None
+    if args.surrogate:
+        surrogate = bench_surrogate(solver, args, step, n_job, names)
     advance(args.warmup)
     dist.barrier()
     sampler = ClockSampler(local)
@@ -440,6 +505,7 @@ def main():
             "step_roofline": {"achieved": whole, "peak": peak, "unit": "GB/s", "frac": whole / peak,
                               "bytes_per_step": step_bytes},
             "cpu_baseline": cpu,
+            **({"surrogate": surrogate} if surrogate else {}),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": STEP_SCALARS_H2D_BYTES,
                     "d2h_bytes_per_step": STATS_D2H_BYTES},
             "gpu_launches": int(launches),

@@ -1718,7 +1718,6 @@ __global__ void __launch_bounds__(GY_G2P_THREADS, THERMAL ? GY_G2P_MINB_TH : GY_
 #pragma unroll
     for (int k = 0; k < NSTAT; k++) s_st[k][tid] = 0.f;  // each thread's own column
     for (int sgi = blockIdx.x; sgi < nseg; sgi += gridDim.x) {
-        prefetch_next_segment(src, perm, seg_start, nseg, sgi + gridDim.x, PF_OX, (HAS_DP ? PF_SMAX : PF_PID) + 1);
         const long long start = seg_start[sgi];
         const int blk = seg_block(skey, start);
         int bx, by, bz;
@@ -1923,7 +1922,6 @@ __global__ void __launch_bounds__(GY_G2PM_THREADS, GY_G2PM_MINB) k_g2p_multi_til
 #pragma unroll
     for (int k = 0; k < NSTAT; k++) s_st[k][tid] = 0.f;  // each thread's own column
     for (int sgi = blockIdx.x; sgi < nseg; sgi += gridDim.x) {
-        prefetch_next_segment(src, perm, seg_start, nseg, sgi + gridDim.x, PF_OX, (HAS_DP ? PF_SMAX : PF_PID) + 1);
         const long long start = seg_start[sgi];
         const int blk = seg_block(skey, start);
         int bx, by, bz;

@@ -634,11 +634,17 @@ __global__ void k_colstats(const float *A, long long n, int w, double *acc)
 // The surrogate pass of a step: the particles G2P deferred (yielding Drucker-Prager particles,
 // their stress still the previous step's) in tiles of 128.  Per particle the MLP predicts the
 // return from the elastic trial stress -- stress = trial + predicted correction, plastic
-// strain + predicted increment -- and the prediction is kept when the yield function there is
-// within tol x cohesion of zero (the exact mapping lands on zero) and the increment is not
-// negative; the plastic strain tensor then follows the flow direction of the trial deviator
-// with the multiplier the increment implies (ConstitutiveModels.cpp:402-416).  Otherwise
-// the exact return mapping runs.  The Grady-Kipp update follows in both cases.
+// strain + predicted increment d -- and the prediction is kept when
+//   * the yield function there is within tol x cohesion of zero (the exact mapping lands on
+//     zero, ConstitutiveModels.cpp:321-344),
+//   * d is not negative, and
+//   * the predicted stress is, within tol x cohesion per component, the stress the flow rule
+//     gives for the multiplier d / xi: the trial deviator scaled by 1 - G dl / sqrt(J2) and
+//     the trial mean stress less K eta_bar dl (:397-416) -- a point of the yield surface that
+//     is not the return of this trial state fails here;
+// the plastic strain tensor then follows the flow direction of the trial deviator with that
+// multiplier.  Otherwise the exact return mapping runs.  The Grady-Kipp update follows in
+// both cases.
 __global__ void __launch_bounds__(128) k_dp_surrogate(PView P, const float4 *pend, const unsigned int *pend_n,
                                                       unsigned int cap, const DevMaterial *mats, const float *prm,
                                                       const StepScalars *scp, const float *flaw, float tol,
@@ -709,12 +715,17 @@ __global__ void __launch_bounds__(128) k_dp_surrogate(PView P, const float4 *pen
             for (int k = 0; k < 6; k++) sp[k] = t[k] + y[k];
             const float deq = y[6];
             const float res = dp_residual(sp, c.eqps + deq, M);
-            if (ok && deq >= 0.f && fabsf(res) <= tol * M.cohesion) {
-                const float I1 = (1.0f / 3.0f) * (t[0] + t[1] + t[2]);
-                const float sd[6] = {t[0] - I1, t[1] - I1, t[2] - I1, t[3], t[4], t[5]};
-                const float J2 = 0.5f * (sd[0] * sd[0] + sd[1] * sd[1] + sd[2] * sd[2] + 2.0f * sd[3] * sd[3] +
-                                         2.0f * sd[4] * sd[4] + 2.0f * sd[5] * sd[5]);
-                const float dL = deq / M.xi, hj = J2 > 0.f ? 0.5f / J2 : 0.f;
+            const float I1 = (1.0f / 3.0f) * (t[0] + t[1] + t[2]);
+            const float sd[6] = {t[0] - I1, t[1] - I1, t[2] - I1, t[3], t[4], t[5]};
+            const float J2 = 0.5f * (sd[0] * sd[0] + sd[1] * sd[1] + sd[2] * sd[2] + 2.0f * sd[3] * sd[3] +
+                                     2.0f * sd[4] * sd[4] + 2.0f * sd[5] * sd[5]);
+            const float dL = deq / M.xi;
+            const float fs = J2 > 0.f ? 1.0f - M.G * dL * rsqrtf(J2) : 1.0f, pm = I1 - M.K * M.eta_bar * dL;
+            float flow_gap = 0.f;  // largest component distance to the flow-rule stress of dL
+#pragma unroll
+            for (int k = 0; k < 6; k++) flow_gap = fmaxf(flow_gap, fabsf(sp[k] - (fs * sd[k] + (k < 3 ? pm : 0.f))));
+            if (ok && deq >= 0.f && fabsf(res) <= tol * M.cohesion && flow_gap <= tol * M.cohesion) {
+                const float hj = J2 > 0.f ? 0.5f / J2 : 0.f;
 #pragma unroll
                 for (int k = 0; k < 6; k++) {
                     c.s[k] = sp[k];

@@ -82,10 +82,11 @@ def test_surrogate_training_reduces_loss(trained):
 
 
 def test_surrogate_run_matches_plain_run(trained):
-    """With the surrogate on (residual tolerance 1e-4 x cohesion), the disc after 250 steps has
-    the plain run's stress, velocity and plastic strain to 1e-3 (relative L2; the plain return
-    mapping judges the surrogate's error), and every deferred particle was either kept or
-    handed back to the exact mapping."""
+    """With the surrogate on (tolerance 1e-4 x cohesion on the yield residual and on the
+    distance to the flow-rule stress of the predicted multiplier), the disc after 250 steps
+    has the plain run's stress, velocity and plastic strain to 1e-3 (relative L2; the plain
+    return mapping judges the surrogate's error), and every deferred particle was either kept
+    or handed back to the exact mapping."""
     sc = trained["scene"]
     plain = _run(sc, STEPS_RUN)
     surr = _run(sc, STEPS_RUN, surrogate=trained["params"], tol=1e-4)
@@ -97,14 +98,15 @@ def test_surrogate_run_matches_plain_run(trained):
 
 
 def test_surrogate_predictions_kept_everywhere(trained):
-    """With the residual check opened wide every deferred particle takes the MLP's return: the
-    run stays finite and its stress stays within 5e-2 of the plain run (the trained network's
-    own accuracy over 250 steps), and no particle falls back."""
+    """With the checks opened wide the deferred particles take the MLP's return (those with a
+    negative predicted plastic strain increment still fall back): the run stays finite and
+    its stress stays within 5e-2 of the plain run -- the trained network's own accuracy over
+    250 steps."""
     sc = trained["scene"]
     plain = _run(sc, STEPS_RUN)
     surr = _run(sc, STEPS_RUN, surrogate=trained["params"], tol=1e30)
     counts = surr.surrogate_counts()
-    assert counts["kept"] > 0 and counts["fallback"] == 0
+    assert counts["kept"] > 0.9 * (counts["kept"] + counts["fallback"]), counts
     s = surr._get_particles("stress")
     assert np.all(np.isfinite(s))
-    assert rel_l2(s, plain._get_particles("stress")) <= 5e-2
+    assert rel_l2(s, plain._get_particles("stress")) <= 5e-2, (rel_l2(s, plain._get_particles("stress")), counts)

@@ -415,7 +415,7 @@ def main():
     advance(max(0, args.preroll - step))
     surrogate = None
     if args.surrogate:
-        surrogate = bench_surrogate(solver, args, step, n_job, names)
+        surrogate = bench_surrogate(solver, args, step, float(n) * world, names)
     advance(args.warmup)
     dist.barrier()
     sampler = ClockSampler(local)

@@ -1448,6 +1448,10 @@ gy_status gy_state_load(gy_solver *h, const void *buf, int64_t bytes)
         hd.has_dp != (int)h->has_dp || hd.track_normals != h->opt.track_normals)
         return fail(h, GY_ERR_ARG, "state belongs to a different model (grid, particles, bodies or options differ)");
     if (bytes < (int64_t)state_bytes(h, hd.thermal != 0)) return fail(h, GY_ERR_ARG, "buffer shorter than the state");
+    // a handle that carries temperatures cannot take a state saved without them: it would
+    // keep its own temperatures and step on differently from the run that was saved
+    if (!hd.thermal && h->d_therm)
+        return fail(h, GY_ERR_ARG, "state saved without heat conduction, this handle has temperatures");
     cudaSetDevice(h->device);
     CK(h, cudaStreamSynchronize(h->stream));
     const char *p = static_cast<const char *>(buf) + sizeof(hd);

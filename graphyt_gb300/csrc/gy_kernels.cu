@@ -487,13 +487,9 @@ constexpr int PP_GROUPS = PP_GPW * (PP_THREADS / 32);   // 40
 constexpr int PP_CH = 2 * PP_THREADS;                   // particles per chunk (a pair per thread)
 constexpr int PP_ROWS = PP_CH + PP_CH / 8;
 __device__ __forceinline__ int pp_row(int q) { return q + (q >> 3); }
-// Runs are handed to the lane groups in order of decreasing length (a counting sort over
-// PP_LBINS length bins, the last bin holding every longer run), so the ten runs a warp sums
-// side by side have nearly equal lengths and few masked iterations; in the flow, where cells
-// hold from a few to a dozen particles, unsorted rounds ran as long as their longest run.
-constexpr int PP_LBINS = 32;
+
 static_assert(PP_CH == PC_CH, "the chunk bounds helper assumes two particles per thread");
-static_assert(PP_LBINS == 32, "the bin scan takes one bin per lane of a warp");
+
 
 __device__ __forceinline__ float2 dup2(float x) { return make_float2(x, x); }
 
@@ -506,8 +502,6 @@ __global__ void __launch_bounds__(PP_THREADS, 4) k_p2g_planes(PView P, const int
     __shared__ float2 SZ[3][PP_ROWS];
     __shared__ int run_start[PP_CH + 1];
     __shared__ int run_cell[PP_CH];
-    __shared__ short run_order[PP_CH];   // runs by decreasing length
-    __shared__ int len_bin[PP_LBINS];
     __shared__ int wcount[PP_THREADS / 32];
     __shared__ long long s_end;
     const int nseg = *nseg_ptr;
@@ -601,33 +595,11 @@ __global__ void __launch_bounds__(PP_THREADS, 4) k_p2g_planes(PView P, const int
                 run_cell[ri] = cb;
             }
             if (tid == 0) run_start[R] = cnt;
-            if (tid < PP_LBINS) len_bin[tid] = 0;
-            __syncthreads();
-            // ---- runs by decreasing length: bin counts, their exclusive scan, placement ----
-            for (int r = tid; r < R; r += PP_THREADS) {
-                const int b = PP_LBINS - 1 - min(run_start[r + 1] - run_start[r], PP_LBINS - 1);
-                atomicAdd(&len_bin[b], 1);
-            }
-            __syncthreads();
-            if (warp == 0) {
-                const int c = len_bin[lane];  // PP_LBINS == 32: one bin per lane
-                int incl = c;
-                for (int off = 1; off < 32; off <<= 1) {
-                    const int y = __shfl_up_sync(0xffffffffu, incl, off);
-                    if (lane >= off) incl += y;
-                }
-                len_bin[lane] = incl - c;
-            }
-            __syncthreads();
-            for (int r = tid; r < R; r += PP_THREADS) {
-                const int b = PP_LBINS - 1 - min(run_start[r + 1] - run_start[r], PP_LBINS - 1);
-                run_order[atomicAdd(&len_bin[b], 1)] = (short)r;
-            }
             __syncthreads();
             // ---- ten runs per warp and round, three plane lanes per run ----
             for (int rb = warp * PP_GPW; rb < R; rb += PP_GROUPS) {
-                const bool rv = grp < PP_GPW && rb + grp < R;
-                const int r = rv ? run_order[rb + grp] : 0;
+                const int r = rb + grp;
+                const bool rv = grp < PP_GPW && r < R;
                 const int p0 = rv ? run_start[r] : 0, len = rv ? run_start[r + 1] - p0 : 0;
                 const int maxlen = __reduce_max_sync(0xffffffffu, len);
                 float2 amp[3][3], app[3][3], afxy[3][3];

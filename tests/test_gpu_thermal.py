@@ -135,6 +135,28 @@ def test_thermal_checkpoint_resume(gpu_lib, tmp_path):
     assert rel_l2(tb - sc.temp, ta - sc.temp) < 1e-5
 
 
+def test_thermal_handle_rejects_state_without_temperatures(gpu_lib, tmp_path):
+    """A state saved by a run without heat conduction does not load into a handle that carries
+    temperatures (it would keep its own temperatures and step on unlike the saved run); the
+    handle is left as it was."""
+    from graphyt_gb300 import _lib, graphyt
+    sc = scenes.thermal_block()
+    cold = sc.__class__(**{**sc.__dict__})
+    cold.temp = np.zeros_like(sc.temp)
+    a = graphyt.from_scene(cold)
+    dt = a.dt
+    for k in range(3):
+        a.iterate_GPU(k * dt, k)
+    path = str(tmp_path / "cold.bin")
+    a.save(path)
+    b = graphyt.from_scene(sc)
+    b.iterate_GPU(0.0, 0)
+    before = b._get_particles("temp")
+    with pytest.raises(_lib.GraphytGPUError):
+        b.load(path)
+    assert np.array_equal(b._get_particles("temp"), before)
+
+
 def test_no_temperature_no_conduction(gpu_lib):
     """With every temperature zero the step runs without the thermal terms and the
     temperature getters report zeros; the first nonzero temperature adds one launch, the

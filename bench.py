@@ -322,7 +322,7 @@ def main():
     ap.add_argument("--column-height", type=float, default=0.765,
                     help="dam break water column height in m (1.5 gives the configuration's 24 M particles)")
     ap.add_argument("--full-sort", action="store_true", help="full radix sort every step (no incremental re-sort)")
-    ap.add_argument("--p2g-lanes", type=int, default=3, choices=[3, 4, 9],
+    ap.add_argument("--p2g-lanes", type=int, default=3, choices=[3, 9],
                     help="single-body P2G lanes per run of equal cell: 3 z-plane lanes or 9 x-column lanes")
     ap.add_argument("--surrogate", action="store_true",
                     help="brazilian_disc: also train the learned Drucker-Prager surrogate on the returns the plain "

@@ -868,8 +868,7 @@ gy_status gy_set_options(gy_solver *h, const gy_options *opt)
     if (!h || !opt) return GY_ERR_ARG;
     if (opt->sort_every < 1) return fail(h, GY_ERR_ARG, "sort_every must be >= 1");
     if (opt->use_graph != 0 && opt->use_graph != 1) return fail(h, GY_ERR_ARG, "use_graph must be 0 or 1");
-    if (opt->p2g_lanes != 3 && opt->p2g_lanes != 4 && opt->p2g_lanes != 9)
-        return fail(h, GY_ERR_ARG, "p2g_lanes must be 3, 4 or 9");
+    if (opt->p2g_lanes != 3 && opt->p2g_lanes != 9) return fail(h, GY_ERR_ARG, "p2g_lanes must be 3 or 9");
     if (h->initialized && (opt->track_normals != h->opt.track_normals || opt->keep_node_fields != h->opt.keep_node_fields))
         return fail(h, GY_ERR_STATE, "track_normals / keep_node_fields must be set before gy_initialize");
     h->opt = *opt;

@@ -688,226 +688,6 @@ __global__ void __launch_bounds__(PP_THREADS, 4) k_p2g_planes(PView P, const int
     }
 }
 
-// Single-body P2G with z-plane lanes and a two-stage copy pipeline.  The lane groups and runs
-// are those of k_p2g_planes; the CTA walks its (segment, chunk) sequence with the 14 raw fields
-// of the next chunk's particles -- offsets, velocity, stress, density, mass, gathered through
-// the sort permutation -- copied into one of two shared buffers by cp.async while the current
-// chunk is summed, so the global loads no longer stall the sums.  There is no staging pass:
-// each lane reads its particle's raw fields (rows swizzled q + q/8) and forms the GIMP weights
-// and the payload itself.
-constexpr int PQ_F = 14;
-__device__ __forceinline__ int pq_field(int f) { return f < 12 ? PF_OX + f : (f == 12 ? PF_RHO : PF_MASS); }
-static_assert(PF_OX == 0 && PF_S5 == 11, "the first twelve raw fields are the slab's first twelve");
-
-__global__ void __launch_bounds__(PP_THREADS, 4) k_p2g_pipe(PView P, const int *perm, const int *skey, long long n,
-                                                            const int *seg_start, const int *nseg_ptr, int sorted,
-                                                            NodeBufs nb, GridGeom g)
-{
-    __shared__ float tile[P2G_FIELDS * PT_NODES];
-    __shared__ float R[2][PQ_F][PP_ROWS];
-    __shared__ int run_start[PP_CH + 1];
-    __shared__ int run_cell[PP_CH];
-    __shared__ int wcount[PP_THREADS / 32];
-    __shared__ long long s_end;
-    const int nseg = *nseg_ptr;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const unsigned lt = (1u << lane) - 1u;
-    const int grp = lane / 3, kk = lane - 3 * grp;  // lanes 30, 31: group 10, no run
-    const float2 z2 = make_float2(0.f, 0.f);
-
-    // keys, count (CTA-uniform) and raw copies into R[buf] of the chunk at `base` of block `blk`
-    auto fetch = [&](long long base, int blk, int buf, int &ka, int &kb, int &kp) -> int {
-        const long long ia = base + 2 * tid, ib = ia + 1;
-        long long ja = 0, jb = 0;
-        int cnt;
-        ka = kb = kp = -1;
-        if (sorted) {
-            ka = ia < n ? skey[ia] : -1;
-            kb = ib < n ? skey[ib] : -1;
-            kp = (ia < n && tid > 0) ? skey[ia - 1] : -1;
-            ja = ia < n ? perm[ia] : 0;
-            jb = ib < n ? perm[ib] : 0;
-            cnt = __syncthreads_count(ia < n && (ka >> CB_SHIFT) == blk);
-            cnt += __syncthreads_count(ib < n && (kb >> CB_SHIFT) == blk);
-        } else {
-            cnt = (int)min((long long)PP_CH, segment_chunk_end2(skey, n, blk, base, &s_end) - base);
-            if (2 * tid < cnt) {
-                ka = skey[ia];
-                kp = tid > 0 ? skey[ia - 1] : -1;
-            }
-            if (2 * tid + 1 < cnt) kb = skey[ib];
-            ja = ia;
-            jb = ib;
-        }
-        if (2 * tid < cnt) {
-            const int row = pp_row(2 * tid);
-#pragma unroll
-            for (int f = 0; f < PQ_F; f++) cp_async4(&R[buf][f][row], &P.f(pq_field(f), ja));
-        }
-        if (2 * tid + 1 < cnt) {
-            const int row = pp_row(2 * tid + 1);
-#pragma unroll
-            for (int f = 0; f < PQ_F; f++) cp_async4(&R[buf][f][row], &P.f(pq_field(f), jb));
-        }
-        cp_async_commit();
-        return cnt;
-    };
-
-    int sgi = blockIdx.x;
-    if (sgi >= nseg) return;
-    long long base = seg_start[sgi];
-    int blk = seg_block(skey, base);
-    int buf = 0, ka, kb, kp;
-    int cnt = fetch(base, blk, 0, ka, kb, kp);
-    for (int t = tid; t < P2G_FIELDS * PT_NODES; t += PP_THREADS) tile[t] = 0.f;
-    while (true) {
-        // the chunk after this one: the next of this segment if this one is full, else the
-        // first of the CTA's next segment; an empty chunk ends the segment
-        int nsgi = sgi, nblk = blk, nka = -1, nkb = -1, nkp = -1, ncnt = 0;
-        long long nbase = base + PP_CH;
-        cp_async_wait_all();
-        __syncthreads();  // the current chunk's rows are in R[buf]; the last chunk's sums are done
-        if (cnt == PP_CH) ncnt = fetch(nbase, nblk, buf ^ 1, nka, nkb, nkp);
-        while (ncnt == 0) {
-            nsgi += gridDim.x;
-            if (nsgi >= nseg) break;
-            nbase = seg_start[nsgi];
-            nblk = seg_block(skey, nbase);
-            ncnt = fetch(nbase, nblk, buf ^ 1, nka, nkb, nkp);
-        }
-        // ---- runs of equal cell of the current chunk ----
-        const bool va = 2 * tid < cnt, vb = 2 * tid + 1 < cnt;
-        const int ca = ka & 63, cb = kb & 63;
-        const bool ha = va && (tid == 0 || (kp & 63) != ca);
-        const bool hb = vb && cb != ca;
-        const unsigned ba = __ballot_sync(0xffffffffu, ha), bb = __ballot_sync(0xffffffffu, hb);
-        if (lane == 0) wcount[warp] = __popc(ba) + __popc(bb);
-        __syncthreads();
-        int wbase = 0, R_ = 0;
-#pragma unroll
-        for (int w2 = 0; w2 < PP_THREADS / 32; w2++) {
-            const int c = wcount[w2];
-            wbase += (w2 < warp) ? c : 0;
-            R_ += c;
-        }
-        int ri = wbase + __popc(ba & lt) + __popc(bb & lt);
-        if (ha) {
-            run_start[ri] = 2 * tid;
-            run_cell[ri] = ca;
-            ri++;
-        }
-        if (hb) {
-            run_start[ri] = 2 * tid + 1;
-            run_cell[ri] = cb;
-        }
-        if (tid == 0) run_start[R_] = cnt;
-        __syncthreads();
-        // ---- ten runs per warp and round, three plane lanes per run ----
-        const float (*Rb)[PP_ROWS] = R[buf];
-        for (int rb = warp * PP_GPW; rb < R_; rb += PP_GROUPS) {
-            const int r = rb + grp;
-            const bool rv = grp < PP_GPW && r < R_;
-            const int p0 = rv ? run_start[r] : 0, len = rv ? run_start[r + 1] - p0 : 0;
-            const int maxlen = __reduce_max_sync(0xffffffffu, len);
-            float2 amp[3][3], app[3][3], afxy[3][3];
-            float afz[3][3];
-#pragma unroll
-            for (int i = 0; i < 3; i++)
-#pragma unroll
-                for (int j = 0; j < 3; j++) {
-                    amp[i][j] = app[i][j] = afxy[i][j] = z2;
-                    afz[i][j] = 0.f;
-                }
-            for (int k = 0; k < maxlen; k++) {
-                const int row = pp_row(p0 + min(k, max(len - 1, 0)));
-                float Sx[3], Gx[3], Sy[3], Gy[3], Sz3[3], Gz3[3];
-                gimp_axis(Rb[0][row], g, Sx, Gx);
-                gimp_axis(Rb[1][row], g, Sy, Gy);
-                if (g.is3d) {
-                    gimp_axis(Rb[2][row], g, Sz3, Gz3);
-                } else {
-                    Sz3[0] = 1.f; Sz3[1] = 0.f; Sz3[2] = 0.f; Gz3[0] = 0.f; Gz3[1] = 0.f; Gz3[2] = 0.f;
-                }
-                float2 Z = make_float2(kk == 0 ? Sz3[0] : (kk == 1 ? Sz3[1] : Sz3[2]),
-                                       kk == 0 ? Gz3[0] : (kk == 1 ? Gz3[1] : Gz3[2]));
-                if (k >= len) Z = z2;  // past the run (or no run): the particle adds nothing
-                const float m = Rb[13][row];
-                const float sc = (m / Rb[12][row]) * g.inv_h;  // V sigma with the gradient's 1/h
-                const float2 mvx = make_float2(m, m * Rb[3][row]), mvyz = make_float2(m * Rb[4][row], m * Rb[5][row]);
-                const float s0 = Rb[6][row] * sc, s1 = Rb[7][row] * sc, s2 = Rb[8][row] * sc;
-                const float s3 = Rb[9][row] * sc, s4 = Rb[10][row] * sc, s5 = Rb[11][row] * sc;
-                const float2 s03 = make_float2(s0, s3), s54 = make_float2(s5, s4), s31 = make_float2(s3, s1);
-#pragma unroll
-                for (int j = 0; j < 3; j++) {
-                    const float syz = Sy[j] * Z.x, gyz = Gy[j] * Z.x, syg = Sy[j] * Z.y;
-                    const float2 syz2 = dup2(syz);
-                    const float2 mp = mul2(syz2, mvx);
-                    const float2 pp = mul2(syz2, mvyz);
-                    const float2 Bxy = mul2(syz2, s03);
-                    const float Bz = s5 * syz;
-                    const float2 Cxy = fma2(dup2(gyz), s31, mul2(dup2(syg), s54));
-                    const float Cz = fmaf(s4, gyz, s2 * syg);
-#pragma unroll
-                    for (int i = 0; i < 3; i++) {
-                        const float2 sx = dup2(Sx[i]), gx = dup2(Gx[i]);
-                        amp[i][j] = fma2(sx, mp, amp[i][j]);
-                        app[i][j] = fma2(sx, pp, app[i][j]);
-                        afxy[i][j] = fma2(gx, Bxy, fma2(sx, Cxy, afxy[i][j]));
-                        afz[i][j] = fmaf(Gx[i], Bz, fmaf(Sx[i], Cz, afz[i][j]));
-                    }
-                }
-            }
-            if (!rv) continue;
-            const int cell = run_cell[r];
-            const int li = cell & 3, lj = (cell >> 2) & 3, lk = cell >> 4;
-#pragma unroll
-            for (int j = 0; j < 3; j++)
-#pragma unroll
-                for (int i = 0; i < 3; i++) {
-                    if (amp[i][j].x == 0.f) continue;  // outside every particle's support
-                    const int t = ((lk + kk) * PT + (lj + j)) * PT + li + i;
-                    atomicAdd(&tile[0 * PT_NODES + t], amp[i][j].x);
-                    atomicAdd(&tile[1 * PT_NODES + t], amp[i][j].y);
-                    atomicAdd(&tile[2 * PT_NODES + t], app[i][j].x);
-                    atomicAdd(&tile[3 * PT_NODES + t], app[i][j].y);
-                    atomicAdd(&tile[4 * PT_NODES + t], -afxy[i][j].x);
-                    atomicAdd(&tile[5 * PT_NODES + t], -afxy[i][j].y);
-                    atomicAdd(&tile[6 * PT_NODES + t], -afz[i][j]);
-                }
-        }
-        // ---- segment end: flush the tile, two vector reductions per touched node ----
-        if (nsgi != sgi) {
-            int bx, by, bz;
-            decode_block(blk, g, bx, by, bz);
-            const int tox = bx * CB, toy = by * CB, toz = g.is3d ? bz * CB : 0;
-            __syncthreads();
-            for (int t = tid; t < PT_NODES; t += PP_THREADS) {
-                const float mm = tile[t], px = tile[PT_NODES + t], py = tile[2 * PT_NODES + t];
-                const float pz = tile[3 * PT_NODES + t], fx = tile[4 * PT_NODES + t];
-                const float fy = tile[5 * PT_NODES + t], fz = tile[6 * PT_NODES + t];
-                tile[t] = tile[PT_NODES + t] = tile[2 * PT_NODES + t] = tile[3 * PT_NODES + t] = 0.f;
-                tile[4 * PT_NODES + t] = tile[5 * PT_NODES + t] = tile[6 * PT_NODES + t] = 0.f;
-                if (mm == 0.f && px == 0.f && py == 0.f && pz == 0.f && fx == 0.f && fy == 0.f && fz == 0.f) continue;
-                const int ni = tox + t % PT, nj = toy + (t / PT) % PT, nk = toz + t / (PT * PT);
-                if (ni >= g.nx || nj >= g.ny || nk >= g.nz) continue;
-                const int nd = node_index(ni, nj, nk, g);
-                red_add4(&nb.acc0[nd], mm, px, py, pz);
-                red_add4(&nb.acc1[nd], fx, fy, fz, 0.f);
-                mark_node(nb, ni, nj, nk, g);
-            }
-        }
-        if (nsgi >= nseg) break;
-        sgi = nsgi;
-        base = nbase;
-        blk = nblk;
-        cnt = ncnt;
-        ka = nka;
-        kb = nkb;
-        kp = nkp;
-        buf ^= 1;
-    }
-}
-
 // Multi-body P2G through a shared-memory node tile: segments, staging and runs of equal cell
 // as in the single-body kernel, with a warp taking one run at a time (lane k = stencil node
 // k), one particle per step, and, per node, the centre-of-mass fields plus the two body
@@ -1221,16 +1001,6 @@ void launch_p2g(const PView &p, const int *perm, const int *skey, long long n, c
                 pgrid = sms * std::max(b, 1);
             }
             k_p2g_planes<<<pgrid, PP_THREADS, 0, s>>>(p, perm, skey, n, seg_start, nseg, perm ? 1 : 0, nb, a.g);
-        } else if (lanes == 4) {
-            static int qgrid = 0;  // persistent grid of the pipelined plane-lane kernel
-            if (qgrid == 0) {
-                int dev = 0, sms = 1, b = 0;
-                cudaGetDevice(&dev);
-                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_p2g_pipe, PP_THREADS, 0);
-                qgrid = sms * std::max(b, 1);
-            }
-            k_p2g_pipe<<<qgrid, PP_THREADS, 0, s>>>(p, perm, skey, n, seg_start, nseg, perm ? 1 : 0, nb, a.g);
         } else {
             k_p2g_cols<false><<<persist_grid, PC_THREADS, 0, s>>>(p, perm, skey, n, seg_start, nseg, perm ? 1 : 0, nb,
                                                                    a.g, nullptr, nullptr, nullptr);

@@ -101,7 +101,7 @@ def test_p2g_lane_variants_agree(gpu_lib, make):
     sc = make()
     for sort_every in (1, 3):
         b = run_gpu(sc, 12, options=dict(p2g_lanes=9, sort_every=sort_every))
-        for lanes in (3, 4):
+        for lanes in (3,):
             a = run_gpu(sc, 12, options=dict(p2g_lanes=lanes, sort_every=sort_every))
             for f in ("pos", "vel", "stress", "density"):
                 assert rel_l2(a._get_particles(f), b._get_particles(f)) < 2e-6, (f, sort_every, lanes)

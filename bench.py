@@ -324,6 +324,9 @@ def main():
     ap.add_argument("--full-sort", action="store_true", help="full radix sort every step (no incremental re-sort)")
     ap.add_argument("--p2g-lanes", type=int, default=3, choices=[3, 9],
                     help="single-body P2G lanes per run of equal cell: 3 z-plane lanes or 9 x-column lanes")
+    ap.add_argument("--autotune", dest="autotune", action="store_true", default=None,
+                    help="run Solver.autotune before the timed window (default: on for impact_batch)")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false")
     ap.add_argument("--surrogate", action="store_true",
                     help="brazilian_disc: also train the learned Drucker-Prager surrogate on the returns the plain "
                          "solver logs up to the timed window, and time the surrogate step beside the plain one")
@@ -412,6 +415,14 @@ def main():
     rest_phase = phases(args.steps)
     rest_movers = mover_fraction()
     # the developed flow: advance to the middle of the configuration's run, warm up, time
+    tuned = None
+    if args.autotune or (args.autotune is None and args.workload == "impact_batch"):
+        # the autotuner's candidates run as real steps of the run, before the timed window
+        res = solver.autotune(step0=step, steps=4)
+        step = res["next_step"]
+        tuned = {k: res[k] for k in ("sort_every", "full_sort", "p2g_lanes")}
+        tuned["candidates_ms_per_step"] = {f"sort_every={a},full_sort={b}": v for (a, b), v in res["ms_per_step"].items()}
+        tuned["p2g_lanes_ms_per_step"] = {str(k): v for k, v in res["lanes_ms_per_step"].items()}
     advance(max(0, args.preroll - step))
     surrogate = None
     if args.surrogate:
@@ -506,6 +517,7 @@ def main():
                               "bytes_per_step": step_bytes},
             "cpu_baseline": cpu,
             **({"surrogate": surrogate} if surrogate else {}),
+            **({"autotune": tuned} if tuned else {}),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": STEP_SCALARS_H2D_BYTES,
                     "d2h_bytes_per_step": STATS_D2H_BYTES},
             "gpu_launches": int(launches),

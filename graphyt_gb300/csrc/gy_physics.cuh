@@ -282,22 +282,42 @@ __device__ __forceinline__ float gk_emin(const Constit &c, const DevMaterial &M,
     return flaw ? emin * __ldg(flaw + pid) : emin;
 }
 
-// Grady-Kipp damage, 3D branch of DamageModels.cpp:71-150.  The stress is rebuilt from the
-// principal values only when damage grew: without growth V diag(s) V^T is the stress
-// itself, which the reference recomputes with rounding only.
+// Largest eigenvalue of a symmetric 3x3 matrix (xx yy zz xy yz xz), by the trigonometric
+// solution of the characteristic cubic (O. K. Smith, "Eigenvalues of a symmetric 3 x 3
+// matrix", Comm. ACM 4(4), 1961): with q = tr/3 and B = (A - q I) / p, p^2 = |A - q I|^2 / 6,
+// the eigenvalues are q + 2 p cos(acos(det(B) / 2) / 3 + 2 pi k / 3); k = 0 is the largest.
+__device__ __forceinline__ float sym3_max_eigenvalue(const float s[6])
+{
+    const float q = (s[0] + s[1] + s[2]) * (1.0f / 3.0f);
+    const float a = s[0] - q, b = s[1] - q, c = s[2] - q;
+    const float off = s[3] * s[3] + s[4] * s[4] + s[5] * s[5];
+    const float p2 = (a * a + b * b + c * c + 2.0f * off) * (1.0f / 6.0f);
+    if (!(p2 > 0.0f)) return q;  // a multiple of the identity
+    const float p = sqrtf(p2), ip = 1.0f / p;
+    const float ba = a * ip, bb = b * ip, bc = c * ip, bxy = s[3] * ip, byz = s[4] * ip, bxz = s[5] * ip;
+    const float det = ba * (bb * bc - byz * byz) - bxy * (bxy * bc - byz * bxz) + bxz * (bxy * byz - bb * bxz);
+    const float r = fminf(fmaxf(0.5f * det, -1.0f), 1.0f);
+    return q + 2.0f * p * cosf(acosf(r) * (1.0f / 3.0f));
+}
+
+// Grady-Kipp damage, 3D branch of DamageModels.cpp:71-150.  The largest principal stress
+// decides whether damage grows; most stressed particles stop there, so it comes from the
+// closed form above, and the eigen-decomposition runs only when damage grows and the stress
+// is rebuilt from the principal values (without growth V diag(s) V^T is the stress itself,
+// which the reference recomputes with rounding only).
 __device__ __forceinline__ void dm_grady_kipp3(Constit &c, const DevMaterial &M, float dt, const float *flaw, int pid)
 {
     const float chk = fabsf(c.s[0] + c.s[1] + c.s[2] + c.s[3] + c.s[4] + c.s[5]);
     if (!(chk > 1e-3f)) return;
-    float A[3][3] = {{c.s[0], c.s[3], c.s[5]}, {c.s[3], c.s[1], c.s[4]}, {c.s[5], c.s[4], c.s[2]}};
-    float V[3][3];
-    sym_eigen3(A, V);
-    float p[3] = {A[0][0], A[1][1], A[2][2]};
-    const float smx = fmaxf(fmaxf(p[0], p[1]), fmaxf(p[2], 0.0f));
+    const float smx = fmaxf(sym3_max_eigenvalue(c.s), 0.0f);
     c.smax = smx;
     if (!(smx > 1e-3f)) return;
     const float eff = smx / (M.K + 4.0f * M.G / 3.0f);
     if (!(eff > gk_emin(c, M, flaw, pid))) return;
+    float A[3][3] = {{c.s[0], c.s[3], c.s[5]}, {c.s[3], c.s[1], c.s[4]}, {c.s[5], c.s[4], c.s[2]}};
+    float V[3][3];
+    sym_eigen3(A, V);
+    float p[3] = {A[0][0], A[1][1], A[2][2]};
     const float rate = M.gk_rate_coef * powf(eff, M.gk_m / 3.0f);
     const float root = cbrtf(c.dmg) + dt * rate;
     float D = root * root * root;

@@ -596,6 +596,18 @@ class Solver:
             setattr(o, k, int(v))
         L.check(self.lib.gy_set_options(self.h, C.byref(o)), self.h, "options")
 
+    def _single_body(self) -> bool:
+        """Whether the step runs the single-body kernels: one object, no rigid material, no
+        tracked contact normals (the library's rule at gy_initialize)."""
+        o = L.Options()
+        L.check(self.lib.gy_get_options(self.h, C.byref(o)), self.h)
+        objs = self.mpts._obj
+        n_obj = len(np.unique(objs)) if objs is not None and len(objs) else 1
+        mats = self.mpts._mat
+        used = np.unique(mats) if mats is not None and len(mats) else np.array([0])
+        rigid = any(bool(getattr(self.materials[int(m)], "isRigid", 0)) for m in used if int(m) < len(self.materials))
+        return n_obj <= 1 and not rigid and not o.track_normals
+
     def autotune(self, step0: int = 0, steps: int = 6,
                  candidates=((1, 0), (2, 0), (4, 0), (1, 1)), lanes=(3, 9)) -> dict:
         """Choose the fastest step configuration for this problem and keep it.
@@ -608,7 +620,8 @@ class Solver:
         are real steps of the run, from step ``step0`` on, since the knobs change speed and
         never results beyond summation order; the returned ``next_step`` is where the caller
         continues.  The cell block (4^3 cells and its 6^3-node shared-memory tile) is fixed by
-        the kernels' key encoding."""
+        the kernels' key encoding; multi-body problems skip the lane stage, whose mapping only
+        the single-body P2G has."""
         ms = C.c_float()
         dt = self.dt
         step = int(step0)
@@ -628,9 +641,13 @@ class Solver:
             times[(int(sort_every), int(full_sort))] = timed(sort_every=int(sort_every), full_sort=int(full_sort))
         best = min(times, key=times.get)
         lane_times = {}
-        for ln in lanes:
-            lane_times[int(ln)] = timed(sort_every=best[0], full_sort=best[1], p2g_lanes=int(ln))
-        best_lanes = min(lane_times, key=lane_times.get)
+        o = L.Options()
+        L.check(self.lib.gy_get_options(self.h, C.byref(o)), self.h)
+        best_lanes = int(o.p2g_lanes)
+        if self._single_body():  # the lane mapping is the single-body P2G's
+            for ln in lanes:
+                lane_times[int(ln)] = timed(sort_every=best[0], full_sort=best[1], p2g_lanes=int(ln))
+            best_lanes = min(lane_times, key=lane_times.get)
         self.set_options(sort_every=best[0], full_sort=best[1], p2g_lanes=best_lanes)
         return dict(sort_every=best[0], full_sort=best[1], p2g_lanes=best_lanes, ms_per_step=times,
                     lanes_ms_per_step=lane_times, next_step=step)

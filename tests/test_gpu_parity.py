@@ -107,6 +107,24 @@ def test_p2g_lane_variants_agree(gpu_lib, make):
                 assert rel_l2(a._get_particles(f), b._get_particles(f)) < 2e-6, (f, sort_every, lanes)
 
 
+def test_autotune_single_body_chooses_lane_mapping(gpu_lib):
+    """On a single-body problem the autotuner also times both P2G lane mappings and keeps the
+    faster; the run it leaves behind follows an untuned run to FP32 summation order."""
+    from graphyt_gb300 import graphyt
+    sc = scenes.dam_break(scale=0.125)
+    tuned = graphyt.from_scene(sc)
+    res = tuned.autotune(step0=0, steps=3)
+    assert set(res["lanes_ms_per_step"]) == {3, 9} and res["p2g_lanes"] in (3, 9)
+    nxt = res["next_step"]
+    dt = tuned.dt
+    for k in range(nxt, nxt + 5):
+        tuned.iterate_GPU(k * dt, k)
+    tuned.Synchronise()
+    plain = run_gpu(sc, nxt + 5)
+    for f in ("vel", "stress"):
+        assert rel_l2(tuned._get_particles(f), plain._get_particles(f)) <= 1e-5, f
+
+
 @pytest.mark.parametrize("make", [lambda: scenes.dam_break(scale=0.125), lambda: scenes.two_blocks()])
 def test_graph_replay_matches_direct_launches(gpu_lib, make):
     """Steps replayed from captured CUDA graphs (per-step scalars in device memory) follow

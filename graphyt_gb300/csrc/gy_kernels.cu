@@ -490,6 +490,9 @@ __global__ void __launch_bounds__(PC_THREADS, GY_PC_MINB) k_p2g_cols(PView P, co
 //   D = (m, m vx, m vy, m vz) E = (s0, s3, s5, s4)      F = (s3, s1, s2, -)
 //   Z[kk] = (Sz_kk, Gz_kk),   s = V sigma / h in the order xx yy zz xy yz xz,
 // laid out so that every packed FP32x2 operand is a stored pair.
+#ifndef GY_PP_MINB
+#define GY_PP_MINB 4  // 115 registers: four CTAs per SM
+#endif
 constexpr int PP_THREADS = 128;
 constexpr int PP_GPW = 10;                              // lane groups per warp
 constexpr int PP_GROUPS = PP_GPW * (PP_THREADS / 32);   // 40
@@ -502,7 +505,7 @@ static_assert(PP_CH == PC_CH, "the chunk bounds helper assumes two particles per
 
 __device__ __forceinline__ float2 dup2(float x) { return make_float2(x, x); }
 
-__global__ void __launch_bounds__(PP_THREADS, 4) k_p2g_planes(PView P, const int *perm, const int *skey, long long n,
+__global__ void __launch_bounds__(PP_THREADS, GY_PP_MINB) k_p2g_planes(PView P, const int *perm, const int *skey, long long n,
                                                               const int *seg_start, const int *nseg_ptr, int sorted,
                                                               NodeBufs nb, GridGeom g)
 {

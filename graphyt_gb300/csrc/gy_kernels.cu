@@ -491,7 +491,7 @@ __global__ void __launch_bounds__(PC_THREADS, GY_PC_MINB) k_p2g_cols(PView P, co
 //   Z[kk] = (Sz_kk, Gz_kk),   s = V sigma / h in the order xx yy zz xy yz xz,
 // laid out so that every packed FP32x2 operand is a stored pair.
 #ifndef GY_PP_MINB
-#define GY_PP_MINB 4  // 115 registers: four CTAs per SM
+#define GY_PP_MINB 5  // 96 registers (a few bytes spilled): five CTAs per SM
 #endif
 constexpr int PP_THREADS = 128;
 constexpr int PP_GPW = 10;                              // lane groups per warp

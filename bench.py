@@ -333,6 +333,12 @@ def main():
     ap.add_argument("--surrogate-train-steps", type=int, default=20000)
     ap.add_argument("--preroll", type=int, default=-1,
                     help="untimed steps before the warm-up (default: half the configuration's run)")
+    ap.add_argument("--save-state", metavar="PATH",
+                    help="write a checkpoint of the state reached after the preroll (Solver.save)")
+    ap.add_argument("--load-state", metavar="PATH",
+                    help="start the timed window from a checkpoint written with --save-state and the same "
+                         "--preroll (no rest-state window, no preroll): the developed flow with few launches "
+                         "before it, for profiling")
     args = ap.parse_args()
     if args.preroll < 0:
         args.preroll = RUN_STEPS[args.workload] // 2
@@ -408,12 +414,18 @@ def main():
     if args.surrogate:
         # the plain solver logs its Drucker-Prager returns up to the timed window
         solver.dp_log_begin(cap=50_000_000, every=1)
-    advance(args.warmup)
     names = ["sort", "p2g", "grid", "g2p_update"]
-    # the same window from rest: few particles change cell, so the re-sort is cheapest here
-    rest_ms = timed(args.steps)
-    rest_phase = phases(args.steps)
-    rest_movers = mover_fraction()
+    rest = None
+    if args.load_state:
+        solver.load(args.load_state)
+        step = args.preroll
+    else:
+        advance(args.warmup)
+        # the same window from rest: few particles change cell, so the re-sort is cheapest here
+        rest_ms = timed(args.steps)
+        rest_phase = phases(args.steps)
+        rest_movers = mover_fraction()
+        rest = (rest_ms, rest_phase, rest_movers)
     # the developed flow: advance to the middle of the configuration's run, warm up, time
     tuned = None
     if args.autotune or (args.autotune is None and args.workload == "impact_batch"):
@@ -424,6 +436,8 @@ def main():
         tuned["candidates_ms_per_step"] = {f"sort_every={a},full_sort={b}": v for (a, b), v in res["ms_per_step"].items()}
         tuned["p2g_lanes_ms_per_step"] = {str(k): v for k, v in res["lanes_ms_per_step"].items()}
     advance(max(0, args.preroll - step))
+    if args.save_state:
+        solver.save(args.save_state)
     surrogate = None
     if args.surrogate:
         surrogate = bench_surrogate(solver, args, step, float(n) * world, names)
@@ -509,9 +523,10 @@ def main():
             "window": {"first_timed_step": step_timed0, "of_run_steps": RUN_STEPS[args.workload],
                        "movers_per_step": movers},
             "phase_ms_per_step": dict(zip(names, per_step)),
-            "rest_state": {"first_timed_step": args.warmup, "ms_per_step": rest_ms / args.steps,
-                           "value": n_job * args.steps / (dist.max(rest_ms) / 1e3),
-                           "phase_ms_per_step": dict(zip(names, rest_phase)), "movers_per_step": rest_movers},
+            "rest_state": {"first_timed_step": args.warmup, "ms_per_step": rest[0] / args.steps,
+                           "value": n_job * args.steps / (dist.max(rest[0]) / 1e3),
+                           "phase_ms_per_step": dict(zip(names, rest[1])), "movers_per_step": rest[2]}
+                          if rest else None,
             "roofline": roofline,
             "step_roofline": {"achieved": whole, "peak": peak, "unit": "GB/s", "frac": whole / peak,
                               "bytes_per_step": step_bytes},

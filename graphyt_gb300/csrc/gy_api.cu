@@ -1101,6 +1101,7 @@ gy_status gy_sync(gy_solver *h)
     if (flags[0]) {
         CK(h, cudaMemsetAsync(h->d_status, 0, sizeof(int), h->stream));
         CK(h, cudaStreamSynchronize(h->stream));
+        if (flags[0] & ERR_TC_TIMEOUT) return fail(h, GY_ERR_CUDA, "a tensor-core wait gave up");
         if (flags[0] & ERR_NONFINITE) return fail(h, GY_ERR_NONFINITE, "NaN or Inf in particle state");
         return fail(h, GY_ERR_RANGE, "a particle left the grid's stencil range (clamped)");
     }

@@ -189,5 +189,6 @@ __device__ __forceinline__ void pdl_prologue()
 
 constexpr int ERR_RANGE = 1;
 constexpr int ERR_NONFINITE = 2;
+constexpr int ERR_TC_TIMEOUT = 4;  // a tensor-core wait gave up (gy_tc.cuh)
 
 }  // namespace gy

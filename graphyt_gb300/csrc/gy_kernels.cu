@@ -1696,6 +1696,99 @@ __device__ __forceinline__ void stats_cta_flush(double *out, float (*col)[NT])
     }
 }
 
+// G2P sums of one particle over its 27 stencil nodes from a 6x6x6 node tile, separable per
+// axis: for every (j, k) node row the three x nodes are contracted first, then weighted by the
+// y/z factors.  TV = (v1x, v1y, v1z, a1z) and TA = (a1x, a1y), zero at massless nodes;
+// THERMAL also sums the node (T, rate) tile TN into th = (grad T, T rate).
+template <bool THERMAL>
+__device__ __forceinline__ void g2p_node_sums(const float4 *TV, const float2 *TA, const float2 *TN, const float o[3],
+                                              int key, const GridGeom &g, float acc[3], float vg[3], float L[3][3],
+                                              float th[4])
+{
+    float Sx[3], Gx[3], Sy[3], Gy[3], Sz[3], Gz[3];
+    gimp_axis(o[0], g, Sx, Gx);
+    gimp_axis(o[1], g, Sy, Gy);
+    if (g.is3d) {
+        gimp_axis(o[2], g, Sz, Gz);
+    } else {
+        Sz[0] = 1.f; Sz[1] = 0.f; Sz[2] = 0.f; Gz[0] = 0.f; Gz[1] = 0.f; Gz[2] = 0.f;
+    }
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        Gx[k] *= g.inv_h;
+        Gy[k] *= g.inv_h;
+        Gz[k] *= g.inv_h;
+    }
+    const int lc = key & 63;
+    const int t0 = ((lc >> 4) * PT + ((lc >> 2) & 3)) * PT + (lc & 3);
+    // FP32x2 sums: x/y components in pairs, the z velocity with the z acceleration
+    const float2 z2 = make_float2(0.f, 0.f);
+    float2 vg01 = z2, acc01 = z2, vz_az = z2;       // (vg_x, vg_y), (a_x, a_y), (vg_z, a_z)
+    float2 Lc0 = z2, Lc1 = z2, Lc2 = z2;            // (L[0][b], L[1][b]) for b = x, y, z
+    float L20 = 0.f, L21 = 0.f, L22 = 0.f;           // L[2][b]
+    float gtx = 0.f, gty = 0.f, gtz = 0.f, trate = 0.f;
+    float2 Sx2[3], Gx2[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        Sx2[k] = make_float2(Sx[k], Sx[k]);
+        Gx2[k] = make_float2(Gx[k], Gx[k]);
+    }
+#pragma unroll
+    for (int kk = 0; kk < 3; kk++) {
+        if (kk > 0 && !g.is3d) break;
+#pragma unroll
+        for (int jj = 0; jj < 3; jj++) {
+            const float4 *tv = TV + t0 + (kk * PT + jj) * PT;
+            const float2 *ta = TA + t0 + (kk * PT + jj) * PT;
+            float2 xv01 = z2, xv2a2 = z2, yv01 = z2, xa01 = z2;
+            float yv2 = 0.f;
+#pragma unroll
+            for (int ii = 0; ii < 3; ii++) {
+                const float4 V = tv[ii];
+                const float2 A = ta[ii];
+                xv01 = fma2(Sx2[ii], lo2(V), xv01);
+                xv2a2 = fma2(Sx2[ii], hi2(V), xv2a2);
+                yv01 = fma2(Gx2[ii], lo2(V), yv01);
+                yv2 = fmaf(Gx[ii], V.z, yv2);
+                xa01 = fma2(Sx2[ii], A, xa01);
+            }
+            const float syz = Sy[jj] * Sz[kk], gyz = Gy[jj] * Sz[kk], syg = Sy[jj] * Gz[kk];
+            const float2 syz2 = make_float2(syz, syz), gyz2 = make_float2(gyz, gyz);
+            const float2 syg2 = make_float2(syg, syg);
+            vg01 = fma2(syz2, xv01, vg01);
+            vz_az = fma2(syz2, xv2a2, vz_az);
+            acc01 = fma2(syz2, xa01, acc01);
+            Lc0 = fma2(syz2, yv01, Lc0);
+            L20 = fmaf(syz, yv2, L20);
+            Lc1 = fma2(gyz2, xv01, Lc1);
+            L21 = fmaf(gyz, xv2a2.x, L21);
+            Lc2 = fma2(syg2, xv01, Lc2);
+            L22 = fmaf(syg, xv2a2.x, L22);
+            if (THERMAL) {
+                const float2 *tn = TN + t0 + (kk * PT + jj) * PT;
+                float xT = 0.f, xgT = 0.f, xR = 0.f;
+#pragma unroll
+                for (int ii = 0; ii < 3; ii++) {
+                    const float2 q = tn[ii];
+                    xT = fmaf(Sx[ii], q.x, xT);
+                    xgT = fmaf(Gx[ii], q.x, xgT);
+                    xR = fmaf(Sx[ii], q.y, xR);
+                }
+                gtx = fmaf(syz, xgT, gtx);
+                gty = fmaf(gyz, xT, gty);
+                gtz = fmaf(syg, xT, gtz);
+                trate = fmaf(syz, xR, trate);
+            }
+        }
+    }
+    acc[0] = acc01.x; acc[1] = acc01.y; acc[2] = vz_az.y;
+    vg[0] = vg01.x; vg[1] = vg01.y; vg[2] = vz_az.x;
+    L[0][0] = Lc0.x; L[0][1] = Lc1.x; L[0][2] = Lc2.x;
+    L[1][0] = Lc0.y; L[1][1] = Lc1.y; L[1][2] = Lc2.y;
+    L[2][0] = L20;   L[2][1] = L21;   L[2][2] = L22;
+    th[0] = gtx; th[1] = gty; th[2] = gtz; th[3] = trate;
+}
+
 // Single-body G2P + update through a shared-memory node tile.  A CTA owns one segment (the
 // particles of one 4x4x4 cell block): it loads the block's 6x6x6 solved node tile once, with
 // massless nodes zeroed (they are skipped, Extrapolation.cpp:301-303), then runs one thread
@@ -1784,84 +1877,8 @@ __global__ void __launch_bounds__(GY_G2P_THREADS, THERMAL ? GY_G2P_MINB_TH : GY_
 #pragma unroll
                 for (int f = 0; f < NST; f++) cp_async4(&stage[f][tid], &src.f(g2p_stage_field(f), j));
                 cp_async_commit();
-                float Sx[3], Gx[3], Sy[3], Gy[3], Sz[3], Gz[3];
-                gimp_axis(st.o[0], g, Sx, Gx);
-                gimp_axis(st.o[1], g, Sy, Gy);
-                if (g.is3d) {
-                    gimp_axis(st.o[2], g, Sz, Gz);
-                } else {
-                    Sz[0] = 1.f; Sz[1] = 0.f; Sz[2] = 0.f; Gz[0] = 0.f; Gz[1] = 0.f; Gz[2] = 0.f;
-                }
-#pragma unroll
-                for (int k = 0; k < 3; k++) {
-                    Gx[k] *= g.inv_h;
-                    Gy[k] *= g.inv_h;
-                    Gz[k] *= g.inv_h;
-                }
-                const int lc = st.key & 63;
-                const int t0 = ((lc >> 4) * PT + ((lc >> 2) & 3)) * PT + (lc & 3);
-                // FP32x2 sums: x/y components in pairs, the z velocity with the z acceleration
-                const float2 z2 = make_float2(0.f, 0.f);
-                float2 vg01 = z2, acc01 = z2, vz_az = z2;       // (vg_x, vg_y), (a_x, a_y), (vg_z, a_z)
-                float2 Lc0 = z2, Lc1 = z2, Lc2 = z2;            // (L[0][b], L[1][b]) for b = x, y, z
-                float L20 = 0.f, L21 = 0.f, L22 = 0.f;           // L[2][b]
-                float gtx = 0.f, gty = 0.f, gtz = 0.f, trate = 0.f;  // heat conduction (THERMAL)
-                float2 Sx2[3], Gx2[3];
-#pragma unroll
-                for (int k = 0; k < 3; k++) {
-                    Sx2[k] = make_float2(Sx[k], Sx[k]);
-                    Gx2[k] = make_float2(Gx[k], Gx[k]);
-                }
-#pragma unroll
-                for (int kk = 0; kk < 3; kk++) {
-                    if (kk > 0 && !g.is3d) break;
-#pragma unroll
-                    for (int jj = 0; jj < 3; jj++) {
-                        const float4 *tv = TV + t0 + (kk * PT + jj) * PT;
-                        const float2 *ta = TA + t0 + (kk * PT + jj) * PT;
-                        float2 xv01 = z2, xv2a2 = z2, yv01 = z2, xa01 = z2;
-                        float yv2 = 0.f;
-#pragma unroll
-                        for (int ii = 0; ii < 3; ii++) {
-                            const float4 V = tv[ii];
-                            const float2 A = ta[ii];
-                            xv01 = fma2(Sx2[ii], lo2(V), xv01);
-                            xv2a2 = fma2(Sx2[ii], hi2(V), xv2a2);
-                            yv01 = fma2(Gx2[ii], lo2(V), yv01);
-                            yv2 = fmaf(Gx[ii], V.z, yv2);
-                            xa01 = fma2(Sx2[ii], A, xa01);
-                        }
-                        const float syz = Sy[jj] * Sz[kk], gyz = Gy[jj] * Sz[kk], syg = Sy[jj] * Gz[kk];
-                        const float2 syz2 = make_float2(syz, syz), gyz2 = make_float2(gyz, gyz);
-                        const float2 syg2 = make_float2(syg, syg);
-                        vg01 = fma2(syz2, xv01, vg01);
-                        vz_az = fma2(syz2, xv2a2, vz_az);
-                        acc01 = fma2(syz2, xa01, acc01);
-                        Lc0 = fma2(syz2, yv01, Lc0);
-                        L20 = fmaf(syz, yv2, L20);
-                        Lc1 = fma2(gyz2, xv01, Lc1);
-                        L21 = fmaf(gyz, xv2a2.x, L21);
-                        Lc2 = fma2(syg2, xv01, Lc2);
-                        L22 = fmaf(syg, xv2a2.x, L22);
-                        if (THERMAL) {
-                            const float2 *tn = TN + t0 + (kk * PT + jj) * PT;
-                            float xT = 0.f, xgT = 0.f, xR = 0.f;
-#pragma unroll
-                            for (int ii = 0; ii < 3; ii++) {
-                                const float2 q = tn[ii];
-                                xT = fmaf(Sx[ii], q.x, xT);
-                                xgT = fmaf(Gx[ii], q.x, xgT);
-                                xR = fmaf(Sx[ii], q.y, xR);
-                            }
-                            gtx = fmaf(syz, xgT, gtx);
-                            gty = fmaf(gyz, xT, gty);
-                            gtz = fmaf(syg, xT, gtz);
-                            trate = fmaf(syz, xR, trate);
-                        }
-                    }
-                }
-                float acc[3] = {acc01.x, acc01.y, vz_az.y}, vg[3] = {vg01.x, vg01.y, vz_az.x};
-                const float L[3][3] = {{Lc0.x, Lc1.x, Lc2.x}, {Lc0.y, Lc1.y, Lc2.y}, {L20, L21, L22}};
+                float acc[3], vg[3], L[3][3], thg[4];
+                g2p_node_sums<THERMAL>(TV, TA, TN, st.o, st.key, g, acc, vg, L, thg);
                 cp_async_wait_all();
 #pragma unroll
                 for (int k = 0; k < 3; k++) st.v[k] = stage[k][tid];
@@ -1894,7 +1911,7 @@ __global__ void __launch_bounds__(GY_G2P_THREADS, THERMAL ? GY_G2P_MINB_TH : GY_
                 if (!g.is3d) c0[2] = 0;
                 update_after_g2p<HAS_DP>(st, c0, acc, vg, L, a, check_finite != 0, i);
                 store_state<HAS_DP>(dst, i, st);
-                if (THERMAL) therm[st.pid] = make_float4(th.x + trate * a.sc->dt, gtx, gty, gtz);
+                if (THERMAL) therm[st.pid] = make_float4(th.x + thg[3] * a.sc->dt, thg[0], thg[1], thg[2]);
                 if (a.stats) particle_stats(s_st, st);
             }
             if (cnt < (int)blockDim.x) break;

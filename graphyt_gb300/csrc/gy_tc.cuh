@@ -16,12 +16,13 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "gy_common.cuh"
+
 namespace gy {
 
 #ifndef GY_TC_SPIN_LIMIT
 #define GY_TC_SPIN_LIMIT (1u << 22)  // polls of an mbarrier (32 ns apart) before a wait gives up
 #endif
-constexpr int ERR_TC_TIMEOUT = 4;  // device status bit: a tensor-core wait gave up
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p)
 {

@@ -74,6 +74,7 @@ SIGNATURES = {
     "gy_set_particle_damage": (C.c_int, [_vp, C.c_int64, _i64p, _dp]),
     "gy_set_particle_flaw": (C.c_int, [_vp, C.c_int64, _i64p, _dp]),
     "gy_tc_gemm_bf16": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int, C.c_int, _vp, _vp]),
+    "gy_tc_wait_check": (C.c_int, [_vp, _vp, _vp]),
     "gy_mlp_param_count": (C.c_int64, []),
     "gy_mlp_forward": (C.c_int, [_vp, _vp, C.c_int64, _vp, _vp, _vp]),
     "gy_mlp_grad": (C.c_int, [_vp, _vp, _vp, C.c_int64, _vp, _vp, _vp, _vp]),

@@ -781,7 +781,32 @@ void launch_dp_surrogate(const PView &P, const float4 *pend, const unsigned int 
     note_launch(1);
 }
 
+// The give-up path of the bounded mbarrier wait: thread 0 initialises an mbarrier that nothing
+// arrives at, every thread waits on it, and the block reports the wait that gave up in the
+// status word -- the route every tensor-core wait of the library takes when its arrival is lost.
+__global__ void k_tc_wait_check(int *status, unsigned long long *elapsed_ns)
+{
+    __shared__ uint64_t mbar;
+    if (threadIdx.x == 0) mbar_init(&mbar, 1);
+    __syncthreads();
+    const unsigned long long t0 = clock_now_ns();
+    const bool ok = __syncthreads_and(mbar_wait(&mbar, 0)) != 0;
+    if (threadIdx.x == 0) {
+        if (!ok) atomicOr(status, ERR_TC_TIMEOUT);
+        *elapsed_ns = clock_now_ns() - t0;
+    }
+}
+
 }  // namespace gy
+
+extern "C" gy_status gy_tc_wait_check(int *d_status, unsigned long long *d_elapsed_ns, void *stream)
+{
+    using namespace gy;
+    if (!d_status || !d_elapsed_ns) return GY_ERR_ARG;
+    k_tc_wait_check<<<1, 64, 0, static_cast<cudaStream_t>(stream)>>>(d_status, d_elapsed_ns);
+    note_launch(1);
+    return cudaPeekAtLastError() == cudaSuccess ? GY_OK : GY_ERR_CUDA;
+}
 
 extern "C" gy_status gy_tc_gemm_bf16(const uint16_t *d_A, const uint16_t *d_B, float *d_C, int M, int N, int K,
                                      int *d_status, void *stream)

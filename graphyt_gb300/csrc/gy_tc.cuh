@@ -104,6 +104,14 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity)
     return false;
 }
 
+// the global nanosecond timer
+__device__ __forceinline__ unsigned long long clock_now_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 // make this thread's generic-proxy shared-memory writes visible to the tensor core (async proxy)

@@ -274,6 +274,13 @@ gy_status gy_time_steps(gy_solver *h, double t0, int step0, int nsteps, float *m
 gy_status gy_tc_gemm_bf16(const uint16_t *d_A, const uint16_t *d_B, float *d_C, int M, int N, int K, int *d_status,
                           void *stream);
 
+/* Self-check of the bounded waits (no reference counterpart): one block waits on an mbarrier
+ * that nothing completes, gives up after the library's poll limit (a fraction of a second),
+ * sets bit 4 in d_status and writes the wait's duration in ns to d_elapsed_ns -- the path every
+ * tensor-core wait takes when its arrival is lost, so a lost arrival ends the kernel with a
+ * status instead of a hang.  Only enqueues work on stream. */
+gy_status gy_tc_wait_check(int *d_status, unsigned long long *d_elapsed_ns, void *stream);
+
 /* ---- learned Drucker-Prager surrogate (no reference counterpart) --------------------------
  * A 16 -> 64 -> 64 -> 7 MLP with SiLU in one packed FP32 parameter vector of
  * gy_mlp_param_count() floats: W1 [16][64], b1 [64], W2 [64][64], b2 [64], W3 [64][7], b3 [7]

@@ -61,6 +61,28 @@ def test_tc_gemm_rejects_bad_shapes(gpu_lib):
         assert gpu_lib.gy_tc_gemm_bf16(p, p, p, M, N, K, None, None) == _lib.GY_ERR_ARG
 
 
+def test_lost_arrival_ends_in_a_status(gpu_lib, torch_cuda):
+    """A tensor-core wait whose arrival never comes gives up: a block waiting on an mbarrier that
+    nothing completes ends within a second with the timeout bit set, and the context stays
+    usable (a GEMM afterwards is exact)."""
+    torch = torch_cuda
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    elapsed = torch.zeros(1, dtype=torch.int64, device="cuda")
+    assert gpu_lib.gy_tc_wait_check(ctypes.c_void_p(status.data_ptr()), ctypes.c_void_p(elapsed.data_ptr()), None) == 0
+    torch.cuda.synchronize()
+    assert status.item() & 4
+    assert 1e6 < elapsed.item() < 2e9, elapsed.item()  # gave up after a fraction of a second
+    a = bf16_bits(np.ones((128, 16), np.float32))
+    A = torch.from_numpy(a.view(np.int16)).cuda()
+    Cm = torch.zeros((128, 16), dtype=torch.float32, device="cuda")
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    assert gpu_lib.gy_tc_gemm_bf16(ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(A.data_ptr()),
+                                   ctypes.c_void_p(Cm.data_ptr()), 128, 16, 16, ctypes.c_void_p(st.data_ptr()),
+                                   None) == 0
+    torch.cuda.synchronize()
+    assert st.item() == 0 and torch.all(Cm == 16.0)
+
+
 def mlp_params(rng, in_mean, in_std, out_mean, out_std):
     """A packed parameter vector in the library's layout, weights ~ N(0, 1/fan_in)."""
     W1 = rng.standard_normal((16, 64)) / 4.0

@@ -802,7 +802,8 @@ gy_status gy_initialize(gy_solver *h, const gy_material *mats, int nmat, const g
         h->resort_valid = false;
     }
     if ((st = dalloc(h, &h->d_perm, h->cap))) return st;
-    if ((st = dalloc(h, &h->d_seg, h->cap))) return st;
+    // multi-body handles: the second half lists the segments the one-object P2G defers
+    if ((st = dalloc(h, &h->d_seg, (h->multi ? 2 : 1) * h->cap))) return st;
     if ((st = dalloc(h, &h->d_nseg, 4))) return st;
     CK(h, cudaMemsetAsync(h->d_nseg, 0, 4 * sizeof(int), h->stream));
     {
@@ -967,8 +968,16 @@ static void issue_step(gy_solver *h, const StepVariant &v, cudaEvent_t *tev)
     // (b) P2G
     // heat conduction: fused into the single-body P2G, a separate pass for body slots
     const bool fused_thermal = h->thermal && !h->multi;
+    // multi-body: the one-object segments take the plane-lane kernel unless normals are tracked
+    int *defer = nullptr, *ndefer = nullptr;
+    if (h->multi && !h->opt.track_normals) {
+        defer = h->d_seg + h->cap;
+        ndefer = h->d_nseg + 2;
+        cudaMemsetAsync(ndefer, 0, sizeof(int), s);
+    }
     launch_p2g(src, perm, skey, h->n, h->d_seg, nseg, h->persist_grid, h->nb, a, s,
-               fused_thermal ? h->d_therm : nullptr, fused_thermal ? h->d_tnode : nullptr, h->opt.p2g_lanes);
+               fused_thermal ? h->d_therm : nullptr, fused_thermal ? h->d_tnode : nullptr, h->opt.p2g_lanes, defer,
+               ndefer);
     if (h->thermal && h->multi)
         launch_thermal_p2g(src, h->d_therm, perm, skey, h->n, h->d_seg, nseg, h->d_tnode, a, s);
     if (tev) cudaEventRecord(tev[2], s);

@@ -505,17 +505,28 @@ static_assert(PP_CH == PC_CH, "the chunk bounds helper assumes two particles per
 
 __device__ __forceinline__ float2 dup2(float x) { return make_float2(x, x); }
 
+// MULTI: the same kernel on a multi-body problem, for the segments it can take whole -- every
+// particle deformable and of one object, every tile node with that object as its only body (or
+// none) -- where a node's slot-0 mass, momentum and force equal its centre-of-mass sums and no
+// normal is read (the solve takes a node's normal only where two bodies meet, and G2P only when
+// normals are tracked, in which case this path is not used).  It adds gravity per node (the
+// multi-body solve does not) and flushes into the centre-of-mass and slot-0 accumulators.  A
+// segment that fails the test, at its start or at any chunk, is appended to `defer`, its tile
+// dropped, and k_p2g_multi_tiled takes it.
+template <bool MULTI>
 __global__ void __launch_bounds__(PP_THREADS, GY_PP_MINB) k_p2g_planes(PView P, const int *perm, const int *skey, long long n,
                                                               const int *seg_start, const int *nseg_ptr, int sorted,
-                                                              NodeBufs nb, GridGeom g)
+                                                              NodeBufs nb, StepArgs a, int *defer, int *ndefer)
 {
     __shared__ float tile[P2G_FIELDS * PT_NODES];
+    __shared__ unsigned char tbh[MULTI ? PT_NODES : 1];  // MULTI: the node has a body (slot 0 exists)
     __shared__ float4 SA[PP_ROWS], SB[PP_ROWS], SC[PP_ROWS], SD[PP_ROWS], SE[PP_ROWS], SF[PP_ROWS];
     __shared__ float2 SZ[3][PP_ROWS];
     __shared__ int run_start[PP_CH + 1];
     __shared__ int run_cell[PP_CH];
     __shared__ int wcount[PP_THREADS / 32];
     __shared__ long long s_end;
+    const GridGeom &g = a.g;
     const int nseg = *nseg_ptr;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const unsigned lt = (1u << lane) - 1u;
@@ -530,6 +541,24 @@ __global__ void __launch_bounds__(PP_THREADS, GY_PP_MINB) k_p2g_planes(PView P, 
         decode_block(blk, g, bx, by, bz);
         const int tox = bx * CB, toy = by * CB, toz = g.is3d ? bz * CB : 0;
         for (int t = tid; t < P2G_FIELDS * PT_NODES; t += PP_THREADS) tile[t] = 0.f;
+        int obj0 = 0;
+        if (MULTI) {
+            const uint32_t info0 = (uint32_t)P.ii(PF_INFO, sorted ? perm[start] : start);
+            obj0 = info_obj(info0);
+            bool ok = !(info0 & INFO_RIGID);
+            for (int t = tid; t < PT_NODES; t += PP_THREADS) {
+                const int ni = tox + t % PT, nj = toy + (t / PT) % PT, nk = toz + t / (PT * PT);
+                const int2 pr = (ni < g.nx && nj < g.ny && nk < g.nz) ? nb.body[node_index(ni, nj, nk, g)]
+                                                                      : make_int2(-1, -1);
+                ok = ok && pr.y == -1 && (pr.x == obj0 || pr.x == -1);
+                tbh[t] = pr.x >= 0;
+            }
+            if (!__syncthreads_and(ok)) {
+                if (tid == 0) defer[atomicAdd(ndefer, 1)] = (int)start;
+                continue;
+            }
+        }
+        bool dropped = false;
         for (long long base = start;; base += PP_CH) {
             const long long ia = base + 2 * tid, ib = ia + 1;
             int cnt, ka = -1, kb = -1, kp = -1;
@@ -554,12 +583,17 @@ __global__ void __launch_bounds__(PP_THREADS, GY_PP_MINB) k_p2g_planes(PView P, 
             }
             if (cnt <= 0) break;
             // ---- stage particles 2 tid and 2 tid + 1 of the chunk ----
+            bool mine_ok = true;
 #pragma unroll
             for (int h2 = 0; h2 < 2; h2++) {
                 const int q = 2 * tid + h2;
                 if (q >= cnt) break;
                 const long long j = h2 ? jb : ja;
                 const int row = pp_row(q);
+                if (MULTI) {
+                    const uint32_t info = (uint32_t)P.ii(PF_INFO, j);
+                    mine_ok = mine_ok && !(info & INFO_RIGID) && info_obj(info) == obj0;
+                }
                 float Sx[3], Gx[3], Sy[3], Gy[3], Sz[3], Gz[3];
                 gimp_axis(P.f(PF_OX, j), g, Sx, Gx);
                 gimp_axis(P.f(PF_OY, j), g, Sy, Gy);
@@ -588,7 +622,14 @@ __global__ void __launch_bounds__(PP_THREADS, GY_PP_MINB) k_p2g_planes(PView P, 
             const bool hb = vb && cb != ca;
             const unsigned ba = __ballot_sync(0xffffffffu, ha), bb = __ballot_sync(0xffffffffu, hb);
             if (lane == 0) wcount[warp] = __popc(ba) + __popc(bb);
-            __syncthreads();
+            if (MULTI) {
+                if (!__syncthreads_and(mine_ok)) {
+                    dropped = true;
+                    break;
+                }
+            } else {
+                __syncthreads();
+            }
             int wbase = 0, R = 0;
 #pragma unroll
             for (int w2 = 0; w2 < PP_THREADS / 32; w2++) {
@@ -674,15 +715,30 @@ __global__ void __launch_bounds__(PP_THREADS, GY_PP_MINB) k_p2g_planes(PView P, 
             }
             if (cnt < PP_CH) break;
         }
+        if (MULTI && dropped) {
+            // another object or a rigid particle: the general kernel takes the whole segment
+            if (tid == 0) defer[atomicAdd(ndefer, 1)] = (int)start;
+            continue;
+        }
         __syncthreads();
         // ---- flush the tile: two vector reductions per touched node ----
         for (int t = tid; t < PT_NODES; t += PP_THREADS) {
             const float m = tile[t], px = tile[PT_NODES + t], py = tile[2 * PT_NODES + t], pz = tile[3 * PT_NODES + t];
-            const float fx = tile[4 * PT_NODES + t], fy = tile[5 * PT_NODES + t], fz = tile[6 * PT_NODES + t];
+            float fx = tile[4 * PT_NODES + t], fy = tile[5 * PT_NODES + t], fz = tile[6 * PT_NODES + t];
             if (m == 0.f && px == 0.f && py == 0.f && pz == 0.f && fx == 0.f && fy == 0.f && fz == 0.f) continue;
             const int ni = tox + t % PT, nj = toy + (t / PT) % PT, nk = toz + t / (PT * PT);
             if (ni >= g.nx || nj >= g.ny || nk >= g.nz) continue;
             const int nd = node_index(ni, nj, nk, g);
+            if (MULTI) {
+                // the multi-body step adds gravity in P2G, as sum w m g (Extrapolation.cpp:226-278)
+                fx += m * a.sc->gravity[0];
+                fy += m * a.sc->gravity[1];
+                fz += m * a.sc->gravity[2];
+                if (tbh[t]) {
+                    red_add4(&nb.bacc0[0][nd], m, px, py, pz);
+                    red_add4(&nb.bacc1[0][nd], fx, fy, fz, 0.f);
+                }
+            }
             red_add4(&nb.acc0[nd], m, px, py, pz);
             red_add4(&nb.acc1[nd], fx, fy, fz, 0.f);
             mark_node(nb, ni, nj, nk, g);
@@ -969,19 +1025,30 @@ __global__ void __launch_bounds__(P2G_CH) k_p2g_multi_tiled(PView P, const int *
 
 void launch_p2g(const PView &p, const int *perm, const int *skey, long long n, const int *seg_start,
                 const int *nseg, int persist_grid, const NodeBufs &nb, const StepArgs &a, cudaStream_t s,
-                const float4 *therm, float2 *tnode, int lanes)
+                const float4 *therm, float2 *tnode, int lanes, int *defer, int *ndefer)
 {
     if (n == 0) return;
     if (a.multi_body) {
-        static int mgrid = 0;  // persistent grid of the multi-body kernel (its own occupancy)
+        static int mgrid = 0, qgrid = 0;  // persistent grids of the two multi-body kernels
         if (mgrid == 0) {
             int dev = 0, sms = 1, b = 0;
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_p2g_multi_tiled, P2G_CH, 0);
             mgrid = sms * std::max(b, 1);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_p2g_planes<true>, PP_THREADS, 0);
+            qgrid = sms * std::max(b, 1);
         }
-        k_p2g_multi_tiled<<<mgrid, P2G_CH, 0, s>>>(p, perm, skey, n, seg_start, nseg, perm ? 1 : 0, nb, a);
+        if (lanes == 3 && defer && ndefer) {
+            // the one-object segments with plane lanes, the rest (listed in defer, whose count
+            // the caller zeroed) with the body-slot kernel
+            k_p2g_planes<true><<<qgrid, PP_THREADS, 0, s>>>(p, perm, skey, n, seg_start, nseg, perm ? 1 : 0, nb, a,
+                                                             defer, ndefer);
+            k_p2g_multi_tiled<<<mgrid, P2G_CH, 0, s>>>(p, perm, skey, n, defer, ndefer, perm ? 1 : 0, nb, a);
+            note_launch(1);
+        } else {
+            k_p2g_multi_tiled<<<mgrid, P2G_CH, 0, s>>>(p, perm, skey, n, seg_start, nseg, perm ? 1 : 0, nb, a);
+        }
     } else {
         if (therm) {
             static int tgrid = 0;  // persistent grid of the variant with heat conduction
@@ -1000,10 +1067,11 @@ void launch_p2g(const PView &p, const int *perm, const int *skey, long long n, c
                 int dev = 0, sms = 1, b = 0;
                 cudaGetDevice(&dev);
                 cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_p2g_planes, PP_THREADS, 0);
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_p2g_planes<false>, PP_THREADS, 0);
                 pgrid = sms * std::max(b, 1);
             }
-            k_p2g_planes<<<pgrid, PP_THREADS, 0, s>>>(p, perm, skey, n, seg_start, nseg, perm ? 1 : 0, nb, a.g);
+            k_p2g_planes<false><<<pgrid, PP_THREADS, 0, s>>>(p, perm, skey, n, seg_start, nseg, perm ? 1 : 0, nb, a,
+                                                              nullptr, nullptr);
         } else {
             k_p2g_cols<false><<<persist_grid, PC_THREADS, 0, s>>>(p, perm, skey, n, seg_start, nseg, perm ? 1 : 0, nb,
                                                                    a.g, nullptr, nullptr, nullptr);

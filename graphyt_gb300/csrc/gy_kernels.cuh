@@ -109,7 +109,8 @@ long long launch_count();
 // the single-body kernel without heat conduction, 3 (z-plane lanes) or 9 (x-column lanes).
 void launch_p2g(const PView &p, const int *perm, const int *skey, long long n, const int *seg_start,
                 const int *nseg, int persist_grid, const NodeBufs &nb, const StepArgs &a, cudaStream_t s,
-                const float4 *therm = nullptr, float2 *tnode = nullptr, int lanes = 3);
+                const float4 *therm = nullptr, float2 *tnode = nullptr, int lanes = 3, int *defer = nullptr,
+                int *ndefer = nullptr);
 void launch_fold(const NodeBufs &nb, const StepArgs &a, cudaStream_t s);
 void launch_solve(const NodeBufs &nb, const StepArgs &a, bool keep_node_fields, cudaStream_t s);
 // therm / tnode non-null: the single-body kernel also runs the heat conduction G2P and the

@@ -557,7 +557,8 @@ static gy_status alloc_nodes(gy_solver *h)
     if (h->multi && h->opt.track_normals) rows += 2;
     size_t bytes = (size_t)rows * nn * sizeof(float4);
     size_t extra = 0;
-    if (h->multi) extra = (size_t)nn * sizeof(int2) + (size_t)nn + 64;
+    const long long ncb = (long long)h->g.nbx * h->g.nby * h->g.nbz;  // cell blocks
+    if (h->multi) extra = (size_t)nn * sizeof(int2) + (size_t)nn + 64 + (size_t)ncb * sizeof(int) + 64;
     extra += (size_t)(2 * h->g.nnb + 16) * sizeof(int) + 64;
     if (h->any_node_bc) extra += (size_t)nn * sizeof(float4) + (size_t)nn + 64;
     char *mem = nullptr;
@@ -611,6 +612,9 @@ static gy_status alloc_nodes(gy_solver *h)
         c += (size_t)nn * sizeof(int2);
         nb.has_rigid = (unsigned char *)c;
         c += (size_t)nn;
+        c = (char *)(((uintptr_t)c + 15) & ~(uintptr_t)15);
+        nb.block_body = (int *)c;
+        c += (size_t)ncb * sizeof(int);
         // per-(cell, object) smallest particle id + rigid bits
         gy_status st = dalloc(h, &h->d_cell_min, (size_t)h->g.nc * (h->nbody + 1));
         if (st) return st;
@@ -1475,6 +1479,7 @@ gy_status gy_state_load(gy_solver *h, const void *buf, int64_t bytes)
         CK(h, cudaMemcpy(h->nb.body, p, (size_t)h->nn * sizeof(int2), cudaMemcpyHostToDevice));
         p += (size_t)h->nn * sizeof(int2);
         CK(h, cudaMemcpy(h->nb.has_rigid, p, (size_t)h->nn, cudaMemcpyHostToDevice));
+        launch_block_body(h->nb, h->g, h->stream);
         p += (size_t)h->nn;
     }
     if (hd.thermal) {

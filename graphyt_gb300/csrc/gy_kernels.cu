@@ -519,7 +519,6 @@ __global__ void __launch_bounds__(PP_THREADS, GY_PP_MINB) k_p2g_planes(PView P, 
                                                               NodeBufs nb, StepArgs a, int *defer, int *ndefer)
 {
     __shared__ float tile[P2G_FIELDS * PT_NODES];
-    __shared__ unsigned char tbh[MULTI ? PT_NODES : 1];  // MULTI: the node has a body (slot 0 exists)
     __shared__ float4 SA[PP_ROWS], SB[PP_ROWS], SC[PP_ROWS], SD[PP_ROWS], SE[PP_ROWS], SF[PP_ROWS];
     __shared__ float2 SZ[3][PP_ROWS];
     __shared__ int run_start[PP_CH + 1];
@@ -540,24 +539,18 @@ __global__ void __launch_bounds__(PP_THREADS, GY_PP_MINB) k_p2g_planes(PView P, 
         int bx, by, bz;
         decode_block(blk, g, bx, by, bz);
         const int tox = bx * CB, toy = by * CB, toz = g.is3d ? bz * CB : 0;
-        for (int t = tid; t < P2G_FIELDS * PT_NODES; t += PP_THREADS) tile[t] = 0.f;
-        int obj0 = 0;
+        int obj0 = 0, tb = -1;
         if (MULTI) {
+            // the same values in every thread: the segment's first particle and its block's tile
             const uint32_t info0 = (uint32_t)P.ii(PF_INFO, sorted ? perm[start] : start);
             obj0 = info_obj(info0);
-            bool ok = !(info0 & INFO_RIGID);
-            for (int t = tid; t < PT_NODES; t += PP_THREADS) {
-                const int ni = tox + t % PT, nj = toy + (t / PT) % PT, nk = toz + t / (PT * PT);
-                const int2 pr = (ni < g.nx && nj < g.ny && nk < g.nz) ? nb.body[node_index(ni, nj, nk, g)]
-                                                                      : make_int2(-1, -1);
-                ok = ok && pr.y == -1 && (pr.x == obj0 || pr.x == -1);
-                tbh[t] = pr.x >= 0;
-            }
-            if (!__syncthreads_and(ok)) {
+            tb = nb.block_body[blk];
+            if ((info0 & INFO_RIGID) || (tb != obj0 && tb != -1)) {
                 if (tid == 0) defer[atomicAdd(ndefer, 1)] = (int)start;
                 continue;
             }
         }
+        for (int t = tid; t < P2G_FIELDS * PT_NODES; t += PP_THREADS) tile[t] = 0.f;
         bool dropped = false;
         for (long long base = start;; base += PP_CH) {
             const long long ia = base + 2 * tid, ib = ia + 1;
@@ -734,7 +727,7 @@ __global__ void __launch_bounds__(PP_THREADS, GY_PP_MINB) k_p2g_planes(PView P, 
                 fx += m * a.sc->gravity[0];
                 fy += m * a.sc->gravity[1];
                 fz += m * a.sc->gravity[2];
-                if (tbh[t]) {
+                if (tb >= 0 && nb.body[nd].x >= 0) {
                     red_add4(&nb.bacc0[0][nd], m, px, py, pz);
                     red_add4(&nb.bacc1[0][nd], fx, fy, fz, 0.f);
                 }
@@ -2349,10 +2342,47 @@ __global__ void __launch_bounds__(64) k_body_assign(NodeBufs nb, GridGeom g, con
     nb.has_rigid[nd] = hr;
 }
 
+// Per 4x4x4 cell block, the body of its 6x6x6 node tile when the tile has one (every node with
+// body pair (b, -1) or (-1, -1)): b, -1 for none, -2 for two or more; one warp per block.
+// P2G sends the one-object segments of such blocks to the plane-lane kernel.
+__global__ void __launch_bounds__(128) k_block_body(NodeBufs nb, GridGeom g)
+{
+    const int lane = threadIdx.x & 31;
+    const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (w >= (long long)g.nbx * g.nby * g.nbz) return;  // whole warps
+    int bx, by, bz;
+    decode_block((int)w, g, bx, by, bz);
+    const int tox = bx * CB, toy = by * CB, toz = g.is3d ? bz * CB : 0;
+    bool two = false;
+    int lo = 0x7fffffff, hi = -1;
+    for (int t = lane; t < PT_NODES; t += 32) {
+        const int ni = tox + t % PT, nj = toy + (t / PT) % PT, nk = toz + t / (PT * PT);
+        if (ni >= g.nx || nj >= g.ny || nk >= g.nz) continue;
+        const int2 pr = nb.body[node_index(ni, nj, nk, g)];
+        two = two || pr.y != -1;
+        if (pr.x >= 0) {
+            lo = min(lo, pr.x);
+            hi = max(hi, pr.x);
+        }
+    }
+    two = __any_sync(0xffffffffu, two);
+    lo = __reduce_min_sync(0xffffffffu, lo);
+    hi = __reduce_max_sync(0xffffffffu, hi);
+    if (lane == 0) nb.block_body[w] = (two || (hi >= 0 && lo != hi)) ? -2 : hi;
+}
+
 void launch_body_assign(const NodeBufs &nb, const StepArgs &a, const int *cell_min, int nbody, const int *nidx_x,
                         const int *nidx_y, const int *nidx_z, cudaStream_t s)
 {
     k_body_assign<<<(unsigned)a.g.nnb, 64, 0, s>>>(nb, a.g, cell_min, nbody, nidx_x, nidx_y, nidx_z);
+    note_launch(1);
+    launch_block_body(nb, a.g, s);
+}
+
+void launch_block_body(const NodeBufs &nb, const GridGeom &g, cudaStream_t s)
+{
+    const long long ncb = (long long)g.nbx * g.nby * g.nbz;
+    k_block_body<<<(unsigned)((ncb + 3) / 4), 128, 0, s>>>(nb, g);
     note_launch(1);
 }
 

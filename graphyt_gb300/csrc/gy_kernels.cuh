@@ -40,6 +40,7 @@ struct NodeBufs {
     int *active_n;                // length of active_list
     unsigned char *has_rigid;     // bit0: slot 0 rigid, bit1: slot 1 rigid
     int *active_count;            // nodes with mass (stats)
+    int *block_body;              // per 4x4x4 cell block: the one body of its 6x6x6 node tile, -1 none, -2 more
 };
 
 // Hooks of the learned Drucker-Prager surrogate into the step (every pointer null when off).
@@ -112,6 +113,7 @@ void launch_p2g(const PView &p, const int *perm, const int *skey, long long n, c
                 const float4 *therm = nullptr, float2 *tnode = nullptr, int lanes = 3, int *defer = nullptr,
                 int *ndefer = nullptr);
 void launch_fold(const NodeBufs &nb, const StepArgs &a, cudaStream_t s);
+void launch_block_body(const NodeBufs &nb, const GridGeom &g, cudaStream_t s);
 void launch_solve(const NodeBufs &nb, const StepArgs &a, bool keep_node_fields, cudaStream_t s);
 // therm / tnode non-null: the single-body kernel also runs the heat conduction G2P and the
 // temperature update (multi-body problems run launch_thermal_g2p instead)

@@ -613,15 +613,16 @@ class Solver:
         """Choose the fastest step configuration for this problem and keep it.
 
         Two stages: the sort cadence and kind (``candidates``: (sort_every, full_sort) pairs),
-        then, with those fixed, the single-body P2G's lane mapping (``lanes``: 3 z-plane lanes
-        per run of equal cell, ten runs per warp, or 9 x-column lanes, three runs per warp --
-        how many particles a warp sums at once).  Each candidate runs a few untimed steps (its
+        then, with those fixed, the P2G lane mapping (``lanes``: 3 z-plane lanes per run of
+        equal cell, ten runs per warp, or 9 x-column lanes, three runs per warp -- how many
+        particles a warp sums at once; on multi-body problems, whether the one-object segments
+        take the 3-lane kernel or all take the body-slot kernel).  Each candidate runs a few untimed steps (its
         CUDA graphs are captured there), then ``steps`` steps timed with CUDA events.  These
         are real steps of the run, from step ``step0`` on, since the knobs change speed and
         never results beyond summation order; the returned ``next_step`` is where the caller
         continues.  The cell block (4^3 cells and its 6^3-node shared-memory tile) is fixed by
-        the kernels' key encoding; multi-body problems skip the lane stage, whose mapping only
-        the single-body P2G has."""
+        the kernels' key encoding; multi-body problems that track normals skip the lane stage
+        (every segment takes the body-slot kernel there)."""
         ms = C.c_float()
         dt = self.dt
         step = int(step0)
@@ -644,7 +645,7 @@ class Solver:
         o = L.Options()
         L.check(self.lib.gy_get_options(self.h, C.byref(o)), self.h)
         best_lanes = int(o.p2g_lanes)
-        if self._single_body():  # the lane mapping is the single-body P2G's
+        if self._single_body() or not o.track_normals:  # tracked normals: the body-slot kernel only
             for ln in lanes:
                 lane_times[int(ln)] = timed(sort_every=best[0], full_sort=best[1], p2g_lanes=int(ln))
             best_lanes = min(lane_times, key=lane_times.get)

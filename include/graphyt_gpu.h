@@ -83,9 +83,13 @@ typedef struct gy_options {
     int track_normals;  /* 1: keep per-particle contact normals (getNormalsArr) */
     int check_finite;   /* 1: flag NaN/Inf in particle state every step */
     int keep_node_fields; /* 1: keep centre-of-mass node velocity/force for node getters */
-    int p2g_lanes;      /* single-body P2G without heat conduction: lanes per run of equal cell,
-                           3 (default: each lane sums a z-plane of nine stencil nodes) or 9 (each
-                           lane a column of three x nodes); same sums, different speed */
+    int p2g_lanes;      /* P2G without heat conduction: lanes per run of equal cell, 3 (default:
+                           each lane sums a z-plane of nine stencil nodes) or 9 (each lane a
+                           column of three x nodes).  Multi-body problems without tracked
+                           normals: 3 sends the segments of one deformable object whose node
+                           tile holds that body only through the 3-lane kernel and the rest
+                           through the body-slot kernel; 9 sends every segment through the
+                           body-slot kernel.  Same sums, different speed */
 } gy_options;
 
 /* FP64 conservation sums and counters, Solver.cpp:264-289's printout made a struct. */

@@ -2011,8 +2011,31 @@ __global__ void __launch_bounds__(GY_G2PM_THREADS, GY_G2PM_MINB) k_g2p_multi_til
         int bx, by, bz;
         decode_block(blk, g, bx, by, bz);
         const int tox = bx * CB, toy = by * CB, toz = g.is3d ? bz * CB : 0;
+        // a tile of one body (the cell block's summary): every node with mass and that body
+        // carries it in slot 0, whose solved fields the solve also stores as the node's gv / ga,
+        // so the particles of that body take the single-body tile and sums; the others see
+        // nothing, as in the slot-by-slot sums.  Not with tracked normals.
+        const int tb = NRM ? -2 : nb.block_body[blk];
+        const bool one = tb >= 0;
+        float4 *TV1 = TVb[0];
+        float2 *TA1 = reinterpret_cast<float2 *>(TAb[0]);
         __syncthreads();  // the previous segment's particles are done with the tile
-        for (int t = tid; t < PT_NODES; t += blockDim.x) {
+        if (one) {
+            const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int t = tid; t < PT_NODES; t += blockDim.x) {
+                const int ni = tox + t % PT, nj = toy + (t / PT) % PT, nk = toz + t / (PT * PT);
+                float4 V = z4, A = z4;
+                if (ni < g.nx && nj < g.ny && nk < g.nz) {
+                    const int nd = node_index(ni, nj, nk, g);
+                    V = __ldg(&nb.gv[nd]);
+                    A = __ldg(&nb.ga[nd]);
+                    if (V.x == 0.0f || __ldg(&nb.body[nd].x) < 0) { V = z4; A = z4; }
+                }
+                TV1[t] = make_float4(V.y, V.z, V.w, A.z);
+                TA1[t] = make_float2(A.x, A.y);
+            }
+        }
+        for (int t = tid; t < (one ? 0 : PT_NODES); t += blockDim.x) {
             const int ni = tox + t % PT, nj = toy + (t / PT) % PT, nk = toz + t / (PT * PT);
             int2 pr = make_int2(-1, -1);
             const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -2065,45 +2088,52 @@ __global__ void __launch_bounds__(GY_G2PM_THREADS, GY_G2PM_MINB) k_g2p_multi_til
 #pragma unroll
                 for (int f = 0; f < NST; f++) cp_async4(&stage[f][tid], &src.f(g2p_stage_field(f), j));
                 cp_async_commit();
-                float S[3][3], G[3][3];
-                gimp_axis(st.o[0], g, S[0], G[0]);
-                gimp_axis(st.o[1], g, S[1], G[1]);
-                if (g.is3d) {
-                    gimp_axis(st.o[2], g, S[2], G[2]);
-                } else {
-                    S[2][0] = 1.f; S[2][1] = 0.f; S[2][2] = 0.f; G[2][0] = 0.f; G[2][1] = 0.f; G[2][2] = 0.f;
-                }
-                const int lc = st.key & 63;
-                const int t0 = ((lc >> 4) * PT + ((lc >> 2) & 3)) * PT + (lc & 3);
                 float acc[3] = {0.f, 0.f, 0.f}, vg[3] = {0.f, 0.f, 0.f};
                 float L[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
                 float nrm[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-                for (int kk = 0; kk < 3; kk++) {
-                    if (kk > 0 && !g.is3d) break;
-#pragma unroll
-                    for (int jj = 0; jj < 3; jj++) {
-                        const float syz = S[1][jj] * S[2][kk];
-                        const float gyz = G[1][jj] * S[2][kk] * g.inv_h, syg = S[1][jj] * G[2][kk] * g.inv_h;
-#pragma unroll
-                        for (int ii = 0; ii < 3; ii++) {
-                            const int t = t0 + (kk * PT + jj) * PT + ii;
-                            const int2 pr = TP[t];
-                            const int slot = (pr.x == obj) ? 0 : ((pr.y == obj) ? 1 : -1);
-                            const int sl = slot > 0 ? 1 : 0;
-                            const float on = slot >= 0 ? 1.f : 0.f;  // a third body sees nothing here
-                            const float4 Vb = TVb[sl][t], Ab = TAb[sl][t];
-                            const float wgt = S[0][ii] * syz * on;
-                            const float gx = G[0][ii] * syz * g.inv_h * on, gy = S[0][ii] * gyz * on;
-                            const float gz = S[0][ii] * syg * on;
-                            acc[0] += wgt * Ab.x; acc[1] += wgt * Ab.y; acc[2] += wgt * Ab.z;
-                            vg[0] += wgt * Vb.y; vg[1] += wgt * Vb.z; vg[2] += wgt * Vb.w;
-                            L[0][0] += Vb.y * gx; L[0][1] += Vb.y * gy; L[0][2] += Vb.y * gz;
-                            L[1][0] += Vb.z * gx; L[1][1] += Vb.z * gy; L[1][2] += Vb.z * gz;
-                            L[2][0] += Vb.w * gx; L[2][1] += Vb.w * gy; L[2][2] += Vb.w * gz;
-                            if (NRM) {
-                                const float4 N = TN[sl][t];
-                                nrm[0] += wgt * N.x; nrm[1] += wgt * N.y; nrm[2] += wgt * N.z;
+                if (one) {
+                    if (obj == tb) {
+                        float thg[4];
+                        g2p_node_sums<false>(TV1, TA1, nullptr, st.o, st.key, g, acc, vg, L, thg);
+                    }
+                } else {
+                    float S[3][3], G[3][3];
+                    gimp_axis(st.o[0], g, S[0], G[0]);
+                    gimp_axis(st.o[1], g, S[1], G[1]);
+                    if (g.is3d) {
+                        gimp_axis(st.o[2], g, S[2], G[2]);
+                    } else {
+                        S[2][0] = 1.f; S[2][1] = 0.f; S[2][2] = 0.f; G[2][0] = 0.f; G[2][1] = 0.f; G[2][2] = 0.f;
+                    }
+                    const int lc = st.key & 63;
+                    const int t0 = ((lc >> 4) * PT + ((lc >> 2) & 3)) * PT + (lc & 3);
+    #pragma unroll
+                    for (int kk = 0; kk < 3; kk++) {
+                        if (kk > 0 && !g.is3d) break;
+    #pragma unroll
+                        for (int jj = 0; jj < 3; jj++) {
+                            const float syz = S[1][jj] * S[2][kk];
+                            const float gyz = G[1][jj] * S[2][kk] * g.inv_h, syg = S[1][jj] * G[2][kk] * g.inv_h;
+    #pragma unroll
+                            for (int ii = 0; ii < 3; ii++) {
+                                const int t = t0 + (kk * PT + jj) * PT + ii;
+                                const int2 pr = TP[t];
+                                const int slot = (pr.x == obj) ? 0 : ((pr.y == obj) ? 1 : -1);
+                                const int sl = slot > 0 ? 1 : 0;
+                                const float on = slot >= 0 ? 1.f : 0.f;  // a third body sees nothing here
+                                const float4 Vb = TVb[sl][t], Ab = TAb[sl][t];
+                                const float wgt = S[0][ii] * syz * on;
+                                const float gx = G[0][ii] * syz * g.inv_h * on, gy = S[0][ii] * gyz * on;
+                                const float gz = S[0][ii] * syg * on;
+                                acc[0] += wgt * Ab.x; acc[1] += wgt * Ab.y; acc[2] += wgt * Ab.z;
+                                vg[0] += wgt * Vb.y; vg[1] += wgt * Vb.z; vg[2] += wgt * Vb.w;
+                                L[0][0] += Vb.y * gx; L[0][1] += Vb.y * gy; L[0][2] += Vb.y * gz;
+                                L[1][0] += Vb.z * gx; L[1][1] += Vb.z * gy; L[1][2] += Vb.z * gz;
+                                L[2][0] += Vb.w * gx; L[2][1] += Vb.w * gy; L[2][2] += Vb.w * gz;
+                                if (NRM) {
+                                    const float4 N = TN[sl][t];
+                                    nrm[0] += wgt * N.x; nrm[1] += wgt * N.y; nrm[2] += wgt * N.z;
+                                }
                             }
                         }
                     }

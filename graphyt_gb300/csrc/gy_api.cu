@@ -553,12 +553,13 @@ static gy_status alloc_nodes(gy_solver *h)
     // node buffers in one allocation of float4 rows
     int rows = 4;                    // acc0, acc1, gv, ga
     if (h->opt.keep_node_fields) rows += 2;
-    if (h->multi) rows += 2 * 5;     // bacc0, bacc1, bnrm, bgv, bga per slot
+    if (h->multi) rows += 2 * 3 + 2;  // bacc0, bacc1, bnrm per slot; bgv, bga of slot 1 (slot 0's are gv, ga)
     if (h->multi && h->opt.track_normals) rows += 2;
     size_t bytes = (size_t)rows * nn * sizeof(float4);
     size_t extra = 0;
     const long long ncb = (long long)h->g.nbx * h->g.nby * h->g.nbz;  // cell blocks
-    if (h->multi) extra = (size_t)nn * sizeof(int2) + (size_t)nn + 64 + (size_t)ncb * sizeof(int) + 64;
+    if (h->multi)
+        extra = (size_t)nn * sizeof(int2) + (size_t)nn + 64 + (size_t)(ncb + h->g.nnb) * sizeof(int) + 64;
     extra += (size_t)(2 * h->g.nnb + 16) * sizeof(int) + 64;
     if (h->any_node_bc) extra += (size_t)nn * sizeof(float4) + (size_t)nn + 64;
     char *mem = nullptr;
@@ -582,9 +583,11 @@ static gy_status alloc_nodes(gy_solver *h)
             nb.bacc0[b] = f4; f4 += nn;
             nb.bacc1[b] = f4; f4 += nn;
             nb.bnrm[b] = f4; f4 += nn;
-            nb.bgv[b] = f4; f4 += nn;
-            nb.bga[b] = f4; f4 += nn;
         }
+        nb.bgv[0] = nb.gv;  // the solve stores slot 0's velocity and acceleration as the node's
+        nb.bga[0] = nb.ga;
+        nb.bgv[1] = f4; f4 += nn;
+        nb.bga[1] = f4; f4 += nn;
         if (h->opt.track_normals) {
             nb.nrm_out[0] = f4; f4 += nn;
             nb.nrm_out[1] = f4; f4 += nn;
@@ -615,6 +618,8 @@ static gy_status alloc_nodes(gy_solver *h)
         c = (char *)(((uintptr_t)c + 15) & ~(uintptr_t)15);
         nb.block_body = (int *)c;
         c += (size_t)ncb * sizeof(int);
+        nb.nblk_two = (int *)c;
+        c += (size_t)h->g.nnb * sizeof(int);
         // per-(cell, object) smallest particle id + rigid bits
         gy_status st = dalloc(h, &h->d_cell_min, (size_t)h->g.nc * (h->nbody + 1));
         if (st) return st;

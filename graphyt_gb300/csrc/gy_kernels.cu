@@ -1214,15 +1214,22 @@ __device__ __forceinline__ bool solve_node(const NodeBufs &nb, const StepArgs &a
             float4 B0[2], B1[2], BN[2];
             int2 body = make_int2(-1, -1);
             unsigned char hr = 0;
+            // a node block whose nodes all hold one body has nothing in slot 1, and its nodes
+            // need no normal unless normals are tracked
+            bool two = false;
             if (MULTI) {
-#pragma unroll
-                for (int b = 0; b < 2; b++) {
-                    B0[b] = nb.bacc0[b][nd];
-                    B1[b] = nb.bacc1[b][nd];
-                    BN[b] = nb.bnrm[b][nd];
-                }
+                two = nb.nblk_two[blk] != 0;
+                B0[0] = nb.bacc0[0][nd];
+                B1[0] = nb.bacc1[0][nd];
                 body = nb.body[nd];
                 hr = nb.has_rigid[nd];
+                BN[0] = (two || nb.nrm_out[0]) ? nb.bnrm[0][nd] : z4;
+                B0[1] = B1[1] = BN[1] = z4;
+                if (two) {
+                    B0[1] = nb.bacc0[1][nd];
+                    B1[1] = nb.bacc1[1][nd];
+                    BN[1] = nb.bnrm[1][nd];
+                }
             }
             const int bt = nb.bc_type ? nb.bc_type[nd] : 0;
             nb.acc0[nd] = z4;
@@ -1246,11 +1253,13 @@ __device__ __forceinline__ bool solve_node(const NodeBufs &nb, const StepArgs &a
                     body_update(m, A0, A1, dtn, v1, a1);
                 }
             } else {
-#pragma unroll
-                for (int b = 0; b < 2; b++) {
-                    nb.bacc0[b][nd] = z4;
-                    nb.bacc1[b][nd] = z4;
-                    nb.bnrm[b][nd] = z4;
+                nb.bacc0[0][nd] = z4;
+                nb.bacc1[0][nd] = z4;
+                nb.bnrm[0][nd] = z4;
+                if (two) {
+                    nb.bacc0[1][nd] = z4;
+                    nb.bacc1[1][nd] = z4;
+                    nb.bnrm[1][nd] = z4;
                 }
                 if (active) {
                     vc[0] = A0.y / m; vc[1] = A0.z / m; vc[2] = A0.w / m;
@@ -1337,11 +1346,13 @@ __device__ __forceinline__ bool solve_node(const NodeBufs &nb, const StepArgs &a
             }
             nb.gv[nd] = make_float4(m, v1[0], v1[1], v1[2]);
             nb.ga[nd] = make_float4(a1[0], a1[1], a1[2], 0.f);
-            if (MULTI) {
-                nb.bgv[0][nd] = make_float4(m, v1[0], v1[1], v1[2]);
-                nb.bga[0][nd] = make_float4(a1[0], a1[1], a1[2], 0.f);
+            if (MULTI && two) {
+                // slot 0's solved fields are gv / ga; slot 1 is read only where a node holds two
+                // bodies
                 nb.bgv[1][nd] = make_float4(m, v2[0], v2[1], v2[2]);
                 nb.bga[1][nd] = make_float4(a2[0], a2[1], a2[2], 0.f);
+            }
+            if (MULTI) {
                 if (nb.nrm_out[0]) {
                     nb.nrm_out[0][nd] = make_float4(n1[0], n1[1], n1[2], 0.f);
                     nb.nrm_out[1][nd] = make_float4(-n1[0], -n1[1], -n1[2], 0.f);
@@ -2409,11 +2420,32 @@ void launch_body_assign(const NodeBufs &nb, const StepArgs &a, const int *cell_m
     launch_block_body(nb, a.g, s);
 }
 
+// Per 4x4x4 node block: whether one of its nodes holds two bodies (one warp per block).
+__global__ void __launch_bounds__(128) k_nblock_two(NodeBufs nb, GridGeom g)
+{
+    const int lane = threadIdx.x & 31;
+    const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (w >= g.nnb) return;  // whole warps
+    const int b32 = (int)w;
+    const int bx = b32 % g.nnbx, tb = b32 / g.nnbx;
+    const int by = tb % g.nnby, bz = tb / g.nnby;
+    bool two = false;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int ln = lane + 32 * h;
+        const int i = bx * 4 + (ln & 3), j = by * 4 + ((ln >> 2) & 3), k = bz * 4 + (ln >> 4);
+        if (i < g.nx && j < g.ny && k < g.nz) two = two || nb.body[node_index(i, j, k, g)].y != -1;
+    }
+    two = __any_sync(0xffffffffu, two);
+    if (lane == 0) nb.nblk_two[w] = two ? 1 : 0;
+}
+
 void launch_block_body(const NodeBufs &nb, const GridGeom &g, cudaStream_t s)
 {
     const long long ncb = (long long)g.nbx * g.nby * g.nbz;
     k_block_body<<<(unsigned)((ncb + 3) / 4), 128, 0, s>>>(nb, g);
-    note_launch(1);
+    k_nblock_two<<<(unsigned)((g.nnb + 3) / 4), 128, 0, s>>>(nb, g);
+    note_launch(2);
 }
 
 // ---------------------------------------------------------------------------------------

@@ -32,7 +32,7 @@ struct NodeBufs {
     // multi-body
     float4 *bacc0[2], *bacc1[2];  // per body slot: (m, p), (f, -)
     float4 *bnrm[2];              // per body slot: (n, -)
-    float4 *bgv[2], *bga[2];      // solved per slot: (m, v), (a, -)
+    float4 *bgv[2], *bga[2];      // solved per slot: (m, v), (a, -); slot 0's are gv / ga
     float4 *nrm_out[2];           // normalised slot normals (only when normals are tracked)
     int2 *body;                   // body slot objects (dense ids) or -1
     int *flags;                   // active 4x4x4 node blocks (set by P2G / fold, cleared by the solve)
@@ -41,6 +41,7 @@ struct NodeBufs {
     unsigned char *has_rigid;     // bit0: slot 0 rigid, bit1: slot 1 rigid
     int *active_count;            // nodes with mass (stats)
     int *block_body;              // per 4x4x4 cell block: the one body of its 6x6x6 node tile, -1 none, -2 more
+    int *nblk_two;                // per 4x4x4 node block: 1 if one of its nodes holds two bodies
 };
 
 // Hooks of the learned Drucker-Prager surrogate into the step (every pointer null when off).

@@ -107,6 +107,25 @@ def test_p2g_lane_variants_agree(gpu_lib, make):
                 assert rel_l2(a._get_particles(f), b._get_particles(f)) < 2e-6, (f, sort_every, lanes)
 
 
+@pytest.mark.parametrize("make", [lambda: scenes.two_blocks(), lambda: scenes.brazilian_disc(scale=0.1),
+                                  lambda: scenes.impact_batch(n_inst=4, seed=6, n_min=3000, n_max=9000)])
+def test_multibody_one_body_paths_agree(gpu_lib, make):
+    """On multi-body problems the paths for parts where one body is present -- P2G's plane-lane
+    kernel for one-object segments, G2P's single-body tile, the solve without slot 1 -- form the
+    same sums as the body-slot paths: the default run, a run with every P2G segment in the
+    body-slot kernel (p2g_lanes 9) and a run with tracked normals (every one-body path off in
+    P2G and G2P) agree to FP32 summation order over 20 steps, sorting every step and between
+    sorts."""
+    sc = make()
+    for sort_every in (1, 3):
+        ref = run_gpu(sc, 20, options=dict(track_normals=1, sort_every=sort_every))
+        for opts in (dict(), dict(p2g_lanes=9)):
+            a = run_gpu(sc, 20, options=dict(sort_every=sort_every, **opts))
+            for f in ("pos", "vel", "stress", "density"):
+                err = rel_l2(a._get_particles(f), ref._get_particles(f))
+                assert err < 1e-5, (f, sort_every, opts, err)
+
+
 def test_autotune_single_body_chooses_lane_mapping(gpu_lib):
     """On a single-body problem the autotuner also times both P2G lane mappings and keeps the
     faster; the run it leaves behind follows an untuned run to FP32 summation order."""

@@ -224,7 +224,7 @@ __device__ bool mlp_forward_tile(MlpSmem &S, uint32_t &phase, float out[MLP_OUT]
 #pragma unroll
     for (int o = 0; o < MLP_OUT; o++) out[o] = (v[o] + S.b3[o]) * S.out_std[o] + S.out_mean[o];
     tc_fence_before();
-    // every row's TMEM read is done before the next tile's first MMA; the verdict is made
+    // every row's TMEM read is done before the next tile's first MMA; the outcome is made
     // CTA-uniform so that all threads leave a tile loop together
     ok = __syncthreads_and(ok) != 0;
     tc_fence_after();
@@ -359,7 +359,7 @@ __device__ __forceinline__ void mma_k(uint32_t tbase, int col, const unsigned ch
                tc_sdesc(smem_u32(B) + 256 * j, 128, sbo), idesc, j > 0);
 }
 
-// all threads: wait for the MMAs committed as phase `ph` (CTA-uniform verdict)
+// all threads: wait for the MMAs committed as phase `ph` (a CTA-uniform outcome)
 __device__ __forceinline__ bool mma_done(uint64_t *mbar, uint32_t &ph)
 {
     const bool ok = __syncthreads_and(mbar_wait(mbar, ph & 1)) != 0;

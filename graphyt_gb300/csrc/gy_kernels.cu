@@ -715,6 +715,9 @@ __global__ void __launch_bounds__(PP_THREADS, GY_PP_MINB) k_p2g_planes(PView P, 
         }
         __syncthreads();
         // ---- flush the tile: two vector reductions per touched node ----
+        float grav[3] = {0.f, 0.f, 0.f};
+        if (MULTI)
+            for (int c = 0; c < 3; c++) grav[c] = __ldg(&a.sc->gravity[c]);
         for (int t = tid; t < PT_NODES; t += PP_THREADS) {
             const float m = tile[t], px = tile[PT_NODES + t], py = tile[2 * PT_NODES + t], pz = tile[3 * PT_NODES + t];
             float fx = tile[4 * PT_NODES + t], fy = tile[5 * PT_NODES + t], fz = tile[6 * PT_NODES + t];
@@ -723,11 +726,12 @@ __global__ void __launch_bounds__(PP_THREADS, GY_PP_MINB) k_p2g_planes(PView P, 
             if (ni >= g.nx || nj >= g.ny || nk >= g.nz) continue;
             const int nd = node_index(ni, nj, nk, g);
             if (MULTI) {
+                const bool slot0 = tb >= 0 && __ldg(&nb.body[nd].x) >= 0;
                 // the multi-body step adds gravity in P2G, as sum w m g (Extrapolation.cpp:226-278)
-                fx += m * a.sc->gravity[0];
-                fy += m * a.sc->gravity[1];
-                fz += m * a.sc->gravity[2];
-                if (tb >= 0 && nb.body[nd].x >= 0) {
+                fx += m * grav[0];
+                fy += m * grav[1];
+                fz += m * grav[2];
+                if (slot0) {
                     red_add4(&nb.bacc0[0][nd], m, px, py, pz);
                     red_add4(&nb.bacc1[0][nd], fx, fy, fz, 0.f);
                 }

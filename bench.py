@@ -339,7 +339,12 @@ def main():
                     help="start the timed window from a checkpoint written with --save-state and the same "
                          "--preroll (no rest-state window, no preroll): the developed flow with few launches "
                          "before it, for profiling")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="the default dam-break run (one GPU) also measures the Brazilian disc and the batch "
+                         "after its own line's measurements and reports them under secondary_workloads; "
+                         "this skips them")
     args = ap.parse_args()
+    explicit_workload = any(a == "--workload" or a.startswith("--workload=") for a in sys.argv[1:])
     if args.preroll < 0:
         args.preroll = RUN_STEPS[args.workload] // 2
     args.warmup = max(args.warmup, 3)
@@ -351,10 +356,38 @@ def main():
     from graphyt_gb300 import build as gbuild
     if not os.path.exists(gbuild.LIB):
         gbuild.build()
+
+    dist = Dist(world, local)
+    line = measure(args, rank, world, local, dist)
+    if (rank == 0 and world == 1 and not explicit_workload and not args.no_secondary and args.workload == "dam_break"
+            and not args.load_state):
+        # the configuration's other single-GPU workloads, measured the same way after the
+        # headline (fewer timed steps, no CPU leg); their own lines come from --workload
+        sec = {}
+        for wl in ("brazilian_disc", "impact_batch"):
+            a2 = argparse.Namespace(**vars(args))
+            a2.workload, a2.scale, a2.temperature, a2.surrogate = wl, 1.0, 0.0, False
+            a2.steps, a2.no_cpu_baseline, a2.autotune = min(args.steps, 10), True, None
+            a2.preroll, a2.save_state, a2.load_state = RUN_STEPS[wl] // 2, None, None
+            a2.sort_every, a2.full_sort, a2.p2g_lanes = 1, False, 3
+            r = measure(a2, rank, world, local, dist)
+            sec[wl] = {k: r.get(k) for k in ("value", "unit", "ms_per_step", "steps", "phase_ms_per_step", "e2e",
+                                             "roofline", "gpu_launches", "clocks", "autotune")}
+            sec[wl]["config"] = {k: r["config"].get(k) for k in ("workload", "particles", "nodes", "model",
+                                                                  "instances", "active_nodes")
+                                 if k in r["config"]}
+            sec[wl]["window"] = r["window"]
+        line["secondary_workloads"] = sec
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    dist.close()
+
+
+def measure(args, rank, world, local, dist):
+    """One workload's measurements; the JSON line's dict on rank 0 (None elsewhere)."""
     from graphyt_gb300 import _lib as L
     from graphyt_gb300 import graphyt, scenes
 
-    dist = Dist(world, local)
     if args.workload == "dam_break":
         sc = scenes.dam_break(scale=args.scale, height=args.column_height)
     elif args.workload == "brazilian_disc":
@@ -538,9 +571,10 @@ def main():
             "gpu_launches": int(launches),
             "clocks": clocks,
         }
-        print(json.dumps(line), flush=True)
+    else:
+        line = None
     solver.close()
-    dist.close()
+    return line
 
 
 if __name__ == "__main__":

@@ -108,14 +108,15 @@ def test_p2g_lane_variants_agree(gpu_lib, make):
 
 
 @pytest.mark.parametrize("make", [lambda: scenes.two_blocks(), lambda: scenes.brazilian_disc(scale=0.1),
-                                  lambda: scenes.impact_batch(n_inst=4, seed=6, n_min=3000, n_max=9000)])
+                                  lambda: scenes.impact_batch(n_inst=4, seed=6, n_min=3000, n_max=9000),
+                                  lambda: scenes.block_2d(model=1, platen=True)])
 def test_multibody_one_body_paths_agree(gpu_lib, make):
     """On multi-body problems the paths for parts where one body is present -- P2G's plane-lane
     kernel for one-object segments, G2P's single-body tile, the solve without slot 1 -- form the
     same sums as the body-slot paths: the default run, a run with every P2G segment in the
     body-slot kernel (p2g_lanes 9) and a run with tracked normals (every one-body path off in
     P2G and G2P) agree to FP32 summation order over 20 steps, sorting every step and between
-    sorts."""
+    sorts, in 3D and 2D."""
     sc = make()
     for sort_every in (1, 3):
         ref = run_gpu(sc, 20, options=dict(track_normals=1, sort_every=sort_every))

@@ -38,6 +38,9 @@ CASES = {
     "two_blocks_rigid": (lambda: scenes.two_blocks(rigid_second=True), 40, None),
     "block_2d_elastic": (lambda: scenes.block_2d(model=1), 200, None),
     "block_2d_dp": (lambda: scenes.block_2d(model=4), 200, None),
+    "block_2d_newtonian": (lambda: scenes.block_2d(model=2), 200, None),
+    "block_2d_vonmises": (lambda: scenes.block_2d(model=3), 200, None),
+    "block_2d_turbulent": (lambda: scenes.block_2d(model=5), 200, None),
     "thermal_block": (lambda: scenes.thermal_block(), 30, None),
     "thermal_2d": (lambda: scenes.thermal_2d(), 40, None),
     "disk_impact_2d": (lambda: scenes.disk_impact_2d(), 300, None),

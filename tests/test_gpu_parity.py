@@ -192,7 +192,8 @@ def test_one_step_parity(gpu_lib, oracle_built, name):
 @pytest.mark.parametrize("name", ["tiny_elastic", "tiny_newtonian", "tiny_vonmises", "tiny_druckerprager",
                                   "cube_particle_bc", "cube_nodal_fixed", "dam_break_coarse", "damage_block",
                                   "two_blocks", "two_blocks_rigid", "brazilian_coarse", "block_2d_elastic",
-                                  "block_2d_dp", "disk_impact_2d"])
+                                  "block_2d_dp", "block_2d_newtonian", "block_2d_vonmises", "block_2d_turbulent",
+                                  "disk_impact_2d"])
 def test_golden_parity(gpu_lib, name):
     """The GPU path reproduces the reference's own output (golden fixture) over many steps."""
     gold = np.load(os.path.join(GOLDEN, name + ".npz"))

@@ -15,7 +15,7 @@ from __future__ import annotations
 
 import dataclasses
 import math
-from typing import Dict, List, Optional
+from typing import Dict, List, Optional, Sequence
 
 import numpy as np
 
@@ -678,3 +678,127 @@ def batch_instance(batch: Scene, index: int) -> Scene:
     sc.dt = batch.dt
     sc.vel = batch.vel[sel].copy()
     return _finish(sc, None)
+
+
+# ---- independent problems packed into one grid --------------------------------------------
+@dataclasses.dataclass
+class PackedInstance:
+    """One problem of a packed batch: ``box`` its cells per axis (its own domain plus the
+    margin on each side in x and y), ``origin`` the box's cell offset in the batch grid,
+    ``first`` / ``n`` its slice of the batch's particles (in insertion order) and ``mat0`` /
+    ``nmat`` its rows of the batch's material list."""
+    index: int
+    name: str
+    box: tuple
+    origin: tuple
+    shift: tuple
+    first: int
+    n: int
+    mat0: int
+    nmat: int
+
+
+def pack_scenes(scenes_: Sequence[Scene], margin: int = 3) -> Scene:
+    """Independent problems advanced as one grid (one launch per kernel for all of them).
+
+    Every scene keeps its own domain as a box of the batch grid, ``margin`` empty cells on each
+    side in x and y (no GIMP stencil, 1.25 cells, and no body window, 2 cells, reaches from
+    one box into the next), the boxes shelf-packed on the x-y plane as in
+    :func:`impact_batch_layout`.  Particles, their fields and node BCs move with their box; the
+    material lists are concatenated (material indices offset per scene; at most 4096 rows), the
+    object ids are kept (the problems never share a node, so they may reuse them).  The scenes
+    must agree on the cell size, particle spacing, dimension, gravity, damping, friction, CFL
+    and grid-BC mode, and on dt when one sets it; every problem then steps with the batch's dt
+    (the Solver formula over all the materials, or the common dt).  The problems' own domain
+    walls are not there in the batch, so a problem packs exactly when its particles stay away
+    from its domain boundary (the periodic wrap, Solver.cpp's fold of the outermost node
+    layers) -- as every scene here does.  ``scene.inst`` gives each particle's problem,
+    ``scene.instances`` the layout (:class:`PackedInstance`), ``scene.sources`` the input
+    scenes; :func:`unpack_instance` rebuilds one problem alone."""
+    if not scenes_:
+        raise ValueError("nothing to pack")
+    s0 = scenes_[0]
+    for sc in scenes_[1:]:
+        for attr in ("cellsize", "psep", "damping", "mu", "CFL", "fixed_grid_bcs"):
+            if getattr(sc, attr) != getattr(s0, attr):
+                raise ValueError(f"pack_scenes: {sc.name} has another {attr} than {s0.name}")
+        if list(sc.gravity) != list(s0.gravity) or sc.is3D != s0.is3D or sc.dt != s0.dt:
+            raise ValueError(f"pack_scenes: {sc.name} has another gravity, dimension or dt than {s0.name}")
+    if sum(len(sc.materials) for sc in scenes_) > 4096:
+        raise ValueError("pack_scenes: more than 4096 materials")
+    h = s0.cellsize
+    boxes = []
+    for sc in scenes_:
+        nx, ny, nz = sc.dims()
+        boxes.append((nx - 1 + 2 * margin, ny - 1 + 2 * margin, max(nz - 1, 0)))
+    order = sorted(range(len(scenes_)), key=lambda i: (-boxes[i][0], i))
+    area = sum(boxes[i][0] * boxes[i][1] for i in order)
+    row_len = max(boxes[order[0]][0], int(math.ceil(math.sqrt(area))))
+    origins = [None] * len(scenes_)
+    x = y = depth = width = 0
+    for i in order:
+        b = boxes[i]
+        if x + b[0] > row_len:
+            y, x, depth = y + depth, 0, 0
+        origins[i] = (x, y, 0)
+        x += b[0]
+        depth = max(depth, b[1])
+        width = max(width, x)
+    dims = (width, y + depth, max(b[2] for b in boxes))
+    L = [dims[0] * h, dims[1] * h, dims[2] * h if s0.is3D else 0.0]
+    nx_b, ny_b = dims[0] + 1, dims[1] + 1
+    fields = {f: [] for f in ("pos", "mat", "obj", "vel", "stress", "pbc_type", "pbc_val", "hold", "temp", "flaw")}
+    materials, insts, inst_of = [], [], []
+    first = 0
+    node_bc = []
+    for i, sc in enumerate(scenes_):
+        ox, oy, oz = origins[i][0] + margin, origins[i][1] + margin, 0
+        shift = (ox * h, oy * h, 0.0)
+        fields["pos"].append(sc.pos + np.array(shift))
+        fields["mat"].append(sc.mat + len(materials))
+        fields["obj"].append(sc.obj)
+        for f in ("vel", "stress", "pbc_type", "pbc_val", "hold", "temp"):
+            fields[f].append(getattr(sc, f))
+        fields["flaw"].append(sc.flaw if sc.flaw is not None else np.ones(sc.n))
+        insts.append(PackedInstance(i, sc.name, boxes[i], origins[i], shift, first, sc.n, len(materials),
+                                    len(sc.materials)))
+        inst_of.append(np.full(sc.n, i, np.int32))
+        if sc.node_bc_type is not None and np.any(sc.node_bc_type):
+            snx, sny, _ = sc.dims()
+            idx = np.nonzero(sc.node_bc_type)[0]
+            ii, jj, kk = idx % snx, (idx // snx) % sny, idx // (snx * sny)
+            node_bc.append(((ii + ox) + (jj + oy) * nx_b + (kk + oz) * nx_b * ny_b, sc.node_bc_type[idx],
+                            sc.node_bc_val[idx]))
+        materials += list(sc.materials)
+        first += sc.n
+    pk = Scene("packed_" + "+".join(sc.name for sc in scenes_)[:200], L, h, s0.psep,
+               np.concatenate(fields["pos"]), np.concatenate(fields["mat"]).astype(np.int32),
+               np.concatenate(fields["obj"]).astype(np.int32), materials)
+    pk.gravity, pk.damping, pk.mu, pk.CFL = list(s0.gravity), s0.damping, s0.mu, s0.CFL
+    pk.fixed_grid_bcs, pk.dt = s0.fixed_grid_bcs, s0.dt
+    pk.tmax = max(sc.tmax for sc in scenes_)
+    for f in ("vel", "stress", "pbc_type", "pbc_val", "hold", "temp", "flaw"):
+        setattr(pk, f, np.concatenate(fields[f]))
+    pk.inst = np.concatenate(inst_of)
+    pk.instances = insts
+    pk.sources = list(scenes_)
+    pk = _finish(pk, None)
+    for nd, t, v in node_bc:
+        pk.node_bc_type[nd] = t
+        pk.node_bc_val[nd] = v
+    return pk
+
+
+def unpack_instance(packed: Scene, index: int) -> Scene:
+    """Problem ``index`` of a :func:`pack_scenes` batch alone on its own domain, with the
+    batch's dt: the scene it was packed from, in the same particle order."""
+    sc = dataclasses.replace(packed.sources[index])
+    if packed.dt is None:
+        # the batch's dt: the Solver formula over every material row (Solver.cpp:15-32,
+        # maxK seeded with 1 and the smallest density with 1e15)
+        maxK = max([1.0] + [m["bulkMod"] for m in packed.materials])
+        rho = min([1e15] + [m["density"] for m in packed.materials])
+        sc.dt = packed.CFL * (packed.cellsize / math.sqrt(maxK / rho))
+    else:
+        sc.dt = packed.dt
+    return sc

@@ -165,3 +165,70 @@ def test_batch_500_steps_per_instance(gpu_lib, oracle_built):
                 assert np.max(np.abs(a[sel])) < 1e-9
                 continue
             assert rel_l2(a[sel], r[sel]) <= tol, (i, f, rel_l2(a[sel], r[sel]))
+
+
+# ---- general packing: independent scenes of any kind as one grid ------------------------------
+def _pack_cases():
+    return {
+        "models": [scenes.tiny_block(model=m, seed=m) for m in (1, 2, 3, 4)]
+                  + [scenes.tiny_block(model=1, n_side=6, seed=9, vel=(-0.2, 0.3, 0.0))],
+        "contact": [scenes.two_blocks(seed=s, speed=1.0 + 0.3 * s) for s in range(3)]
+                   + [scenes.two_blocks(rigid_second=True)],
+    }
+
+
+def test_pack_scenes_layout():
+    """Boxes do not overlap, every particle lies inside its box at least the margin from its
+    edges in x and y, materials and fields keep their rows, node BCs move with their box, and
+    scenes that disagree on the grid are refused."""
+    for name, scs in _pack_cases().items():
+        pk = scenes.pack_scenes(scs, margin=3)
+        h = pk.cellsize
+        assert pk.n == sum(s.n for s in scs) and len(pk.materials) == sum(len(s.materials) for s in scs)
+        for a in pk.instances:
+            for b in pk.instances:
+                if a.index < b.index:
+                    sep = any(a.origin[d] + a.box[d] <= b.origin[d] or b.origin[d] + b.box[d] <= a.origin[d]
+                              for d in (0, 1))
+                    assert sep, (name, a, b)
+            sl = slice(a.first, a.first + a.n)
+            src = scs[a.index]
+            assert np.allclose(pk.pos[sl] - np.array(a.shift), src.pos)
+            assert np.array_equal(pk.mat[sl], src.mat + a.mat0) and np.array_equal(pk.obj[sl], src.obj)
+            assert np.array_equal(pk.vel[sl], src.vel) and np.all(pk.inst[sl] == a.index)
+            cells = pk.pos[sl, :2] / h
+            assert np.all(cells >= np.array(a.origin[:2]) + 3) and np.all(cells <= np.array(a.origin[:2]) + np.array(a.box[:2]) - 3)
+    # node BCs: a BC node of the source lands at its shifted index in the packed grid
+    src = scenes.tiny_block(model=1)
+    src.node_bc_type[5] = 33
+    src.node_bc_val[5] = [1.0, 2.0, 3.0, 4.0]
+    pk = scenes.pack_scenes([scenes.tiny_block(model=2), src])
+    a = pk.instances[1]
+    snx, sny, _ = src.dims()
+    nx, ny, _ = pk.dims()
+    i, j, k = 5 % snx, (5 // snx) % sny, 5 // (snx * sny)
+    nd = (i + a.origin[0] + 3) + (j + a.origin[1] + 3) * nx + k * nx * ny
+    assert pk.node_bc_type[nd] == 33 and np.array_equal(pk.node_bc_val[nd], [1.0, 2.0, 3.0, 4.0])
+    assert np.count_nonzero(pk.node_bc_type) == 1
+    with pytest.raises(ValueError):
+        scenes.pack_scenes([scenes.tiny_block(), scenes.two_blocks()])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["models", "contact"])
+def test_packed_scenes_equal_their_own_runs(gpu_lib, case):
+    """Independent scenes packed into one grid -- four constitutive models side by side, or
+    two-body contact problems with a rigid platen among them -- follow their standalone runs
+    (each with the batch's dt) to FP32 summation order over 30 steps."""
+    scs = _pack_cases()[case]
+    pk = scenes.pack_scenes(scs)
+    batch = run_gpu(pk, 30)
+    for a in pk.instances:
+        alone = run_gpu(scenes.unpack_instance(pk, a.index), 30)
+        assert abs(alone.dt - batch.dt) <= 1e-12 * batch.dt
+        sl = slice(a.first, a.first + a.n)
+        for f in ("vel", "stress", "density"):
+            err = rel_l2(batch._get_particles(f)[sl], alone._get_particles(f))
+            assert err < 1e-5, (case, a.name, f, err)
+        pos = batch._get_particles("pos")[sl] - np.array(a.shift)
+        assert np.max(np.abs(pos - alone._get_particles("pos"))) < 1e-6 * max(pk.L)

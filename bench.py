@@ -370,7 +370,11 @@ def main():
             a2.steps, a2.no_cpu_baseline, a2.autotune = min(args.steps, 10), True, None
             a2.preroll, a2.save_state, a2.load_state = RUN_STEPS[wl] // 2, None, None
             a2.sort_every, a2.full_sort, a2.p2g_lanes = 1, False, 3
-            r = measure(a2, rank, world, local, dist)
+            try:
+                r = measure(a2, rank, world, local, dist)
+            except Exception as e:  # the headline line is printed whatever happens here
+                sec[wl] = {"error": f"{type(e).__name__}: {e}"[:300]}
+                continue
             sec[wl] = {k: r.get(k) for k in ("value", "unit", "ms_per_step", "steps", "phase_ms_per_step", "e2e",
                                              "roofline", "gpu_launches", "clocks", "autotune")}
             sec[wl]["config"] = {k: r["config"].get(k) for k in ("workload", "particles", "nodes", "model",

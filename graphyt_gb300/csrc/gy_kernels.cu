@@ -513,13 +513,22 @@ __device__ __forceinline__ float2 dup2(float x) { return make_float2(x, x); }
 // multi-body solve does not) and flushes into the centre-of-mass and slot-0 accumulators.  A
 // segment that fails the test, at its start or at any chunk, is appended to `defer`, its tile
 // dropped, and k_p2g_multi_tiled takes it.
-template <bool MULTI>
-__global__ void __launch_bounds__(PP_THREADS, GY_PP_MINB) k_p2g_planes(PView P, const int *perm, const int *skey, long long n,
-                                                              const int *seg_start, const int *nseg_ptr, int sorted,
-                                                              NodeBufs nb, StepArgs a, int *defer, int *ndefer)
+// THERMAL (single body): the heat conduction sums as in k_p2g_cols -- per node the temperature
+// sum S T m c and the rate sum grad S . ((m / rho) k grad T / h) -- staged as one more float4
+// per particle and two more tile fields, at four CTAs per SM.
+#ifndef GY_PP_MINB_TH
+#define GY_PP_MINB_TH 4
+#endif
+template <bool MULTI, bool THERMAL = false>
+__global__ void __launch_bounds__(PP_THREADS, THERMAL ? GY_PP_MINB_TH : GY_PP_MINB)
+    k_p2g_planes(PView P, const int *perm, const int *skey, long long n, const int *seg_start, const int *nseg_ptr,
+                 int sorted, NodeBufs nb, StepArgs a, int *defer, int *ndefer, const float4 *therm = nullptr,
+                 float2 *tnode = nullptr)
 {
-    __shared__ float tile[P2G_FIELDS * PT_NODES];
+    constexpr int TF = P2G_FIELDS + (THERMAL ? 2 : 0);  // tile fields
+    __shared__ float tile[TF * PT_NODES];
     __shared__ float4 SA[PP_ROWS], SB[PP_ROWS], SC[PP_ROWS], SD[PP_ROWS], SE[PP_ROWS], SF[PP_ROWS];
+    __shared__ float4 SG[THERMAL ? PP_ROWS : 1];  // (T m c, g_x, g_y, g_z), g = (m / rho) k grad T / h
     __shared__ float2 SZ[3][PP_ROWS];
     __shared__ int run_start[PP_CH + 1];
     __shared__ int run_cell[PP_CH];
@@ -550,7 +559,7 @@ __global__ void __launch_bounds__(PP_THREADS, GY_PP_MINB) k_p2g_planes(PView P, 
                 continue;
             }
         }
-        for (int t = tid; t < P2G_FIELDS * PT_NODES; t += PP_THREADS) tile[t] = 0.f;
+        for (int t = tid; t < TF * PT_NODES; t += PP_THREADS) tile[t] = 0.f;
         bool dropped = false;
         for (long long base = start;; base += PP_CH) {
             const long long ia = base + 2 * tid, ib = ia + 1;
@@ -605,6 +614,12 @@ __global__ void __launch_bounds__(PP_THREADS, GY_PP_MINB) k_p2g_planes(PView P, 
                 SD[row] = make_float4(m, m * P.f(PF_VX, j), m * P.f(PF_VY, j), m * P.f(PF_VZ, j));
                 SE[row] = make_float4(s0, s3, s5, s4);
                 SF[row] = make_float4(s3, s1, s2, 0.f);
+                if (THERMAL) {
+                    const DevMaterial &Mt = a.mats[info_mat((uint32_t)P.ii(PF_INFO, j))];
+                    const float4 th = therm[P.ii(PF_PID, j)];
+                    const float vk = (m / P.f(PF_RHO, j)) * Mt.k_th * g.inv_h;
+                    SG[row] = make_float4(th.x * m * Mt.c_th, vk * th.y, vk * th.z, vk * th.w);
+                }
 #pragma unroll
                 for (int z = 0; z < 3; z++) SZ[z][row] = make_float2(Sz[z], Gz[z]);
             }
@@ -650,18 +665,22 @@ __global__ void __launch_bounds__(PP_THREADS, GY_PP_MINB) k_p2g_planes(PView P, 
                 const int maxlen = __reduce_max_sync(0xffffffffu, len);
                 float2 amp[3][3], app[3][3], afxy[3][3];
                 float afz[3][3];
+                float atT[THERMAL ? 3 : 1][3], atR[THERMAL ? 3 : 1][3];  // THERMAL: temperature and rate sums
 #pragma unroll
                 for (int i = 0; i < 3; i++)
 #pragma unroll
                     for (int j = 0; j < 3; j++) {
                         amp[i][j] = app[i][j] = afxy[i][j] = z2;
                         afz[i][j] = 0.f;
+                        if (THERMAL) atT[i][j] = atR[i][j] = 0.f;
                     }
                 for (int k = 0; k < maxlen; k++) {
                     const int row = pp_row(p0 + min(k, max(len - 1, 0)));
                     const float4 A = SA[row], B = SB[row], C = SC[row], D = SD[row], E = SE[row], F = SF[row];
                     float2 Z = SZ[kk][row];
                     if (k >= len) Z = z2;  // past the run (or no run): the particle adds nothing
+                    float4 TG = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (THERMAL) TG = SG[row];
                     const float Sx[3] = {A.x, A.y, A.z}, Gx[3] = {A.w, B.x, B.y};
                     const float Sy[3] = {B.z, B.w, C.x}, Gy[3] = {C.y, C.z, C.w};
                     const float2 mvx = make_float2(D.x, D.y), mvyz = make_float2(D.z, D.w);
@@ -685,6 +704,14 @@ __global__ void __launch_bounds__(PP_THREADS, GY_PP_MINB) k_p2g_planes(PView P, 
                             afxy[i][j] = fma2(gx, Bxy, fma2(sx, Cxy, afxy[i][j]));
                             afz[i][j] = fmaf(Gx[i], Bz, fmaf(Sx[i], Cz, afz[i][j]));
                         }
+                        if (THERMAL) {
+                            const float tS = syz * TG.x, Bt = TG.y * syz, Ct = fmaf(TG.z, gyz, TG.w * syg);
+#pragma unroll
+                            for (int i = 0; i < 3; i++) {
+                                atT[i][j] = fmaf(Sx[i], tS, atT[i][j]);
+                                atR[i][j] = fmaf(Gx[i], Bt, fmaf(Sx[i], Ct, atR[i][j]));
+                            }
+                        }
                     }
                 }
                 if (!rv) continue;
@@ -704,6 +731,10 @@ __global__ void __launch_bounds__(PP_THREADS, GY_PP_MINB) k_p2g_planes(PView P, 
                         atomicAdd(&tile[4 * PT_NODES + t], -afxy[i][j].x);
                         atomicAdd(&tile[5 * PT_NODES + t], -afxy[i][j].y);
                         atomicAdd(&tile[6 * PT_NODES + t], -afz[i][j]);
+                        if (THERMAL) {
+                            atomicAdd(&tile[7 * PT_NODES + t], atT[i][j]);
+                            atomicAdd(&tile[8 * PT_NODES + t], -atR[i][j]);
+                        }
                     }
             }
             if (cnt < PP_CH) break;
@@ -738,6 +769,10 @@ __global__ void __launch_bounds__(PP_THREADS, GY_PP_MINB) k_p2g_planes(PView P, 
             }
             red_add4(&nb.acc0[nd], m, px, py, pz);
             red_add4(&nb.acc1[nd], fx, fy, fz, 0.f);
+            if (THERMAL) {
+                atomicAdd(&tnode[nd].x, tile[7 * PT_NODES + t]);
+                atomicAdd(&tnode[nd].y, tile[8 * PT_NODES + t]);
+            }
             mark_node(nb, ni, nj, nk, g);
         }
         __syncthreads();
@@ -1047,7 +1082,18 @@ void launch_p2g(const PView &p, const int *perm, const int *skey, long long n, c
             k_p2g_multi_tiled<<<mgrid, P2G_CH, 0, s>>>(p, perm, skey, n, seg_start, nseg, perm ? 1 : 0, nb, a);
         }
     } else {
-        if (therm) {
+        if (therm && lanes == 3) {
+            static int hgrid = 0;  // persistent grid of the plane-lane variant with heat conduction
+            if (hgrid == 0) {
+                int dev = 0, sms = 1, b = 0;
+                cudaGetDevice(&dev);
+                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_p2g_planes<false, true>, PP_THREADS, 0);
+                hgrid = sms * std::max(b, 1);
+            }
+            k_p2g_planes<false, true><<<hgrid, PP_THREADS, 0, s>>>(p, perm, skey, n, seg_start, nseg, perm ? 1 : 0, nb,
+                                                                    a, nullptr, nullptr, therm, tnode);
+        } else if (therm) {
             static int tgrid = 0;  // persistent grid of the variant with heat conduction
             if (tgrid == 0) {
                 int dev = 0, sms = 1, b = 0;

@@ -193,3 +193,18 @@ def test_thermal_between_sorts(gpu_lib, oracle_built):
     gpu = run_gpu(sc, 12, options=dict(sort_every=3))
     ref = run_oracle(sc, 12)
     assert rel_l2(_dT(gpu._get_particles("temp"), sc), _dT(ref.pfield("temp"), sc)) <= MANY_STEP_TOL
+
+
+@pytest.mark.parametrize("make", [lambda: scenes.thermal_block(), lambda: scenes.thermal_2d()])
+def test_thermal_p2g_lane_variants_agree(gpu_lib, make):
+    """The heat conduction variants of the two P2G lane mappings (three z-plane lanes or nine
+    x-column lanes per run of equal cell) form the same sums in another order: temperatures,
+    gradients, velocity and stress agree to FP32 summation order, sorting every step and
+    between sorts, in 3D and 2D."""
+    sc = make()
+    for sort_every in (1, 3):
+        a = run_gpu(sc, 20, options=dict(p2g_lanes=3, sort_every=sort_every))
+        b = run_gpu(sc, 20, options=dict(p2g_lanes=9, sort_every=sort_every))
+        assert rel_l2(_dT(a._get_particles("temp"), sc), _dT(b._get_particles("temp"), sc)) < 1e-5
+        for f in ("tempgrad", "vel", "stress"):
+            assert rel_l2(a._get_particles(f), b._get_particles(f)) < 1e-5, (f, sort_every)

@@ -83,7 +83,7 @@ typedef struct gy_options {
     int track_normals;  /* 1: keep per-particle contact normals (getNormalsArr) */
     int check_finite;   /* 1: flag NaN/Inf in particle state every step */
     int keep_node_fields; /* 1: keep centre-of-mass node velocity/force for node getters */
-    int p2g_lanes;      /* P2G without heat conduction: lanes per run of equal cell, 3 (default:
+    int p2g_lanes;      /* P2G (with or without heat conduction): lanes per run of equal cell, 3 (default:
                            each lane sums a z-plane of nine stencil nodes) or 9 (each lane a
                            column of three x nodes).  Multi-body problems without tracked
                            normals: 3 sends the segments of one deformable object whose node

@@ -920,6 +920,9 @@ static StepArgs make_args(gy_solver *h)
     a.mats = h->d_mats;
     a.pbc_val = h->d_pbc_val;
     a.flaw = h->d_flaw;
+    // G2P flags the particles that change cell for the next incremental re-sort
+    a.mover_mask = h->rs.wmask;
+    a.mover_cnt = h->rs.wcnt;
     if (h->dplog_on) {
         a.dp.log_x = h->d_dplog;
         a.dp.log_y = h->d_dplog + (size_t)h->dplog_cap * 16;
@@ -952,8 +955,10 @@ static void issue_step(gy_solver *h, const StepVariant &v, cudaEvent_t *tev)
         const long long maxkey = (long long)h->g.nbx * h->g.nby * h->g.nbz * 64;
         while ((1LL << key_bits) < maxkey) key_bits++;
         if (v.sort == 1) {
-            // the slab is in the order of the last sort: re-sort only the particles that moved
-            resort_keys(skey, h->skey_buf[v.sk ^ 1], out, h->d_perm, h->n, key_bits, h->rs, s);
+            // the slab is in the order of the last sort: re-sort only the particles that moved,
+            // which every G2P since that sort has flagged (the mover words start clear, and
+            // each re-sort clears them after use)
+            resort_keys(skey, h->skey_buf[v.sk ^ 1], out, h->d_perm, h->n, key_bits, h->rs, s, true);
         } else {
             const int *sorted = sort_pairs(skey, h->d_perm, h->n, key_bits, h->ws, s);
             if (h->n > 0 && sorted != out)

@@ -94,6 +94,14 @@ __device__ __forceinline__ void store_state(const PView &P, long long i, const P
 }
 
 
+// A particle whose cell key changed: its bit in the next re-sort's mover words (slot i of the
+// order this step writes), and the word's count when the bit was clear
+__device__ __forceinline__ void flag_mover(const StepArgs &a, long long i)
+{
+    const unsigned bit = 1u << (i & 31);
+    if (!(atomicOr(&a.mover_mask[i >> 5], bit) & bit)) atomicAdd(&a.mover_cnt[i >> 5], 1);
+}
+
 // L2 prefetch of the segment a CTA takes next: the window of PF_WINDOW source slots that
 // starts at the slot of the segment's first particle (the slab is in the order of the last
 // sort, so a segment's particles sit close together there), for the fields [f0, f1), one
@@ -2034,6 +2042,7 @@ __global__ void __launch_bounds__(GY_G2P_THREADS, THERMAL ? GY_G2P_MINB_TH : GY_
                 if (!g.is3d) c0[2] = 0;
                 update_after_g2p<HAS_DP>(st, c0, acc, vg, L, a, check_finite != 0, i);
                 store_state<HAS_DP>(dst, i, st);
+                if (a.mover_mask && st.key != key) flag_mover(a, i);
                 if (THERMAL) therm[st.pid] = make_float4(th.x + thg[3] * a.sc->dt, thg[0], thg[1], thg[2]);
                 if (a.stats) particle_stats(s_st, st);
             }
@@ -2230,6 +2239,7 @@ __global__ void __launch_bounds__(GY_G2PM_THREADS, GY_G2PM_MINB) k_g2p_multi_til
                 if (!g.is3d) c0[2] = 0;
                 update_after_g2p<HAS_DP>(st, c0, acc, vg, L, a, check_finite != 0, i);
                 store_state<HAS_DP>(dst, i, st);
+                if (a.mover_mask && st.key != key) flag_mover(a, i);
                 if (NRM) {
                     dst.f(PF_NX, i) = nrm[0];
                     dst.f(PF_NY, i) = nrm[1];

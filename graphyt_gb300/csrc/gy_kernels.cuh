@@ -71,6 +71,8 @@ struct StepArgs {
     int *status;
     double *stats;           // STATS_SLOTS x 8 conservation partials written by G2P, or null
     DpHooks dp;              // learned-surrogate logging / deferral (zero when off)
+    unsigned *mover_mask;    // G2P flags the slots whose key changed, one bit per slot (or null),
+    int *mover_cnt;          //   with the flagged count per 32 slots, for the next re-sort
 };
 
 // partials of the conservation sums (mass, momentum, kinetic and strain energy); the host
@@ -159,15 +161,17 @@ size_t sort_scratch_bytes(long long n);
 struct ResortScratch {
     unsigned *wmask;
     int *wcnt, *wpref, *wscan_tmp;
-    int *bkey, *bidx, *tkey, *tidx, *gap;
+    int *bkey, *bidx, *gap, *bslot;       // the movers in slot order
+    int *stk, *sti, *tval;                // the movers grouped by key bucket; fallback sort buffers
     int *gapcnt, *gwcnt, *gwpref, *gscan_tmp;
-    int *hist, *hscan_tmp;
+    int *big;                             // a bucket too crowded to rank by counting
+    int *mlast;                           // the last re-sort's mover count
     long long cap, ngw;
 };
 size_t resort_scratch_ints(long long cap);
 void resort_bind(ResortScratch &rs, int *mem, long long cap);
 void resort_keys(const int *key, const int *prev_skey, int *skey_out, int *perm_out, long long n, int key_bits,
-                 ResortScratch &rs, cudaStream_t s);
+                 ResortScratch &rs, cudaStream_t s, bool mask_ready = false);
 // err (may be null) receives the first launch failure of the sort's kernels
 const int *sort_pairs(const int *keys_in, int *perm_out, long long n, int key_bits, SortScratch &ws, cudaStream_t s,
                       cudaError_t *err = nullptr);

@@ -4,11 +4,15 @@
 // particles that changed cell since ("movers") break it: the others ("stayers") still have
 // the key stored at their slot in the previous sorted key array, which is non-decreasing, so
 // they form a sorted run by (key, slot).  The stable order of the new keys is the merge of
-// the stayers with the movers sorted by (key, slot):
-//   * the movers, compacted in slot order, are sorted stably by key (a radix sort whose
-//     length lives on the device, so the host never waits for it); mover q of that order
-//     lands at q + g(q), g = the stayers below it -- one binary search on the previous keys;
+// the stayers with the movers ordered by (key, slot):
+//   * mover (k, i) has a gap g = the stayers below it in (key, slot) order, one search of the
+//     previous keys, and lands at g + (movers before it in (key, slot) order).  The movers
+//     before it are those of lower key buckets (a bucket is a range of 2^shift keys, a 4x4x4
+//     cell block on grids of up to 2^24 cells), counted per bucket and prefix-summed, plus
+//     those of its own bucket that precede it, counted over the bucket's few movers;
 //   * stayer r (r-th stayer in slot order) lands at r + (movers with g <= r).
+// A bucket holding more than RS_BUCKET_MAX movers (a flow far outside the time-step limit,
+// or keys that are not cells) sends all movers through a one-CTA stable radix sort instead.
 // The result is the permutation the full stable radix sort produces, at a fraction of its
 // traffic when few particles move; the full sort runs whenever the previous order is not
 // known (first step, restored state).
@@ -19,12 +23,14 @@
 namespace gy {
 
 constexpr int RS_THREADS = 256;
-constexpr int RS_ITEMS = 8;                          // per thread in the mover sort
-constexpr int RS_TILE = RS_THREADS * RS_ITEMS;       // 2048
 constexpr int RS_WARPS = RS_THREADS / 32;
 constexpr int RS_RADIX = 256;
-constexpr int RS_MAX_CTAS = 1024;                    // mover-sort CTAs (2 per SM)
-constexpr int RS_MAX_PASSES = 4;                     // 8-bit digits of a non-negative int key
+constexpr int RS_BUCKET_BITS = 18;     // at most 2^18 key buckets
+constexpr int RS_BUCKET_MAX = 512;     // movers per bucket ranked by counting
+constexpr int RB_THREADS = 1024;       // the one-CTA fallback sort
+constexpr int RB_ITEMS = 8;
+constexpr int RB_TILE = RB_THREADS * RB_ITEMS;
+constexpr int RB_WARPS = RB_THREADS / 32;
 
 __device__ __forceinline__ long long movers_before(long long P, const unsigned *wmask, const int *wpref)
 {
@@ -33,34 +39,14 @@ __device__ __forceinline__ long long movers_before(long long P, const unsigned *
     return (long long)wpref[w] + (b ? __popc(wmask[w] & ((1u << b) - 1u)) : 0);
 }
 
-// CTA c of the mover sort owns [m c / G, m (c+1) / G); the owner of position pos is the
-// largest c with floor(m c / G) <= pos
-__device__ __forceinline__ int owner_cta(int pos, int m, int G)
-{
-    const int c = (int)(((long long)(pos + 1) * G - 1) / m);
-    return c < G - 1 ? c : G - 1;
-}
-
-// mover mask and count per 32 slots: a warp takes four words at a time, all loads first.
-// The kernel also clears the gap counters the previous re-sort left (its m movers are still
-// listed in gap[] and wpref[nw]) and the digit histograms this re-sort accumulates.
+// mover mask and count per 32 slots from the two key arrays, for callers whose particle
+// update did not flag the movers: a warp takes four words at a time, all loads first
 __global__ void __launch_bounds__(RS_THREADS) k_rs_mask(const int *key, const int *prev, long long n, unsigned *wmask,
-                                                          int *wcnt, long long nw, const int *gap, const int *wpref,
-                                                          int *gapcnt, int *gwcnt, int *hist, int hist_ints)
+                                                          int *wcnt, long long nw)
 {
     pdl_prologue();
     const int lane = threadIdx.x & 31;
     const long long wstride = ((long long)gridDim.x * blockDim.x) >> 5;
-    {
-        const int mprev = wpref[nw];
-        const int t = blockIdx.x * blockDim.x + threadIdx.x, tstride = gridDim.x * blockDim.x;
-        for (int q = t; q < mprev; q += tstride) {
-            gapcnt[gap[q]] = 0;
-            gwcnt[gap[q] >> 5] = 0;
-        }
-        for (int q = t; q < hist_ints; q += tstride) hist[q] = 0;
-        if (t == 0) wcnt[nw] = 0;  // the scan's last entry, so that wpref[nw] is the mover count
-    }
     for (long long w0 = (((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 4; w0 < nw; w0 += wstride * 4) {
         int ka[4], kb[4];
 #pragma unroll
@@ -83,12 +69,25 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_mask(const int *key, const in
 }
 
 // movers (key, slot) in slot order.  A warp takes 32 words at once (one mask per lane) and
-// visits only the words that hold movers.
+// visits only the words that hold movers.  The kernel also clears the gap counters the
+// previous re-sort left (its *mlast movers are still listed in gap[]), this re-sort's bucket
+// counters and the fallback flag.
 __global__ void __launch_bounds__(RS_THREADS) k_rs_compact(const int *key, const unsigned *wmask, const int *wpref,
-                                                             long long nw, int *bkey, int *bidx, int *hist0, int G)
+                                                             long long nw, int *bkey, int *bidx, const int *gap,
+                                                             const int *mlast, int *gapcnt, int *gwcnt, int *bcnt,
+                                                             int nbk, int *big)
 {
     pdl_prologue();
-    const int mtot = wpref[nw];
+    {
+        const int mprev = *mlast;
+        const int t = blockIdx.x * blockDim.x + threadIdx.x, tstride = gridDim.x * blockDim.x;
+        for (int q = t; q < mprev; q += tstride) {
+            gapcnt[gap[q]] = 0;
+            gwcnt[gap[q] >> 5] = 0;
+        }
+        for (int q = t; q < nbk; q += tstride) bcnt[q] = 0;
+        if (t == 0) *big = 0;
+    }
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     const long long wstride = ((long long)gridDim.x * blockDim.x) >> 5;
@@ -105,98 +104,24 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_compact(const int *key, const
             if ((m >> lane) & 1u) {
                 const long long i = (w0 + u) * 32 + lane;
                 const int pos = base + __popc(m & lt);
-                const int k = key[i];
-                bkey[pos] = k;
+                bkey[pos] = key[i];
                 bidx[pos] = (int)i;
-                atomicAdd(&hist0[(k & 0xFF) * G + owner_cta(pos, mtot, G)], 1);  // first pass's digit counts
             }
         }
     }
 }
 
-// ---- stable LSD radix sort of the m movers, m read on the device ----------------------
-// CTA c of the G owns the contiguous range [m c / G, m (c+1) / G) and walks it in tiles of
-// RS_TILE; ranks inside a tile follow k_radix_scatter (warps in order, peers by
-// __match_any_sync), and per-digit bases carry from tile to tile.
-
-__device__ __forceinline__ void cta_range(int m, int &c0, int &c1)
-{
-    c0 = (int)((long long)m * blockIdx.x / gridDim.x);
-    c1 = (int)((long long)m * (blockIdx.x + 1) / gridDim.x);
-}
-
-// hist_next (or null on the last pass) receives the next pass's digit counts per owner CTA of
-// each output position, so no separate histogram launch is needed
-__global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const int *keys_in, const int *vals_in, int *keys_out,
-                                                             int *vals_out, const int *m_ptr, int shift,
-                                                             const int *offsets, int *hist_next)
-{
-    pdl_prologue();
-    __shared__ int wcnt[RS_WARPS][RS_RADIX];  // per-warp digit counts, then per-warp bases
-    __shared__ int base[RS_RADIX];            // running per-digit base of this CTA
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const unsigned lt = (1u << lane) - 1u;
-    for (int d = threadIdx.x; d < RS_RADIX; d += RS_THREADS) base[d] = offsets[d * gridDim.x + blockIdx.x];
-    int c0, c1;
-    cta_range(*m_ptr, c0, c1);
-    for (int t0 = c0; t0 < c1; t0 += RS_TILE) {
-        for (int d = lane; d < RS_RADIX; d += 32) wcnt[warp][d] = 0;
-        __syncthreads();  // the bases of the previous tile are final; the counters are clear
-        const int wb = t0 + warp * (32 * RS_ITEMS);
-        int key[RS_ITEMS], val[RS_ITEMS], rnk[RS_ITEMS];
-        for (int r = 0; r < RS_ITEMS; r++) {
-            const int e = wb + r * 32 + lane;
-            const bool ok = e < c1;
-            key[r] = ok ? keys_in[e] : 0;
-            val[r] = ok ? vals_in[e] : 0;
-            const int d = ok ? ((key[r] >> shift) & 0xFF) : RS_RADIX;
-            const unsigned peers = __match_any_sync(0xffffffffu, d);
-            const int before = __popc(peers & lt);
-            int bc = 0;
-            if (ok) bc = wcnt[warp][d];
-            __syncwarp();
-            rnk[r] = bc + before;
-            if (ok && before == 0) wcnt[warp][d] = bc + __popc(peers);
-            __syncwarp();
-        }
-        __syncthreads();
-        for (int d = threadIdx.x; d < RS_RADIX; d += RS_THREADS) {
-            int run = base[d];
-            for (int w = 0; w < RS_WARPS; w++) {
-                const int c = wcnt[w][d];
-                wcnt[w][d] = run;
-                run += c;
-            }
-            base[d] = run;
-        }
-        __syncthreads();
-        for (int r = 0; r < RS_ITEMS; r++) {
-            const int e = wb + r * 32 + lane;
-            if (e < c1) {
-                const int d = (key[r] >> shift) & 0xFF;
-                const int pos = wcnt[warp][d] + rnk[r];
-                keys_out[pos] = key[r];
-                vals_out[pos] = val[r];
-                if (hist_next)
-                    atomicAdd(&hist_next[((key[r] >> (shift + 8)) & 0xFF) * gridDim.x + owner_cta(pos, *m_ptr, gridDim.x)], 1);
-            }
-        }
-        __syncthreads();  // wcnt is reused by the next tile
-    }
-}
-
-// ---- placement ----------------------------------------------------------------------
-
-// mover q of the sorted order: stayers below it (gap g), placed at q + g; gaps counted
-__global__ void __launch_bounds__(RS_THREADS) k_rs_place_movers(const int *prev, long long n, const unsigned *wmask,
-                                                                  const int *wpref, long long nw, const int *skey,
-                                                                  const int *sidx, int *gap, int *gapcnt, int *gwcnt,
-                                                                  int *skey_out, int *perm_out)
+// mover q (slot order): its gap g, the stayers below it in (key, slot) order, counted per gap
+// and per 32-gap word, and its arrival order within its key bucket
+__global__ void __launch_bounds__(RS_THREADS) k_rs_gaps(const int *prev, long long n, const unsigned *wmask,
+                                                          const int *wpref, long long nw, const int *bkey,
+                                                          const int *bidx, int shift, int *gap, int *gapcnt, int *gwcnt,
+                                                          int *bcnt, int *bslot)
 {
     pdl_prologue();
     const int m = wpref[nw];
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < m; q += gridDim.x * blockDim.x) {
-        const int k = skey[q], i = sidx[q];
+        const int k = bkey[q], i = bidx[q];
         // first slot s with (prev[s], s) >= (k, i): a mover's new key is usually near its
         // old one, so gallop out from its old slot i before bisecting (cache-near probes)
         long long lo, hi;
@@ -230,22 +155,171 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_place_movers(const int *prev,
         gap[q] = g;
         atomicAdd(&gapcnt[g], 1);
         atomicAdd(&gwcnt[g >> 5], 1);
-        const long long pos = (long long)q + g;
+        bslot[q] = atomicAdd(&bcnt[k >> shift], 1);
+    }
+}
+
+// the movers grouped by key bucket, in arrival order inside a bucket: bucket b's occupy
+// [bpref[b] - m, bpref[b] - m + bcnt[b]) of the staging arrays (bpref is the bucket part of a
+// scan that starts with the m gap-word counts)
+__global__ void __launch_bounds__(RS_THREADS) k_rs_stage(const int *wpref, long long nw, const int *bkey,
+                                                           const int *bidx, const int *bslot, const int *bpref,
+                                                           int shift, int *stk, int *sti)
+{
+    pdl_prologue();
+    const int m = wpref[nw];
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < m; q += gridDim.x * blockDim.x) {
+        const int k = bkey[q];
+        const int j = bpref[k >> shift] - m + bslot[q];
+        stk[j] = k;
+        sti[j] = bidx[q];
+    }
+}
+
+// mover q lands at g + (movers of lower buckets) + (movers of its bucket before it in (key,
+// slot) order), the last counted over the bucket's staged movers.  A bucket of more than
+// RS_BUCKET_MAX movers raises *big, and k_rs_big places every mover instead.
+__global__ void __launch_bounds__(RS_THREADS) k_rs_rank(const int *wpref, long long nw, const int *bkey,
+                                                          const int *bidx, const int *gap, const int *bcnt,
+                                                          const int *bpref, int shift, const int *stk, const int *sti,
+                                                          int *big, int *skey_out, int *perm_out)
+{
+    pdl_prologue();
+    const int m = wpref[nw];
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < m; q += gridDim.x * blockDim.x) {
+        const int k = bkey[q], i = bidx[q], b = k >> shift;
+        const int c = bcnt[b];
+        if (c > RS_BUCKET_MAX) {
+            *big = 1;
+            continue;
+        }
+        const int j0 = bpref[b] - m;
+        int r = 0;
+        for (int j = j0; j < j0 + c; j++) {
+            const int kj = stk[j];
+            r += (kj < k || (kj == k && sti[j] < i)) ? 1 : 0;
+        }
+        const long long pos = (long long)gap[q] + j0 + r;
         skey_out[pos] = k;
         perm_out[pos] = i;
     }
 }
 
+// Fallback for crowded buckets: one CTA sorts all m movers stably by key (LSD, 8-bit digits;
+// tiles in slot order, ranks inside a tile by warps in order and peers by __match_any_sync,
+// per-digit bases carried from tile to tile) and places every one of them at g + its index.
+// Movers k_rs_rank placed already get the same position and value again.
+__global__ void __launch_bounds__(RB_THREADS) k_rs_big(const int *big, const int *wpref, long long nw,
+                                                         const int *bkey, const int *bidx, const int *gap, int passes,
+                                                         int *ka, int *va, int *kb, int *vb, int *skey_out,
+                                                         int *perm_out)
+{
+    pdl_prologue();
+    if (!*big) return;
+    __shared__ int wcnt[RB_WARPS][RS_RADIX];  // per-warp digit counts, then per-warp bases
+    __shared__ int base[RS_RADIX];            // running per-digit base
+    const int m = wpref[nw];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const int *kin = bkey, *vin = nullptr;  // pass 0's value is the slot-order index itself
+    int *kout = ka, *vout = va;
+    for (int p = 0; p < passes; p++) {
+        const int shift = 8 * p;
+        for (int d = threadIdx.x; d < RS_RADIX; d += RB_THREADS) base[d] = 0;
+        __syncthreads();
+        for (int e = threadIdx.x; e < m; e += RB_THREADS) atomicAdd(&base[(kin[e] >> shift) & 0xFF], 1);
+        __syncthreads();
+        if (warp == 0) {  // exclusive scan of the 256 digit counts, eight per lane
+            int v[RS_RADIX / 32], sum = 0;
+#pragma unroll
+            for (int u = 0; u < RS_RADIX / 32; u++) {
+                v[u] = base[lane * (RS_RADIX / 32) + u];
+                sum += v[u];
+            }
+            int inc = sum;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, inc, off);
+                if (lane >= off) inc += y;
+            }
+            int run = inc - sum;
+#pragma unroll
+            for (int u = 0; u < RS_RADIX / 32; u++) {
+                base[lane * (RS_RADIX / 32) + u] = run;
+                run += v[u];
+            }
+        }
+        __syncthreads();
+        for (int t0 = 0; t0 < m; t0 += RB_TILE) {
+            for (int d = lane; d < RS_RADIX; d += 32) wcnt[warp][d] = 0;
+            __syncthreads();  // the bases of the previous tile are final; the counters are clear
+            const int wb = t0 + warp * (32 * RB_ITEMS);
+            int key[RB_ITEMS], val[RB_ITEMS], rnk[RB_ITEMS];
+            for (int r = 0; r < RB_ITEMS; r++) {
+                const int e = wb + r * 32 + lane;
+                const bool ok = e < m;
+                key[r] = ok ? kin[e] : 0;
+                val[r] = ok ? (vin ? vin[e] : e) : 0;
+                const int d = ok ? ((key[r] >> shift) & 0xFF) : RS_RADIX;
+                const unsigned peers = __match_any_sync(0xffffffffu, d);
+                const int before = __popc(peers & lt);
+                int bc = 0;
+                if (ok) bc = wcnt[warp][d];
+                __syncwarp();
+                rnk[r] = bc + before;
+                if (ok && before == 0) wcnt[warp][d] = bc + __popc(peers);
+                __syncwarp();
+            }
+            __syncthreads();
+            for (int d = threadIdx.x; d < RS_RADIX; d += RB_THREADS) {
+                int run = base[d];
+                for (int w = 0; w < RB_WARPS; w++) {
+                    const int c = wcnt[w][d];
+                    wcnt[w][d] = run;
+                    run += c;
+                }
+                base[d] = run;
+            }
+            __syncthreads();
+            for (int r = 0; r < RB_ITEMS; r++) {
+                const int e = wb + r * 32 + lane;
+                if (e < m) {
+                    const int pos = wcnt[warp][(key[r] >> shift) & 0xFF] + rnk[r];
+                    kout[pos] = key[r];
+                    vout[pos] = val[r];
+                }
+            }
+            __syncthreads();  // wcnt is reused by the next tile; this pass's output is complete
+        }
+        kin = kout;
+        vin = vout;
+        kout = (kout == ka) ? kb : ka;
+        vout = (vout == va) ? vb : va;
+    }
+    for (int j = threadIdx.x; j < m; j += RB_THREADS) {
+        const int q = vin[j];
+        const long long pos = (long long)gap[q] + j;
+        skey_out[pos] = kin[j];
+        perm_out[pos] = bidx[q];
+    }
+}
+
+// ---- placement ----------------------------------------------------------------------
+
 // stayer r lands at r + (movers with gap <= r).  A warp takes 32 words at once: their masks,
 // prefixes and gap-word data load one per lane; the keys load eight words ahead.  The stayer
 // ranks of one word lie in at most two consecutive 32-gap words, whose counts the warp loads
-// and prefix-sums only when they hold movers.
-__global__ void __launch_bounds__(RS_THREADS) k_rs_place_stayers(const int *key, long long n, const unsigned *wmask,
-                                                                   const int *wpref, long long nw, const int *gapcnt,
-                                                                   const int *gwcnt, const int *gwpref, int *skey_out,
-                                                                   int *perm_out)
+// and prefix-sums only when they hold movers.  The kernel is the last reader of the mover
+// words, so it clears them for the particle update that flags the next movers, and it records
+// the mover count for the next re-sort's clearing.
+__global__ void __launch_bounds__(RS_THREADS) k_rs_place_stayers(const int *key, long long n, unsigned *wmask,
+                                                                   int *wcnt, const int *wpref, long long nw,
+                                                                   const int *gapcnt, const int *gwcnt,
+                                                                   const int *gwpref, int *skey_out, int *perm_out,
+                                                                   int *mlast)
 {
     pdl_prologue();
+    if (blockIdx.x == 0 && threadIdx.x == 0) *mlast = wpref[nw];
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     const long long wstride = ((long long)gridDim.x * blockDim.x) >> 5;
@@ -253,6 +327,10 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_place_stayers(const int *key,
         const long long wl = w0 + lane;
         const bool wv = wl < nw;
         const unsigned mk = wv ? wmask[wl] : 0u;
+        if (wv && mk) {  // the last read of the word: clear it for the next step's movers
+            wmask[wl] = 0u;
+            wcnt[wl] = 0;
+        }
         const long long rb = wv ? wl * 32 - wpref[wl] : 0;  // rank of the word's first stayer
         const long long gwl = rb >> 5;
         const int gb = wv ? gwpref[gwl] : 0;
@@ -304,20 +382,20 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_place_stayers(const int *key,
 
 // ---- scratch and driver ---------------------------------------------------------------
 
+constexpr long long RS_NBK = 1LL << RS_BUCKET_BITS;
+
 size_t resort_scratch_ints(long long cap)
 {
     const long long nw = (cap + 31) / 32;
     const long long ngw = (cap + 2 + 63) / 32 + 2;  // 32-gap words, one spare word past the end
-    const long long hist = (long long)RS_RADIX * RS_MAX_CTAS;
-    return (size_t)(3 * (nw + 1) + scan_tmp_ints(nw + 1) + 5 * cap + ngw * 32 + 2 * (ngw + 1) +
-                    scan_tmp_ints(ngw + 1) + (RS_MAX_PASSES + 1) * hist + scan_tmp_ints(hist) + 64);
+    return (size_t)(3 * (nw + 1) + scan_tmp_ints(nw + 1) + 7 * cap + ngw * 32 + 2 * (ngw + 1 + RS_NBK) +
+                    scan_tmp_ints(ngw + 1 + RS_NBK) + 64);
 }
 
 void resort_bind(ResortScratch &rs, int *mem, long long cap)
 {
     const long long nw = (cap + 31) / 32;
     const long long ngw = (cap + 2 + 63) / 32 + 2;
-    const long long hist = (long long)RS_RADIX * RS_MAX_CTAS;
     int *p = mem;
     rs.wmask = reinterpret_cast<unsigned *>(p); p += nw + 1;
     rs.wcnt = p; p += nw + 1;
@@ -325,23 +403,28 @@ void resort_bind(ResortScratch &rs, int *mem, long long cap)
     rs.wscan_tmp = p; p += scan_tmp_ints(nw + 1);
     rs.bkey = p; p += cap;
     rs.bidx = p; p += cap;
-    rs.tkey = p; p += cap;
-    rs.tidx = p; p += cap;
     rs.gap = p; p += cap;
+    rs.bslot = p; p += cap;
+    rs.stk = p; p += cap;
+    rs.sti = p; p += cap;
+    rs.tval = p; p += cap;
     rs.gapcnt = p; p += ngw * 32;
-    rs.gwcnt = p; p += ngw + 1;
-    rs.gwpref = p; p += ngw + 1;
-    rs.gscan_tmp = p; p += scan_tmp_ints(ngw + 1);
-    rs.hist = p; p += (RS_MAX_PASSES + 1) * hist;  // a digit histogram per pass, then the offsets
-    rs.hscan_tmp = p;
+    rs.gwcnt = p; p += ngw + 1 + RS_NBK;  // the gap-word counts, then the bucket counts: one scan
+    rs.gwpref = p; p += ngw + 1 + RS_NBK;
+    rs.gscan_tmp = p; p += scan_tmp_ints(ngw + 1 + RS_NBK);
+    rs.big = p;
+    rs.mlast = p + 1;
     rs.cap = cap;
     rs.ngw = ngw;
 }
 
 // The scratch must be zero before the first call (it is zeroed once); each call clears the
-// gap counters its predecessor left and the digit histograms it uses.
+// gap counters its predecessor left and the bucket counters it uses.  mask_ready: the mover
+// words (wmask, wcnt) already flag every slot whose key differs from prev_skey -- the particle
+// update sets them, and flagging more slots than that is harmless -- so the two key arrays are
+// not compared here; otherwise k_rs_mask builds them.
 void resort_keys(const int *key, const int *prev_skey, int *skey_out, int *perm_out, long long n, int key_bits,
-                 ResortScratch &rs, cudaStream_t s)
+                 ResortScratch &rs, cudaStream_t s, bool mask_ready)
 {
     if (n <= 0) return;
     int dev = 0, sms = 1;
@@ -351,34 +434,35 @@ void resort_keys(const int *key, const int *prev_skey, int *skey_out, int *perm_
     const unsigned wgrid = (unsigned)std::min<long long>((nw + 4 * RS_WARPS - 1) / (4 * RS_WARPS), (long long)sms * 16);
     const long long nw32 = (nw + 31) / 32;  // 32-word batches (compaction, stayer placement)
     const unsigned bgrid = (unsigned)std::max<long long>(1, std::min<long long>((nw32 + RS_WARPS - 1) / RS_WARPS, (long long)sms * 16));
-    const unsigned qgrid = (unsigned)std::min<long long>((n + RS_THREADS - 1) / RS_THREADS, (long long)sms * 8);
-    const int G = std::min(2 * sms, RS_MAX_CTAS);
-    const int passes = std::min(RS_MAX_PASSES, std::max(1, (key_bits + 7) / 8));
-    const int hg = RS_RADIX * G;                                    // one pass's histogram
-    int *offsets = rs.hist + (long long)RS_MAX_PASSES * RS_RADIX * RS_MAX_CTAS;
-    launch_pdl(k_rs_mask, wgrid, RS_THREADS, s, key, prev_skey, n, rs.wmask, rs.wcnt, nw, rs.gap, rs.wpref, rs.gapcnt,
-                                           rs.gwcnt, rs.hist, passes * hg);
-    exclusive_scan_int(rs.wcnt, rs.wpref, nw + 1, rs.wscan_tmp, s);
-    // movers in slot order, with the first pass's digit counts per mover-sort CTA
-    launch_pdl(k_rs_compact, bgrid, RS_THREADS, s, key, rs.wmask, rs.wpref, nw, rs.bkey, rs.bidx, rs.hist, G);
-    note_launch(2);
-    // stable sort of the movers by key; their count is wpref[nw]
-    const int *m_ptr = rs.wpref + nw;
-    int *kin = rs.bkey, *vin = rs.bidx, *kout = rs.tkey, *vout = rs.tidx;
-    for (int p = 0; p < passes; p++) {
-        exclusive_scan_int(rs.hist + (long long)p * hg, offsets, hg, rs.hscan_tmp, s);
-        launch_pdl(k_rs_scatter, G, RS_THREADS, s, kin, vin, kout, vout, m_ptr, 8 * p, offsets,
-                                              p + 1 < passes ? rs.hist + (long long)(p + 1) * hg : nullptr);
+    const unsigned qgrid = (unsigned)std::min<long long>((n + RS_THREADS - 1) / RS_THREADS, (long long)sms * 4);
+    const int bits = std::max(1, key_bits);
+    const int shift = std::max(0, bits - RS_BUCKET_BITS);
+    const int nbk = 1 << (bits - shift);
+    const int passes = std::max(1, std::min(4, (bits + 7) / 8));
+    int *bcnt = rs.gwcnt + rs.ngw + 1;
+    const int *bpref = rs.gwpref + rs.ngw + 1;
+    if (!mask_ready) {
+        launch_pdl(k_rs_mask, wgrid, RS_THREADS, s, key, prev_skey, n, rs.wmask, rs.wcnt, nw);
         note_launch(1);
-        std::swap(kin, kout);
-        std::swap(vin, vout);
     }
-    launch_pdl(k_rs_place_movers, qgrid, RS_THREADS, s, prev_skey, n, rs.wmask, rs.wpref, nw, kin, vin, rs.gap, rs.gapcnt,
-                                                   rs.gwcnt, skey_out, perm_out);
-    exclusive_scan_int(rs.gwcnt, rs.gwpref, rs.ngw + 1, rs.gscan_tmp, s);
-    launch_pdl(k_rs_place_stayers, bgrid, RS_THREADS, s, key, n, rs.wmask, rs.wpref, nw, rs.gapcnt, rs.gwcnt, rs.gwpref,
-                                                    skey_out, perm_out);
+    exclusive_scan_int(rs.wcnt, rs.wpref, nw + 1, rs.wscan_tmp, s);
+    // movers in slot order (their count is wpref[nw]), their gaps and bucket counts
+    launch_pdl(k_rs_compact, bgrid, RS_THREADS, s, key, rs.wmask, rs.wpref, nw, rs.bkey, rs.bidx, rs.gap, rs.mlast,
+                                              rs.gapcnt, rs.gwcnt, bcnt, nbk, rs.big);
+    launch_pdl(k_rs_gaps, qgrid, RS_THREADS, s, prev_skey, n, rs.wmask, rs.wpref, nw, rs.bkey, rs.bidx, shift, rs.gap,
+                                           rs.gapcnt, rs.gwcnt, bcnt, rs.bslot);
     note_launch(2);
+    // gap-word prefixes for the stayers, bucket bases for the movers
+    exclusive_scan_int(rs.gwcnt, rs.gwpref, rs.ngw + 1 + nbk, rs.gscan_tmp, s);
+    launch_pdl(k_rs_stage, qgrid, RS_THREADS, s, rs.wpref, nw, rs.bkey, rs.bidx, rs.bslot, bpref, shift, rs.stk,
+                                            rs.sti);
+    launch_pdl(k_rs_rank, qgrid, RS_THREADS, s, rs.wpref, nw, rs.bkey, rs.bidx, rs.gap, bcnt, bpref, shift, rs.stk,
+                                           rs.sti, rs.big, skey_out, perm_out);
+    launch_pdl(k_rs_big, 1, RB_THREADS, s, rs.big, rs.wpref, nw, rs.bkey, rs.bidx, rs.gap, passes, rs.stk, rs.sti,
+                                          rs.bslot, rs.tval, skey_out, perm_out);
+    launch_pdl(k_rs_place_stayers, bgrid, RS_THREADS, s, key, n, rs.wmask, rs.wcnt, rs.wpref, nw, rs.gapcnt, rs.gwcnt,
+                                                    rs.gwpref, skey_out, perm_out, rs.mlast);
+    note_launch(4);
 }
 
 }  // namespace gy

@@ -60,6 +60,29 @@ def test_resort_matches_full_stable_sort(gpu_lib, n, frac):
     assert np.array_equal(srt, keys[want])
 
 
+@pytest.mark.parametrize("case", ["crowded", "wide_keys", "wide_crowded"])
+def test_resort_key_buckets(gpu_lib, case):
+    """Movers are ranked within buckets of neighbouring keys: single keys when keys have up
+    to 18 bits, ranges of keys above.  A bucket with more than 512 movers (here: most movers
+    piled onto a few keys) sends every mover through the one-CTA fallback sort; both ways the
+    result is the stable order."""
+    from graphyt_gb300 import _lib
+    rng = np.random.default_rng({"crowded": 1, "wide_keys": 2, "wide_crowded": 3}[case])
+    n = 200_003
+    hi = 25_000 if case == "crowded" else (1 << 26) - 1
+    prev = np.sort(rng.integers(0, hi, n)).astype(np.int32)
+    keys = prev.copy()
+    mv = rng.random(n) < (0.6 if case != "wide_keys" else 0.05)
+    if case == "wide_keys":
+        keys[mv] = np.clip(prev[mv] + rng.integers(-300, 301, mv.sum()), 0, hi)
+    else:
+        keys[mv] = rng.integers(0, 64, mv.sum()) * (1 if case == "crowded" else 97)
+    perm, srt = _lib.resort_keys(keys, prev)
+    want = np.argsort(keys, kind="stable")
+    assert np.array_equal(perm, want)
+    assert np.array_equal(srt, keys[want])
+
+
 def test_resort_edge_cases(gpu_lib):
     from graphyt_gb300 import _lib
     # every key equal; all moved onto one key; movers tied with stayers on both sides

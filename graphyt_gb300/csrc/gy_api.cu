@@ -83,6 +83,7 @@ struct gy_solver {
     ResortScratch rs{};
     void *resort_mem = nullptr;
     int *skey_buf[2] = {nullptr, nullptr};  // sorted keys of the last sort and its successor
+    int *d_blk_first = nullptr;             // first position of each cell block at the last sort
     int sk = 0;
     bool resort_valid = false;              // slab order = order of the sort in skey_buf[sk]
     StepScalars *d_sc = nullptr;            // this step's scalars (device)
@@ -205,6 +206,7 @@ void free_device(gy_solver *h)
     h->sort_mem = nullptr;
     h->resort_mem = nullptr;
     h->skey_buf[0] = h->skey_buf[1] = nullptr;
+    h->d_blk_first = nullptr;
     h->d_pbc_val = nullptr;
     h->d_flaw = nullptr;
     h->d_dplog = nullptr;
@@ -798,14 +800,17 @@ gy_status gy_initialize(gy_solver *h, const gy_material *mats, int nmat, const g
         h->ws.cap = h->cap;
         h->ws.nblocks_cap = (int)nbk;
     }
-    // incremental re-sort scratch and the two sorted-key buffers, zeroed once
+    // incremental re-sort scratch, the two sorted-key buffers and the cell blocks' first
+    // positions, zeroed once
     {
-        const size_t rints = resort_scratch_ints(h->cap) + 2 * (size_t)h->cap;
+        const size_t nblk = (size_t)h->g.nbx * h->g.nby * h->g.nbz;
+        const size_t rints = resort_scratch_ints(h->cap) + 2 * (size_t)h->cap + nblk;
         CK(h, cudaMalloc(&h->resort_mem, rints * sizeof(int) + 4096));
         CK(h, cudaMemsetAsync(h->resort_mem, 0, rints * sizeof(int) + 4096, h->stream));
         int *p = (int *)h->resort_mem;
         h->skey_buf[0] = p; p += h->cap;
         h->skey_buf[1] = p; p += h->cap;
+        h->d_blk_first = p; p += nblk;
         resort_bind(h->rs, p, h->cap);
         h->sk = 0;
         h->resort_valid = false;
@@ -958,7 +963,7 @@ static void issue_step(gy_solver *h, const StepVariant &v, cudaEvent_t *tev)
             // the slab is in the order of the last sort: re-sort only the particles that moved,
             // which every G2P since that sort has flagged (the mover words start clear, and
             // each re-sort clears them after use)
-            resort_keys(skey, h->skey_buf[v.sk ^ 1], out, h->d_perm, h->n, key_bits, h->rs, s, true);
+            resort_keys(skey, h->skey_buf[v.sk ^ 1], out, h->d_perm, h->n, key_bits, h->rs, s, true, h->d_blk_first);
         } else {
             const int *sorted = sort_pairs(skey, h->d_perm, h->n, key_bits, h->ws, s);
             if (h->n > 0 && sorted != out)
@@ -971,7 +976,8 @@ static void issue_step(gy_solver *h, const StepVariant &v, cudaEvent_t *tev)
     // heads fill one and zero the other for the next step, and zero this step's active
     // node-block count and list length
     int *nseg = h->d_nseg + v.cur;
-    launch_block_heads(skey, h->n, h->d_seg, nseg, s, h->nb.active_n, h->nb.active_count, h->d_nseg + (v.cur ^ 1));
+    launch_block_heads(skey, h->n, h->d_seg, nseg, s, h->nb.active_n, h->nb.active_count, h->d_nseg + (v.cur ^ 1),
+                       v.sort ? h->d_blk_first : nullptr);
     PView src = pview(h, v.cur), dst = pview(h, v.cur ^ 1);
     // body slots from the sort table of the reference's cadence (Solver.cpp:91)
     if (v.tables) {

@@ -171,13 +171,15 @@ struct ResortScratch {
 size_t resort_scratch_ints(long long cap);
 void resort_bind(ResortScratch &rs, int *mem, long long cap);
 void resort_keys(const int *key, const int *prev_skey, int *skey_out, int *perm_out, long long n, int key_bits,
-                 ResortScratch &rs, cudaStream_t s, bool mask_ready = false);
+                 ResortScratch &rs, cudaStream_t s, bool mask_ready = false, const int *blk_first = nullptr);
 // err (may be null) receives the first launch failure of the sort's kernels
 const int *sort_pairs(const int *keys_in, int *perm_out, long long n, int key_bits, SortScratch &ws, cudaStream_t s,
                       cudaError_t *err = nullptr);
-// nseg must be zero on entry; clear0..2 (may be null): counters the kernel zeroes on the way
+// nseg must be zero on entry; clear0..2 (may be null): counters the kernel zeroes on the way;
+// blk_first (may be null, one int per cell block): each non-empty block's first position
 void launch_block_heads(const int *skey, long long n, int *seg_start, int *nseg, cudaStream_t s,
-                        int *clear0 = nullptr, int *clear1 = nullptr, int *clear2 = nullptr);
+                        int *clear0 = nullptr, int *clear1 = nullptr, int *clear2 = nullptr,
+                        int *blk_first = nullptr);
 void exclusive_scan_int(const int *in, int *out, long long n, int *tmp, cudaStream_t s, cudaError_t *err = nullptr);
 
 // exclusive scan of ints: tiles of SCAN_TILE, scanned recursively over the tile sums

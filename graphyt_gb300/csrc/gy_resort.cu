@@ -90,10 +90,13 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_compact(const int *key, const
     }
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
-    const long long wstride = ((long long)gridDim.x * blockDim.x) >> 5;
-    for (long long w0 = (((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; w0 < nw; w0 += wstride * 32) {
+    // warp w takes the words [nw w / W, nw (w+1) / W), 32 at a time
+    const long long W = ((long long)gridDim.x * blockDim.x) >> 5;
+    const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long wend = nw * (wid + 1) / W;
+    for (long long w0 = nw * wid / W; w0 < wend; w0 += 32) {
         const long long wl = w0 + lane;
-        const unsigned mk = wl < nw ? wmask[wl] : 0u;
+        const unsigned mk = wl < wend ? wmask[wl] : 0u;
         const int pref = mk ? wpref[wl] : 0;
         unsigned nz = __ballot_sync(0xffffffffu, mk != 0u);
         while (nz) {
@@ -112,20 +115,40 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_compact(const int *key, const
 }
 
 // mover q (slot order): its gap g, the stayers below it in (key, slot) order, counted per gap
-// and per 32-gap word, and its arrival order within its key bucket
+// and per 32-gap word, and its arrival order within its key bucket.  blk_first (may be null)
+// holds the first position of each cell block in the order of prev, as the segment heads of
+// that sort wrote it; an entry is used only where prev confirms it.
 __global__ void __launch_bounds__(RS_THREADS) k_rs_gaps(const int *prev, long long n, const unsigned *wmask,
                                                           const int *wpref, long long nw, const int *bkey,
-                                                          const int *bidx, int shift, int *gap, int *gapcnt, int *gwcnt,
-                                                          int *bcnt, int *bslot)
+                                                          const int *bidx, int shift, const int *blk_first, int *gap,
+                                                          int *gapcnt, int *gwcnt, int *bcnt, int *bslot)
 {
     pdl_prologue();
     const int m = wpref[nw];
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < m; q += gridDim.x * blockDim.x) {
         const int k = bkey[q], i = bidx[q];
-        // first slot s with (prev[s], s) >= (k, i): a mover's new key is usually near its
-        // old one, so gallop out from its old slot i before bisecting (cache-near probes)
+        // first slot s with (prev[s], s) >= (k, i).  From the head p of k's cell block in
+        // prev, every slot below p holds a smaller key: gallop up from p.  Otherwise (the
+        // block was empty) a mover's new key is usually near its old one: gallop out from its
+        // old slot i.  Then bisect.
+        int p = -1;
+        if (blk_first) {
+            const int b = k >> CB_SHIFT;
+            const int c = blk_first[b];
+            if (c >= 0 && c < n && (prev[c] >> CB_SHIFT) == b && (c == 0 || (prev[c - 1] >> CB_SHIFT) != b)) p = c;
+        }
         long long lo, hi;
-        if (prev[i] < k) {  // the answer lies above i
+        if (p >= 0) {
+            long long step = 1;
+            lo = p;
+            hi = p;
+            while (hi < n && (prev[hi] < k || (prev[hi] == k && hi < i))) {
+                lo = hi + 1;
+                hi = p + step;
+                step <<= 1;
+            }
+            if (hi > n) hi = n;
+        } else if (prev[i] < k) {  // the answer lies above i
             long long step = 1;
             lo = i + 1;
             hi = i + 1;
@@ -322,10 +345,13 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_place_stayers(const int *key,
     if (blockIdx.x == 0 && threadIdx.x == 0) *mlast = wpref[nw];
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
-    const long long wstride = ((long long)gridDim.x * blockDim.x) >> 5;
-    for (long long w0 = (((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; w0 < nw; w0 += wstride * 32) {
+    // warp w takes the words [nw w / W, nw (w+1) / W), 32 at a time
+    const long long W = ((long long)gridDim.x * blockDim.x) >> 5;
+    const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long wend = nw * (wid + 1) / W;
+    for (long long w0 = nw * wid / W; w0 < wend; w0 += 32) {
         const long long wl = w0 + lane;
-        const bool wv = wl < nw;
+        const bool wv = wl < wend;
         const unsigned mk = wv ? wmask[wl] : 0u;
         if (wv && mk) {  // the last read of the word: clear it for the next step's movers
             wmask[wl] = 0u;
@@ -335,7 +361,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_place_stayers(const int *key,
         const long long gwl = rb >> 5;
         const int gb = wv ? gwpref[gwl] : 0;
         const int gc = wv ? (gwcnt[gwl] | gwcnt[gwl + 1]) : 0;
-        const int nwords = (int)min((long long)32, nw - w0);
+        const int nwords = (int)min((long long)32, wend - w0);
         for (int u0 = 0; u0 < nwords; u0 += 8) {
             int kv[8];
 #pragma unroll
@@ -424,7 +450,7 @@ void resort_bind(ResortScratch &rs, int *mem, long long cap)
 // update sets them, and flagging more slots than that is harmless -- so the two key arrays are
 // not compared here; otherwise k_rs_mask builds them.
 void resort_keys(const int *key, const int *prev_skey, int *skey_out, int *perm_out, long long n, int key_bits,
-                 ResortScratch &rs, cudaStream_t s, bool mask_ready)
+                 ResortScratch &rs, cudaStream_t s, bool mask_ready, const int *blk_first)
 {
     if (n <= 0) return;
     int dev = 0, sms = 1;
@@ -432,8 +458,19 @@ void resort_keys(const int *key, const int *prev_skey, int *skey_out, int *perm_
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long long nw = (n + 31) / 32;
     const unsigned wgrid = (unsigned)std::min<long long>((nw + 4 * RS_WARPS - 1) / (4 * RS_WARPS), (long long)sms * 16);
-    const long long nw32 = (nw + 31) / 32;  // 32-word batches (compaction, stayer placement)
-    const unsigned bgrid = (unsigned)std::max<long long>(1, std::min<long long>((nw32 + RS_WARPS - 1) / RS_WARPS, (long long)sms * 16));
+    // compaction and stayer placement: one resident wave of CTAs, the words split evenly over
+    // their warps (at least 32 words a warp)
+    static int occ_c = 0, occ_s = 0;
+    if (!occ_c) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_c, k_rs_compact, RS_THREADS, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, k_rs_place_stayers, RS_THREADS, 0);
+        occ_c = std::max(occ_c, 1);
+        occ_s = std::max(occ_s, 1);
+    }
+    const long long nw32 = (nw + 31) / 32;
+    const long long cmax = (nw32 + RS_WARPS - 1) / RS_WARPS;
+    const unsigned cgrid = (unsigned)std::max<long long>(1, std::min<long long>(cmax, (long long)sms * occ_c));
+    const unsigned sgrid = (unsigned)std::max<long long>(1, std::min<long long>(cmax, (long long)sms * occ_s));
     const unsigned qgrid = (unsigned)std::min<long long>((n + RS_THREADS - 1) / RS_THREADS, (long long)sms * 4);
     const int bits = std::max(1, key_bits);
     const int shift = std::max(0, bits - RS_BUCKET_BITS);
@@ -447,10 +484,10 @@ void resort_keys(const int *key, const int *prev_skey, int *skey_out, int *perm_
     }
     exclusive_scan_int(rs.wcnt, rs.wpref, nw + 1, rs.wscan_tmp, s);
     // movers in slot order (their count is wpref[nw]), their gaps and bucket counts
-    launch_pdl(k_rs_compact, bgrid, RS_THREADS, s, key, rs.wmask, rs.wpref, nw, rs.bkey, rs.bidx, rs.gap, rs.mlast,
+    launch_pdl(k_rs_compact, cgrid, RS_THREADS, s, key, rs.wmask, rs.wpref, nw, rs.bkey, rs.bidx, rs.gap, rs.mlast,
                                               rs.gapcnt, rs.gwcnt, bcnt, nbk, rs.big);
-    launch_pdl(k_rs_gaps, qgrid, RS_THREADS, s, prev_skey, n, rs.wmask, rs.wpref, nw, rs.bkey, rs.bidx, shift, rs.gap,
-                                           rs.gapcnt, rs.gwcnt, bcnt, rs.bslot);
+    launch_pdl(k_rs_gaps, qgrid, RS_THREADS, s, prev_skey, n, rs.wmask, rs.wpref, nw, rs.bkey, rs.bidx, shift,
+                                           blk_first, rs.gap, rs.gapcnt, rs.gwcnt, bcnt, rs.bslot);
     note_launch(2);
     // gap-word prefixes for the stayers, bucket bases for the movers
     exclusive_scan_int(rs.gwcnt, rs.gwpref, rs.ngw + 1 + nbk, rs.gscan_tmp, s);
@@ -460,7 +497,7 @@ void resort_keys(const int *key, const int *prev_skey, int *skey_out, int *perm_
                                            rs.sti, rs.big, skey_out, perm_out);
     launch_pdl(k_rs_big, 1, RB_THREADS, s, rs.big, rs.wpref, nw, rs.bkey, rs.bidx, rs.gap, passes, rs.stk, rs.sti,
                                           rs.bslot, rs.tval, skey_out, perm_out);
-    launch_pdl(k_rs_place_stayers, bgrid, RS_THREADS, s, key, n, rs.wmask, rs.wcnt, rs.wpref, nw, rs.gapcnt, rs.gwcnt,
+    launch_pdl(k_rs_place_stayers, sgrid, RS_THREADS, s, key, n, rs.wmask, rs.wcnt, rs.wpref, nw, rs.gapcnt, rs.gwcnt,
                                                     rs.gwpref, skey_out, perm_out, rs.mlast);
     note_launch(4);
 }

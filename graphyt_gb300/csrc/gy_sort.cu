@@ -227,9 +227,10 @@ constexpr int BH_TILE = 16 * BH_THREADS;
 constexpr int BH_BUF = 2 * BH_TILE;
 
 // nseg must be zero on entry.  The kernel also zeroes up to three counters of the caller
-// (clear0..2, may be null) that nothing reads while it runs.
+// (clear0..2, may be null) that nothing reads while it runs, and writes each head's position
+// at its block's entry of blk_first (may be null).
 __global__ void __launch_bounds__(BH_THREADS) k_block_heads(const int *skey, long long n, int *seg_start, int *nseg,
-                                                            int *clear0, int *clear1, int *clear2)
+                                                            int *clear0, int *clear1, int *clear2, int *blk_first)
 {
     pdl_prologue();
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -282,7 +283,10 @@ __global__ void __launch_bounds__(BH_THREADS) k_block_heads(const int *skey, lon
                 int base = 0;
                 if (lane == 0) base = atomicAdd(&bcount, __popc(mask));
                 base = __shfl_sync(0xffffffffu, base, 0);
-                if (head) buf[base + __popc(mask & lt)] = (int)ie;
+                if (head) {
+                    buf[base + __popc(mask & lt)] = (int)ie;
+                    if (blk_first) blk_first[e[q] >> CB_SHIFT] = (int)ie;
+                }
             }
         }
         __syncthreads();
@@ -300,14 +304,15 @@ __global__ void __launch_bounds__(BH_THREADS) k_block_heads(const int *skey, lon
 }
 
 void launch_block_heads(const int *skey, long long n, int *seg_start, int *nseg, cudaStream_t s, int *clear0,
-                        int *clear1, int *clear2)
+                        int *clear1, int *clear2, int *blk_first)
 {
     if (n > 0) {
         int dev = 0, sms = 1;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         const long long grid = std::min<long long>((n + BH_TILE - 1) / BH_TILE, (long long)sms * 4);
-        launch_pdl(k_block_heads, (unsigned)grid, BH_THREADS, s, skey, n, seg_start, nseg, clear0, clear1, clear2);
+        launch_pdl(k_block_heads, (unsigned)grid, BH_THREADS, s, skey, n, seg_start, nseg, clear0, clear1, clear2,
+                   blk_first);
         note_launch(1);
     } else {
         for (int *c : {clear0, clear1, clear2})

@@ -95,18 +95,27 @@ def test_resort_edge_cases(gpu_lib):
         _lib.resort_keys(np.zeros(4, np.int32), np.array([0, 2, 1, 3], np.int32))
 
 
-def test_incremental_resort_gives_the_full_sort_trajectory(gpu_lib):
+@pytest.mark.parametrize("case", ["dam", "dam_every3", "two_blocks_every3"])
+def test_incremental_resort_gives_the_full_sort_trajectory(gpu_lib, case):
     """The step's incremental re-sort produces the full sort's order: particles sit in the
     same device slots as in a run that sorts from scratch every step, and the state agrees
     to FP32 summation noise (the shared-memory and global reductions add in run-dependent
-    order, so two runs are not bit-identical even with the same sort)."""
-    sc = scenes.dam_break(scale=0.125)
+    order, so two runs are not bit-identical even with the same sort).  The re-sort takes
+    its movers from the bits G2P sets; sorting every third step, the bits of the unsorted
+    steps accumulate, which the multi-body case also covers."""
     rng = np.random.default_rng(5)
-    # a fast, uneven drift so that a varying share of particles changes cell every step
-    sc.vel[:, 0] = 30.0 + rng.normal(0.0, 4.0, len(sc.vel))
-    sc.vel[:, 1] = rng.normal(0.0, 4.0, len(sc.vel))
-    a = run_gpu(sc, 15, options=dict(full_sort=1))
-    b = run_gpu(sc, 15, options=dict(full_sort=0))
+    if case.startswith("dam"):
+        sc = scenes.dam_break(scale=0.125)
+        # a fast, uneven drift so that a varying share of particles changes cell every step
+        sc.vel[:, 0] = 30.0 + rng.normal(0.0, 4.0, len(sc.vel))
+        sc.vel[:, 1] = rng.normal(0.0, 4.0, len(sc.vel))
+    else:
+        # the blocks meet slowly along x while both drift across cells along y
+        sc = scenes.two_blocks()
+        sc.vel[:, 1] += 20.0 + rng.normal(0.0, 2.0, len(sc.vel))
+    every = 3 if case.endswith("every3") else 1
+    a = run_gpu(sc, 15, options=dict(full_sort=1, sort_every=every))
+    b = run_gpu(sc, 15, options=dict(full_sort=0, sort_every=every))
     moved = run_gpu(sc, 0)._get_particles_int("cellid") != b._get_particles_int("cellid")
     assert moved.mean() > 0.5
     slot_a, slot_b = a._get_particles_int("device_slot"), b._get_particles_int("device_slot")

@@ -162,7 +162,8 @@ struct ResortScratch {
     unsigned *wmask;
     int *wcnt, *wpref, *wscan_tmp;
     int *bkey, *bidx, *gap, *bslot;       // the movers in slot order
-    int *stk, *sti, *tval;                // the movers grouped by key bucket; fallback sort buffers
+    unsigned long long *stage;            // the movers grouped by key bucket, as (key, slot) words
+    int *tval;                            // a buffer of the fallback sort
     int *gapcnt, *gwcnt, *gwpref, *gscan_tmp;
     int *big;                             // a bucket too crowded to rank by counting
     int *mlast;                           // the last re-sort's mover count

@@ -17,6 +17,7 @@
 // traffic when few particles move; the full sort runs whenever the previous order is not
 // known (first step, restored state).
 #include <algorithm>
+#include <cstdint>
 
 #include "gy_kernels.cuh"
 
@@ -182,30 +183,37 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_gaps(const int *prev, long lo
     }
 }
 
+// a mover as one word ordered like (key, slot): both are non-negative ints
+__device__ __forceinline__ unsigned long long key_slot(int k, int i)
+{
+    return ((unsigned long long)(unsigned)k << 32) | (unsigned)i;
+}
+
 // the movers grouped by key bucket, in arrival order inside a bucket: bucket b's occupy
-// [bpref[b] - m, bpref[b] - m + bcnt[b]) of the staging arrays (bpref is the bucket part of a
+// [bpref[b] - m, bpref[b] - m + bcnt[b]) of the staging array (bpref is the bucket part of a
 // scan that starts with the m gap-word counts)
 __global__ void __launch_bounds__(RS_THREADS) k_rs_stage(const int *wpref, long long nw, const int *bkey,
                                                            const int *bidx, const int *bslot, const int *bpref,
-                                                           int shift, int *stk, int *sti)
+                                                           int shift, unsigned long long *stage)
 {
     pdl_prologue();
     const int m = wpref[nw];
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < m; q += gridDim.x * blockDim.x) {
         const int k = bkey[q];
-        const int j = bpref[k >> shift] - m + bslot[q];
-        stk[j] = k;
-        sti[j] = bidx[q];
+        stage[bpref[k >> shift] - m + bslot[q]] = key_slot(k, bidx[q]);
     }
 }
 
 // mover q lands at g + (movers of lower buckets) + (movers of its bucket before it in (key,
-// slot) order), the last counted over the bucket's staged movers.  A bucket of more than
-// RS_BUCKET_MAX movers raises *big, and k_rs_big places every mover instead.
+// slot) order), the last counted over the bucket's staged movers, eight independent loads at
+// a time (a bucket can hold a few hundred movers when a layer of particles crosses a cell
+// boundary at once).  A bucket of more than RS_BUCKET_MAX movers raises *big, and k_rs_big
+// places every mover instead.
 __global__ void __launch_bounds__(RS_THREADS) k_rs_rank(const int *wpref, long long nw, const int *bkey,
                                                           const int *bidx, const int *gap, const int *bcnt,
-                                                          const int *bpref, int shift, const int *stk, const int *sti,
-                                                          int *big, int *skey_out, int *perm_out)
+                                                          const int *bpref, int shift,
+                                                          const unsigned long long *stage, int *big, int *skey_out,
+                                                          int *perm_out)
 {
     pdl_prologue();
     const int m = wpref[nw];
@@ -216,12 +224,17 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_rank(const int *wpref, long l
             *big = 1;
             continue;
         }
-        const int j0 = bpref[b] - m;
-        int r = 0;
-        for (int j = j0; j < j0 + c; j++) {
-            const int kj = stk[j];
-            r += (kj < k || (kj == k && sti[j] < i)) ? 1 : 0;
+        const unsigned long long me = key_slot(k, i);
+        const int j0 = bpref[b] - m, j1 = j0 + c;
+        int r = 0, j = j0;
+        for (; j + 8 <= j1; j += 8) {
+            unsigned long long v[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) v[u] = __ldg(&stage[j + u]);
+#pragma unroll
+            for (int u = 0; u < 8; u++) r += v[u] < me ? 1 : 0;
         }
+        for (; j < j1; j++) r += __ldg(&stage[j]) < me ? 1 : 0;
         const long long pos = (long long)gap[q] + j0 + r;
         skey_out[pos] = k;
         perm_out[pos] = i;
@@ -431,8 +444,8 @@ void resort_bind(ResortScratch &rs, int *mem, long long cap)
     rs.bidx = p; p += cap;
     rs.gap = p; p += cap;
     rs.bslot = p; p += cap;
-    rs.stk = p; p += cap;
-    rs.sti = p; p += cap;
+    p = reinterpret_cast<int *>((reinterpret_cast<uintptr_t>(p) + 7) & ~(uintptr_t)7);  // 8-byte words next
+    rs.stage = reinterpret_cast<unsigned long long *>(p); p += 2 * cap;
     rs.tval = p; p += cap;
     rs.gapcnt = p; p += ngw * 32;
     rs.gwcnt = p; p += ngw + 1 + RS_NBK;  // the gap-word counts, then the bucket counts: one scan
@@ -491,12 +504,14 @@ void resort_keys(const int *key, const int *prev_skey, int *skey_out, int *perm_
     note_launch(2);
     // gap-word prefixes for the stayers, bucket bases for the movers
     exclusive_scan_int(rs.gwcnt, rs.gwpref, rs.ngw + 1 + nbk, rs.gscan_tmp, s);
-    launch_pdl(k_rs_stage, qgrid, RS_THREADS, s, rs.wpref, nw, rs.bkey, rs.bidx, rs.bslot, bpref, shift, rs.stk,
-                                            rs.sti);
-    launch_pdl(k_rs_rank, qgrid, RS_THREADS, s, rs.wpref, nw, rs.bkey, rs.bidx, rs.gap, bcnt, bpref, shift, rs.stk,
-                                           rs.sti, rs.big, skey_out, perm_out);
-    launch_pdl(k_rs_big, 1, RB_THREADS, s, rs.big, rs.wpref, nw, rs.bkey, rs.bidx, rs.gap, passes, rs.stk, rs.sti,
-                                          rs.bslot, rs.tval, skey_out, perm_out);
+    launch_pdl(k_rs_stage, qgrid, RS_THREADS, s, rs.wpref, nw, rs.bkey, rs.bidx, rs.bslot, bpref, shift, rs.stage);
+    launch_pdl(k_rs_rank, qgrid, RS_THREADS, s, rs.wpref, nw, rs.bkey, rs.bidx, rs.gap, bcnt, bpref, shift, rs.stage,
+                                           rs.big, skey_out, perm_out);
+    // the fallback's two key/value buffers: the staging words' ints, and the slot of each
+    // mover in the bucket (not needed after the staging) with tval
+    int *st_ints = reinterpret_cast<int *>(rs.stage);
+    launch_pdl(k_rs_big, 1, RB_THREADS, s, rs.big, rs.wpref, nw, rs.bkey, rs.bidx, rs.gap, passes, st_ints,
+                                          st_ints + rs.cap, rs.bslot, rs.tval, skey_out, perm_out);
     launch_pdl(k_rs_place_stayers, sgrid, RS_THREADS, s, key, n, rs.wmask, rs.wcnt, rs.wpref, nw, rs.gapcnt, rs.gwcnt,
                                                     rs.gwpref, skey_out, perm_out, rs.mlast);
     note_launch(4);

@@ -69,14 +69,13 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_mask(const int *key, const in
     }
 }
 
-// movers (key, slot) in slot order.  A warp takes 32 words at once (one mask per lane) and
+// the movers' slots in slot order.  A warp takes 32 words at once (one mask per lane) and
 // visits only the words that hold movers.  The kernel also clears the gap counters the
 // previous re-sort left (its *mlast movers are still listed in gap[]), this re-sort's bucket
 // counters and the fallback flag.
-__global__ void __launch_bounds__(RS_THREADS) k_rs_compact(const int *key, const unsigned *wmask, const int *wpref,
-                                                             long long nw, int *bkey, int *bidx, const int *gap,
-                                                             const int *mlast, int *gapcnt, int *gwcnt, int *bcnt,
-                                                             int nbk, int *big)
+__global__ void __launch_bounds__(RS_THREADS) k_rs_compact(const unsigned *wmask, const int *wpref, long long nw,
+                                                             int *bidx, const int *gap, const int *mlast, int *gapcnt,
+                                                             int *gwcnt, int *bcnt, int nbk, int *big)
 {
     pdl_prologue();
     {
@@ -105,29 +104,25 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_compact(const int *key, const
             nz &= nz - 1u;
             const unsigned m = __shfl_sync(0xffffffffu, mk, u);
             const int base = __shfl_sync(0xffffffffu, pref, u);
-            if ((m >> lane) & 1u) {
-                const long long i = (w0 + u) * 32 + lane;
-                const int pos = base + __popc(m & lt);
-                bkey[pos] = key[i];
-                bidx[pos] = (int)i;
-            }
+            if ((m >> lane) & 1u) bidx[base + __popc(m & lt)] = (int)((w0 + u) * 32 + lane);
         }
     }
 }
 
-// mover q (slot order): its gap g, the stayers below it in (key, slot) order, counted per gap
-// and per 32-gap word, and its arrival order within its key bucket.  blk_first (may be null)
+// mover q (slot order): its key, its gap g -- the stayers below it in (key, slot) order --
+// counted per gap and per 32-gap word, and its arrival order within its key bucket.  blk_first (may be null)
 // holds the first position of each cell block in the order of prev, as the segment heads of
 // that sort wrote it; an entry is used only where prev confirms it.
-__global__ void __launch_bounds__(RS_THREADS) k_rs_gaps(const int *prev, long long n, const unsigned *wmask,
-                                                          const int *wpref, long long nw, const int *bkey,
-                                                          const int *bidx, int shift, const int *blk_first, int *gap,
-                                                          int *gapcnt, int *gwcnt, int *bcnt, int *bslot)
+__global__ void __launch_bounds__(RS_THREADS) k_rs_gaps(const int *key, const int *prev, long long n,
+                                                          const unsigned *wmask, const int *wpref, long long nw,
+                                                          const int *bidx, int shift, const int *blk_first, int *bkey,
+                                                          int *gap, int *gapcnt, int *gwcnt, int *bcnt, int *bslot)
 {
     pdl_prologue();
     const int m = wpref[nw];
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < m; q += gridDim.x * blockDim.x) {
-        const int k = bkey[q], i = bidx[q];
+        const int i = bidx[q], k = key[i];
+        bkey[q] = k;
         // first slot s with (prev[s], s) >= (k, i).  From the head p of k's cell block in
         // prev, every slot below p holds a smaller key: gallop up from p.  Otherwise (the
         // block was empty) a mover's new key is usually near its old one: gallop out from its
@@ -370,8 +365,8 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_place_stayers(const int *key,
             wmask[wl] = 0u;
             wcnt[wl] = 0;
         }
-        const long long rb = wv ? wl * 32 - wpref[wl] : 0;  // rank of the word's first stayer
-        const long long gwl = rb >> 5;
+        const int rb = wv ? (int)(wl * 32 - wpref[wl]) : 0;  // rank of the word's first stayer (n < 2^31)
+        const int gwl = rb >> 5;
         const int gb = wv ? gwpref[gwl] : 0;
         const int gc = wv ? (gwcnt[gwl] | gwcnt[gwl + 1]) : 0;
         const int nwords = (int)min((long long)32, wend - w0);
@@ -387,12 +382,17 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_place_stayers(const int *key,
                 const int u = u0 + v;
                 if (u >= nwords) break;  // warp-uniform
                 const unsigned m = __shfl_sync(0xffffffffu, mk, u);
-                const long long rbase = __shfl_sync(0xffffffffu, rb, u);
-                const long long gw0 = rbase >> 5;
-                int c0 = 0, c1 = 0;
+                const int rbase = __shfl_sync(0xffffffffu, rb, u);
+                const int gbase = __shfl_sync(0xffffffffu, gb, u);
+                const long long i = (w0 + u) * 32 + lane;
+                const bool stay = i < n && !((m >> lane) & 1u);
+                const int r = rbase + lane - __popc(m & lt);
+                int add = 0;
                 if (__shfl_sync(0xffffffffu, gc, u)) {
-                    c0 = gapcnt[gw0 * 32 + lane];
-                    c1 = gapcnt[gw0 * 32 + 32 + lane];
+                    // movers in the gaps of the word's stayer ranks, which lie in two 32-gap
+                    // words: their counts prefix-summed across the lanes
+                    const int gw0 = rbase >> 5;
+                    int c0 = gapcnt[gw0 * 32 + lane], c1 = gapcnt[gw0 * 32 + 32 + lane];
 #pragma unroll
                     for (int off = 1; off < 32; off <<= 1) {
                         const int y0 = __shfl_up_sync(0xffffffffu, c0, off), y1 = __shfl_up_sync(0xffffffffu, c1, off);
@@ -401,16 +401,13 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_place_stayers(const int *key,
                             c1 += y1;
                         }
                     }
+                    const int tot0 = __shfl_sync(0xffffffffu, c0, 31);
+                    const int rr = r - gw0 * 32;  // 0..62 for a stayer
+                    const int in0 = __shfl_sync(0xffffffffu, c0, rr & 31), in1 = __shfl_sync(0xffffffffu, c1, rr & 31);
+                    add = rr < 32 ? in0 : tot0 + in1;
                 }
-                const int gbase = __shfl_sync(0xffffffffu, gb, u);
-                const int tot0 = __shfl_sync(0xffffffffu, c0, 31);
-                const long long i = (w0 + u) * 32 + lane;
-                const bool stay = i < n && !((m >> lane) & 1u);
-                const long long r = rbase + lane - __popc(m & lt);
-                const int rr = (int)(r - gw0 * 32);  // 0..62 for a stayer
-                const int in0 = __shfl_sync(0xffffffffu, c0, rr & 31), in1 = __shfl_sync(0xffffffffu, c1, rr & 31);
                 if (stay) {
-                    const long long pos = r + gbase + (rr < 32 ? in0 : tot0 + in1);
+                    const long long pos = (long long)r + gbase + add;
                     skey_out[pos] = kv[v];
                     perm_out[pos] = (int)i;
                 }
@@ -497,10 +494,10 @@ void resort_keys(const int *key, const int *prev_skey, int *skey_out, int *perm_
     }
     exclusive_scan_int(rs.wcnt, rs.wpref, nw + 1, rs.wscan_tmp, s);
     // movers in slot order (their count is wpref[nw]), their gaps and bucket counts
-    launch_pdl(k_rs_compact, cgrid, RS_THREADS, s, key, rs.wmask, rs.wpref, nw, rs.bkey, rs.bidx, rs.gap, rs.mlast,
-                                              rs.gapcnt, rs.gwcnt, bcnt, nbk, rs.big);
-    launch_pdl(k_rs_gaps, qgrid, RS_THREADS, s, prev_skey, n, rs.wmask, rs.wpref, nw, rs.bkey, rs.bidx, shift,
-                                           blk_first, rs.gap, rs.gapcnt, rs.gwcnt, bcnt, rs.bslot);
+    launch_pdl(k_rs_compact, cgrid, RS_THREADS, s, rs.wmask, rs.wpref, nw, rs.bidx, rs.gap, rs.mlast, rs.gapcnt,
+                                              rs.gwcnt, bcnt, nbk, rs.big);
+    launch_pdl(k_rs_gaps, qgrid, RS_THREADS, s, key, prev_skey, n, rs.wmask, rs.wpref, nw, rs.bidx, shift, blk_first,
+                                           rs.bkey, rs.gap, rs.gapcnt, rs.gwcnt, bcnt, rs.bslot);
     note_launch(2);
     // gap-word prefixes for the stayers, bucket bases for the movers
     exclusive_scan_int(rs.gwcnt, rs.gwpref, rs.ngw + 1 + nbk, rs.gscan_tmp, s);

@@ -13,9 +13,11 @@
 //   * stayer r (r-th stayer in slot order) lands at r + (movers with g <= r).
 // A bucket holding more than RS_BUCKET_MAX movers (a flow far outside the time-step limit,
 // or keys that are not cells) sends all movers through a one-CTA stable radix sort instead.
-// The result is the permutation the full stable radix sort produces, at a fraction of its
-// traffic when few particles move; the full sort runs whenever the previous order is not
-// known (first step, restored state).
+// In the step the movers come flagged: G2P sets a bit per slot whose key it changes (with a
+// count per 32 slots), and the stayer placement, their last reader, clears the bits.  The
+// result is the permutation the full stable radix sort produces, at a fraction of its traffic
+// when few particles move; the full sort runs whenever the previous order is not known
+// (initialisation, restored state).
 #include <algorithm>
 #include <cstdint>
 
@@ -424,6 +426,7 @@ size_t resort_scratch_ints(long long cap)
 {
     const long long nw = (cap + 31) / 32;
     const long long ngw = (cap + 2 + 63) / 32 + 2;  // 32-gap words, one spare word past the end
+    // + 64: the fallback flag, the last mover count and the 8-byte alignment of the staging
     return (size_t)(3 * (nw + 1) + scan_tmp_ints(nw + 1) + 7 * cap + ngw * 32 + 2 * (ngw + 1 + RS_NBK) +
                     scan_tmp_ints(ngw + 1 + RS_NBK) + 64);
 }
@@ -469,7 +472,8 @@ void resort_keys(const int *key, const int *prev_skey, int *skey_out, int *perm_
     const long long nw = (n + 31) / 32;
     const unsigned wgrid = (unsigned)std::min<long long>((nw + 4 * RS_WARPS - 1) / (4 * RS_WARPS), (long long)sms * 16);
     // compaction and stayer placement: one resident wave of CTAs, the words split evenly over
-    // their warps (at least 32 words a warp)
+    // their warps (at least 32 words a warp).  The resident CTAs per SM depend only on the
+    // kernels, built for one architecture, so they are looked up once per process.
     static int occ_c = 0, occ_s = 0;
     if (!occ_c) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_c, k_rs_compact, RS_THREADS, 0);

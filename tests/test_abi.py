@@ -52,3 +52,24 @@ def test_null_handles_are_errors(gpu_lib):
     assert gpu_lib.gy_step(None, 0.0, 0) == _lib.GY_ERR_ARG
     assert gpu_lib.gy_destroy(None) == _lib.GY_ERR_ARG
     assert gpu_lib.gy_last_error(None) == b"null handle"
+
+
+def test_resort_rejects_bad_input_before_cuda(gpu_lib):
+    """gy_resort_keys checks its host arrays before any CUDA work: previous keys that are not
+    non-decreasing, negative keys and negative counts are argument errors; nothing to sort
+    is success."""
+    import numpy as np
+    from graphyt_gb300 import _lib
+
+    def call(keys, prev, n=None):
+        keys = np.ascontiguousarray(keys, np.int32)
+        prev = np.ascontiguousarray(prev, np.int32)
+        out = np.zeros(max(len(keys), 1), np.int32)
+        srt = np.zeros(max(len(keys), 1), np.int32)
+        ip = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+        return gpu_lib.gy_resort_keys(ip(keys), ip(prev), len(keys) if n is None else n, ip(out), ip(srt), -1)
+
+    assert call([0, 1, 2, 3], [0, 2, 1, 3]) == _lib.GY_ERR_ARG     # previous order not sorted
+    assert call([0, -1, 2, 3], [0, 1, 2, 3]) == _lib.GY_ERR_ARG    # negative key
+    assert call([0, 1], [0, 1], n=-1) == _lib.GY_ERR_ARG
+    assert call([], [], n=0) == _lib.GY_OK
